@@ -1,0 +1,263 @@
+/*
+ * pms.h -- C ABI of libpms, the GB300-native particle-to-surface pipeline.
+ *
+ * libpms reimplements, for one GB300 (sm_103a), the per-frame hot path of the
+ * reference VisFluid program (xiaoxiaoyu1872/PostMPS): spatial hashing,
+ * surface-particle detection, anisotropic kernels, narrow-band vertex
+ * detection, narrow-band scalar field, marching cubes and diffuse-particle
+ * generation.  The reference exposes that path only as a C++ class chain
+ * (GPUPOST -> NeighborSearch / SurfaceReconstruction(Anisotropic,
+ * MarchingCube) / DiffuseGeneration sharing one GPUmemory); every entry point
+ * below names the member function it replaces.
+ *
+ * Conventions
+ *   - Every call returns pms_status; PMS_OK == 0.  A failing call leaves a
+ *     message retrievable with pms_last_error(ctx).  Nothing aborts.
+ *   - Host buffers are caller-owned plain arrays; positions and velocities are
+ *     xyz-interleaved float32 (the reference's float3 layout).
+ *   - Device buffers are owned by the context and reused (grow-only) across
+ *     frames.  A context is bound to one device and one CUDA stream and is not
+ *     thread-safe; use one context per host thread.
+ *   - Counts stay on the device between stages; calls that return counts or
+ *     data synchronise the context's stream.
+ */
+#ifndef PMS_H
+#define PMS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PMS_ABI_VERSION 1
+
+typedef enum pms_status {
+    PMS_OK = 0,
+    PMS_ERR_INVALID_ARGUMENT = 1,  /* null pointer, bad size, bad enum */
+    PMS_ERR_CUDA = 2,              /* a CUDA runtime call failed */
+    PMS_ERR_OUT_OF_MEMORY = 3,     /* device or host allocation failed */
+    PMS_ERR_CAPACITY = 4,          /* a caller-provided buffer or a fixed cap is too small */
+    PMS_ERR_IO = 5,                /* file could not be read or written */
+    PMS_ERR_CONFIG = 6,            /* config.txt missing or unusable */
+    PMS_ERR_STATE = 7,             /* stage called before its inputs exist */
+    PMS_ERR_TIMEOUT = 8,           /* a bounded device wait gave up */
+    PMS_ERR_UNSUPPORTED = 9        /* input outside what the kernels handle */
+} pms_status;
+
+/* ---------------------------------------------------------------------------
+ * Configuration: the reference's config.txt (Params.cpp:24-152, Define.h:85-202)
+ * ------------------------------------------------------------------------- */
+typedef struct pms_config {
+    /* [Sim] */
+    double mass;                       /* Mass (default 0) */
+    double particle_spacing;           /* ParticleSpacing (0.01) */
+    /* [Surface] */
+    double smoothing_radius_ratio;     /* SmoothingRadiusRatio (4), truncated to int */
+    long   min_num_neighbors;          /* MinNumNeighbors (8) */
+    long   isolate_num_neighbors;      /* IsolateNumNeighbors (4) */
+    double lambda_for_smoothed;        /* LambdaForSmoothed (0.5) */
+    double iso_value;                  /* IsoValue (0.5) */
+    /* [Diffuse] */
+    double min_wave_crests, max_wave_crests;        /* Min/MaxWaveCrestsThreshold (0, 100) */
+    double min_trapped_air, max_trapped_air;        /* Min/MaxTrappedAirThreshold (0, 100) */
+    double min_kinetic_energy, max_kinetic_energy;  /* Min/MaxKineticEnergyThreshold (0, 100) */
+    double trapped_air_multiplier;     /* DiffuseTrappedAirMultiplier (800) */
+    double wave_crests_multiplier;     /* DiffuseWaveCrestsMultiplier (4000) */
+    double time_step;                  /* TimeStep (0.01) */
+    double life_time;                  /* LifefimeMultiplier (10) */
+    double buoyancy_control;           /* BuoyancyControl (0.8) */
+    double drag_control;               /* DragControl (0.5) */
+    /* [Domain] */
+    double sp_scale;                   /* SpatialGridSizeScale (2) */
+    double sc_scale;                   /* SclarGridSizeScale (2) */
+    double domain_min[3], domain_max[3]; /* Min_x.. / Max_x.. (unused: the grid follows each frame's bbox) */
+    /* [Config] */
+    int gpu_id;                        /* GpuId (0) */
+    int frame_start, frame_end, frame_step;  /* Framefrom (0), Frameto (10), FrameStep (1) */
+    int num_zeros;                     /* NumZeros (4) */
+    int is_surface;                    /* IsSurfaceReconstruct (false) */
+    int is_diffuse;                    /* IsDiffuseGeneration (true) */
+    char fluid_path[512], fluid_prefix[128];
+    char surface_path[512], surface_prefix[128];
+    char diffuse_path[512], diffuse_prefix[128];
+    /* GB300 build additions (no reference counterpart) */
+    double fp64_svd_cond;              /* covariances with condition number above this use the FP64 eigen solver (1e6) */
+    uint64_t rng_seed;                 /* seed of the diffuse spawn uniforms (replaces std::random_device) */
+} pms_config;
+
+/* Derived float32 parameters (SimParams, SurfaceParams, DiffuseParams, Define.h:85-139). */
+typedef struct pms_params {
+    float mass, particle_spacing;
+    int   smoothing_radius_ratio;
+    float h, h_inv, h_sq, aniso_radius;
+    int   min_num_neighbors, isolate_num_neighbors;
+    float lambda_for_smoothed, iso_value;
+    float hd, hd_inv, hd_sq, hd_aniso, coefficient;
+    int   d_min_num_neighbors;
+    float min_wc, max_wc, min_ta, max_ta, min_ke, max_ke;
+    int   ta_mult, wc_mult, life_time;
+    float time_step, buoyancy, drag;
+    int   sp_scale, sc_scale;
+    float sp_grid_size, sc_grid_size;
+    int   spexpand, scexpand, spexpand_diffuse;
+} pms_params;
+
+/* Per-frame grid (GridParams, Define.h:142-174). */
+typedef struct pms_grid {
+    float min_pos[3], max_pos[3];      /* spatial grid: bbox -/+ 4h */
+    float scmin_pos[3], scmax_pos[3];  /* scalar grid: bbox -/+ 2h */
+    float sp_grid_size, sc_grid_size;
+    uint32_t spres[3], scres[3];
+    int32_t spexpand, scexpand, spexpand_diffuse;
+    uint32_t sp_size, sc_size;
+} pms_grid;
+
+/* Counters of one frame (GPUmemory.h:17-31). */
+typedef struct pms_counts {
+    uint32_t n_particles;
+    uint32_t n_surface_particles;      /* NumSurfaceParticles */
+    uint32_t n_band_vertices;          /* NumSurfaceVertices */
+    uint32_t n_valid_cubes;            /* NumValidSurfaceCubes */
+    uint64_t n_mesh_vertices;          /* NumSurfaceMeshVertices (3 per triangle) */
+    uint32_t n_free_surface;           /* NumFreeSurfaceParticles */
+    uint32_t n_generated_diffuse;      /* GeneratedNumDiffuseParticles */
+    uint32_t n_spawning;               /* NumIsDiffuseParticles */
+    uint32_t n_diffuse;                /* OldNumDiffuseParticles after delete/append */
+    uint32_t n_spray, n_foam, n_bubble;
+    uint32_t n_fp64_svd;               /* covariances re-solved in FP64 */
+} pms_counts;
+
+typedef struct pms_ctx pms_ctx;
+
+/* Parses config.txt with the reference's INI rules (inih: case-insensitive
+ * keys, ';' inline and '#'/';' line comments, continuation lines) and its
+ * defaults.  Replaces Params::setFilname/setParams (Params.cpp:17-152). */
+pms_status pms_config_default(pms_config* out);
+pms_status pms_config_load(const char* path, pms_config* out);
+
+/* Bit-exact restatement of Params.cpp:53-118. */
+pms_status pms_params_derive(const pms_config* cfg, pms_params* out);
+
+/* Bit-exact restatement of the per-frame grid, FileData.cpp:259-279 (NOBOUND). */
+pms_status pms_grid_from_bbox(const pms_params* p, const float bmin[3], const float bmax[3], pms_grid* out);
+
+/* Context lifetime: GPUPOST::initialize (GPUPOST.cpp:20-31) and
+ * GPUmemory::initGPUmemory (GPUmemory.cpp:14-18).  device < 0 uses cfg->gpu_id. */
+pms_status pms_create(const pms_config* cfg, int device, pms_ctx** out);
+void       pms_destroy(pms_ctx* ctx);
+const char* pms_last_error(const pms_ctx* ctx);
+const char* pms_status_string(pms_status s);
+
+/* Runs the context on a caller-provided cudaStream_t (NULL: the context's own stream). */
+pms_status pms_set_stream(pms_ctx* ctx, void* cuda_stream);
+
+/* Preallocates device buffers for frames up to these sizes (0: leave as is).
+ * GPUmemory's per-frame cudaMalloc/cudaFree pairs (GPUmemory.cpp:47-363) are
+ * replaced by this grow-only reservation. */
+pms_status pms_reserve(pms_ctx* ctx, uint32_t max_particles, uint64_t max_scalar_vertices);
+
+/* Uploads one frame from host arrays (vel and rhop may be NULL -> zeros).
+ * Replaces FileData::loadFluidFile + GPUmemory::memAlcandCpy_fluid
+ * (FileData.cpp:214-305, GPUmemory.cpp:47-72). */
+pms_status pms_upload_particles(pms_ctx* ctx, const float* pos_xyz, const float* vel_xyz,
+                                const float* rhop, uint32_t n);
+/* Same, from device-resident arrays (copied device-to-device on the context stream). */
+pms_status pms_upload_particles_device(pms_ctx* ctx, const float* d_pos_xyz, const float* d_vel_xyz,
+                                       const float* d_rhop, uint32_t n);
+
+/* Stages (asynchronous on the context stream unless stated). */
+pms_status pms_build_grid(pms_ctx* ctx);        /* NeighborSearch::SpatialGridBuilding, NeighborSearch.cu:37-76 */
+pms_status pms_anisotropy(pms_ctx* ctx);        /* Anisotropic::processingOfParticles, Anisotropic.cu:30-40 */
+pms_status pms_band(pms_ctx* ctx);              /* Anisotropic::processingOfVertices, Anisotropic.cu:43-50 */
+pms_status pms_field(pms_ctx* ctx);             /* Anisotropic::estimationOfscalarField, Anisotropic.cu:53-56 */
+pms_status pms_marching_cubes(pms_ctx* ctx);    /* MarchingCube::triangulation, MarchingCube.cu:32-68 */
+pms_status pms_surface(pms_ctx* ctx);           /* SurfaceReconstruction::runsimulation, SurfaceReconstruction.cu:34-60 */
+pms_status pms_diffuse(pms_ctx* ctx);           /* DiffuseGeneration::runsimulation, DiffuseGeneration.cu:89-104 */
+pms_status pms_run_frame(pms_ctx* ctx);         /* one iteration of GPUPOST::runSimulation, GPUPOST.cpp:56-81 */
+
+/* Results (synchronise the stream). */
+pms_status pms_get_counts(pms_ctx* ctx, pms_counts* out);
+pms_status pms_get_grid(pms_ctx* ctx, pms_grid* out);
+/* Triangle soup, 3 vertices per triangle (positions and normals xyz float32);
+ * nrm_xyz may be NULL.  Replaces the D2H copies of FileData::saveSurfacePLYfile
+ * (FileData.cpp:1297-1300).  *n_vertices receives the count even on PMS_ERR_CAPACITY. */
+pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices,
+                             uint64_t* n_vertices);
+/* Live diffuse particles of one type (0 spray, 1 foam, 2 bubble, -1 all), in the
+ * reference's generated-then-old order (DiffuseGeneration.cu:760-867).  Any of
+ * the arrays may be NULL; ttl is int32, energies are float32. */
+pms_status pms_download_diffuse(pms_ctx* ctx, int type, float* pos_xyz, float* vel_xyz, int32_t* type_out,
+                                int32_t* ttl, float* wave_crest, float* trapped_air, float* energy,
+                                uint32_t cap, uint32_t* n_out);
+
+/* Intermediate arrays, for parity tests.  Bytes needed are written to *needed;
+ * nothing is copied when dst is NULL or cap_bytes is too small. */
+typedef enum pms_array {
+    PMS_ARRAY_KEYS_SORTED = 1,   /* uint32[n]  cell key of each sorted particle */
+    PMS_ARRAY_PERM = 2,          /* uint32[n]  input index of each sorted particle */
+    PMS_ARRAY_CELL_START = 3,    /* uint32[sp_size]  (0 for empty cells, as the reference) */
+    PMS_ARRAY_CELL_END = 4,      /* uint32[sp_size] */
+    PMS_ARRAY_SURF_COUNT = 5,    /* uint32[sp_size]  numSurParticleGrid */
+    PMS_ARRAY_SURF_LIST = 6,     /* uint32[ns]  sorted index of each surface particle */
+    PMS_ARRAY_DENSITY = 7,       /* float[n]   density of each sorted particle */
+    PMS_ARRAY_MEAN = 8,          /* float[3 ns] weighted mean of each surface particle */
+    PMS_ARRAY_G = 9,             /* float[10 ns] G row-major + maxvalue (MatrixValue layout) */
+    PMS_ARRAY_NORMAL = 10,       /* float[3 ns] oriented normal of each surface particle */
+    PMS_ARRAY_FLAG = 11,         /* uint8[ns]  thin-feature / isolated flag */
+    PMS_ARRAY_BAND_BITMAP = 12,  /* uint32[ceil(sc_size/32)] band-vertex bitmap */
+    PMS_ARRAY_BAND_LIST = 13,    /* uint32[nv] band vertices, ascending linear index */
+    PMS_ARRAY_FIELD = 14,        /* float[nv] scalar field at band vertices */
+    PMS_ARRAY_CUBE_CASE = 15,    /* uint32[nv] marching-cubes case (0 when not all corners are band) */
+    PMS_ARRAY_CUBE_NVERT = 16,   /* uint32[nv] mesh vertices emitted by each cube */
+    PMS_ARRAY_POS_SORTED = 17,   /* float[3 n] sorted positions */
+    PMS_ARRAY_NEIGHBORS = 18,    /* uint32[ns] neighbours within h of each surface particle */
+    PMS_ARRAY_DIFFUSE_POTENTIAL = 19, /* float[3 n] waveCrest, Ita, energy after the phi clamps */
+    PMS_ARRAY_DIFFUSE_COUNT = 20,     /* int32[n] spawned diffuse particles per sorted particle */
+    PMS_ARRAY_FREE_NORMAL = 21        /* float[3 n] particle normals after the diffuse colour-gradient pass */
+} pms_array;
+pms_status pms_debug_download(pms_ctx* ctx, int array_id, void* dst, uint64_t cap_bytes, uint64_t* needed);
+
+/* Device time of each stage of the last frame, in milliseconds (CUDA events on
+ * the context stream): [grid, anisotropy, band, field, marching cubes, diffuse]. */
+pms_status pms_stage_times(pms_ctx* ctx, float* ms, int count);
+
+/* Number of kernels libpms launched since the context was created. */
+uint64_t pms_kernel_launches(const pms_ctx* ctx);
+
+/* Copies the marching-cubes tables in use (derived != 0: the tables libpms
+ * derives itself when built without the reference tree).  Returns 1 when the
+ * active tables are the reference's (MarchingCubesHelper.cpp:3-587), else 0. */
+int pms_mc_tables(uint32_t* edge_flags /*256*/, int32_t* tri /*256*16*/, uint32_t* num_vertices /*256*/,
+                  uint32_t* edge_vertices /*24*/, int derived);
+
+/* ---------------------------------------------------------------------------
+ * File formats (host)
+ * ------------------------------------------------------------------------- */
+/* Legacy-VTK polydata particles (ASCII or BINARY, float or double points,
+ * point arrays "Vel" and "Rhop", FileData.cpp:191-230).  Arrays are malloc'ed;
+ * release with pms_free_host. */
+pms_status pms_read_vtk_particles(const char* path, float** pos_xyz, float** vel_xyz, float** rhop, uint32_t* n);
+/* Writes particles as BINARY legacy VTK polydata with Vel and Rhop arrays. */
+pms_status pms_write_vtk_particles(const char* path, const float* pos_xyz, const float* vel_xyz,
+                                   const float* rhop, uint32_t n);
+/* ASCII PLY triangle soup in tinyply 2.3's layout (FileData.cpp:1277-1332). */
+pms_status pms_write_ply(const char* path, const float* pos_xyz, uint64_t n_vertices);
+/* Diffuse particles as BINARY legacy VTK with Velocity, Size, energy, Ita and
+ * waveCrest arrays (FileData.cpp:945-1036). */
+pms_status pms_write_diffuse_vtk(const char* path, const float* pos_xyz, const float* vel_xyz,
+                                 const float* energy, const float* ita, const float* wave_crest,
+                                 uint32_t n, float size);
+void pms_free_host(void* p);
+
+/* The VisGPU program: reads config_path, then for each frame reads
+ * FluidPath/FluidPrefix%0NNd.vtk, reconstructs, and writes
+ * SurfacePath/SurfacePrefix%0NNd.ply and (diffuse on) the PartSpary_/PartFoam_/
+ * PartBubble_ VTK files.  Replaces Main.cpp:4-11 / GPUPOST::runSimulation. */
+pms_status pms_run_config(const char* config_path, int verbose);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMS_H */

@@ -1,0 +1,2 @@
+/* empty stand-in: the emulation harness performs sorts and scans itself */
+#pragma once

@@ -1,0 +1,323 @@
+// k_aniso.cu -- density of every particle and the anisotropy of every surface
+// particle (weighted mean, covariance, eigen decomposition, eigenvalue clamp,
+// G matrix, oriented normal, thin-feature flag).
+//
+// Reference: Anisotropic_kernel.cuh:158-213 (calculationOfDensity),
+// 216-281 (calculationOfSmoothed), 350-519 (calculationOfTransformMatrices),
+// myCuda.cuh:84-119, 193-203, 403-415 (wij, matrixMul, determinant,
+// wij_density), SVD3.cuh (a float32 3x3 SVD).
+//
+// GB300 design: one thread per particle walks the sorted cells around it;
+// cells whose box lies beyond the kernel support are skipped (their
+// contributions are exactly zero), so the (4e+1)^3 box shrinks to the cells
+// that can matter.  The covariance is symmetric positive definite (it is seeded
+// with h^2 I), so its SVD is its eigen decomposition: a cyclic Jacobi solver
+// with exact rotations runs in float32, and covariances whose condition
+// number exceeds cfg.fp64_svd_cond are re-solved in float64.  Sums are
+// accumulated relative to the particle's own position for accuracy.
+#include "pms_internal.h"
+#include "k_common.cuh"
+
+namespace pms {
+
+static constexpr int kThreads = 128;
+static constexpr float kSigma = 1.56668147f;      // Define.h:11, 315/(64 pi)
+
+struct AnisoParams {
+    float h, h_sq, h_inv, r2h, mass, kdens, inv_h2;
+    int min_nn;
+    double cond_limit;
+};
+
+// Gap test: does the box of spatial cell (x,y,z) come within sqrt(r2) of p?
+// The box is widened by `pad` so that particles whose key rounded into the
+// cell from just outside are still covered.
+__device__ __forceinline__ float cell_gap2(const KGrid& g, float3 p, uint32_t x, uint32_t y, uint32_t z, float pad) {
+    float x0 = g.min_pos[0] + (float)x * g.sp_cs - pad, x1 = x0 + g.sp_cs + 2.f * pad;
+    float y0 = g.min_pos[1] + (float)y * g.sp_cs - pad, y1 = y0 + g.sp_cs + 2.f * pad;
+    float z0 = g.min_pos[2] + (float)z * g.sp_cs - pad, z1 = z0 + g.sp_cs + 2.f * pad;
+    float dx = axis_gap(p.x, x0, x1), dy = axis_gap(p.y, y0, y1), dz = axis_gap(p.z, z0, z1);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// ---------------------------------------------------------------------------
+// density (calculationOfDensity): rho_i = sum_j sigma/h^3 (1 - (d/h)^2)^3, d < h,
+// over cells [c - e, c + e]; also stores m / rho into spos.w for the field.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
+                                                      const uint2* __restrict__ cell_info, float4* __restrict__ spos,
+                                                      float* __restrict__ rho, uint32_t n) {
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    const float pad = 1e-4f * g.sp_cs;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 pi4 = spos[i];
+        float3 p = make_float3(pi4.x, pi4.y, pi4.z);
+        uint32_t key = skeys[i];
+        uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
+        uint3 lo, hi;
+        box_clamp(g, c, (uint32_t)g.spexpand, lo, hi);
+        float w = 0.f;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    if (cell_gap2(g, p, x, y, z, pad) >= ap.h_sq) continue;
+                    uint2 ci = cell_info[z * rxy + y * rx + x];
+                    uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        float4 q = spos[j];
+                        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                        float d2 = dx * dx + dy * dy + dz * dz;
+                        if (d2 < ap.h_sq) {
+                            float s = 1.f - d2 * ap.inv_h2;
+                            w += ap.kdens * s * s * s;
+                        }
+                    }
+                }
+        rho[i] = w;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_inv_density(float4* __restrict__ spos, const float* __restrict__ rho,
+                                                          float mass, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float r = rho[i];
+        spos[i].w = r == 0.f ? 0.f : mass / r;   // particles with rho == 0 are skipped by the field
+    }
+}
+
+// ---------------------------------------------------------------------------
+// symmetric 3x3 eigen decomposition, cyclic Jacobi with exact rotations
+// (Golub & Van Loan, Algorithm 8.4.2 / the classical Jacobi method)
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void jacobi_rotate(T a[3][3], T v[3][3], int p, int q) {
+    T apq = a[p][q];
+    if (apq == T(0)) return;
+    T theta = (a[q][q] - a[p][p]) / (T(2) * apq);
+    T t = (theta >= T(0) ? T(1) : T(-1)) / (fabs(theta) + sqrt(theta * theta + T(1)));
+    T c = T(1) / sqrt(t * t + T(1)), s = t * c;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        T akp = a[k][p], akq = a[k][q];
+        a[k][p] = c * akp - s * akq;
+        a[k][q] = s * akp + c * akq;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        T apk = a[p][k], aqk = a[q][k];
+        a[p][k] = c * apk - s * aqk;
+        a[q][k] = s * apk + c * aqk;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        T vkp = v[k][p], vkq = v[k][q];
+        v[k][p] = c * vkp - s * vkq;
+        v[k][q] = s * vkp + c * vkq;
+    }
+}
+
+// On return e[0..2] are eigenvalues sorted by decreasing magnitude and
+// column k of v the matching unit eigenvector.
+template <class T>
+__device__ __forceinline__ void eig_sym3(T a[3][3], T e[3], T v[3][3], T tol) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[i][j] = (i == j) ? T(1) : T(0);
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        T off = fabs(a[0][1]) + fabs(a[0][2]) + fabs(a[1][2]);
+        T dia = fabs(a[0][0]) + fabs(a[1][1]) + fabs(a[2][2]);
+        if (off <= tol * dia) break;
+        jacobi_rotate<T>(a, v, 0, 1);
+        jacobi_rotate<T>(a, v, 0, 2);
+        jacobi_rotate<T>(a, v, 1, 2);
+    }
+    T d[3] = {a[0][0], a[1][1], a[2][2]};
+    int i0 = 0, i1 = 1, i2 = 2;
+    if (fabs(d[i1]) > fabs(d[i0])) { int t = i0; i0 = i1; i1 = t; }
+    if (fabs(d[i2]) > fabs(d[i0])) { int t = i0; i0 = i2; i2 = t; }
+    if (fabs(d[i2]) > fabs(d[i1])) { int t = i1; i1 = i2; i2 = t; }
+    int idx[3] = {i0, i1, i2};
+    T w[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        e[k] = d[idx[k]];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) w[r][k] = v[r][idx[k]];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v[r][k] = w[r][k];
+}
+
+// ---------------------------------------------------------------------------
+// anisotropy of one surface particle per thread
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
+                                                    const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
+                                                    const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                    float4* __restrict__ aniso, float4* __restrict__ nrm4,
+                                                    float4* __restrict__ mean4, float* __restrict__ gdebug,
+                                                    uint32_t* __restrict__ nnb, uint32_t* __restrict__ n_fp64) {
+    const uint32_t ns = cnt->ns;
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    const float pad = 1e-4f * g.sp_cs;
+    const float r2h_sq = ap.r2h * ap.r2h;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const uint32_t i = slist[s];
+        const float4 pi4 = spos[i];
+        const float3 p = make_float3(pi4.x, pi4.y, pi4.z);
+        const uint32_t key = skeys[i];
+        const uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
+        uint3 lo, hi;
+        box_clamp(g, c, 2u * (uint32_t)g.spexpand, lo, hi);
+
+        // pass 1: weighted mean (calculationOfSmoothed), support 2h
+        float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    if (cell_gap2(g, p, x, y, z, pad) >= r2h_sq) continue;
+                    uint2 ci = cell_info[z * rxy + y * rx + x];
+                    uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        float4 q = spos[j];
+                        float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                        float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                        if (d < ap.r2h) {
+                            float t = d / ap.r2h;
+                            float w = 1.f - t * t * t;
+                            ws += w; mx += w * dx; my += w * dy; mz += w * dz;
+                        }
+                    }
+                }
+        // the particle itself contributes w = 1, so ws > 0
+        const float ox = mx / ws, oy = my / ws, oz = mz / ws;   // mean - p
+
+        // pass 2: covariance about the mean and neighbour count within h
+        float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f, wsum = 0.f;
+        uint32_t nn = 0;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    if (cell_gap2(g, p, x, y, z, pad) >= r2h_sq) continue;
+                    uint2 ci = cell_info[z * rxy + y * rx + x];
+                    uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        float4 q = spos[j];
+                        // neighbour count: u = x_j - x_i, |u| <= h, each operation rounded once
+                        float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
+                        float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
+                        float d = __fsqrt_rn(d2);
+                        nn += (d <= ap.h) ? 1u : 0u;
+                        if (d < ap.r2h) {
+                            float t = d / ap.r2h;
+                            float w = 1.f - t * t * t;
+                            float vx = ux - ox, vy = uy - oy, vz = uz - oz;
+                            wsum += w;
+                            c00 += w * vx * vx; c11 += w * vy * vy; c22 += w * vz * vz;
+                            c01 += w * vx * vy; c02 += w * vx * vz; c12 += w * vy * vz;
+                        }
+                    }
+                }
+        float G[3][3], nv[3], maxv;
+        float flag;
+        if ((int)nn < ap.min_nn) {
+            // isolated particle: isotropic kernel (Anisotropic_kernel.cuh:435-443)
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) G[a][b] = (a == b) ? ap.h_inv : 0.f;
+            maxv = 1.f; flag = 1.f; nv[0] = 1.f; nv[1] = 0.f; nv[2] = 0.f;
+        } else {
+            float A[3][3] = {{(ap.h_sq + c00) / wsum, c01 / wsum, c02 / wsum},
+                             {c01 / wsum, (ap.h_sq + c11) / wsum, c12 / wsum},
+                             {c02 / wsum, c12 / wsum, (ap.h_sq + c22) / wsum}};
+            float e[3], U[3][3];
+            float Acopy[3][3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) Acopy[a][b] = A[a][b];
+            eig_sym3<float>(A, e, U, 1e-7f);
+            float sv0 = fabsf(e[0]), sv1 = fabsf(e[1]), sv2 = fabsf(e[2]);
+            if ((double)sv0 > ap.cond_limit * (double)sv2) {
+                // near-degenerate covariance: solve again in float64
+                double Ad[3][3], ed[3], Ud[3][3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) Ad[a][b] = (double)Acopy[a][b];
+                eig_sym3<double>(Ad, ed, Ud, 1e-15);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    e[k] = (float)ed[k];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) U[r][k] = (float)Ud[r][k];
+                }
+                sv0 = fabsf(e[0]); sv1 = fabsf(e[1]); sv2 = fabsf(e[2]);
+                atomicAdd(n_fp64, 1u);
+            }
+            // clamp and scale (Anisotropic_kernel.cuh:459-509)
+            float smax = fmaxf(sv0, fmaxf(sv1, sv2)), smin = fminf(sv0, fminf(sv1, sv2));
+            flag = (smin <= smax * 0.25f) ? 1.f : 0.f;
+            float lim = smax / 4.0f;
+            sv0 = fmaxf(sv0, lim); sv1 = fmaxf(sv1, lim); sv2 = fmaxf(sv2, lim);
+            float scale = cbrtf(sv0 * sv1 * sv2);
+            float cof = ap.h_inv * scale;
+            float k0 = cof / sv0, k1 = cof / sv1, k2 = cof / sv2;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b)
+                    G[a][b] = U[a][0] * k0 * U[b][0] + U[a][1] * k1 * U[b][1] + U[a][2] * k2 * U[b][2];
+            nv[0] = U[0][2]; nv[1] = U[1][2]; nv[2] = U[2][2];
+            maxv = sv0 / scale;
+        }
+        // orient the normal away from the mean (Anisotropic_kernel.cuh:512-515)
+        if (nv[0] * (-ox) + nv[1] * (-oy) + nv[2] * (-oz) < 0.f) { nv[0] = -nv[0]; nv[1] = -nv[1]; nv[2] = -nv[2]; }
+        // determinant as the reference evaluates it (myCuda.cuh:193-203)
+        float det = G[0][0] * G[1][1] * G[2][2] + G[0][1] * G[1][2] * G[2][0] + G[0][2] * G[1][0] * G[2][1]
+                  - G[0][0] * G[1][2] * G[2][1] - G[0][1] * G[1][0] * G[2][2] - G[0][2] * G[1][1] * G[2][0];
+        const float hs = maxv * ap.h;
+        aniso[3 * (size_t)i + 0] = make_float4(G[0][0], G[0][1], G[0][2], hs);
+        aniso[3 * (size_t)i + 1] = make_float4(G[1][0], G[1][1], G[1][2], kSigma * det);
+        aniso[3 * (size_t)i + 2] = make_float4(G[2][0], G[2][1], G[2][2], maxv);
+        nrm4[i] = make_float4(nv[0], nv[1], nv[2], flag);
+        mean4[s] = make_float4(p.x + ox, p.y + oy, p.z + oz, ws);
+        float* gd = gdebug + 10 * (size_t)s;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) gd[3 * a + b] = G[a][b];
+        gd[9] = maxv;
+        nnb[s] = nn;
+    }
+}
+
+pms_status launch_density_aniso(pms_ctx* ctx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const pms_params& P = ctx->prm;
+    AnisoParams ap;
+    ap.h = P.h; ap.h_sq = P.h_sq; ap.h_inv = P.h_inv; ap.r2h = P.aniso_radius; ap.mass = P.mass;
+    ap.kdens = kSigma / (P.h * P.h * P.h);
+    ap.inv_h2 = 1.f / (P.h * P.h);
+    ap.min_nn = P.min_num_neighbors;
+    ap.cond_limit = ctx->cfg.fp64_svd_cond;
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ap, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->rho.as<float>(), ctx->n);
+    PMS_LAUNCHED(ctx);
+    k_inv_density<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(), P.mass, ctx->n);
+    PMS_LAUNCHED(ctx);
+    // ns is on the device; size the grid by the particle count (upper bound)
+    k_aniso<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(),
+        ctx->spos.as<float4>(), ctx->aniso.as<float4>(), ctx->nrm4.as<float4>(), ctx->mean4.as<float4>(),
+        ctx->gdebug.as<float>(), ctx->nnb.as<uint32_t>(), &cnt->n_fp64);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+}  // namespace pms

@@ -1,0 +1,202 @@
+// k_mc.cu -- marching cubes over the narrow band.
+//
+// Reference: MarchingCube_kernel.cuh:20-157 and MarchingCube.cu:32-151.
+// detectValidSurfaceCubes: the cube whose origin is band vertex (x,y,z) is
+// classified only if all 8 corners are band vertices; its case has bit k set
+// when field(corner k) <= iso (corner k at offset {000,001,011,010,100,101,
+// 111,110} in (x,y,z), myCuda.cuh:205-257); numVertices[case] mesh vertices
+// follow.  Two thrust scans give valid-cube and vertex offsets,
+// compactValidSurfaceCubes lists valid cubes, generateTriangles interpolates
+// the 12 edge points (getLerpFac, myCuda.cuh:332-339) and normals (central
+// differences of the field, zero outside the grid and outside the band,
+// myCuda.cuh:259-289) and writes the triangle soup in table order.
+//
+// GB300 design: the field lives compactly in band order; a vertex's value is
+// found through the band bitmap (rank = word prefix + popcount).  One scan
+// over packed 64-bit keys (valid << 32 | nvert) yields both offsets.  Tables
+// sit in constant memory.
+#include "pms_internal.h"
+#include "k_common.cuh"
+
+namespace pms {
+
+__constant__ uint32_t c_edge_flags[256];
+__constant__ int8_t c_tri[256][16];
+__constant__ uint8_t c_num_vertices[256];
+__constant__ uint8_t c_edge_vertex[12][2];
+
+static constexpr int kThreads = 128;
+__device__ __constant__ int c_corner[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {0, 1, 0},
+                                              {1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}};
+
+pms_status upload_mc_tables(pms_ctx* ctx) {
+    const McTables& T = mc_tables_host();
+    int8_t tri[256][16];
+    uint8_t nv[256];
+    uint8_t ev[12][2];
+    for (int c = 0; c < 256; ++c) {
+        nv[c] = (uint8_t)T.num_vertices[c];
+        for (int k = 0; k < 16; ++k) tri[c][k] = (int8_t)T.tri[c][k];
+    }
+    for (int e = 0; e < 12; ++e) { ev[e][0] = (uint8_t)T.edge_vertex[e][0]; ev[e][1] = (uint8_t)T.edge_vertex[e][1]; }
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_edge_flags, T.edge_flags, sizeof(T.edge_flags)));
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_tri, tri, sizeof(tri)));
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_num_vertices, nv, sizeof(nv)));
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_edge_vertex, ev, sizeof(ev)));
+    return PMS_OK;
+}
+
+__device__ __forceinline__ bool band_value(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
+                                           const float* __restrict__ field, uint64_t nbits, uint64_t id, float& f) {
+    if (!bit_get(bm, nbits, id)) return false;
+    f = __ldg(&field[bit_rank(bm, wprefix, (uint32_t)id)]);
+    return true;
+}
+
+// detectValidSurfaceCubes (6-argument version)
+__global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, const Counters* __restrict__ cnt,
+                                                          const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ bm,
+                                                          const uint32_t* __restrict__ wprefix, const float* __restrict__ field,
+                                                          uint32_t* __restrict__ mc_case, unsigned long long* __restrict__ mc_key) {
+    const uint32_t nv = cnt->nv;
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    const uint64_t nbits = g.sc_size;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x) {
+        const uint32_t id = vlist[t];
+        const uint32_t z = id / rxy, rem = id - z * rxy, y = rem / rx, x = rem - y * rx;
+        uint32_t cs = 0, nvert = 0;
+        bool all = true;
+        float f[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            // uint32 corner index as getCornerIndex1Ds computes it
+            const uint32_t cid = (z + c_corner[k][2]) * rxy + (y + c_corner[k][1]) * rx + (x + c_corner[k][0]);
+            if (!band_value(bm, wprefix, field, nbits, cid, f[k])) { all = false; }
+        }
+        if (all) {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) cs |= (f[k] <= iso ? 1u : 0u) << k;
+            nvert = c_num_vertices[cs];
+        }
+        mc_case[t] = cs;
+        mc_key[t] = nvert ? ((1ull << 32) | nvert) : 0ull;
+    }
+}
+
+// unpack the scanned total {valid cubes << 32 | mesh vertices} into the counters
+__global__ void k_mc_totals(const unsigned long long* __restrict__ total, Counters* __restrict__ cnt) {
+    const unsigned long long t = *total;
+    cnt->nvalid = (uint32_t)(t >> 32);
+    cnt->nmesh = t & 0xffffffffull;
+}
+
+__global__ void __launch_bounds__(256) k_mc_compact(const Counters* __restrict__ cnt,
+                                                    const unsigned long long* __restrict__ mc_key,
+                                                    const unsigned long long* __restrict__ mc_off,
+                                                    uint32_t* __restrict__ valid) {
+    const uint32_t nv = cnt->nv;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x)
+        if (mc_key[t]) valid[(uint32_t)(mc_off[t] >> 32)] = t;
+}
+
+__device__ __forceinline__ float grid_value(const KGrid& g, const uint32_t* __restrict__ bm,
+                                            const uint32_t* __restrict__ wprefix, const float* __restrict__ field,
+                                            int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0 || (uint32_t)x >= g.scres[0] || (uint32_t)y >= g.scres[1] || (uint32_t)z >= g.scres[2])
+        return 0.f;
+    const uint64_t id = (uint64_t)z * g.scres[0] * g.scres[1] + (uint64_t)y * g.scres[0] + (uint64_t)x;
+    float f = 0.f;
+    band_value(bm, wprefix, field, g.sc_size, id, f);
+    return f;
+}
+
+__device__ __forceinline__ float3 normalized(float3 v) {
+    const float inv = 1.f / sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    return make_float3(v.x * inv, v.y * inv, v.z * inv);
+}
+
+// generateTriangles: one thread per valid cube
+__global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, const Counters* __restrict__ cnt,
+                                                      const uint32_t* __restrict__ valid, const uint32_t* __restrict__ vlist,
+                                                      const uint32_t* __restrict__ mc_case,
+                                                      const unsigned long long* __restrict__ mc_off,
+                                                      const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
+                                                      const float* __restrict__ field, float* __restrict__ vert,
+                                                      float* __restrict__ vnorm) {
+    const uint32_t nvalid = cnt->nvalid;
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    const float sgn = (iso < 0.f) ? -1.f : 1.f;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nvalid; k += gridDim.x * blockDim.x) {
+        const uint32_t t = valid[k];
+        const uint32_t id = vlist[t];
+        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
+        const uint32_t cs = mc_case[t];
+        const uint32_t base = (uint32_t)(mc_off[t] & 0xffffffffull);
+        float3 cp[8], cn[8];
+        float cf[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int X = x + c_corner[c][0], Y = y + c_corner[c][1], Z = z + c_corner[c][2];
+            cp[c] = make_float3(sc_coord_i(g, X, 0), sc_coord_i(g, Y, 1), sc_coord_i(g, Z, 2));
+            cf[c] = grid_value(g, bm, wprefix, field, X, Y, Z);
+            float3 n;
+            n.x = grid_value(g, bm, wprefix, field, X - 1, Y, Z) - grid_value(g, bm, wprefix, field, X + 1, Y, Z);
+            n.y = grid_value(g, bm, wprefix, field, X, Y - 1, Z) - grid_value(g, bm, wprefix, field, X, Y + 1, Z);
+            n.z = grid_value(g, bm, wprefix, field, X, Y, Z - 1) - grid_value(g, bm, wprefix, field, X, Y, Z + 1);
+            cn[c] = normalized(n);
+        }
+        const uint32_t ef = c_edge_flags[cs];
+        float3 ip[12], in[12];
+#pragma unroll
+        for (int e = 0; e < 12; ++e) {
+            if (!(ef & (1u << e))) continue;
+            const int a = c_edge_vertex[e][0], b = c_edge_vertex[e][1];
+            const float d = cf[b] - cf[a];
+            // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5
+            const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
+            ip[e] = make_float3(cp[a].x + tt * (cp[b].x - cp[a].x), cp[a].y + tt * (cp[b].y - cp[a].y),
+                                cp[a].z + tt * (cp[b].z - cp[a].z));
+            const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x), cn[a].y + tt * (cn[b].y - cn[a].y),
+                                                     cn[a].z + tt * (cn[b].z - cn[a].z)));
+            in[e] = make_float3(sgn * nn.x, sgn * nn.y, sgn * nn.z);
+        }
+        const uint32_t nvert = c_num_vertices[cs];
+        for (uint32_t v = 0; v < nvert; ++v) {
+            const int e = c_tri[cs][v];
+            const size_t o = 3 * ((size_t)base + v);
+            vert[o] = ip[e].x; vert[o + 1] = ip[e].y; vert[o + 2] = ip[e].z;
+            vnorm[o] = in[e].x; vnorm[o + 1] = in[e].y; vnorm[o + 2] = in[e].z;
+        }
+    }
+}
+
+pms_status launch_mc_classify(pms_ctx* ctx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_mc_classify<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(),
+        ctx->field.as<float>(), ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
+    PMS_LAUNCHED(ctx);
+    pms_status st = scan_u64(ctx, ctx->mc_key.as<unsigned long long>(), ctx->mc_off.as<unsigned long long>(), ctx->nv,
+                             ctx->tmp.as<unsigned long long>());
+    if (st != PMS_OK) return st;
+    k_mc_totals<<<1, 1, 0, ctx->stream>>>(ctx->tmp.as<unsigned long long>(), cnt);
+    PMS_LAUNCHED(ctx);
+    k_mc_compact<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(cnt, ctx->mc_key.as<unsigned long long>(),
+                                                                  ctx->mc_off.as<unsigned long long>(), ctx->valid.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_mc_emit(pms_ctx* ctx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ctx->prm.iso_value, cnt, ctx->valid.as<uint32_t>(), ctx->vlist.as<uint32_t>(), ctx->mc_case.as<uint32_t>(),
+        ctx->mc_off.as<unsigned long long>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(),
+        ctx->vert.as<float>(), ctx->vnorm.as<float>());
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+}  // namespace pms

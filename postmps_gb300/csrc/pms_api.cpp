@@ -1,0 +1,563 @@
+// pms_api.cpp -- the C ABI of libpms: context lifetime, frame upload, stage
+// orchestration, result download.  Mirrors the reference's host class chain
+// (GPUPOST.cpp:20-96, NeighborSearch.cu:37-76, Anisotropic.cu:30-254,
+// MarchingCube.cu:32-197, GPUmemory.cpp) with these differences:
+//   * device buffers are grow-only and reused across frames instead of
+//     cudaMalloc/cudaFree per stage;
+//   * counts stay on the device; the host reads them only where it must size
+//     the next buffers (grid, band, mesh) or return results;
+//   * every failure is a returned pms_status with a message, never an abort.
+#include "pms_internal.h"
+
+#include <cstdarg>
+#include <algorithm>
+
+using namespace pms;
+
+pms_status pms_fail(pms_ctx* ctx, pms_status s, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->last_error = buf;
+    return s;
+}
+
+extern "C" const char* pms_status_string(pms_status s) {
+    switch (s) {
+        case PMS_OK: return "ok";
+        case PMS_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case PMS_ERR_CUDA: return "CUDA error";
+        case PMS_ERR_OUT_OF_MEMORY: return "out of memory";
+        case PMS_ERR_CAPACITY: return "capacity exceeded";
+        case PMS_ERR_IO: return "I/O error";
+        case PMS_ERR_CONFIG: return "configuration error";
+        case PMS_ERR_STATE: return "stage called out of order";
+        case PMS_ERR_TIMEOUT: return "device wait timed out";
+        case PMS_ERR_UNSUPPORTED: return "unsupported input";
+    }
+    return "unknown status";
+}
+
+extern "C" const char* pms_last_error(const pms_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+extern "C" uint64_t pms_kernel_launches(const pms_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// lifetime
+// ---------------------------------------------------------------------------
+static void release_all(pms_ctx* c) {
+    DBuf* bufs[] = {&c->in_pos, &c->in_vel, &c->in_rho, &c->keys, &c->slot, &c->order, &c->skeys, &c->spos,
+                    &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
+                    &c->surf_start, &c->big_cells, &c->slist, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
+                    &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
+                    &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->d_isfree, &c->d_freescan,
+                    &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
+                    &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
+                    &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp};
+    for (DBuf* b : bufs) b->release();
+}
+
+extern "C" pms_status pms_create(const pms_config* cfg, int device, pms_ctx** out) {
+    if (!cfg || !out) return PMS_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    pms_ctx* c = new (std::nothrow) pms_ctx();
+    if (!c) return PMS_ERR_OUT_OF_MEMORY;
+    c->cfg = *cfg;
+    pms_status st = pms_params_derive(cfg, &c->prm);
+    if (st != PMS_OK) { delete c; return st; }
+    c->device = device >= 0 ? device : cfg->gpu_id;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { delete c; return PMS_ERR_CUDA; }
+    if (c->device >= ndev) { delete c; return PMS_ERR_INVALID_ARGUMENT; }
+    if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return PMS_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return PMS_ERR_CUDA; }
+    c->own_stream = true;
+    if (cudaMallocHost(&c->h_counters, sizeof(Counters)) != cudaSuccess) { cudaStreamDestroy(c->stream); delete c; return PMS_ERR_OUT_OF_MEMORY; }
+    memset(c->h_counters, 0, sizeof(Counters));
+    for (int i = 0; i <= kNumStages; ++i) cudaEventCreate(&c->ev[i]);
+    if (c->counters.ensure(sizeof(Counters)) != cudaSuccess || c->tmp.ensure(64) != cudaSuccess) {
+        pms_destroy(c);
+        return PMS_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemsetAsync(c->counters.p, 0, sizeof(Counters), c->stream);
+    st = upload_mc_tables(c);
+    if (st != PMS_OK) { pms_destroy(c); return st; }
+    *out = c;
+    return PMS_OK;
+}
+
+extern "C" void pms_destroy(pms_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release_all(c);
+    for (int i = 0; i <= kNumStages; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->h_counters) cudaFreeHost(c->h_counters);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" pms_status pms_set_stream(pms_ctx* c, void* s) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    cudaStream_t ns = (cudaStream_t)s;
+    if (!ns) {
+        if (!c->own_stream) {
+            if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return PMS_ERR_CUDA;
+            c->own_stream = true;
+        }
+        return PMS_OK;
+    }
+    if (c->own_stream && c->stream) { cudaStreamSynchronize(c->stream); cudaStreamDestroy(c->stream); }
+    c->stream = ns;
+    c->own_stream = false;
+    return PMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// capacity
+// ---------------------------------------------------------------------------
+static pms_status ensure_particles(pms_ctx* c, uint32_t n) {
+    const size_t N = n ? n : 1;
+    PMS_CUDA(c, c->in_pos.ensure(12 * N));
+    PMS_CUDA(c, c->in_vel.ensure(12 * N));
+    PMS_CUDA(c, c->in_rho.ensure(4 * N));
+    PMS_CUDA(c, c->keys.ensure(4 * N));
+    PMS_CUDA(c, c->slot.ensure(4 * N));
+    PMS_CUDA(c, c->order.ensure(4 * N));
+    PMS_CUDA(c, c->skeys.ensure(4 * N));
+    PMS_CUDA(c, c->spos.ensure(16 * N));
+    PMS_CUDA(c, c->svel.ensure(16 * N));
+    PMS_CUDA(c, c->rho.ensure(4 * N));
+    PMS_CUDA(c, c->slist.ensure(4 * N));
+    PMS_CUDA(c, c->aniso.ensure(48 * N));
+    PMS_CUDA(c, c->nrm4.ensure(16 * N));
+    PMS_CUDA(c, c->mean4.ensure(16 * N));
+    PMS_CUDA(c, c->gdebug.ensure(40 * N));
+    PMS_CUDA(c, c->nnb.ensure(4 * N));
+    PMS_CUDA(c, c->big_cells.ensure(4 * (N / 64 + 2)));
+    return PMS_OK;
+}
+
+static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) {
+    const size_t S = g.sp_size ? g.sp_size : 1;
+    PMS_CUDA(c, c->cell_count.ensure(4 * S));
+    PMS_CUDA(c, c->cell_start.ensure(4 * S));
+    PMS_CUDA(c, c->cell_info.ensure(8 * S));
+    PMS_CUDA(c, c->surf_count.ensure(4 * S));
+    PMS_CUDA(c, c->surf_start.ensure(4 * S));
+    const size_t W = ((uint64_t)g.sc_size + 31) / 32 + 1;
+    PMS_CUDA(c, c->bm0.ensure(4 * W));
+    PMS_CUDA(c, c->bm.ensure(4 * W));
+    PMS_CUDA(c, c->wcount.ensure(4 * W));
+    PMS_CUDA(c, c->wprefix.ensure(4 * W));
+    return PMS_OK;
+}
+
+static pms_status ensure_band(pms_ctx* c, uint32_t nv) {
+    const size_t V = nv ? nv : 1;
+    PMS_CUDA(c, c->vlist.ensure(4 * V));
+    PMS_CUDA(c, c->field.ensure(4 * V));
+    PMS_CUDA(c, c->mc_case.ensure(4 * V));
+    PMS_CUDA(c, c->mc_key.ensure(8 * V));
+    PMS_CUDA(c, c->mc_off.ensure(8 * V));
+    PMS_CUDA(c, c->valid.ensure(4 * V));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_reserve(pms_ctx* c, uint32_t max_particles, uint64_t max_scalar_vertices) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (max_particles) { pms_status st = ensure_particles(c, max_particles); if (st) return st; }
+    if (max_scalar_vertices) {
+        if (max_scalar_vertices >= (1ull << 32)) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "scalar grid above 2^32 vertices");
+        pms_grid g = {};
+        g.sc_size = (uint32_t)max_scalar_vertices;
+        g.sp_size = (uint32_t)std::min<uint64_t>(max_scalar_vertices, 0xffffffffu);
+        pms_status st = ensure_grid(c, g);
+        if (st) return st;
+    }
+    return PMS_OK;
+}
+
+namespace pms {
+pms_status sync_counters(pms_ctx* c) {
+    PMS_CUDA(c, cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+}  // namespace pms
+
+static pms_status check_device_errors(pms_ctx* c) {
+    const uint32_t e = c->h_counters->err;
+    if (e & kErrNonFinite) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "particle positions contain NaN or Inf");
+    if (e & kErrBigCell)
+        return pms_fail(c, PMS_ERR_UNSUPPORTED, "a spatial cell holds more than 4096 particles (particles nearly coincide)");
+    if (e & kErrKeyRange) return pms_fail(c, PMS_ERR_CUDA, "internal: a cell key fell outside the grid");
+    if (e & kErrCapacity) return pms_fail(c, PMS_ERR_CAPACITY, "internal: device capacity exceeded");
+    return PMS_OK;
+}
+
+// Stage timing: ev[0] opens a frame, ev[k + 1] closes stage k; a stage's time
+// runs from the most recent earlier event.
+static void mark(pms_ctx* c, int boundary) {
+    cudaEventRecord(c->ev[boundary], c->stream);
+    if (boundary == 0) {
+        c->last_event = 0;
+        for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
+        return;
+    }
+    c->ev_from[boundary - 1] = c->last_event;
+    c->ev_recorded[boundary - 1] = true;
+    c->last_event = boundary;
+}
+
+// ---------------------------------------------------------------------------
+// upload (FileData::loadFluidFile + GPUmemory::memAlcandCpy_fluid)
+// ---------------------------------------------------------------------------
+static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n,
+                                cudaMemcpyKind kind) {
+    if (!c || (n && !pos)) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    pms_status st = ensure_particles(c, n);
+    if (st) return st;
+    if (n) {
+        PMS_CUDA(c, cudaMemcpyAsync(c->in_pos.p, pos, 12 * (size_t)n, kind, c->stream));
+        if (vel) PMS_CUDA(c, cudaMemcpyAsync(c->in_vel.p, vel, 12 * (size_t)n, kind, c->stream));
+        else PMS_CUDA(c, cudaMemsetAsync(c->in_vel.p, 0, 12 * (size_t)n, c->stream));
+        if (rho) PMS_CUDA(c, cudaMemcpyAsync(c->in_rho.p, rho, 4 * (size_t)n, kind, c->stream));
+        else PMS_CUDA(c, cudaMemsetAsync(c->in_rho.p, 0, 4 * (size_t)n, c->stream));
+    }
+    c->n = n;
+    c->have_particles = true;
+    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = false;
+    c->ns = c->nv = c->nvalid = 0;
+    c->nmesh = 0;
+    for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_upload_particles(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n) {
+    return upload_common(c, pos, vel, rho, n, cudaMemcpyHostToDevice);
+}
+extern "C" pms_status pms_upload_particles_device(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n) {
+    return upload_common(c, pos, vel, rho, n, cudaMemcpyDeviceToDevice);
+}
+
+// ---------------------------------------------------------------------------
+// stages
+// ---------------------------------------------------------------------------
+static inline float decode_ordered(uint32_t u) {
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+extern "C" pms_status pms_build_grid(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_particles) return pms_fail(c, PMS_ERR_STATE, "pms_build_grid before pms_upload_particles");
+    cudaSetDevice(c->device);
+    mark(c, kStageGrid);
+    pms_status st = launch_bbox(c);
+    if (st) return st;
+    if ((st = sync_counters(c))) return st;
+    if ((st = check_device_errors(c))) return st;
+    if (c->n == 0) {
+        memset(&c->grid, 0, sizeof(c->grid));
+        c->have_grid = true;
+        mark(c, kStageGrid + 1);
+        return PMS_OK;
+    }
+    float bmin[3], bmax[3];
+    for (int k = 0; k < 3; ++k) { bmin[k] = decode_ordered(c->h_counters->bbox_min[k]); bmax[k] = decode_ordered(c->h_counters->bbox_max[k]); }
+    if ((st = pms_grid_from_bbox(&c->prm, bmin, bmax, &c->grid))) return pms_fail(c, st, "grid: domain too large for 32-bit cell indices");
+    if ((st = ensure_grid(c, c->grid))) return st;
+    if ((st = launch_hash_sort(c))) return st;
+    c->have_grid = true;
+    mark(c, kStageGrid + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_anisotropy(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_grid) return pms_fail(c, PMS_ERR_STATE, "pms_anisotropy before pms_build_grid");
+    cudaSetDevice(c->device);
+    if (c->n == 0) { c->have_aniso = true; return PMS_OK; }
+    pms_status st;
+    if ((st = launch_surface_cells(c))) return st;
+    if ((st = launch_density_aniso(c))) return st;
+    c->have_aniso = true;
+    mark(c, kStageAniso + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_band(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
+    cudaSetDevice(c->device);
+    if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
+    pms_status st;
+    if ((st = launch_band(c))) return st;
+    if ((st = sync_counters(c))) return st;
+    if ((st = check_device_errors(c))) return st;
+    c->ns = c->h_counters->ns;
+    c->nv = c->h_counters->nv;
+    if ((st = ensure_band(c, c->nv))) return st;
+    if ((st = launch_band_list(c))) return st;
+    c->have_band = true;
+    mark(c, kStageBand + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_field(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_band) return pms_fail(c, PMS_ERR_STATE, "pms_field before pms_band");
+    cudaSetDevice(c->device);
+    if (c->nv) { pms_status st = launch_field(c); if (st) return st; }
+    c->have_field = true;
+    mark(c, kStageField + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_field) return pms_fail(c, PMS_ERR_STATE, "pms_marching_cubes before pms_field");
+    cudaSetDevice(c->device);
+    c->nvalid = 0;
+    c->nmesh = 0;
+    if (c->nv) {
+        pms_status st;
+        if ((st = launch_mc_classify(c))) return st;
+        if ((st = sync_counters(c))) return st;
+        c->nvalid = c->h_counters->nvalid;
+        c->nmesh = c->h_counters->nmesh;
+        const size_t M = c->nmesh ? c->nmesh : 1;
+        PMS_CUDA(c, c->vert.ensure(12 * M));
+        PMS_CUDA(c, c->vnorm.ensure(12 * M));
+        if ((st = launch_mc_emit(c))) return st;
+    }
+    c->have_mc = true;
+    mark(c, kStageMc + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_surface(pms_ctx* c) {
+    pms_status st;
+    if ((st = pms_anisotropy(c))) return st;
+    if ((st = pms_band(c))) return st;
+    if ((st = pms_field(c))) return st;
+    return pms_marching_cubes(c);
+}
+
+extern "C" pms_status pms_diffuse(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_grid) return pms_fail(c, PMS_ERR_STATE, "pms_diffuse before pms_build_grid");
+    cudaSetDevice(c->device);
+    pms_status st = launch_diffuse(c);
+    if (st) return st;
+    c->have_diffuse = true;
+    mark(c, kStageDiffuse + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_run_frame(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    pms_status st;
+    if ((st = pms_build_grid(c))) return st;
+    if (c->cfg.is_surface && (st = pms_surface(c))) return st;
+    if (c->cfg.is_diffuse && (st = pms_diffuse(c))) return st;
+    c->frame_index++;
+    return PMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// results
+// ---------------------------------------------------------------------------
+extern "C" pms_status pms_get_counts(pms_ctx* c, pms_counts* out) {
+    if (!c || !out) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    pms_status st = sync_counters(c);
+    if (st) return st;
+    const Counters& h = *c->h_counters;
+    memset(out, 0, sizeof(*out));
+    out->n_particles = c->n;
+    out->n_surface_particles = c->have_aniso ? h.ns : 0;
+    out->n_band_vertices = c->have_band ? h.nv : 0;
+    out->n_valid_cubes = c->have_mc ? h.nvalid : 0;
+    out->n_mesh_vertices = c->have_mc ? h.nmesh : 0;
+    out->n_fp64_svd = h.n_fp64;
+    out->n_free_surface = h.n_free;
+    out->n_generated_diffuse = h.n_generated;
+    out->n_spawning = h.n_spawning;
+    out->n_diffuse = c->diffuse_old;
+    out->n_spray = h.n_type[0];
+    out->n_foam = h.n_type[1];
+    out->n_bubble = h.n_type[2];
+    return check_device_errors(c);
+}
+
+extern "C" pms_status pms_get_grid(pms_ctx* c, pms_grid* out) {
+    if (!c || !out) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_grid) return pms_fail(c, PMS_ERR_STATE, "no grid yet");
+    *out = c->grid;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_download_mesh(pms_ctx* c, float* pos, float* nrm, uint64_t cap, uint64_t* n_out) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_mc) return pms_fail(c, PMS_ERR_STATE, "no mesh yet");
+    cudaSetDevice(c->device);
+    if (n_out) *n_out = c->nmesh;
+    if (c->nmesh == 0) return PMS_OK;
+    if (cap < c->nmesh || !pos) return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices", (unsigned long long)c->nmesh);
+    PMS_CUDA(c, cudaMemcpyAsync(pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
+    if (nrm) PMS_CUDA(c, cudaMemcpyAsync(nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_stage_times(pms_ctx* c, float* ms, int count) {
+    if (!c || !ms) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < count && i < kNumStages; ++i) {
+        ms[i] = 0.f;
+        if (!c->ev_recorded[i]) continue;
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, c->ev[c->ev_from[i]], c->ev[i + 1]) == cudaSuccess) ms[i] = t;
+    }
+    return PMS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// debug downloads
+// ---------------------------------------------------------------------------
+template <class T>
+static pms_status d2h(pms_ctx* c, std::vector<T>& v, const void* src, size_t count) {
+    v.resize(count);
+    if (count) PMS_CUDA(c, cudaMemcpyAsync(v.data(), src, sizeof(T) * count, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_debug_download(pms_ctx* c, int id, void* dst, uint64_t cap, uint64_t* needed) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    pms_status st = sync_counters(c);
+    if (st) return st;
+    const uint32_t n = c->n, ns = c->h_counters->ns, nv = c->h_counters->nv, S = c->grid.sp_size;
+    std::vector<uint8_t> out;
+    auto put = [&](const void* p, size_t bytes) { out.resize(bytes); if (bytes) memcpy(out.data(), p, bytes); };
+    switch (id) {
+        case PMS_ARRAY_KEYS_SORTED: case PMS_ARRAY_PERM: case PMS_ARRAY_DENSITY: {
+            if (!c->have_grid) return PMS_ERR_STATE;
+            if (id == PMS_ARRAY_DENSITY && !c->have_aniso) return PMS_ERR_STATE;
+            const DBuf& b = id == PMS_ARRAY_KEYS_SORTED ? c->skeys : id == PMS_ARRAY_PERM ? c->order : c->rho;
+            std::vector<uint32_t> v;
+            if ((st = d2h(c, v, b.p, n))) return st;
+            put(v.data(), 4 * (size_t)n);
+            break;
+        }
+        case PMS_ARRAY_POS_SORTED: {
+            if (!c->have_grid) return PMS_ERR_STATE;
+            std::vector<float> v;
+            if ((st = d2h(c, v, c->spos.p, 4 * (size_t)n))) return st;
+            std::vector<float> o(3 * (size_t)n);
+            for (size_t i = 0; i < n; ++i) for (int k = 0; k < 3; ++k) o[3 * i + k] = v[4 * i + k];
+            put(o.data(), 4 * o.size());
+            break;
+        }
+        case PMS_ARRAY_CELL_START: case PMS_ARRAY_CELL_END: {
+            if (!c->have_grid) return PMS_ERR_STATE;
+            std::vector<uint32_t> s, m;
+            if ((st = d2h(c, s, c->cell_start.p, S))) return st;
+            if ((st = d2h(c, m, c->cell_count.p, S))) return st;
+            std::vector<uint32_t> o(S);
+            for (size_t i = 0; i < S; ++i) o[i] = m[i] ? (id == PMS_ARRAY_CELL_START ? s[i] : s[i] + m[i]) : 0u;
+            put(o.data(), 4 * o.size());
+            break;
+        }
+        case PMS_ARRAY_SURF_COUNT: {
+            if (!c->have_aniso) return PMS_ERR_STATE;
+            std::vector<uint32_t> v;
+            if ((st = d2h(c, v, c->surf_count.p, S))) return st;
+            put(v.data(), 4 * v.size());
+            break;
+        }
+        case PMS_ARRAY_SURF_LIST: case PMS_ARRAY_NEIGHBORS: {
+            if (!c->have_aniso) return PMS_ERR_STATE;
+            std::vector<uint32_t> v;
+            if ((st = d2h(c, v, id == PMS_ARRAY_SURF_LIST ? c->slist.p : c->nnb.p, ns))) return st;
+            put(v.data(), 4 * v.size());
+            break;
+        }
+        case PMS_ARRAY_MEAN: {
+            if (!c->have_aniso) return PMS_ERR_STATE;
+            std::vector<float> v;
+            if ((st = d2h(c, v, c->mean4.p, 4 * (size_t)ns))) return st;
+            std::vector<float> o(3 * (size_t)ns);
+            for (size_t i = 0; i < ns; ++i) for (int k = 0; k < 3; ++k) o[3 * i + k] = v[4 * i + k];
+            put(o.data(), 4 * o.size());
+            break;
+        }
+        case PMS_ARRAY_G: {
+            if (!c->have_aniso) return PMS_ERR_STATE;
+            std::vector<float> v;
+            if ((st = d2h(c, v, c->gdebug.p, 10 * (size_t)ns))) return st;
+            put(v.data(), 4 * v.size());
+            break;
+        }
+        case PMS_ARRAY_NORMAL: case PMS_ARRAY_FLAG: {
+            if (!c->have_aniso) return PMS_ERR_STATE;
+            std::vector<uint32_t> sl;
+            std::vector<float> nr;
+            if ((st = d2h(c, sl, c->slist.p, ns))) return st;
+            if ((st = d2h(c, nr, c->nrm4.p, 4 * (size_t)n))) return st;
+            if (id == PMS_ARRAY_NORMAL) {
+                std::vector<float> o(3 * (size_t)ns);
+                for (size_t s = 0; s < ns; ++s) for (int k = 0; k < 3; ++k) o[3 * s + k] = nr[4 * (size_t)sl[s] + k];
+                put(o.data(), 4 * o.size());
+            } else {
+                std::vector<uint8_t> o(ns);
+                for (size_t s = 0; s < ns; ++s) o[s] = nr[4 * (size_t)sl[s] + 3] != 0.f;
+                put(o.data(), o.size());
+            }
+            break;
+        }
+        case PMS_ARRAY_BAND_BITMAP: {
+            if (!c->have_band) return PMS_ERR_STATE;
+            std::vector<uint32_t> v;
+            if ((st = d2h(c, v, c->bm.p, ((uint64_t)c->grid.sc_size + 31) / 32))) return st;
+            put(v.data(), 4 * v.size());
+            break;
+        }
+        case PMS_ARRAY_BAND_LIST: case PMS_ARRAY_FIELD: case PMS_ARRAY_CUBE_CASE: {
+            const bool ok = id == PMS_ARRAY_BAND_LIST ? c->have_band : id == PMS_ARRAY_FIELD ? c->have_field : c->have_mc;
+            if (!ok) return PMS_ERR_STATE;
+            const DBuf& b = id == PMS_ARRAY_BAND_LIST ? c->vlist : id == PMS_ARRAY_FIELD ? c->field : c->mc_case;
+            std::vector<uint32_t> v;
+            if ((st = d2h(c, v, b.p, nv))) return st;
+            put(v.data(), 4 * v.size());
+            break;
+        }
+        case PMS_ARRAY_CUBE_NVERT: {
+            if (!c->have_mc) return PMS_ERR_STATE;
+            std::vector<unsigned long long> v;
+            if ((st = d2h(c, v, c->mc_key.p, nv))) return st;
+            std::vector<uint32_t> o(nv);
+            for (size_t i = 0; i < nv; ++i) o[i] = (uint32_t)(v[i] & 0xffffffffull);
+            put(o.data(), 4 * o.size());
+            break;
+        }
+        default: {
+            st = diffuse_debug(c, id, out);
+            if (st) return st;
+        }
+    }
+    if (needed) *needed = out.size();
+    if (!dst || cap < out.size()) return dst ? PMS_ERR_CAPACITY : PMS_OK;
+    if (!out.empty()) memcpy(dst, out.data(), out.size());
+    return PMS_OK;
+}

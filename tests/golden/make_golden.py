@@ -1,0 +1,103 @@
+"""Generates the golden fixtures in tests/golden/ from the reference itself.
+
+The reference ships no tests or fixtures, so the fixtures are produced by
+running the reference's own kernels (NeighborSearch_kernel.cuh,
+Anisotropic_kernel.cuh, MarchingCube_kernel.cuh, SVD3.cuh, myCuda.cuh) and its
+Params.cpp, compiled unmodified for the CPU by ``make -C oracle ref`` (see
+oracle/ref_emu/).  Needs the reference tree (default /root/reference, or
+$PMS_REFERENCE_DIR); the committed .npz files are what the tests read.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from postmps_gb300 import synth  # noqa: E402
+
+
+def drops_and_sheet():
+    """A 12^3 block, a thin two-layer sheet above it (flat covariances:
+    thin-feature flag) and isolated droplets (fewer than MinNumNeighbors
+    neighbours: isotropic kernel)."""
+    pos, vel, rho = synth.water_block(12)
+    sheet = synth.lattice(14, 14, 2, 0.01, 0.001, seed=11, origin=(-0.01, -0.01, 0.16))
+    drops = synth.lattice(3, 3, 1, 0.05, 0.004, seed=12, origin=(0.0, 0.0, 0.24))
+    tiny = synth.lattice(2, 2, 2, 0.009, 0.0005, seed=13, origin=(0.2, 0.2, 0.05))
+    p = np.concatenate([pos, sheet, drops, tiny]).astype(np.float32)
+    v = (synth.uniform(14, 0, 3 * len(p)).reshape(-1, 3) - 0.5).astype(np.float32)
+    return p, v, np.full(len(p), 1000.0, np.float32)
+
+
+CASES = {
+    # name: (particles, config overrides)
+    "block10": (lambda: synth.water_block(10), {}),
+    "block16": (lambda: synth.water_block(16), {}),
+    "drops_sheet": (drops_and_sheet, {}),
+    "block12_ratio4": (lambda: synth.water_block(12), {"surface.smoothingradiusratio": 4}),
+    "block12_iso03_scale3": (lambda: synth.water_block(12),
+                             {"surface.isovalue": 0.3, "domain.sclargridsizescale": 3}),
+}
+
+
+def tables_digest() -> str:
+    e, t, nv, ev = O.ref_mc_tables()
+    h = hashlib.sha256()
+    for a in (e, t, nv, ev):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make(name: str) -> str:
+    gen, over = CASES[name]
+    pos, vel, rho = gen()
+    text = synth.config_text(**over)
+    with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+        f.write(text)
+        cfg_path = f.name
+    try:
+        R = O.ref_surface_run(cfg_path, pos, vel, rho)
+    finally:
+        os.unlink(cfg_path)
+    assert R["rc"] == 0, (name, R["rc"])
+    sl = R["surf_list"]
+    out = dict(
+        config=np.array(text), pos=pos, vel=vel, rho_in=rho,
+        min_pos=R["min_pos"], max_pos=R["max_pos"], scmin_pos=R["scmin_pos"], scmax_pos=R["scmax_pos"],
+        spres=R["spres"], scres=R["scres"], h=np.float32(R["h"]), h_inv=np.float32(R["h_inv"]),
+        iso=np.float32(R["iso"]), keys_sorted=R["keys_sorted"], perm=R["perm"], cell_start=R["cell_start"],
+        cell_end=R["cell_end"], surf_count=R["surf_count"], surf_list=sl, rho=R["rho"], mean=R["mean"], G=R["G"],
+        nrm=R["nrm"][sl], flag=(R["flag"][sl] != 0).astype(np.uint8), band_list=R["band_list"], field=R["field"],
+        cube_flag=R["cube_flag"], nvert=R["nvert"], vpos=R["vpos"], vnrm=R["vnrm"],
+        n_surface=np.uint32(R["n_surface"]), n_band=np.uint32(R["n_band"]), n_valid=np.uint32(R["n_valid"]),
+        n_mesh=np.uint32(R["n_mesh"]), mc_tables_sha256=np.array(tables_digest()),
+    )
+    path = os.path.join(HERE, f"surface_{name}.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
+def main() -> int:
+    O.build()
+    if not O.ref_available():
+        print("reference tree not found: cannot generate fixtures", file=sys.stderr)
+        return 1
+    for name in CASES:
+        p = make(name)
+        print(f"{p}: {os.path.getsize(p) / 1024:.0f} KiB")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

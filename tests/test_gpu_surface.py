@@ -1,0 +1,185 @@
+"""GPU parity of the surface path (libpms through its C ABI) against the
+golden fixtures made by the reference's own kernels and against the CPU
+oracle.
+
+Bit-exact (integer stages):
+  cell keys, sort permutation, cell ranges, surface cells and list -- against
+  the reference fixtures and the oracle;
+  band vertices -- against the oracle's band test run on the GPU's normals
+  and flags (the test's float32 arithmetic is mirrored operation by operation);
+  marching-cubes cases, vertex counts and mesh size -- against the oracle's
+  classification of the GPU's field.
+Float stages against the float64 oracle:
+  density           relative 1e-5
+  G                 relative 1e-4 of its largest entry
+  scalar field      relative 1e-5 of max(|f|, iso) (vertices below the
+                    early-exit threshold 2*iso; above it both must exceed it)
+  mesh vertices     within 1e-4 cell sizes of the oracle's float64 emit from
+                    the GPU field
+Against the reference's float32 results (whose SVD is less accurate):
+  triangle count within 1 %, mesh Hausdorff distance <= 0.05 h.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(pms, cfg_path, pos, vel=None, rho=None):
+    cfg = pms.load_config(cfg_path)
+    with pms.Context(cfg, 0) as ctx:
+        ctx.upload(pos, vel, rho)
+        ctx.build_grid()
+        ctx.anisotropy()
+        ctx.band()
+        ctx.field()
+        ctx.marching_cubes()
+        out = {k: ctx.debug(k) for k in ("keys_sorted", "perm", "cell_start", "cell_end", "surf_count", "surf_list",
+                                          "density", "mean", "G", "normal", "flag", "neighbors", "band_bitmap",
+                                          "band_list", "field", "cube_case", "cube_nvert")}
+        out["vpos"], out["vnrm"] = ctx.mesh()
+        out["counts"] = ctx.counts().as_dict()
+        out["launches"] = ctx.launches
+        g = ctx.grid()
+        out["grid"] = g
+    return out
+
+
+def oracle_setup(oracle, cfg_text, pos):
+    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(cfg_text)))
+    g = oracle.grid_from_positions(p, pos)
+    return p, g
+
+
+def check_against_oracle(oracle, pms, cfg_text, pos, G_out, field_tol=1e-5):
+    p, g = oracle_setup(oracle, cfg_text, pos)
+    r = oracle.run_surface(p, pos, g)
+    # hashing and surface particles: exact
+    np.testing.assert_array_equal(G_out["keys_sorted"], r.keys_sorted)
+    np.testing.assert_array_equal(G_out["perm"], r.perm)
+    np.testing.assert_array_equal(G_out["cell_start"], r.cell_start)
+    np.testing.assert_array_equal(G_out["cell_end"], r.cell_end)
+    np.testing.assert_array_equal(G_out["surf_count"], r.surf_count)
+    np.testing.assert_array_equal(G_out["surf_list"], r.surf_list)
+    # density
+    assert float((np.abs(G_out["density"] - r.rho) / r.rho).max()) < 1e-5
+    # anisotropy
+    Gg = G_out["G"][:, :9].astype(np.float64)
+    scale = np.abs(r.G).max(axis=1, keepdims=True)
+    assert float((np.abs(Gg - r.G) / scale).max()) < 1e-4
+    assert float(np.abs(G_out["G"][:, 9] - r.maxv).max()) < 1e-4
+    assert np.mean(G_out["flag"] == r.flag) > 0.995
+    assert np.mean(G_out["neighbors"] == r.nnb) > 0.999
+    # band: exact given the GPU's float32 normals and flags
+    sp = np.ascontiguousarray(pos[r.perm])
+    bm, band = oracle.band_bitmap(g, p.h, sp, r.surf_list, G_out["normal"], G_out["flag"])
+    np.testing.assert_array_equal(G_out["band_list"], band)
+    np.testing.assert_array_equal(G_out["band_bitmap"], bm[: len(G_out["band_bitmap"])])
+    # field against float64 at the GPU's band (float64 G, float64 density)
+    import ctypes as C
+    fld = np.zeros(len(band))
+    if len(band):
+        oracle.lib().orc_field(C.byref(p), C.byref(g), np.ascontiguousarray(sp.reshape(-1)), len(pos), r.rho,
+                               r.cell_start, r.cell_end, r.surf_count, r.surf_scan,
+                               np.ascontiguousarray(r.G.reshape(-1)), np.ascontiguousarray(r.maxv), band, len(band), fld)
+    thr = 2 * p.iso_value
+    f32 = G_out["field"].astype(np.float64)
+    below = (fld < thr * 0.999) & (f32 < thr * 0.999)
+    err = np.abs(f32 - fld) / np.maximum(np.abs(fld), p.iso_value)
+    assert float(err[below].max(initial=0.0)) < field_tol, float(err[below].max(initial=0.0))
+    above = ~((fld < thr * 1.001) & (f32 < thr * 1.001))
+    assert np.all((fld[above] > thr * 0.99) & (f32[above] > thr * 0.99))
+    # marching cubes: exact classification of the GPU's field
+    e, t, nv, ev, _ = pms.mc_tables()
+    oracle.set_mc_tables(e, t, nv, ev)
+    cases, nvert, total = oracle.mc_classify(g, p.iso_value, bm, band, G_out["field"])
+    np.testing.assert_array_equal(G_out["cube_case"], cases)
+    np.testing.assert_array_equal(G_out["cube_nvert"], nvert)
+    assert total == len(G_out["vpos"]) == G_out["counts"]["n_mesh_vertices"]
+    vpos, vnrm = oracle.mc_emit(g, p.iso_value, bm, band, f32, cases, nvert)
+    if total:
+        assert float(np.abs(vpos - G_out["vpos"]).max()) < 1e-4 * g.sc_grid_size
+        ok = np.isfinite(vnrm).all(axis=1)
+        assert float(np.abs(vnrm[ok] - G_out["vnrm"][ok]).max()) < 1e-3
+    return p, g, r
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_surface_matches_reference_fixtures(pms_lib, oracle, tmp_config, case):
+    d = load_golden(case)
+    out = run_gpu(pms_lib, tmp_config(d["config"]), d["pos"], d["vel"], d["rho_in"])
+    for k in ("keys_sorted", "perm", "cell_start", "cell_end", "surf_count", "surf_list"):
+        np.testing.assert_array_equal(out[k], d[k], err_msg=k)
+    assert out["counts"]["n_surface_particles"] == int(d["n_surface"])
+    assert float((np.abs(out["density"] - d["rho"]) / d["rho"]).max()) < 1e-5
+    # against the reference's mesh: its float32 SVD differs from the exact G
+    n_ref, n_gpu = int(d["n_mesh"]), len(out["vpos"])
+    assert abs(n_gpu - n_ref) <= max(3, 0.01 * n_ref)
+    if n_ref and n_gpu:
+        p, g = oracle_setup(oracle, d["config"], d["pos"])
+        h1 = oracle.lib().orc_hausdorff_vertices_to_mesh(out["vpos"].astype(np.float64).reshape(-1), n_gpu,
+                                                         d["vpos"].astype(np.float64).reshape(-1), n_ref, p.h)
+        h2 = oracle.lib().orc_hausdorff_vertices_to_mesh(d["vpos"].astype(np.float64).reshape(-1), n_ref,
+                                                         out["vpos"].astype(np.float64).reshape(-1), n_gpu, p.h)
+        assert max(h1, h2) <= 0.05 * p.h
+    assert out["launches"] > 0
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_surface_matches_oracle(pms_lib, oracle, tmp_config, case):
+    d = load_golden(case)
+    out = run_gpu(pms_lib, tmp_config(d["config"]), d["pos"], d["vel"], d["rho_in"])
+    check_against_oracle(oracle, pms_lib, d["config"], d["pos"], out)
+
+
+def test_water_block_64_full_size(pms_lib, oracle, tmp_config):
+    """The 262,144-particle plain case at full size against the oracle."""
+    from postmps_gb300 import synth
+    pos, vel, rho = synth.water_block(64)
+    text = synth.config_text()
+    out = run_gpu(pms_lib, tmp_config(text), pos, vel, rho)
+    check_against_oracle(oracle, pms_lib, text, pos, out)
+    c = out["counts"]
+    assert c["n_particles"] == 262144 and c["n_mesh_vertices"] > 0 and c["n_mesh_vertices"] % 3 == 0
+
+
+def test_empty_and_single_particle(pms_lib, tmp_config):
+    from postmps_gb300 import synth
+    path = tmp_config(synth.config_text())
+    cfg = pms_lib.load_config(path)
+    with pms_lib.Context(cfg, 0) as ctx:
+        ctx.upload(np.zeros((0, 3), np.float32))
+        ctx.run_frame()
+        assert ctx.counts().n_mesh_vertices == 0
+        assert len(ctx.mesh()[0]) == 0
+        # one particle: isotropic kernel, a small closed blob
+        ctx.upload(np.array([[0.1, 0.2, 0.3]], np.float32))
+        ctx.run_frame()
+        c = ctx.counts()
+        assert c.n_surface_particles == 1
+        assert c.n_mesh_vertices % 3 == 0
+
+
+def test_nonfinite_positions_rejected(pms_lib, tmp_config):
+    from postmps_gb300 import synth
+    cfg = pms_lib.load_config(tmp_config(synth.config_text()))
+    pos = np.zeros((10, 3), np.float32)
+    pos[3, 1] = np.nan
+    with pms_lib.Context(cfg, 0) as ctx:
+        ctx.upload(pos)
+        with pytest.raises(pms_lib.PmsError) as ei:
+            ctx.build_grid()
+        assert ei.value.status == 1
+
+
+def test_stage_order_enforced(pms_lib, tmp_config):
+    from postmps_gb300 import synth
+    cfg = pms_lib.load_config(tmp_config(synth.config_text()))
+    with pms_lib.Context(cfg, 0) as ctx:
+        with pytest.raises(pms_lib.PmsError) as ei:
+            ctx.field()
+        assert ei.value.status == 7
