@@ -309,7 +309,7 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     k_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
         g, ap, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->rho.as<float>(), ctx->n);
     PMS_LAUNCHED(ctx);
-    k_inv_density<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(), P.mass, ctx->n);
+    k_inv_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(), P.mass, ctx->n);
     PMS_LAUNCHED(ctx);
     // ns is on the device; size the grid by the particle count (upper bound)
     k_aniso<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
