@@ -76,7 +76,8 @@ def algorithmic_bytes(c: dict, g, diffuse: bool) -> dict:
     band = 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
     field = 16 * N + 44 * Ns + 8 * Vs
     mc = (4 * Vs + Ssc / 8 + 9 * Vs) + (12 * 8 * Cv + 24 * M)
-    return {"grid": grid, "anisotropy": aniso, "band": band, "field": field, "marching_cubes": mc}
+    dif = (64 * N + 44 * (c["n_generated_diffuse"] + c["n_diffuse"])) if diffuse else 0
+    return {"grid": grid, "anisotropy": aniso, "band": band, "field": field, "marching_cubes": mc, "diffuse": dif}
 
 
 # ---------------------------------------------------------------------------
@@ -190,7 +191,7 @@ def run_pms(args) -> None:
     cfg = pms.load_config(cfg_path)
     os.unlink(cfg_path)
     cfg.is_surface = 1
-    cfg.is_diffuse = 0
+    cfg.is_diffuse = 0 if args.no_diffuse else 1
     stream = torch.cuda.current_stream()
     ctx = pms.Context(cfg, local)
     ctx.set_stream(stream.cuda_stream)
@@ -213,6 +214,8 @@ def run_pms(args) -> None:
         ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
         ctx.run_frame()
         mesh_host[0] = ctx.mesh(normals=False)[0]
+        if cfg.is_diffuse:
+            mesh_host.append(ctx.diffuse_particles(-1))
 
     for _ in range(args.warmup):
         step_device()
@@ -256,7 +259,7 @@ def run_pms(args) -> None:
     value = world * n / (ms / 1e3)
     e2e_value = world * n / (ms_e2e / 1e3)
     stage_ms = {k: v / args.steps for k, v in stage_sum.items()}
-    alg = algorithmic_bytes(counts, grid, diffuse=False)
+    alg = algorithmic_bytes(counts, grid, diffuse=bool(cfg.is_diffuse))
     dom = max(alg, key=lambda k: stage_ms.get(k, 0.0))
     peaks = {}
     try:
@@ -276,10 +279,11 @@ def run_pms(args) -> None:
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": dict(desc, path="plain surface (diffuse off)", band="plain", l2="flushed (256 MiB write) between steps",
+        "config": dict(desc, path="surface + diffuse" if cfg.is_diffuse else "surface (diffuse off)", band="plain",
+                       l2="flushed (256 MiB write) between steps",
                        parallelism=f"replicas x{world}"),
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": ms_e2e, "h2d_bytes_per_step": 28 * n,
-                "d2h_bytes_per_step": 12 * m_vertices},
+                "d2h_bytes_per_step": 12 * m_vertices + 32 * int(counts["n_diffuse"])},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "algorithmic_bytes": alg[dom], "peak_source": peak_src},
@@ -306,6 +310,7 @@ def main() -> None:
     ap.add_argument("--workload", default="crown", choices=["crown", "block"])
     ap.add_argument("--cpu-fraction", type=float, default=0.25)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-diffuse", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

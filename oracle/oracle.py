@@ -119,6 +119,17 @@ def lib():
                                   _u64p, _f64p, _f64p]
         L.orc_hausdorff_vertices_to_mesh.argtypes = [_f64p, C.c_uint64, _f64p, C.c_uint64, C.c_double]
         L.orc_hausdorff_vertices_to_mesh.restype = C.c_double
+        P, G = C.POINTER(Params), C.POINTER(Grid)
+        L.orc_spawn_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64]
+        L.orc_spawn_uniform.restype = C.c_float
+        L.orc_df_normals.argtypes = [P, G, _f32p, C.c_uint32, _u32p, _u32p, C.c_uint32, _f64p]
+        L.orc_df_trapped.argtypes = [P, G, _f32p, _f32p, C.c_uint32, _u32p, _u32p, _f64p, _f64p]
+        L.orc_df_crests.argtypes = [P, G, _f32p, _f32p, _u32p, _u32p, _u32p, C.c_uint32, _f32p, _f64p]
+        L.orc_df_counts.argtypes = [P, _f32p, C.c_uint32, _f32p, _i32p]
+        L.orc_df_counts_from_clamped.argtypes = [P, _f32p, C.c_uint32, _i32p]
+        L.orc_df_spawn.argtypes = [P, G, _f32p, _f32p, C.c_uint32, _u32p, _u32p, _i32p, C.c_uint64, C.c_uint32, _f32p]
+        L.orc_df_spawn.restype = C.c_uint64
+        L.orc_df_update.argtypes = [P, G, _f32p, _f32p, _u32p, _u32p, _f32p, C.c_uint32]
         _lib = L
     return _lib
 
@@ -429,3 +440,95 @@ def ref_mc_tables():
     R.ref_mc_tables.argtypes = [_u32p, _i32p, _u32p, _u32p]
     R.ref_mc_tables(e, t, nv, ev)
     return e, t.reshape(256, 16), nv, ev.reshape(12, 2)
+
+
+# --------------------------------------------------------------------------
+# diffuse particles
+# --------------------------------------------------------------------------
+def spawn_uniforms(seed: int, frame: int, count: int) -> np.ndarray:
+    L = lib()
+    return np.array([L.orc_spawn_uniform(seed, frame, k) for k in range(count)], np.float32)
+
+
+def diffuse_frame(p: Params, g: Grid, spos, svel, start, end, free_list, nrm_init, seed: int, frame: int,
+                  old=None, nrm_for_crests=None, pot_clamped=None):
+    """Float64 oracle of one diffuse frame on sorted particles.  Returns a dict
+    with normals, raw and clamped potentials, counts, generated particles (8
+    floats each: pos, vel, ttl, type), the advected old particles and the live
+    list (generated then old, type 3 dropped).  `nrm_for_crests` (float32)
+    replaces the oracle's own normals in the wave-crest sum; `pot_clamped`
+    replaces its clamped potentials when deriving the counts."""
+    L = lib()
+    spos = np.ascontiguousarray(spos, np.float32).reshape(-1)
+    svel = np.ascontiguousarray(svel, np.float32).reshape(-1)
+    n = spos.size // 3
+    nrm = np.ascontiguousarray(nrm_init, np.float64).reshape(-1).copy()
+    L.orc_df_normals(C.byref(p), C.byref(g), spos, n, start, end, len(free_list), nrm)
+    ita = np.zeros(n); en = np.zeros(n); wc = np.zeros(n)
+    L.orc_df_trapped(C.byref(p), C.byref(g), spos, svel, n, start, end, ita, en)
+    nc = np.ascontiguousarray(nrm.astype(np.float32) if nrm_for_crests is None else nrm_for_crests, np.float32).reshape(-1)
+    L.orc_df_crests(C.byref(p), C.byref(g), spos, svel, start, end, np.ascontiguousarray(free_list, np.uint32),
+                    len(free_list), nc, wc)
+    raw = np.ascontiguousarray(np.stack([wc, ita, en], 1).astype(np.float32).reshape(-1))
+    clamped = np.zeros_like(raw)
+    num = np.zeros(n, np.int32)
+    L.orc_df_counts(C.byref(p), raw, n, clamped, num)
+    if pot_clamped is not None:
+        num = np.zeros(n, np.int32)
+        L.orc_df_counts_from_clamped(C.byref(p), np.ascontiguousarray(pot_clamped, np.float32).reshape(-1), n, num)
+    total = int(np.clip(num, 0, None).sum())
+    gen = np.zeros(8 * max(total, 1), np.float32)
+    k = L.orc_df_spawn(C.byref(p), C.byref(g), spos, svel, n, start, end, num, seed, frame, gen)
+    gen = gen[: 8 * k].reshape(-1, 8)
+    old_after = np.zeros((0, 8), np.float32)
+    if old is not None and len(old):
+        rec = np.ascontiguousarray(old, np.float32).reshape(-1).copy()
+        L.orc_df_update(C.byref(p), C.byref(g), spos, svel, start, end, rec, len(old))
+        old_after = rec.reshape(-1, 8)
+    live = np.concatenate([gen[gen[:, 7] != 3], old_after[old_after[:, 7] != 3]]) if (len(gen) or len(old_after)) \
+        else np.zeros((0, 8), np.float32)
+    return {"nrm": nrm.reshape(-1, 3), "pot_raw": raw.reshape(-1, 3), "pot": clamped.reshape(-1, 3), "num": num,
+            "gen": gen, "old_after": old_after, "live": live}
+
+
+class RefDiffuse(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("n_free", C.c_uint32), ("n_spawning", C.c_uint32), ("n_generated", C.c_uint32),
+                ("n_old", C.c_uint32), ("n_live", C.c_uint32),
+                ("perm", C.POINTER(C.c_uint32)), ("free_list", C.POINTER(C.c_uint32)), ("nrm", C.POINTER(C.c_float)),
+                ("pot", C.POINTER(C.c_float)), ("num", C.POINTER(C.c_int32)), ("gen", C.POINTER(C.c_float)),
+                ("old_after", C.POINTER(C.c_float)), ("live", C.POINTER(C.c_float))]
+
+
+def ref_diffuse_frame(config_path: str, pos, vel, rho, run_surface: bool, old, seed: int, frame: int) -> dict:
+    """The reference's diffuse kernels (CPU emulation) on one frame, with the
+    spawn uniforms of the counter-based generator injected."""
+    R = C.CDLL(REF_PATH)
+    R.ref_diffuse_frame.argtypes = [C.c_char_p, _f32p, _f32p, _f32p, C.c_uint32, C.c_int, _f32p, C.c_uint32, _f32p,
+                                    C.c_uint64, C.POINTER(RefDiffuse)]
+    R.ref_diffuse_frame.restype = C.c_int
+    R.ref_diffuse_free.argtypes = [C.POINTER(RefDiffuse)]
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1)
+    vel = np.ascontiguousarray(vel, np.float32).reshape(-1)
+    rho = np.ascontiguousarray(rho, np.float32)
+    n = pos.size // 3
+    old = np.zeros((0, 8), np.float32) if old is None else np.ascontiguousarray(old, np.float32)
+    old_flat = np.ascontiguousarray(old.reshape(-1) if len(old) else np.zeros(8, np.float32))
+    # enough uniforms for any plausible spawn count: grow until the frame fits
+    count = 3 * max(1024, 64 * n)
+    uni = np.array([lib().orc_spawn_uniform(seed, frame, k) for k in range(count)], np.float32)
+    res = RefDiffuse()
+    rc = R.ref_diffuse_frame(config_path.encode(), pos, vel, rho, n, 1 if run_surface else 0, old_flat, len(old), uni,
+                             len(uni), C.byref(res))
+    out = {"rc": rc}
+    out["perm"] = _arr(res.perm, res.n, np.uint32)
+    out["free_list"] = _arr(res.free_list, res.n_free, np.uint32)
+    out["nrm"] = _arr(res.nrm, 3 * res.n, np.float32).reshape(-1, 3)
+    out["pot"] = _arr(res.pot, 3 * res.n, np.float32).reshape(-1, 3)
+    out["num"] = _arr(res.num, res.n, np.int32)
+    out["gen"] = _arr(res.gen, 8 * res.n_generated, np.float32).reshape(-1, 8)
+    out["old_after"] = _arr(res.old_after, 8 * res.n_old, np.float32).reshape(-1, 8)
+    out["live"] = _arr(res.live, 8 * res.n_live, np.float32).reshape(-1, 8)
+    for k in ("n_free", "n_spawning", "n_generated", "n_old", "n_live"):
+        out[k] = getattr(res, k)
+    R.ref_diffuse_free(C.byref(res))
+    return out

@@ -139,6 +139,23 @@ void orc_mc_emit(const orc_grid* g, float iso, const uint32_t* bitmap,
                  const uint32_t* cases, const uint32_t* nvert, const uint64_t* offsets,
                  double* vpos, double* vnrm);
 
+/* ---- diffuse particles (pms_diffuse_oracle.c) ------------------------------- */
+float orc_spawn_uniform(uint64_t seed, uint32_t frame, uint64_t idx);
+void orc_df_normals(const orc_params* p, const orc_grid* g, const float* spos, uint32_t n,
+                    const uint32_t* start, const uint32_t* end, uint32_t nfree, double* nrm);
+void orc_df_trapped(const orc_params* p, const orc_grid* g, const float* spos, const float* svel, uint32_t n,
+                    const uint32_t* start, const uint32_t* end, double* ita, double* energy);
+void orc_df_crests(const orc_params* p, const orc_grid* g, const float* spos, const float* svel,
+                   const uint32_t* start, const uint32_t* end, const uint32_t* free_list, uint32_t nfree,
+                   const float* nrm, double* wc);
+void orc_df_counts(const orc_params* p, const float* pot_raw, uint32_t n, float* pot_clamped, int32_t* num);
+void orc_df_counts_from_clamped(const orc_params* p, const float* pot_clamped, uint32_t n, int32_t* num);
+uint64_t orc_df_spawn(const orc_params* p, const orc_grid* g, const float* spos, const float* svel, uint32_t n,
+                      const uint32_t* start, const uint32_t* end, const int32_t* num, uint64_t seed, uint32_t frame,
+                      float* gen);
+void orc_df_update(const orc_params* p, const orc_grid* g, const float* spos, const float* svel,
+                   const uint32_t* start, const uint32_t* end, float* rec, uint32_t n_old);
+
 /* ---- mesh comparison ------------------------------------------------------- */
 /* One-sided Hausdorff distance from the vertices of soup A to the triangles
  * of soup B (both xyz float64, 3 vertices per triangle).                     */

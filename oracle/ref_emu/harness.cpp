@@ -23,6 +23,7 @@
 #include "NeighborSearch_kernel.cuh"
 #include "Anisotropic_kernel.cuh"
 #include "MarchingCube_kernel.cuh"
+#include "DiffuseGeneration_kernel.cuh"
 
 #include <vector>
 #include <numeric>
@@ -316,6 +317,190 @@ void ref_mc_tables(uint32_t* edge_flags, int32_t* tri, uint32_t* num_vertices, u
     std::memcpy(tri, MarchingCubesHelper::edgeIndexesOfTriangle, 256 * 16 * 4);
     std::memcpy(num_vertices, MarchingCubesHelper::numVertices, 256 * 4);
     std::memcpy(edge_vertices, MarchingCubesHelper::vertexIndexesOfEdge, 24 * 4);
+}
+
+/* ------------------------------------------------------------------------- */
+/* diffuse particles: DiffuseGeneration::runsimulation (DiffuseGeneration.cu:89-104) */
+/* ------------------------------------------------------------------------- */
+struct ref_diffuse_result {
+    uint32_t n, n_free, n_spawning, n_generated, n_old, n_live;
+    uint32_t* perm;            /* n */
+    uint32_t* free_list;       /* n_free */
+    float* nrm;                /* 3n: particle normals after calculationofNormal */
+    float* pot;                /* 3n: waveCrest, Ita, energy after the phi clamps */
+    int32_t* num;              /* n */
+    float* gen;                /* 8 n_generated: pos xyz, vel xyz, ttl, type */
+    float* old_after;          /* 8 n_old: the old particles after updateDiffuseParticle */
+    float* live;               /* 8 n_live: generated then old, type 3 removed */
+};
+
+void ref_diffuse_free(ref_diffuse_result* r)
+{
+    void* ptrs[] = {r->perm, r->free_list, r->nrm, r->pot, r->num, r->gen, r->old_after, r->live};
+    for (void* p : ptrs) std::free(p);
+    std::memset(r, 0, sizeof(*r));
+}
+
+static void pack_diffuse(const DiffuseParticle& d, float* o)
+{
+    o[0] = d.pos.x; o[1] = d.pos.y; o[2] = d.pos.z;
+    o[3] = d.vel.x; o[4] = d.vel.y; o[5] = d.vel.z;
+    o[6] = (float)d.TTL; o[7] = (float)d.type;
+}
+
+/* One frame.  `uniforms(3 * idif + k)` replaces the host mt19937 stream
+ * (DiffuseGeneration.cu:381-395); old particles are given as 8-float records
+ * (pos, vel, ttl, type).  With run_surface the surface path's anisotropy runs
+ * first, as in GPUPOST.cpp:65-71, leaving its normals on surface particles. */
+int ref_diffuse_frame(const char* config_path, const float* pos, const float* vel, const float* rhop, uint32_t n,
+                      int run_surface, const float* old_rec, uint32_t n_old, const float* uniforms, uint64_t n_uniforms,
+                      ref_diffuse_result* out)
+{
+    std::memset(out, 0, sizeof(*out));
+    if (n == 0) return 1;
+    Params params;
+    params.mConfigParams.FileName_Param = config_path;
+    params.setParams();
+    std::vector<FluidParticle> fp(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        FluidParticle p;
+        std::memset(&p, 0, sizeof(p));
+        p.pos = make_float3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        p.vel = make_float3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+        p.rhop = rhop[i];
+        fp[i] = p;
+    }
+    float3 mx = fp[0].pos, mn = fp[0].pos;
+    for (uint32_t i = 1; i < n; ++i) {
+        if (mx.x <= fp[i].pos.x) mx.x = fp[i].pos.x;
+        if (mx.y <= fp[i].pos.y) mx.y = fp[i].pos.y;
+        if (mx.z <= fp[i].pos.z) mx.z = fp[i].pos.z;
+        if (mn.x >= fp[i].pos.x) mn.x = fp[i].pos.x;
+        if (mn.y >= fp[i].pos.y) mn.y = fp[i].pos.y;
+        if (mn.z >= fp[i].pos.z) mn.z = fp[i].pos.z;
+    }
+    GridParams& g = params.mGridParams;
+    g.scminPos = mn - 2 * params.mSurfaceParams.smoothingRadius;
+    g.scmaxPos = mx + 2 * params.mSurfaceParams.smoothingRadius;
+    g.minPos = mn - 4 * params.mSurfaceParams.smoothingRadius;
+    g.maxPos = mx + 4 * params.mSurfaceParams.smoothingRadius;
+    g.spresolution = make_uint3((uint)((g.maxPos.x - g.minPos.x) / g.spGridSize),
+                                (uint)((g.maxPos.y - g.minPos.y) / g.spGridSize),
+                                (uint)((g.maxPos.z - g.minPos.z) / g.spGridSize));
+    g.scresolution = make_uint3((uint)(((g.scmaxPos.x - g.scminPos.x) / g.scGridSize) + 0.5),
+                                (uint)(((g.scmaxPos.y - g.scminPos.y) / g.scGridSize) + 0.5),
+                                (uint)(((g.scmaxPos.z - g.scminPos.z) / g.scGridSize) + 0.5));
+    g.spSize = g.spresolution.x * g.spresolution.y * g.spresolution.z;
+    g.scSize = g.scresolution.x * g.scresolution.y * g.scresolution.z;
+    dSimParams = params.mSimParams;
+    dSurfaceParams = params.mSurfaceParams;
+    dDiffuseParams = params.mDiffuseParams;
+    dGridParams = g;
+    const uint spSize = g.spSize;
+    std::vector<SpatialGrid> spatialGrid(spSize);
+    std::memset(spatialGrid.data(), 0, sizeof(SpatialGrid) * spSize);
+    std::vector<IndexRange> range(spSize, IndexRange{0, 0});
+    /* NeighborSearch.cu:37-76 */
+    std::vector<uint> hash(n);
+    FluidParticle* P = fp.data();
+    launch(n, [&] { calculateHash(hash.data(), P, n, spatialGrid.data()); });
+    std::vector<uint> order(n);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint a, uint b) { return hash[a] < hash[b]; });
+    std::vector<FluidParticle> sorted(n);
+    std::vector<uint> skeys(n);
+    for (uint i = 0; i < n; ++i) { sorted[i] = fp[order[i]]; skeys[i] = hash[order[i]]; }
+    fp.swap(sorted);
+    P = fp.data();
+    launch(n, [&] { calCellRange(range.data(), n, skeys.data(), P); });
+    out->n = n;
+    out->perm = dup(order.data(), n);
+    if (run_surface) {
+        /* Anisotropic::processingOfParticles: leaves normals and flags on surface particles */
+        std::vector<uint> numSur(spSize, 0), numInv(spSize, 0), numSurScan(spSize, 0);
+        launch(spSize, [&] { estimationOfSurfaceParticles(spatialGrid.data(), numSur.data(), numInv.data(), range.data()); });
+        uint ns = exclusive_scan(numSur.data(), numSurScan.data(), spSize);
+        if (ns) {
+            dNumSurfaceParticles = ns;
+            std::vector<Index> surfIdx(ns, 0);
+            std::vector<SmoothedPos> smoothed(ns);
+            std::vector<MeanPos> meanP(ns);
+            std::vector<MatrixValue> svd(ns);
+            std::memset(meanP.data(), 0, sizeof(MeanPos) * ns);
+            launch(spSize, [&] { compactationOfParticles(numSur.data(), numSurScan.data(), range.data(), surfIdx.data()); });
+            launch(ns, [&] { calculationOfSmoothed(P, meanP.data(), smoothed.data(), range.data(), surfIdx.data(), spatialGrid.data()); });
+            launch(n, [&] { calculationOfDensity(P, range.data(), spatialGrid.data(), n); });
+            launch(ns, [&] { calculationOfTransformMatrices(meanP.data(), P, range.data(), surfIdx.data(), svd.data()); });
+        }
+    }
+    /* processingOfFreesurface (DiffuseGeneration.cu:187-198) */
+    dNumParticles = n;
+    std::vector<IsSurface> isFree(n, 0);
+    std::vector<IsSurfaceScan> isFreeScan(n, 0);
+    launch(spSize, [&] { estimationOfFreeSurfaceParticles(spatialGrid.data(), isFree.data(), range.data()); });
+    uint nFree = exclusive_scan(isFree.data(), isFreeScan.data(), n);
+    dNumFreeSurfaceParticles = nFree;
+    std::vector<Index> freeIdx(nFree ? nFree : 1, 0);
+    launch(n, [&] { compactationOfFreeParticles(isFree.data(), isFreeScan.data(), freeIdx.data()); });
+    launch(nFree, [&] { calculationofNormal(P, range.data(), freeIdx.data()); });
+    out->n_free = nFree;
+    out->free_list = dup(freeIdx.data(), nFree);
+    /* estimatingOfPotention (DiffuseGeneration.cu:200-212) */
+    std::vector<DiffusePotential> pot(n);
+    std::memset(pot.data(), 0, sizeof(DiffusePotential) * n);
+    std::vector<IsDiffuse> isDiff(n, 0);
+    std::vector<IsDiffuseScan> isDiffScan(n, 0);
+    std::vector<NumDiffuseParticle> num(n, 0);
+    std::vector<NumDiffuseParticleScan> numScan(n, 0);
+    launch(n, [&] { calculationofTrappedairpotential(P, range.data(), pot.data()); });
+    launch(nFree, [&] { calculationofWavecrests(P, range.data(), freeIdx.data(), pot.data()); });
+    out->nrm = (float*)std::malloc(12 * (size_t)n);
+    for (uint i = 0; i < n; ++i) std::memcpy(out->nrm + 3 * i, &fp[i].nor, 12);
+    /* generatingOfDiffuse (DiffuseGeneration.cu:214-228) */
+    launch(n, [&] { calculateofNumberofdiffuseparticles(pot.data(), num.data(), isDiff.data()); });
+    out->pot = (float*)std::malloc(12 * (size_t)n);
+    for (uint i = 0; i < n; ++i) { out->pot[3 * i] = pot[i].waveCrest; out->pot[3 * i + 1] = pot[i].Ita; out->pot[3 * i + 2] = pot[i].energy; }
+    out->num = dup(num.data(), n);
+    uint nGen = 0;
+    { uint64_t acc = 0; for (uint i = 0; i < n; ++i) { numScan[i] = (uint)acc; acc += (uint)num[i]; } nGen = (uint)acc; }
+    uint nSpawn = exclusive_scan(isDiff.data(), isDiffScan.data(), n);
+    dGeneratedNumDiffuseParticles = nGen;
+    dNumIsDiffuseParticles = nSpawn;
+    out->n_spawning = nSpawn;
+    out->n_generated = nGen;
+    std::vector<Index> diffIdx(nSpawn ? nSpawn : 1, 0);
+    std::vector<DiffuseParticle> gen(nGen ? nGen : 1);
+    std::memset(gen.data(), 0, sizeof(DiffuseParticle) * gen.size());
+    launch(n, [&] { compactationOfDiffuseParticle(isDiff.data(), isDiffScan.data(), diffIdx.data()); });
+    if (nGen && (uint64_t)3 * nGen > n_uniforms) return 5;
+    std::vector<float> rnd(uniforms, uniforms + (size_t)3 * nGen);
+    launch(nSpawn, [&] { calculateofDiffusePosition(P, num.data(), numScan.data(), gen.data(), rnd.data(), pot.data(), diffIdx.data()); });
+    launch(nGen, [&] { calculateofDiffuseType(P, range.data(), gen.data(), spatialGrid.data()); });
+    out->gen = (float*)std::malloc(32 * (size_t)(nGen ? nGen : 1));
+    for (uint k = 0; k < nGen; ++k) pack_diffuse(gen[k], out->gen + 8 * k);
+    /* updatingOfDiffuse (DiffuseGeneration.cu:426-442) */
+    std::vector<DiffuseParticle> old(n_old ? n_old : 1);
+    std::memset(old.data(), 0, sizeof(DiffuseParticle) * old.size());
+    for (uint k = 0; k < n_old; ++k) {
+        const float* o = old_rec + 8 * (size_t)k;
+        old[k].pos = make_float3(o[0], o[1], o[2]);
+        old[k].vel = make_float3(o[3], o[4], o[5]);
+        old[k].TTL = (int)o[6];
+        old[k].type = (int)o[7];
+        old[k].life = 1;
+    }
+    dOldNumDiffuseParticles = n_old;
+    if (n_old) launch(n_old, [&] { updateDiffuseParticle(P, range.data(), old.data(), spatialGrid.data()); });
+    out->n_old = n_old;
+    out->old_after = (float*)std::malloc(32 * (size_t)(n_old ? n_old : 1));
+    for (uint k = 0; k < n_old; ++k) pack_diffuse(old[k], out->old_after + 8 * k);
+    /* deleteAndappendParticles (DiffuseGeneration.cu:760-867): generated, then old; type 3 dropped */
+    std::vector<float> live;
+    for (uint k = 0; k < nGen; ++k) if (gen[k].type != 3) { float r[8]; pack_diffuse(gen[k], r); live.insert(live.end(), r, r + 8); }
+    for (uint k = 0; k < n_old; ++k) if (old[k].type != 3) { float r[8]; pack_diffuse(old[k], r); live.insert(live.end(), r, r + 8); }
+    out->n_live = (uint32_t)(live.size() / 8);
+    out->live = dup(live.data(), live.size());
+    return 0;
 }
 
 } /* extern "C" */

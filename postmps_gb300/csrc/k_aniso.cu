@@ -152,18 +152,22 @@ __device__ __forceinline__ void eig_sym3(T a[3][3], T e[3], T v[3][3], T tol) {
 }
 
 // ---------------------------------------------------------------------------
-// anisotropy of one surface particle per thread
+// anisotropy, pass 1: weighted moments of the neighbourhood, one surface
+// particle per thread, ONE walk over the cells.  With u = x_j - x_i and
+// w = 1 - (|u| / 2h)^3 (wij with support 2h):
+//   S0 = sum w, S1 = sum w u, S2 = sum w u u^T, J = #{|u| <= h}.
+// The reference's two passes (mean, then covariance about the mean) follow
+// from these: mean = x_i + S1/S0 and sum w (u - o)(u - o)^T = S2 - S1 S1^T / S0.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
-                                                    const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
-                                                    const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
-                                                    float4* __restrict__ aniso, float4* __restrict__ nrm4,
-                                                    float4* __restrict__ mean4, float* __restrict__ gdebug,
-                                                    uint32_t* __restrict__ nnb, uint32_t* __restrict__ n_fp64) {
+__global__ void __launch_bounds__(kThreads, 8) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
+                                                      const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
+                                                      const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                      float4* __restrict__ mom) {
     const uint32_t ns = cnt->ns;
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
     const float pad = 1e-4f * g.sp_cs;
     const float r2h_sq = ap.r2h * ap.r2h;
+    const float inv_r2h = 1.f / ap.r2h;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         const uint32_t i = slist[s];
         const float4 pi4 = spos[i];
@@ -172,57 +176,59 @@ __global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, con
         const uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
         uint3 lo, hi;
         box_clamp(g, c, 2u * (uint32_t)g.spexpand, lo, hi);
-
-        // pass 1: weighted mean (calculationOfSmoothed), support 2h
-        float ws = 0.f, mx = 0.f, my = 0.f, mz = 0.f;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    if (cell_gap2(g, p, x, y, z, pad) >= r2h_sq) continue;
-                    uint2 ci = cell_info[z * rxy + y * rx + x];
-                    uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        float4 q = spos[j];
-                        float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-                        float d = sqrtf(dx * dx + dy * dy + dz * dz);
-                        if (d < ap.r2h) {
-                            float t = d / ap.r2h;
-                            float w = 1.f - t * t * t;
-                            ws += w; mx += w * dx; my += w * dy; mz += w * dz;
-                        }
-                    }
-                }
-        // the particle itself contributes w = 1, so ws > 0
-        const float ox = mx / ws, oy = my / ws, oz = mz / ws;   // mean - p
-
-        // pass 2: covariance about the mean and neighbour count within h
-        float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f, wsum = 0.f;
+        float s0 = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+        float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
         uint32_t nn = 0;
         for (uint32_t z = lo.z; z <= hi.z; ++z)
             for (uint32_t y = lo.y; y <= hi.y; ++y)
                 for (uint32_t x = lo.x; x <= hi.x; ++x) {
                     if (cell_gap2(g, p, x, y, z, pad) >= r2h_sq) continue;
-                    uint2 ci = cell_info[z * rxy + y * rx + x];
-                    uint32_t m = ci.y & 0x7fffffffu;
+                    const uint2 ci = __ldg(&cell_info[z * rxy + y * rx + x]);
+                    const uint32_t m = ci.y & 0x7fffffffu;
                     for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        float4 q = spos[j];
-                        // neighbour count: u = x_j - x_i, |u| <= h, each operation rounded once
-                        float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
-                        float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
-                        float d = __fsqrt_rn(d2);
+                        const float4 q = __ldg(&spos[j]);
+                        // |u| rounded operation by operation, as the reference's neighbour count sees it
+                        const float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
+                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
+                        const float d = __fsqrt_rn(d2);
                         nn += (d <= ap.h) ? 1u : 0u;
                         if (d < ap.r2h) {
-                            float t = d / ap.r2h;
-                            float w = 1.f - t * t * t;
-                            float vx = ux - ox, vy = uy - oy, vz = uz - oz;
-                            wsum += w;
-                            c00 += w * vx * vx; c11 += w * vy * vy; c22 += w * vz * vz;
-                            c01 += w * vx * vy; c02 += w * vx * vz; c12 += w * vy * vz;
+                            const float t = d * inv_r2h;
+                            const float w = 1.f - t * t * t;
+                            const float wx = w * ux, wy = w * uy, wz = w * uz;
+                            s0 += w; sx += wx; sy += wy; sz += wz;
+                            sxx += wx * ux; sxy += wx * uy; sxz += wx * uz;
+                            syy += wy * uy; syz += wy * uz; szz += wz * uz;
                         }
                     }
                 }
-        float G[3][3], nv[3], maxv;
-        float flag;
+        mom[3 * (size_t)s + 0] = make_float4(s0, sx, sy, sz);
+        mom[3 * (size_t)s + 1] = make_float4(sxx, sxy, sxz, syy);
+        mom[3 * (size_t)s + 2] = make_float4(syz, szz, __uint_as_float(nn), 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// anisotropy, pass 2: covariance, eigen decomposition, clamp, G, normal, flag
+// (Anisotropic_kernel.cuh:431-518) from the moments; also the per-cell
+// support radius max(maxvalue * h) that lets the field skip far cells.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_eigen(AnisoParams ap, const uint32_t* __restrict__ slist,
+                                                    const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
+                                                    const float4* __restrict__ spos, const float4* __restrict__ mom,
+                                                    float4* __restrict__ aniso, float4* __restrict__ nrm4,
+                                                    float4* __restrict__ mean4, float* __restrict__ gdebug,
+                                                    uint32_t* __restrict__ nnb, float* __restrict__ cell_rad,
+                                                    Counters* __restrict__ cnt_w) {
+    const uint32_t ns = cnt->ns;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const uint32_t i = slist[s];
+        const float4 pi4 = spos[i];
+        const float4 m0 = mom[3 * (size_t)s + 0], m1 = mom[3 * (size_t)s + 1], m2 = mom[3 * (size_t)s + 2];
+        const float ws = m0.x;                               // >= 1: the particle itself
+        const float ox = m0.y / ws, oy = m0.z / ws, oz = m0.w / ws;   // mean - p
+        const uint32_t nn = __float_as_uint(m2.z);
+        float G[3][3], nv[3], maxv, flag;
         if ((int)nn < ap.min_nn) {
             // isolated particle: isotropic kernel (Anisotropic_kernel.cuh:435-443)
 #pragma unroll
@@ -231,24 +237,19 @@ __global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, con
                 for (int b = 0; b < 3; ++b) G[a][b] = (a == b) ? ap.h_inv : 0.f;
             maxv = 1.f; flag = 1.f; nv[0] = 1.f; nv[1] = 0.f; nv[2] = 0.f;
         } else {
-            float A[3][3] = {{(ap.h_sq + c00) / wsum, c01 / wsum, c02 / wsum},
-                             {c01 / wsum, (ap.h_sq + c11) / wsum, c12 / wsum},
-                             {c02 / wsum, c12 / wsum, (ap.h_sq + c22) / wsum}};
+            // (h^2 I + S2 - S1 S1^T / S0) / S0
+            const float inv = 1.f / ws;
+            const float c00 = (ap.h_sq + (m1.x - m0.y * ox)) * inv, c01 = (m1.y - m0.y * oy) * inv;
+            const float c02 = (m1.z - m0.y * oz) * inv, c11 = (ap.h_sq + (m1.w - m0.z * oy)) * inv;
+            const float c12 = (m2.x - m0.z * oz) * inv, c22 = (ap.h_sq + (m2.y - m0.w * oz)) * inv;
+            float A[3][3] = {{c00, c01, c02}, {c01, c11, c12}, {c02, c12, c22}};
             float e[3], U[3][3];
-            float Acopy[3][3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-                for (int b = 0; b < 3; ++b) Acopy[a][b] = A[a][b];
             eig_sym3<float>(A, e, U, 1e-7f);
             float sv0 = fabsf(e[0]), sv1 = fabsf(e[1]), sv2 = fabsf(e[2]);
             if ((double)sv0 > ap.cond_limit * (double)sv2) {
-                // near-degenerate covariance: solve again in float64
-                double Ad[3][3], ed[3], Ud[3][3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-#pragma unroll
-                    for (int b = 0; b < 3; ++b) Ad[a][b] = (double)Acopy[a][b];
+                // ill-conditioned covariance: solve again in float64
+                double Ad[3][3] = {{c00, c01, c02}, {c01, c11, c12}, {c02, c12, c22}};
+                double ed[3], Ud[3][3];
                 eig_sym3<double>(Ad, ed, Ud, 1e-15);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
@@ -257,16 +258,16 @@ __global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, con
                     for (int r = 0; r < 3; ++r) U[r][k] = (float)Ud[r][k];
                 }
                 sv0 = fabsf(e[0]); sv1 = fabsf(e[1]); sv2 = fabsf(e[2]);
-                atomicAdd(n_fp64, 1u);
+                atomicAdd(&cnt_w->n_fp64, 1u);
             }
             // clamp and scale (Anisotropic_kernel.cuh:459-509)
-            float smax = fmaxf(sv0, fmaxf(sv1, sv2)), smin = fminf(sv0, fminf(sv1, sv2));
+            const float smax = fmaxf(sv0, fmaxf(sv1, sv2)), smin = fminf(sv0, fminf(sv1, sv2));
             flag = (smin <= smax * 0.25f) ? 1.f : 0.f;
-            float lim = smax / 4.0f;
+            const float lim = smax / 4.0f;
             sv0 = fmaxf(sv0, lim); sv1 = fmaxf(sv1, lim); sv2 = fmaxf(sv2, lim);
-            float scale = cbrtf(sv0 * sv1 * sv2);
-            float cof = ap.h_inv * scale;
-            float k0 = cof / sv0, k1 = cof / sv1, k2 = cof / sv2;
+            const float scale = cbrtf(sv0 * sv1 * sv2);
+            const float cof = ap.h_inv * scale;
+            const float k0 = cof / sv0, k1 = cof / sv1, k2 = cof / sv2;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -278,14 +279,14 @@ __global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, con
         // orient the normal away from the mean (Anisotropic_kernel.cuh:512-515)
         if (nv[0] * (-ox) + nv[1] * (-oy) + nv[2] * (-oz) < 0.f) { nv[0] = -nv[0]; nv[1] = -nv[1]; nv[2] = -nv[2]; }
         // determinant as the reference evaluates it (myCuda.cuh:193-203)
-        float det = G[0][0] * G[1][1] * G[2][2] + G[0][1] * G[1][2] * G[2][0] + G[0][2] * G[1][0] * G[2][1]
-                  - G[0][0] * G[1][2] * G[2][1] - G[0][1] * G[1][0] * G[2][2] - G[0][2] * G[1][1] * G[2][0];
+        const float det = G[0][0] * G[1][1] * G[2][2] + G[0][1] * G[1][2] * G[2][0] + G[0][2] * G[1][0] * G[2][1]
+                        - G[0][0] * G[1][2] * G[2][1] - G[0][1] * G[1][0] * G[2][2] - G[0][2] * G[1][1] * G[2][0];
         const float hs = maxv * ap.h;
-        aniso[3 * (size_t)i + 0] = make_float4(G[0][0], G[0][1], G[0][2], hs);
-        aniso[3 * (size_t)i + 1] = make_float4(G[1][0], G[1][1], G[1][2], kSigma * det);
-        aniso[3 * (size_t)i + 2] = make_float4(G[2][0], G[2][1], G[2][2], maxv);
+        // symmetric G packed in two float4: {g00, g01, g02, hs^2}, {g11, g12, g22, sigma * det}
+        aniso[2 * (size_t)i + 0] = make_float4(G[0][0], G[0][1], G[0][2], hs * hs);
+        aniso[2 * (size_t)i + 1] = make_float4(G[1][1], G[1][2], G[2][2], kSigma * det);
         nrm4[i] = make_float4(nv[0], nv[1], nv[2], flag);
-        mean4[s] = make_float4(p.x + ox, p.y + oy, p.z + oz, ws);
+        mean4[s] = make_float4(pi4.x + ox, pi4.y + oy, pi4.z + oz, ws);
         float* gd = gdebug + 10 * (size_t)s;
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -293,6 +294,9 @@ __global__ void __launch_bounds__(kThreads) k_aniso(KGrid g, AnisoParams ap, con
             for (int b = 0; b < 3; ++b) gd[3 * a + b] = G[a][b];
         gd[9] = maxv;
         nnb[s] = nn;
+        // per-cell and global support radius (positive floats order like their bits)
+        atomicMax(reinterpret_cast<unsigned int*>(&cell_rad[skeys[i]]), __float_as_uint(hs));
+        atomicMax(&cnt_w->rad_max_bits, __float_as_uint(hs));
     }
 }
 
@@ -311,11 +315,16 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     PMS_LAUNCHED(ctx);
     k_inv_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(), P.mass, ctx->n);
     PMS_LAUNCHED(ctx);
-    // ns is on the device; size the grid by the particle count (upper bound)
-    k_aniso<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
+    // ns is on the device; grids are sized by the particle count (an upper bound)
+    k_moments<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
         g, ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(),
-        ctx->spos.as<float4>(), ctx->aniso.as<float4>(), ctx->nrm4.as<float4>(), ctx->mean4.as<float4>(),
-        ctx->gdebug.as<float>(), ctx->nnb.as<uint32_t>(), &cnt->n_fp64);
+        ctx->spos.as<float4>(), ctx->moments.as<float4>());
+    PMS_LAUNCHED(ctx);
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->cell_rad.p, 0, sizeof(float) * (size_t)g.sp_size, ctx->stream));
+    k_eigen<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
+        ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->spos.as<float4>(), ctx->moments.as<float4>(),
+        ctx->aniso.as<float4>(), ctx->nrm4.as<float4>(), ctx->mean4.as<float4>(), ctx->gdebug.as<float>(),
+        ctx->nnb.as<uint32_t>(), ctx->cell_rad.as<float>(), cnt);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -1,27 +1,622 @@
 // k_diffuse.cu -- diffuse (spray / foam / bubble) particle generation.
-// (stage entry points; kernels follow)
+//
+// Reference: DiffuseGeneration::runsimulation (DiffuseGeneration.cu:89-104,
+// 187-442, 760-867) with the kernels of DiffuseGeneration_kernel.cuh:18-118,
+// 528-1199 and the helpers of myCuda.cuh:341-401.  Per frame:
+//   free-surface particles  = particles of surface cells (:18-118)
+//   colour-gradient normals  for particles 0 .. NumFree-1 -- the reference
+//                            launches NumFree threads and indexes particles by
+//                            thread id, not through the free-surface list
+//                            (:528-609, DiffuseGeneration.cu:288-297); kept.
+//   trapped air, energy      all particles (:689-761)
+//   wave crests              free-surface particles (:611-687)
+//   spawn counts             phi clamps, floor(E (kta Ita + kwc WC) dt) (:763-791)
+//   spawn                    children sit on the parent, velocity jittered in
+//                            the plane normal to v (:812-922)
+//   classify                 neighbours within hd: spray < 6 <= foam <= 20 < bubble (:924-999)
+//   advect last frame's      gravity / buoyancy-drag / Wendland-averaged fluid
+//   diffuse particles        velocity, deletion out of bounds or TTL <= 0 (:1001-1199)
+//   delete and append        generated then old, type 3 removed (DiffuseGeneration.cu:760-867)
+//
+// GB300 design differences: the spawn uniforms come from a counter-based
+// generator on the device (seed, frame, index) instead of std::random_device
+// on the host plus a host-to-device copy; delete/append and the split by type
+// are a device stream compaction instead of a device-host-device round trip;
+// a child's type depends only on its parent's position, so it is computed
+// once per parent.  Operations that decide integers (thresholds, neighbour
+// counts, floor) are rounded one by one so the oracle can mirror them.
 #include "pms_internal.h"
 #include "k_common.cuh"
 
+#include <cmath>
+
 namespace pms {
-pms_status launch_diffuse(pms_ctx* ctx) {
-    return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "diffuse generation is not built yet");
+
+static constexpr int kThreads = 128;
+static constexpr double kEps = 1.0e-7;          // EPSILON_, Define.h:10 (double)
+static constexpr float kPiF = 3.14159265f;      // PI, Define.h:9
+static constexpr int kSpray = 6, kBubble = 20;  // SPARY, BUBBLE, Define.h:13-14
+
+struct DiffuseParticle {   // 32 bytes: two float4-aligned halves
+    float px, py, pz;
+    int ttl;
+    float vx, vy, vz;
+    int type;
+};
+
+struct DiffuseParams {
+    float hd, hd_sq, coefficient, mass, time_step, buoyancy, drag;
+    float min_wc, max_wc, min_ta, max_ta, min_ke, max_ke;
+    int ta_mult, wc_mult, life_time;
+    float lo_bound[3], hi_bound[3];    // grid min + 4.5 spacing, grid max - 4.5 spacing
+    uint64_t seed;
+    uint32_t frame;
+};
+
+// counter-based uniform in [0, 1): splitmix64 finaliser of (seed, frame, index)
+__host__ __device__ __forceinline__ float spawn_uniform(uint64_t seed, uint32_t frame, uint64_t idx) {
+    uint64_t x = seed * 0x9E3779B97F4A7C15ull + (uint64_t)frame * 0xD1B54A32D192ED03ull + idx;
+    x ^= x >> 30; x *= 0xBF58476D1CE4E5B9ull;
+    x ^= x >> 27; x *= 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    return (float)((double)(x >> 40) * (1.0 / 16777216.0));
 }
+
+// a.b with every product and sum rounded on its own (x, y, z order)
+__device__ __forceinline__ float dot_rn(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+__device__ __forceinline__ void diffuse_box(const KGrid& g, float x, float y, float z, uint3& lo, uint3& hi) {
+    const uint3 c = sp_cell(g, x, y, z);
+    box_clamp(g, c, (uint32_t)g.spexpand_diffuse, lo, hi);
+}
+
+// ---------------------------------------------------------------------------
+// free-surface list and the starting normals
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_df_free(const uint32_t* __restrict__ skeys, const uint2* __restrict__ cell_info,
+                                                 const float4* __restrict__ nrm4, int have_surface_normals, uint32_t n,
+                                                 uint32_t* __restrict__ isfree, float4* __restrict__ nrm) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const bool surf = (cell_info[skeys[j]].y & 0x80000000u) != 0;
+        isfree[j] = surf ? 1u : 0u;
+        // the surface pass leaves normals on surface particles; other particles start at zero
+        const float4 q = (surf && have_surface_normals) ? nrm4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        nrm[j] = make_float4(q.x, q.y, q.z, 0.f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_df_freelist(const uint32_t* __restrict__ isfree, const uint32_t* __restrict__ scan,
+                                                     uint32_t n, uint32_t* __restrict__ list) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        if (isfree[j]) list[scan[j]] = j;
+}
+
+// calculationofNormal: thread t < NumFree computes the normal of particle t
+__global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
+                                                        const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                        uint32_t n, float4* __restrict__ nrm) {
+    const uint32_t nf = min(cnt->n_free, n);
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
+        const float4 p = spos[t];
+        uint3 lo, hi;
+        diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        float nx = 0.f, ny = 0.f, nz = 0.f;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    const uint2 ci = cell_info[z * rxy + y * rx + x];
+                    const uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        const float4 q = spos[j];
+                        const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
+                        const float mp2 = sx * sx + sy * sy + sz * sz;
+                        const float mp = sqrtf(mp2);
+                        const float qq = mp / dp.hd;
+                        if (qq > 0.f && qq < 1.f) {
+                            const float d = dp.hd_sq - mp2;
+                            const float derivative = d * d * 6.f;
+                            const float c = dp.coefficient / mp * derivative;
+                            nx += c * sx; ny += c * sy; nz += c * sz;
+                        }
+                    }
+                }
+        const float mn2 = nx * nx + ny * ny + nz * nz;
+        if ((double)mn2 < kEps) continue;              // keeps the previous normal
+        const float inv = 1.f / sqrtf(mn2);
+        nrm[t] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// potentials
+// ---------------------------------------------------------------------------
+// calculationofTrappedairpotential: every particle
+__global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffuseParams dp, const uint2* __restrict__ cell_info,
+                                                         const float4* __restrict__ spos, const float4* __restrict__ svel,
+                                                         uint32_t n, float4* __restrict__ pot) {
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = spos[i], v = svel[i];
+        uint3 lo, hi;
+        diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        float ita = 0.f;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    const uint2 ci = cell_info[z * rxy + y * rx + x];
+                    const uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        const float4 q = spos[j];
+                        const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
+                        const float mp = sqrtf(sx * sx + sy * sy + sz * sz);
+                        if ((double)mp > kEps && mp <= dp.hd) {
+                            const float4 w = svel[j];
+                            const float ux = v.x - w.x, uy = v.y - w.y, uz = v.z - w.z;
+                            float mv = ux * ux + uy * uy + uz * uz;
+                            if ((double)mv > kEps) {
+                                mv = sqrtf(mv);
+                                const float qq = mp / dp.hd;
+                                const float e = 1.f - (ux / mv * (sx / mp) + uy / mv * (sy / mp) + uz / mv * (sz / mp));
+                                const float wgt = 1.f - qq;
+                                ita += mv * e * wgt;
+                            }
+                        }
+                    }
+                }
+        pot[i].y = ita;
+        pot[i].z = (float)(0.5 * (double)dp.mass * (double)(v.x * v.x + v.y * v.y + v.z * v.z));
+    }
+}
+
+// calculationofWavecrests: free-surface particles
+__global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
+                                                        const uint32_t* __restrict__ freelist, const uint2* __restrict__ cell_info,
+                                                        const float4* __restrict__ spos, const float4* __restrict__ svel,
+                                                        const float4* __restrict__ nrm, float4* __restrict__ pot) {
+    const uint32_t nf = cnt->n_free;
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
+        const uint32_t i = freelist[t];
+        const float4 p = spos[i], v = svel[i], ni = nrm[i];
+        const float nn = dot_rn(ni.x, ni.y, ni.z, ni.x, ni.y, ni.z);
+        const float vv = dot_rn(v.x, v.y, v.z, v.x, v.y, v.z);
+        if ((double)nn <= kEps || (double)vv <= kEps || (double)dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < 0.6) {
+            pot[i].x = 0.f;
+            continue;
+        }
+        uint3 lo, hi;
+        diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        float wc = 0.f;
+        for (uint32_t z = lo.z; z <= hi.z; ++z)
+            for (uint32_t y = lo.y; y <= hi.y; ++y)
+                for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                    const uint2 ci = cell_info[z * rxy + y * rx + x];
+                    const uint32_t m = ci.y & 0x7fffffffu;
+                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                        const float4 nj = nrm[j];
+                        if ((double)dot_rn(nj.x, nj.y, nj.z, nj.x, nj.y, nj.z) <= kEps) continue;
+                        const float4 q = spos[j];
+                        // crests2p: x_ji = normalize(x_j - x_i); counts if x_ji . n_i < -eps
+                        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+                        const float l2 = dx * dx + dy * dy + dz * dz;
+                        if (l2 == 0.f) continue;                 // normalize(0) is NaN: contributes 0
+                        const float il = 1.f / sqrtf(l2);
+                        const float c = (dx * il) * ni.x + (dy * il) * ni.y + (dz * il) * ni.z;
+                        if ((double)c < -kEps) {
+                            // curvature2p: (1 - n_i . n_j) * Weend(x_i - x_j, h)
+                            const float e1 = 1.f - (ni.x * nj.x + ni.y * nj.y + ni.z * nj.z);
+                            const float mx = sqrtf(l2);
+                            const float w = (mx <= dp.hd && mx > 0.f) ? (float)(1.0 - (double)(mx / dp.hd)) : 0.f;
+                            wc += e1 * w;
+                        }
+                    }
+                }
+        pot[i].x = wc;
+    }
+}
+
+__device__ __forceinline__ float phi_clamp(float I, float tmin, float tmax) {
+    return __fdiv_rn(__fsub_rn(fminf(I, tmax), fminf(I, tmin)), __fsub_rn(tmax, tmin));
+}
+
+// calculateofNumberofdiffuseparticles; key = spawning << 32 | count for one 64-bit scan
+__global__ void __launch_bounds__(256) k_df_count(DiffuseParams dp, float4* __restrict__ pot, uint32_t n,
+                                                  int32_t* __restrict__ num, unsigned long long* __restrict__ key) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 q = pot[i];
+        q.x = phi_clamp(q.x, dp.min_wc, dp.max_wc);
+        q.y = phi_clamp(q.y, dp.min_ta, dp.max_ta);
+        q.z = phi_clamp(q.z, dp.min_ke, dp.max_ke);
+        pot[i] = q;
+        const float a = __fmul_rn((float)dp.ta_mult, q.y), b = __fmul_rn((float)dp.wc_mult, q.x);
+        const float f = __fmul_rn(__fmul_rn(q.z, __fadd_rn(a, b)), dp.time_step);
+        const int k = (int)floorf(f);
+        num[i] = k;
+        key[i] = k >= 1 ? ((1ull << 32) | (unsigned long long)(uint32_t)k) : 0ull;
+    }
+}
+
+__global__ void k_df_totals(const unsigned long long* __restrict__ total, Counters* __restrict__ cnt) {
+    const unsigned long long t = *total;
+    cnt->n_spawning = (uint32_t)(t >> 32);
+    cnt->n_generated = (uint32_t)(t & 0xffffffffull);
+}
+
+__global__ void __launch_bounds__(256) k_df_spawnlist(const unsigned long long* __restrict__ key,
+                                                      const unsigned long long* __restrict__ off, uint32_t n,
+                                                      uint32_t* __restrict__ list) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (key[i]) list[(uint32_t)(off[i] >> 32)] = i;
+}
+
+// neighbours of x within hd (squared distance <= hd^2), calculateofDiffuseType
+__device__ __forceinline__ int count_within(const KGrid& g, const DiffuseParams& dp, const uint2* __restrict__ cell_info,
+                                            const float4* __restrict__ spos, float px, float py, float pz, bool squared) {
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    uint3 lo, hi;
+    diffuse_box(g, px, py, pz, lo, hi);
+    int count = 0;
+    for (uint32_t z = lo.z; z <= hi.z; ++z)
+        for (uint32_t y = lo.y; y <= hi.y; ++y)
+            for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                const uint2 ci = cell_info[z * rxy + y * rx + x];
+                const uint32_t m = ci.y & 0x7fffffffu;
+                for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                    const float4 q = spos[j];
+                    const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
+                    const float d2 = dot_rn(sx, sy, sz, sx, sy, sz);
+                    // the generator compares |s|^2 <= hd^2, the advection |s| <= hd
+                    if (squared ? (d2 <= dp.hd_sq) : (__fsqrt_rn(d2) <= dp.hd)) ++count;
+                }
+            }
+    return count;
+}
+
+__device__ __forceinline__ int type_of(int density) { return density > kBubble ? 2 : (density < kSpray ? 0 : 1); }
+
+// calculateofDiffusePosition + calculateofDiffuseType, one spawning parent per thread
+__global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
+                                                       const uint32_t* __restrict__ spawnlist,
+                                                       const unsigned long long* __restrict__ off,
+                                                       const int32_t* __restrict__ num, const uint2* __restrict__ cell_info,
+                                                       const float4* __restrict__ spos, const float4* __restrict__ svel,
+                                                       DiffuseParticle* __restrict__ gen) {
+    const uint32_t ns = cnt->n_spawning;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ns; t += gridDim.x * blockDim.x) {
+        const uint32_t i = spawnlist[t];
+        const float4 p = spos[i], v = svel[i];
+        // a vector normal to v (solveEq, myCuda.cuh:385-389), then the second axis
+        float e1x, e1y, e1z;
+        if (v.x != 0.f) {
+            e1x = ((-(0.f - p.z) * v.z - (1.f - p.y) * v.y) / v.x) + p.x; e1y = 1.f; e1z = 0.f;
+        } else if (v.y != 0.f) {
+            e1x = 1.f; e1z = 0.f; e1y = ((-(1.f - p.x) * v.x - (0.f - p.z) * v.z) / v.y) + p.y;
+        } else {
+            e1x = 1.f; e1y = 0.f; e1z = ((-(1.f - p.x) * v.x - (0.f - p.y) * v.y) / v.z) + p.z;
+        }
+        float il = 1.f / sqrtf(e1x * e1x + e1y * e1y + e1z * e1z);
+        e1x *= il; e1y *= il; e1z *= il;
+        float e2x = e1y * v.z - v.y * e1z, e2y = e1x * v.z - v.x * e1z, e2z = e1x * v.y - v.x * e1y;
+        il = 1.f / sqrtf(e2x * e2x + e2y * e2y + e2z * e2z);
+        e2x *= il; e2y *= il; e2z *= il;
+        const int k = num[i];
+        const uint32_t start = (uint32_t)(off[i] & 0xffffffffull);
+        const int type = type_of(count_within(g, dp, cell_info, spos, p.x, p.y, p.z, true));
+        for (int c = 0; c < k; ++c) {
+            const uint64_t idif = (uint64_t)start + (uint64_t)c;
+            const float u1 = spawn_uniform(dp.seed, dp.frame, 3 * idif + 1);
+            const float u2 = spawn_uniform(dp.seed, dp.frame, 3 * idif + 2);
+            const float r = dp.hd * sqrtf(u1);
+            const float theta = u2 * 2.f * kPiF;
+            const float ct = (float)cos((double)theta), st = (float)sin((double)theta);
+            DiffuseParticle d;
+            d.px = p.x; d.py = p.y; d.pz = p.z;      // the reference overwrites the offset position with the parent's
+            d.vx = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(r, ct), e1x), __fmul_rn(__fmul_rn(r, st), e2x)), v.x);
+            d.vy = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(r, ct), e1y), __fmul_rn(__fmul_rn(r, st), e2y)), v.y);
+            d.vz = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(r, ct), e1z), __fmul_rn(__fmul_rn(r, st), e2z)), v.z);
+            d.ttl = k * dp.life_time;
+            d.type = type;
+            gen[idif] = d;
+        }
+    }
+}
+
+// Wwendland, myCuda.cuh:391-401: ad and e1 are float variables set from double
+// expressions; ad*e1^4 runs in float, the last factor (2q + 1.) in double
+__device__ __forceinline__ float wendland(float rx, float ry, float rz, float h) {
+    const float mx = __fsqrt_rn(dot_rn(rx, ry, rz, rx, ry, rz));
+    const float q = __fdiv_rn(mx, h);
+    if (q >= 0.f && q <= 2.f) {
+        const float ad = (float)(21.0 / (16.0 * (double)kPiF * (double)h * (double)h * (double)h));
+        const float e1 = (float)(1.0 - ((double)q / 2.0));
+        const float d = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(ad, e1), e1), e1), e1);
+        return (float)((double)d * ((double)__fmul_rn(2.0f, q) + 1.0));
+    }
+    return 0.f;
+}
+
+// updateDiffuseParticle, one diffuse particle of the previous frame per thread
+__global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParams dp, uint32_t n_old,
+                                                        const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                        const float4* __restrict__ svel, DiffuseParticle* __restrict__ old) {
+    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_old; t += gridDim.x * blockDim.x) {
+        DiffuseParticle d = old[t];
+        const float px = d.px, py = d.py, pz = d.pz, vx = d.vx, vy = d.vy, vz = d.vz;
+        const int density = count_within(g, dp, cell_info, spos, px, py, pz, false);
+        float nx = 0.f, ny = 0.f, nz = 0.f, wsum = 0.f;
+        if (density >= kSpray) {
+            uint3 lo, hi;
+            diffuse_box(g, px, py, pz, lo, hi);
+            for (uint32_t z = lo.z; z <= hi.z; ++z)
+                for (uint32_t y = lo.y; y <= hi.y; ++y)
+                    for (uint32_t x = lo.x; x <= hi.x; ++x) {
+                        const uint2 ci = cell_info[z * rxy + y * rx + x];
+                        const uint32_t m = ci.y & 0x7fffffffu;
+                        for (uint32_t j = ci.x; j < ci.x + m; ++j) {
+                            const float4 q = spos[j], w = svel[j];
+                            const float tv = wendland(__fsub_rn(px, q.x), __fsub_rn(py, q.y), __fsub_rn(pz, q.z), dp.hd);
+                            nx = __fadd_rn(nx, __fmul_rn(w.x, tv));
+                            ny = __fadd_rn(ny, __fmul_rn(w.y, tv));
+                            nz = __fadd_rn(nz, __fmul_rn(w.z, tv));
+                            wsum = __fadd_rn(wsum, tv);
+                        }
+                    }
+        }
+        const float gz = -9.81f, dt = dp.time_step;
+        if (density < kSpray) {
+            d.vx = __fadd_rn(d.vx, __fmul_rn(0.f, dt));
+            d.vy = __fadd_rn(d.vy, __fmul_rn(0.f, dt));
+            d.vz = __fadd_rn(d.vz, __fmul_rn(gz, dt));
+            d.px = __fadd_rn(d.px, __fmul_rn(dt, d.vx));
+            d.py = __fadd_rn(d.py, __fmul_rn(dt, d.vy));
+            d.pz = __fadd_rn(d.pz, __fmul_rn(dt, d.vz));
+        }
+        if (density > kBubble) {
+            nx = __fdiv_rn(nx, wsum); ny = __fdiv_rn(ny, wsum); nz = __fdiv_rn(nz, wsum);
+            // vel + dt * (-buoyancy * g + drag * (num - vel) / dt), per component
+            d.vx = __fadd_rn(vx, __fmul_rn(dt, __fadd_rn(__fmul_rn(-dp.buoyancy, 0.f), __fdiv_rn(__fmul_rn(dp.drag, __fsub_rn(nx, vx)), dt))));
+            d.vz = __fadd_rn(vz, __fmul_rn(dt, __fadd_rn(__fmul_rn(-dp.buoyancy, gz), __fdiv_rn(__fmul_rn(dp.drag, __fsub_rn(nz, vz)), dt))));
+            d.vy = __fadd_rn(vy, __fmul_rn(dt, __fadd_rn(__fmul_rn(-dp.buoyancy, 0.f), __fdiv_rn(__fmul_rn(dp.drag, __fsub_rn(ny, vy)), dt))));
+            d.px = __fadd_rn(d.px, __fmul_rn(dt, d.vx));
+            d.py = __fadd_rn(d.py, __fmul_rn(dt, d.vy));
+            d.pz = __fadd_rn(d.pz, __fmul_rn(dt, d.vz));
+        }
+        if (density <= kBubble && density >= kSpray) {
+            nx = __fdiv_rn(nx, wsum); ny = __fdiv_rn(ny, wsum); nz = __fdiv_rn(nz, wsum);
+            d.vx = nx; d.vy = ny; d.vz = nz;
+            d.px = __fadd_rn(d.px, __fmul_rn(dt, nx));
+            d.py = __fadd_rn(d.py, __fmul_rn(dt, ny));
+            d.pz = __fadd_rn(d.pz, __fmul_rn(dt, nz));
+            d.ttl -= 1;
+        }
+        const bool outside = (d.px > dp.hi_bound[0] || d.py > dp.hi_bound[1] || d.pz > dp.hi_bound[2]) ||
+                             (d.px < dp.lo_bound[0] || d.py < dp.lo_bound[1] || d.pz < dp.lo_bound[2]);
+        if (outside || d.ttl <= 0) {
+            d.type = 3;
+            d.ttl = 0;
+        } else {
+            d.type = type_of(count_within(g, dp, cell_info, spos, d.px, d.py, d.pz, false));
+        }
+        old[t] = d;
+    }
+}
+
+// delete and append: generated then old, dropping type 3; per-type counts
+__global__ void __launch_bounds__(256) k_df_keep(const DiffuseParticle* __restrict__ gen, uint32_t n_gen,
+                                                 const DiffuseParticle* __restrict__ old, uint32_t n_old,
+                                                 uint32_t* __restrict__ keep, Counters* __restrict__ cnt) {
+    const uint32_t total = n_gen + n_old;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+        const int type = k < n_gen ? gen[k].type : old[k - n_gen].type;
+        keep[k] = type != 3 ? 1u : 0u;
+        atomicAdd(&cnt->n_type[type == 0 ? 0 : (type == 2 ? 2 : (type == 3 ? 3 : 1))], 1u);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_df_append(const DiffuseParticle* __restrict__ gen, uint32_t n_gen,
+                                                   const DiffuseParticle* __restrict__ old, uint32_t n_old,
+                                                   const uint32_t* __restrict__ keep, const uint32_t* __restrict__ scan,
+                                                   DiffuseParticle* __restrict__ out) {
+    const uint32_t total = n_gen + n_old;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x)
+        if (keep[k]) out[scan[k]] = k < n_gen ? gen[k] : old[k - n_gen];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static DiffuseParams diffuse_params(const pms_ctx* ctx) {
+    const pms_params& P = ctx->prm;
+    DiffuseParams d;
+    d.hd = P.hd; d.hd_sq = P.hd_sq; d.coefficient = P.coefficient; d.mass = P.mass; d.time_step = P.time_step;
+    d.buoyancy = P.buoyancy; d.drag = P.drag;
+    d.min_wc = P.min_wc; d.max_wc = P.max_wc; d.min_ta = P.min_ta; d.max_ta = P.max_ta;
+    d.min_ke = P.min_ke; d.max_ke = P.max_ke;
+    d.ta_mult = P.ta_mult; d.wc_mult = P.wc_mult; d.life_time = P.life_time;
+    // dGridParams.maxPos - particleSpacing * 4.5 (a double product passed as float)
+    const float m = (float)((double)P.particle_spacing * 4.5);
+    for (int k = 0; k < 3; ++k) { d.lo_bound[k] = ctx->grid.min_pos[k] + m; d.hi_bound[k] = ctx->grid.max_pos[k] - m; }
+    d.seed = ctx->cfg.rng_seed;
+    d.frame = ctx->frame_index;
+    return d;
+}
+
+pms_status launch_diffuse(pms_ctx* ctx) {
+    const uint32_t n = ctx->n;
+    if (n == 0) { ctx->diffuse_old = 0; return PMS_OK; }
+    const KGrid g = kgrid_of(ctx->grid);
+    const DiffuseParams dp = diffuse_params(ctx);
+    Counters* cnt = ctx->counters.as<Counters>();
+    pms_status st;
+    if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
+    const size_t N = n;
+    PMS_CUDA(ctx, ctx->d_isfree.ensure(4 * N));
+    PMS_CUDA(ctx, ctx->d_freescan.ensure(4 * N));
+    PMS_CUDA(ctx, ctx->d_freelist.ensure(4 * N));
+    PMS_CUDA(ctx, ctx->d_nrm_free.ensure(16 * N));
+    PMS_CUDA(ctx, ctx->d_pot.ensure(16 * N));
+    PMS_CUDA(ctx, ctx->d_num.ensure(4 * N));
+    PMS_CUDA(ctx, ctx->d_isdiff.ensure(8 * N));      // 64-bit spawn keys
+    PMS_CUDA(ctx, ctx->d_isdiffscan.ensure(8 * N));
+    PMS_CUDA(ctx, ctx->d_difflist.ensure(4 * N));
+    const unsigned gb = grid_for(n, 256), gk = grid_for(n, kThreads);
+    k_df_free<<<gb, 256, 0, ctx->stream>>>(ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->nrm4.as<float4>(),
+                                           ctx->have_aniso ? 1 : 0, n, ctx->d_isfree.as<uint32_t>(), ctx->d_nrm_free.as<float4>());
+    PMS_LAUNCHED(ctx);
+    if ((st = scan_u32(ctx, ctx->d_isfree.as<uint32_t>(), ctx->d_freescan.as<uint32_t>(), n, &cnt->n_free))) return st;
+    k_df_freelist<<<gb, 256, 0, ctx->stream>>>(ctx->d_isfree.as<uint32_t>(), ctx->d_freescan.as<uint32_t>(), n,
+                                               ctx->d_freelist.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    k_df_normal<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), n,
+                                                  ctx->d_nrm_free.as<float4>());
+    PMS_LAUNCHED(ctx);
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->d_pot.p, 0, 16 * N, ctx->stream));
+    k_df_trapped<<<gk, kThreads, 0, ctx->stream>>>(g, dp, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(),
+                                                   ctx->svel.as<float4>(), n, ctx->d_pot.as<float4>());
+    PMS_LAUNCHED(ctx);
+    k_df_crests<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->d_freelist.as<uint32_t>(), ctx->cell_info.as<uint2>(),
+                                                  ctx->spos.as<float4>(), ctx->svel.as<float4>(),
+                                                  ctx->d_nrm_free.as<float4>(), ctx->d_pot.as<float4>());
+    PMS_LAUNCHED(ctx);
+    k_df_count<<<gb, 256, 0, ctx->stream>>>(dp, ctx->d_pot.as<float4>(), n, ctx->d_num.as<int32_t>(),
+                                            ctx->d_isdiff.as<unsigned long long>());
+    PMS_LAUNCHED(ctx);
+    if ((st = scan_u64(ctx, ctx->d_isdiff.as<unsigned long long>(), ctx->d_isdiffscan.as<unsigned long long>(), n,
+                       ctx->tmp.as<unsigned long long>())))
+        return st;
+    k_df_totals<<<1, 1, 0, ctx->stream>>>(ctx->tmp.as<unsigned long long>(), cnt);
+    PMS_LAUNCHED(ctx);
+    k_df_spawnlist<<<gb, 256, 0, ctx->stream>>>(ctx->d_isdiff.as<unsigned long long>(),
+                                                ctx->d_isdiffscan.as<unsigned long long>(), n, ctx->d_difflist.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    if ((st = sync_counters(ctx))) return st;
+    const uint32_t n_gen = ctx->h_counters->n_generated, n_spawn = ctx->h_counters->n_spawning;
+    const uint32_t n_old = ctx->diffuse_old;
+    const size_t total = (size_t)n_gen + n_old;
+    PMS_CUDA(ctx, ctx->d_gen.ensure(sizeof(DiffuseParticle) * (n_gen ? n_gen : 1)));
+    PMS_CUDA(ctx, ctx->d_all.ensure(sizeof(DiffuseParticle) * (total ? total : 1)));
+    PMS_CUDA(ctx, ctx->d_typescan.ensure(8 * (total ? total : 1)));
+    if (n_spawn)
+        k_df_spawn<<<grid_for(n_spawn, kThreads), kThreads, 0, ctx->stream>>>(
+            g, dp, cnt, ctx->d_difflist.as<uint32_t>(), ctx->d_isdiffscan.as<unsigned long long>(), ctx->d_num.as<int32_t>(),
+            ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>());
+    if (n_spawn) PMS_LAUNCHED(ctx);
+    if (n_old) {
+        k_df_update<<<grid_for(n_old, kThreads), kThreads, 0, ctx->stream>>>(
+            g, dp, n_old, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
+            ctx->d_old.as<DiffuseParticle>());
+        PMS_LAUNCHED(ctx);
+    }
+    uint32_t* keep = ctx->d_typescan.as<uint32_t>();
+    uint32_t* kscan = keep + (total ? total : 1);
+    if (total) {
+        k_df_keep<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(), n_gen,
+                                                                 ctx->d_old.as<DiffuseParticle>(), n_old, keep, cnt);
+        PMS_LAUNCHED(ctx);
+        if ((st = scan_u32(ctx, keep, kscan, total, &cnt->n_live))) return st;
+        k_df_append<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(), n_gen,
+                                                                   ctx->d_old.as<DiffuseParticle>(), n_old, keep, kscan,
+                                                                   ctx->d_all.as<DiffuseParticle>());
+        PMS_LAUNCHED(ctx);
+    }
+    if ((st = sync_counters(ctx))) return st;
+    ctx->diffuse_old = total ? ctx->h_counters->n_live : 0;
+    std::swap(ctx->d_all, ctx->d_old);               // the survivors are next frame's old particles
+    return PMS_OK;
+}
+
 }  // namespace pms
 
+using pms::DiffuseParticle;
+
 pms_status pms::diffuse_debug(pms_ctx* ctx, int id, std::vector<uint8_t>& out) {
-    (void)out;
-    return pms_fail(ctx, PMS_ERR_INVALID_ARGUMENT, "unknown array id %d", id);
+    if (!ctx->have_diffuse) return pms_fail(ctx, PMS_ERR_STATE, "no diffuse stage yet");
+    const size_t n = ctx->n;
+    const DBuf* src = nullptr;
+    size_t bytes = 0;
+    switch (id) {
+        case PMS_ARRAY_DIFFUSE_POTENTIAL: src = &ctx->d_pot; bytes = 16 * n; break;
+        case PMS_ARRAY_DIFFUSE_COUNT: src = &ctx->d_num; bytes = 4 * n; break;
+        case PMS_ARRAY_FREE_NORMAL: src = &ctx->d_nrm_free; bytes = 16 * n; break;
+        default: return pms_fail(ctx, PMS_ERR_INVALID_ARGUMENT, "unknown array id %d", id);
+    }
+    std::vector<uint8_t> raw(bytes);
+    PMS_CUDA(ctx, cudaMemcpyAsync(raw.data(), src->p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    PMS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (id == PMS_ARRAY_DIFFUSE_COUNT) { out.swap(raw); return PMS_OK; }
+    // float4 -> xyz
+    out.resize(12 * n);
+    for (size_t i = 0; i < n; ++i) memcpy(out.data() + 12 * i, raw.data() + 16 * i, 12);
+    return PMS_OK;
 }
 
-pms_status pms::write_diffuse_frame(pms_ctx* ctx, const pms_config& cfg, int frame) {
-    (void)cfg; (void)frame;
-    return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "diffuse generation is not built yet");
+static pms_status download_live(pms_ctx* ctx, std::vector<DiffuseParticle>& v) {
+    v.resize(ctx->diffuse_old);
+    if (!v.empty())
+        PMS_CUDA(ctx, cudaMemcpyAsync(v.data(), ctx->d_old.p, sizeof(DiffuseParticle) * v.size(), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+    PMS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMS_OK;
 }
 
 extern "C" pms_status pms_download_diffuse(pms_ctx* ctx, int type, float* pos, float* vel, int32_t* type_out,
                                            int32_t* ttl, float* wc, float* ta, float* en, uint32_t cap, uint32_t* n_out) {
-    (void)type; (void)pos; (void)vel; (void)type_out; (void)ttl; (void)wc; (void)ta; (void)en; (void)cap;
-    if (n_out) *n_out = 0;
-    return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "diffuse generation is not built yet");
+    if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
+    if (type < -1 || type > 2) return pms_fail(ctx, PMS_ERR_INVALID_ARGUMENT, "diffuse type must be -1, 0, 1 or 2");
+    cudaSetDevice(ctx->device);
+    std::vector<DiffuseParticle> v;
+    pms_status st = download_live(ctx, v);
+    if (st) return st;
+    uint32_t k = 0;
+    for (const DiffuseParticle& d : v) {
+        // the reference's split: 0 spray, 2 bubble, anything else foam (DiffuseGeneration.cu:808-826)
+        const int cls = d.type == 0 ? 0 : (d.type == 2 ? 2 : 1);
+        if (type != -1 && cls != type) continue;
+        if (k < cap) {
+            if (pos) { pos[3 * k] = d.px; pos[3 * k + 1] = d.py; pos[3 * k + 2] = d.pz; }
+            if (vel) { vel[3 * k] = d.vx; vel[3 * k + 1] = d.vy; vel[3 * k + 2] = d.vz; }
+            if (type_out) type_out[k] = d.type;
+            if (ttl) ttl[k] = d.ttl;
+            // the reference never fills a diffuse particle's waveCrest / Ita / energy (always 0)
+            if (wc) wc[k] = 0.f;
+            if (ta) ta[k] = 0.f;
+            if (en) en[k] = 0.f;
+        }
+        ++k;
+    }
+    if (n_out) *n_out = k;
+    if (k > cap && (pos || vel || type_out || ttl || wc || ta || en))
+        return pms_fail(ctx, PMS_ERR_CAPACITY, "%u diffuse particles", k);
+    return PMS_OK;
+}
+
+pms_status pms::write_diffuse_frame(pms_ctx* ctx, const pms_config& cfg, int frame) {
+    std::vector<DiffuseParticle> v;
+    pms_status st = download_live(ctx, v);
+    if (st) return st;
+    static const char* prefixes[3] = {"PartSpary_", "PartFoam_", "PartBubble_"};
+    for (int cls = 0; cls < 3; ++cls) {
+        std::vector<float> pos, vel;
+        for (const DiffuseParticle& d : v) {
+            const int c = d.type == 0 ? 0 : (d.type == 2 ? 2 : 1);
+            if (c != cls) continue;
+            pos.insert(pos.end(), {d.px, d.py, d.pz});
+            vel.insert(vel.end(), {d.vx, d.vy, d.vz});
+        }
+        const uint32_t m = (uint32_t)(pos.size() / 3);
+        std::vector<float> zeros(m, 0.f);
+        char num[64];
+        snprintf(num, sizeof(num), "%.*d", cfg.num_zeros, frame);
+        std::string dir = cfg.diffuse_path;
+        if (!dir.empty() && dir.back() != '/') dir += "/";
+        std::string path = dir + prefixes[cls] + num + ".vtk";
+        st = pms_write_diffuse_vtk(path.c_str(), pos.data(), vel.data(), zeros.data(), zeros.data(), zeros.data(), m,
+                                   ctx->prm.hd / 10.f);
+        if (st) return pms_fail(ctx, st, "cannot write %s", path.c_str());
+    }
+    return PMS_OK;
 }

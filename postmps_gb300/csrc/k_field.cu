@@ -13,13 +13,13 @@
 //
 // GB300 design: thread per band vertex, consecutive threads on consecutive
 // band vertices (neighbours along x share almost all cells, so the particle
-// loads hit in L1).  A cell whose box lies beyond the largest possible support
-// (h for isotropic cells, 4^(2/3) h for anisotropic ones -- the clamp bounds
-// maxvalue by 4^(2/3)) contributes exactly zero and is skipped, except that
-// the first cell of a row is still visited once the threshold is crossed;
-// both keep the reference's sum bit-for-bit in its semantics.  Particle data
-// come from SoA float4 (x, y, z, m/rho) and three float4 of G, h_s and
-// sigma*det precomputed per surface particle.
+// loads hit in L1).  A cell whose box lies beyond the support of every
+// particle in it (h for isotropic cells, the cell's largest maxvalue * h for
+// anisotropic ones, recorded by the anisotropy pass) contributes exactly zero
+// and is skipped, except that the first cell of a row is still visited once
+// the threshold is crossed; both keep the reference's sum in its semantics.
+// Particle data come from SoA float4 (x, y, z, m/rho) and two float4 of the
+// symmetric G, h_s^2 and sigma*det precomputed per surface particle.
 #include "pms_internal.h"
 #include "k_common.cuh"
 
@@ -30,7 +30,8 @@ static constexpr float kSigma = 1.56668147f;
 
 struct FieldParams {
     float h, h_sq, inv_h2, c_iso, thr;
-    float r_aniso2, r_iso2;   // culling radii squared
+    float r_iso2;             // culling radius of isotropic cells, squared
+    float grow;               // relative margin on culling radii
 };
 
 __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pad) {
@@ -47,13 +48,12 @@ __device__ __forceinline__ float cell_sum(const uint2 ci, const float3 v, const 
             const float4 q = __ldg(&spos[j]);
             const float rx = q.x - v.x, ry = q.y - v.y, rz = q.z - v.z;
             const float l2 = rx * rx + ry * ry + rz * rz;
-            const float4 a0 = __ldg(&aniso[3 * (size_t)j]);
-            if (l2 >= a0.w * a0.w) continue;              // |r| >= maxvalue * h
-            const float4 a1 = __ldg(&aniso[3 * (size_t)j + 1]);
-            const float4 a2 = __ldg(&aniso[3 * (size_t)j + 2]);
+            const float4 a0 = __ldg(&aniso[2 * (size_t)j]);
+            if (l2 >= a0.w) continue;                    // |r| >= maxvalue * h
+            const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);
             const float tx = rx * a0.x + ry * a0.y + rz * a0.z;
-            const float ty = rx * a1.x + ry * a1.y + rz * a1.z;
-            const float tz = rx * a2.x + ry * a2.y + rz * a2.z;
+            const float ty = rx * a0.y + ry * a1.x + rz * a1.y;
+            const float tz = rx * a0.z + ry * a1.y + rz * a1.z;
             const float d2 = tx * tx + ty * ty + tz * tz;
             if (d2 >= 1.f) continue;
             const float x = 1.f - d2;
@@ -72,15 +72,25 @@ __device__ __forceinline__ float cell_sum(const uint2 ci, const float3 v, const 
     return sum;
 }
 
-__global__ void __launch_bounds__(kThreads) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
+// culling radius of one cell: maxvalue * h of its particles (anisotropic cells) or h
+__device__ __forceinline__ float cell_lim2(uint2 ci, const float* __restrict__ cell_rad, uint32_t c, const FieldParams& fp) {
+    if (!(ci.y & 0x80000000u)) return fp.r_iso2;
+    const float r = __ldg(&cell_rad[c]) * fp.grow;
+    return r * r;
+}
+
+__global__ void __launch_bounds__(kThreads, 8) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
                                                     const uint32_t* __restrict__ vlist, const uint2* __restrict__ cell_info,
-                                                    const float4* __restrict__ spos, const float4* __restrict__ aniso,
-                                                    float* __restrict__ field) {
+                                                    const float* __restrict__ cell_rad, const float4* __restrict__ spos,
+                                                    const float4* __restrict__ aniso, float* __restrict__ field) {
     const uint32_t nv = cnt->nv;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], srxy = g.spres[0] * g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
     const float pad = 1e-4f * g.sp_cs;
+    // largest support of any particle this frame
+    const float rmax = fmaxf(__uint_as_float(cnt->rad_max_bits), fp.h) * fp.grow;
+    const float rmax2 = rmax * rmax;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x) {
         const uint32_t id = vlist[t];
         const uint32_t iz = id / rxy, rem = id - iz * rxy, iy = rem / rx, ix = rem - iy * rx;
@@ -90,30 +100,28 @@ __global__ void __launch_bounds__(kThreads) k_field(KGrid g, FieldParams fp, con
         box_clamp(g, c, e2, lo, hi);
         float sum = 0.f;
         for (uint32_t z = lo.z; z < hi.z; ++z) {
-            const float z0 = g.min_pos[2] + (float)z * g.sp_cs;
-            const float gz = gap2_axis(v.z, z0, g.sp_cs, pad);
-            if (gz >= fp.r_aniso2) continue;
+            const float gz = gap2_axis(v.z, g.min_pos[2] + (float)z * g.sp_cs, g.sp_cs, pad);
+            if (gz >= rmax2) continue;
             for (uint32_t y = lo.y; y < hi.y; ++y) {
-                const float y0 = g.min_pos[1] + (float)y * g.sp_cs;
-                const float gyz = gz + gap2_axis(v.y, y0, g.sp_cs, pad);
-                if (gyz >= fp.r_aniso2) continue;
+                const float gyz = gz + gap2_axis(v.y, g.min_pos[1] + (float)y * g.sp_cs, g.sp_cs, pad);
+                if (gyz >= rmax2) continue;
                 const uint32_t row = z * srxy + y * srx;
                 if (sum > fp.thr) {
                     // threshold crossed: the reference adds this row's first cell, then breaks
-                    const float gx = gyz + gap2_axis(v.x, g.min_pos[0] + (float)lo.x * g.sp_cs, g.sp_cs, pad);
-                    if (lo.x < hi.x && gx < fp.r_aniso2) {
-                        const uint2 ci = __ldg(&cell_info[row + lo.x]);
-                        const float lim = (ci.y & 0x80000000u) ? fp.r_aniso2 : fp.r_iso2;
-                        if (gx < lim) sum = cell_sum(ci, v, fp, spos, aniso, sum);
+                    if (lo.x < hi.x) {
+                        const float gx = gyz + gap2_axis(v.x, g.min_pos[0] + (float)lo.x * g.sp_cs, g.sp_cs, pad);
+                        if (gx < rmax2) {
+                            const uint2 ci = __ldg(&cell_info[row + lo.x]);
+                            if (gx < cell_lim2(ci, cell_rad, row + lo.x, fp)) sum = cell_sum(ci, v, fp, spos, aniso, sum);
+                        }
                     }
                     continue;
                 }
                 for (uint32_t x = lo.x; x < hi.x; ++x) {
                     const float gx = gyz + gap2_axis(v.x, g.min_pos[0] + (float)x * g.sp_cs, g.sp_cs, pad);
-                    if (gx >= fp.r_aniso2) continue;
+                    if (gx >= rmax2) continue;
                     const uint2 ci = __ldg(&cell_info[row + x]);
-                    const float lim = (ci.y & 0x80000000u) ? fp.r_aniso2 : fp.r_iso2;
-                    if (gx >= lim) continue;
+                    if ((ci.y & 0x7fffffffu) == 0 || gx >= cell_lim2(ci, cell_rad, row + x, fp)) continue;
                     sum = cell_sum(ci, v, fp, spos, aniso, sum);
                     if (sum > fp.thr) break;
                 }
@@ -133,14 +141,13 @@ pms_status launch_field(pms_ctx* ctx) {
     fp.inv_h2 = inv * inv;
     fp.c_iso = kSigma * (inv * inv * inv);
     fp.thr = 2.f * P.iso_value;
-    // largest support: maxvalue <= 4^(2/3) after the eigenvalue clamp
-    const float ra = 2.5198421f * 1.0001f * P.h, ri = 1.0001f * P.h;
-    fp.r_aniso2 = ra * ra;
+    fp.grow = 1.0001f;
+    const float ri = fp.grow * P.h;
     fp.r_iso2 = ri * ri;
     Counters* cnt = ctx->counters.as<Counters>();
     k_field<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
-        g, fp, cnt, ctx->vlist.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(),
-        ctx->aniso.as<float4>(), ctx->field.as<float>());
+        g, fp, cnt, ctx->vlist.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->cell_rad.as<float>(),
+        ctx->spos.as<float4>(), ctx->aniso.as<float4>(), ctx->field.as<float>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -186,7 +186,7 @@ pms_status launch_hash_sort(pms_ctx* ctx) {
         ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), g.sp_size, ctx->order.as<uint32_t>(),
         ctx->big_cells.as<uint32_t>(), cnt);
     PMS_LAUNCHED(ctx);
-    k_cell_sort_big<<<152, 1024, 0, ctx->stream>>>(ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
+    k_cell_sort_big<<<32, 1024, 0, ctx->stream>>>(ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
                                                    ctx->big_cells.as<uint32_t>(), cnt, ctx->order.as<uint32_t>());
     PMS_LAUNCHED(ctx);
     k_gather<<<gb, kThreads, 0, ctx->stream>>>(ctx->order.as<uint32_t>(), ctx->keys.as<uint32_t>(),

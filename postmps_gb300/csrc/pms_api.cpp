@@ -50,7 +50,7 @@ extern "C" uint64_t pms_kernel_launches(const pms_ctx* ctx) { return ctx ? ctx->
 static void release_all(pms_ctx* c) {
     DBuf* bufs[] = {&c->in_pos, &c->in_vel, &c->in_rho, &c->keys, &c->slot, &c->order, &c->skeys, &c->spos,
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
-                    &c->surf_start, &c->big_cells, &c->slist, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
+                    &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
                     &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
                     &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
@@ -131,7 +131,8 @@ static pms_status ensure_particles(pms_ctx* c, uint32_t n) {
     PMS_CUDA(c, c->svel.ensure(16 * N));
     PMS_CUDA(c, c->rho.ensure(4 * N));
     PMS_CUDA(c, c->slist.ensure(4 * N));
-    PMS_CUDA(c, c->aniso.ensure(48 * N));
+    PMS_CUDA(c, c->moments.ensure(48 * N));
+    PMS_CUDA(c, c->aniso.ensure(32 * N));
     PMS_CUDA(c, c->nrm4.ensure(16 * N));
     PMS_CUDA(c, c->mean4.ensure(16 * N));
     PMS_CUDA(c, c->gdebug.ensure(40 * N));
@@ -147,6 +148,7 @@ static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) {
     PMS_CUDA(c, c->cell_info.ensure(8 * S));
     PMS_CUDA(c, c->surf_count.ensure(4 * S));
     PMS_CUDA(c, c->surf_start.ensure(4 * S));
+    PMS_CUDA(c, c->cell_rad.ensure(4 * S));
     const size_t W = ((uint64_t)g.sc_size + 31) / 32 + 1;
     PMS_CUDA(c, c->bm0.ensure(4 * W));
     PMS_CUDA(c, c->bm.ensure(4 * W));

@@ -50,7 +50,8 @@ struct Counters {
     uint32_t n_old;         // live diffuse particles carried from the last frame
     uint32_t n_live;        // after delete/append
     uint32_t n_type[4];     // spray, foam, bubble, deleted
-    uint32_t pad[2];
+    uint32_t rad_max_bits;  // largest anisotropic support maxvalue * h (float bits)
+    uint32_t pad[1];
 };
 
 enum : uint32_t {
@@ -108,7 +109,7 @@ struct pms_ctx {
     pms::DBuf keys, slot, order, skeys, spos, svel, rho;
     pms::DBuf cell_count, cell_start, cell_info, surf_count, surf_start, big_cells;
     // anisotropy
-    pms::DBuf slist, aniso, nrm4, mean4, gdebug, nnb;
+    pms::DBuf slist, moments, aniso, nrm4, mean4, gdebug, nnb, cell_rad;
     // band
     pms::DBuf bm0, bm, wcount, wprefix, vlist;
     // field and marching cubes

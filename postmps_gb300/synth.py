@@ -68,23 +68,37 @@ def water_block(n: int = 64, spacing: float = 0.01, seed: int = 1):
 
 
 def crown_splash(n_slab=(200, 200, 40), spacing: float = 0.005, n_ring: int = 400_000, seed: int = 2,
-                 ring_seed: int = 3, t: float = 0.05):
-    """2M crown splash: a jittered pool slab plus a seeded ring launched
+                 ring_seed: int = 3, t: float = 0.05, radius: float = 0.3, layers: int = 10):
+    """2M crown splash: a jittered pool slab plus a seeded crown ring launched
     radially with speed ~ N(1.5, 0.3) m/s, advected ballistically for t seconds
-    under gravity -9.81 m/s^2 along z."""
+    under gravity -9.81 m/s^2 along z.
+
+    The ring is a cylindrical wall of `layers` radial layers at the lattice
+    spacing (SPH particle density, a few particles per cell), centred on the
+    slab and standing on its top; its particles fly outward and upward (the
+    tilt grows with height, as in a crown), each with its own speed."""
     nx, ny, nz = n_slab
     slab = lattice(nx, ny, nz, spacing, 0.1 * spacing, seed)
     cx, cy = nx * spacing / 2.0, ny * spacing / 2.0
     top = nz * spacing
-    u = uniform(ring_seed, 0, n_ring).astype(np.float64)
-    w = uniform(ring_seed, 1, n_ring).astype(np.float64)
-    v = uniform(ring_seed, 2, n_ring).astype(np.float64)
-    theta = 2.0 * np.pi * u
-    r0 = 0.2 * min(cx, cy) + 0.02 * (w - 0.5)
-    z0 = top + 0.01 * v
+    # wall lattice: (layer, angle, level) at spacing-sized steps
+    rs = radius + spacing * (np.arange(layers) + 0.5)
+    per_level = np.maximum(1, np.round(2.0 * np.pi * rs / spacing).astype(np.int64))
+    levels = int(np.ceil(n_ring / per_level.sum()))
+    lay = np.repeat(np.arange(layers), per_level)
+    ang = np.concatenate([np.arange(k) / k for k in per_level]) * 2.0 * np.pi
+    lay = np.tile(lay, levels)[:n_ring]
+    ang = np.tile(ang, levels)[:n_ring]
+    lev = np.repeat(np.arange(levels), per_level.sum())[:n_ring]
+    jit = (uniform(ring_seed, 0, 3 * n_ring).astype(np.float64).reshape(-1, 3) * 2.0 - 1.0) * 0.1 * spacing
+    r0 = rs[lay] + jit[:, 0]
+    theta = ang + jit[:, 1] / rs[lay]
+    z0 = top + spacing * (lev + 0.5) + jit[:, 2]
+    height = spacing * levels
     speed = 1.5 + 0.3 * normal(ring_seed, 3, n_ring).astype(np.float64)
-    up = 1.2 + 0.4 * uniform(ring_seed, 5, n_ring).astype(np.float64)
-    vx, vy, vz = speed * np.cos(theta), speed * np.sin(theta), up * speed
+    tilt = 0.4 + 0.8 * (z0 - top) / height
+    dn = np.sqrt(1.0 + tilt * tilt)
+    vx, vy, vz = speed * np.cos(theta) / dn, speed * np.sin(theta) / dn, speed * tilt / dn
     x = cx + r0 * np.cos(theta) + vx * t
     y = cy + r0 * np.sin(theta) + vy * t
     z = z0 + vz * t - 0.5 * 9.81 * t * t

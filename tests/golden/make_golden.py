@@ -88,6 +88,42 @@ def make(name: str) -> str:
     return path
 
 
+DIFFUSE_SEED = 4
+
+
+def diffuse_frames():
+    """Two frames of a 14^3 block stirred with random velocities (sigma 2.5 m/s):
+    frame 1 is frame 0 advected by v * 0.02 s, and carries frame 0's diffuse
+    particles.  Diffuse keys as the reference's bin/config.txt."""
+    pos0, _, rho = synth.water_block(14)
+    vel = (synth.normal(21, 0, 3 * len(pos0)).reshape(-1, 3) * 2.5).astype(np.float32)
+    pos1 = (pos0 + 0.02 * vel).astype(np.float32)
+    return [(pos0, vel, rho), (pos1, vel, rho)]
+
+
+def make_diffuse() -> str:
+    text = synth.config_text(**{"config.isdiffusegeneration": "true"})
+    with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+        f.write(text)
+        cfg_path = f.name
+    out = {"config": np.array(text), "seed": np.uint64(DIFFUSE_SEED)}
+    old = None
+    try:
+        for fr, (pos, vel, rho) in enumerate(diffuse_frames()):
+            R = O.ref_diffuse_frame(cfg_path, pos, vel, rho, True, old, DIFFUSE_SEED, fr)
+            assert R["rc"] == 0, R["rc"]
+            out[f"f{fr}_pos"], out[f"f{fr}_vel"], out[f"f{fr}_rho"] = pos, vel, rho
+            for k in ("perm", "free_list", "nrm", "pot", "num", "gen", "old_after", "live"):
+                out[f"f{fr}_{k}"] = R[k]
+            out[f"f{fr}_old_in"] = np.zeros((0, 8), np.float32) if old is None else old
+            old = R["live"]
+    finally:
+        os.unlink(cfg_path)
+    path = os.path.join(HERE, "diffuse_block14.npz")
+    np.savez_compressed(path, **out)
+    return path
+
+
 def main() -> int:
     O.build()
     if not O.ref_available():
@@ -96,6 +132,8 @@ def main() -> int:
     for name in CASES:
         p = make(name)
         print(f"{p}: {os.path.getsize(p) / 1024:.0f} KiB")
+    p = make_diffuse()
+    print(f"{p}: {os.path.getsize(p) / 1024:.0f} KiB")
     return 0
 
 

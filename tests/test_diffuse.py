@@ -1,0 +1,139 @@
+"""Diffuse (spray/foam/bubble) particles.
+
+CPU: the oracle is pinned to fixtures made by the reference's own diffuse
+kernels (tests/golden/make_golden.py, two frames, spawn uniforms injected):
+  free-surface list                exact
+  spawn counts from the reference's clamped potentials      exact
+  spawned particles (position, TTL, type) from its counts   exact; velocity 1e-5
+  advection of the previous frame's particles               exact
+  clamped potentials (float64 vs its float32)               1e-3 absolute
+GPU (through the C ABI), same frames:
+  free-surface count                exact
+  spawn counts from the GPU's own clamped potentials        exact (oracle)
+  spawned particles from the GPU's counts                   exact position/TTL/type, velocity 1e-5
+  advected particles from the GPU's previous live set       exact
+  potentials vs the reference fixtures                      1e-3 absolute
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+GPATH = os.path.join(GOLDEN, "diffuse_block14.npz")
+
+
+def golden():
+    z = np.load(GPATH)
+    d = {k: z[k] for k in z.files}
+    d["config"] = str(d["config"])
+    return d
+
+
+def sorted_frame(oracle, p, pos):
+    g = oracle.grid_from_positions(p, pos)
+    keys, perm, sk, start, end = oracle.hash_sort(p, g, pos)
+    surf, scan, slist = oracle.surface_particles(g, start, end)
+    return g, perm, start, end, slist
+
+
+@pytest.mark.parametrize("frame", [0, 1])
+def test_diffuse_oracle_matches_reference(oracle, frame):
+    d = golden()
+    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(d["config"])))
+    pos, vel = d[f"f{frame}_pos"], d[f"f{frame}_vel"]
+    g, perm, start, end, slist = sorted_frame(oracle, p, pos)
+    np.testing.assert_array_equal(perm, d[f"f{frame}_perm"])
+    np.testing.assert_array_equal(slist, d[f"f{frame}_free_list"])
+    spos, svel = pos[perm], vel[perm]
+    res = oracle.diffuse_frame(p, g, spos, svel, start, end, slist, np.zeros_like(spos, np.float64),
+                               int(d["seed"]), frame, old=d[f"f{frame}_old_in"], nrm_for_crests=d[f"f{frame}_nrm"],
+                               pot_clamped=d[f"f{frame}_pot"])
+    np.testing.assert_array_equal(res["num"], d[f"f{frame}_num"])
+    gen, rgen = res["gen"], d[f"f{frame}_gen"]
+    assert gen.shape == rgen.shape
+    np.testing.assert_array_equal(gen[:, [0, 1, 2, 6, 7]], rgen[:, [0, 1, 2, 6, 7]])
+    assert float(np.abs(gen[:, 3:6] - rgen[:, 3:6]).max(initial=0)) <= 1e-5 * max(1.0, float(np.abs(rgen[:, 3:6]).max(initial=0)))
+    np.testing.assert_array_equal(res["old_after"], d[f"f{frame}_old_after"])
+    # float64 potentials against the reference's float32 ones (clamped to [0, 1])
+    assert float(np.abs(res["pot"] - d[f"f{frame}_pot"]).max()) < 1e-3
+
+
+def run_gpu_frames(pms, tmp_config, d, frames=(0, 1)):
+    cfg = pms.load_config(tmp_config(d["config"]))
+    cfg.rng_seed = int(d["seed"])
+    out = []
+    with pms.Context(cfg, 0) as ctx:
+        for fr in frames:
+            ctx.upload(d[f"f{fr}_pos"], d[f"f{fr}_vel"], d[f"f{fr}_rho"])
+            ctx.run_frame()
+            c = ctx.counts().as_dict()
+            r = {"counts": c, "pot": ctx.debug("diffuse_potential"), "num": ctx.debug("diffuse_count"),
+                 "nrm": ctx.debug("free_normal"), "perm": ctx.debug("perm"), "live": ctx.diffuse_particles(-1),
+                 "launches": ctx.launches}
+            out.append(r)
+    return out
+
+
+def live_records(live: dict) -> np.ndarray:
+    return np.concatenate([live["pos"], live["vel"], live["ttl"][:, None].astype(np.float32),
+                           live["type"][:, None].astype(np.float32)], 1)
+
+
+@pytest.mark.gpu
+def test_diffuse_gpu_two_frames(pms_lib, oracle, tmp_config):
+    d = golden()
+    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(d["config"])))
+    gpu = run_gpu_frames(pms_lib, tmp_config, d)
+    prev_live = np.zeros((0, 8), np.float32)
+    for fr, r in enumerate(gpu):
+        pos, vel = d[f"f{fr}_pos"], d[f"f{fr}_vel"]
+        g, perm, start, end, slist = sorted_frame(oracle, p, pos)
+        np.testing.assert_array_equal(r["perm"], perm)
+        assert r["counts"]["n_free_surface"] == len(slist) == len(d[f"f{fr}_free_list"])
+        # potentials against the reference (float32 vs float32, different summation order)
+        assert float(np.abs(r["pot"] - d[f"f{fr}_pot"]).max()) < 1e-3
+        # counts: exact from the GPU's own clamped potentials
+        spos, svel = pos[perm], vel[perm]
+        res = oracle.diffuse_frame(p, g, spos, svel, start, end, slist, np.zeros_like(spos, np.float64),
+                                   int(d["seed"]), fr, old=prev_live, nrm_for_crests=r["nrm"], pot_clamped=r["pot"])
+        np.testing.assert_array_equal(r["num"], res["num"])
+        assert np.mean(r["num"] == d[f"f{fr}_num"]) > 0.99
+        assert r["counts"]["n_generated_diffuse"] == int(np.clip(res["num"], 0, None).sum())
+        # live particles: generated (from the GPU's counts) then advected old ones, type 3 dropped
+        live = live_records(r["live"])
+        want = res["live"]
+        assert live.shape == want.shape, (live.shape, want.shape)
+        np.testing.assert_array_equal(live[:, [0, 1, 2, 6, 7]], want[:, [0, 1, 2, 6, 7]])
+        assert float(np.abs(live[:, 3:6] - want[:, 3:6]).max(initial=0)) <= 1e-5 * max(1.0, float(np.abs(want[:, 3:6]).max(initial=0)))
+        assert r["counts"]["n_diffuse"] == len(live)
+        t = want[:, 7].astype(int)
+        assert (r["counts"]["n_spray"], r["counts"]["n_foam"], r["counts"]["n_bubble"]) == \
+            (int((t == 0).sum()), int((t == 1).sum()), int((t == 2).sum()))
+        prev_live = live
+
+
+@pytest.mark.gpu
+def test_diffuse_files_written(pms_lib, tmp_path):
+    from postmps_gb300 import synth
+    d = golden()
+    frames = tmp_path / "frames"
+    frames.mkdir()
+    for fr in (0, 1):
+        pms_lib.write_vtk(str(frames / f"PartFluid_{fr:04d}.vtk"), d[f"f{fr}_pos"], d[f"f{fr}_vel"], d[f"f{fr}_rho"])
+    text = synth.config_text(**{"config.isdiffusegeneration": "true", "config.framefrom": 0, "config.frameto": 1,
+                                "config.fluidpath": str(frames), "config.surfacepath": str(tmp_path),
+                                "config.diffusepath": str(tmp_path), "config.surfaceprefix": "PartSurface_"})
+    cfg = tmp_path / "config.txt"
+    cfg.write_text(text)
+    pms_lib.run_config(str(cfg))
+    for fr in (0, 1):
+        assert (tmp_path / f"PartSurface_{fr:04d}.ply").exists()
+        for pre in ("PartSpary_", "PartFoam_", "PartBubble_"):
+            p = tmp_path / f"{pre}{fr:04d}.vtk"
+            assert p.exists()
+            pos, vel, _ = pms_lib.read_vtk(str(p))
+            assert pos.shape[1] == 3
