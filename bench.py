@@ -208,14 +208,22 @@ def run_pms(args) -> None:
         ctx.upload_device(d_pos.data_ptr(), d_vel.data_ptr(), d_rho.data_ptr(), n)
         ctx.run_frame()
 
-    mesh_host = [None]
+    mesh_host = {}
 
     def step_e2e():
+        # the user's calls: upload from pinned host memory, reconstruct, read the
+        # triangle soup (and the live diffuse particles) back into pinned memory
         ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
         ctx.run_frame()
-        mesh_host[0] = ctx.mesh(normals=False)[0]
+        import ctypes as C
+        nv = C.c_uint64()
+        pms.lib().pms_download_mesh(ctx.handle, None, None, 0, C.byref(nv))
+        buf = mesh_host.get("mesh")
+        if buf is None or buf.numel() < 3 * nv.value:
+            buf = mesh_host["mesh"] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
+        ctx._call("pms_download_mesh", buf.data_ptr(), None, buf.numel() // 3, C.byref(nv))
         if cfg.is_diffuse:
-            mesh_host.append(ctx.diffuse_particles(-1))
+            mesh_host["diffuse"] = ctx.diffuse_particles(-1)
 
     for _ in range(args.warmup):
         step_device()

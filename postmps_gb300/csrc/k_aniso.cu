@@ -29,59 +29,46 @@ struct AnisoParams {
     double cond_limit;
 };
 
-// Gap test: does the box of spatial cell (x,y,z) come within sqrt(r2) of p?
-// The box is widened by `pad` so that particles whose key rounded into the
-// cell from just outside are still covered.
-__device__ __forceinline__ float cell_gap2(const KGrid& g, float3 p, uint32_t x, uint32_t y, uint32_t z, float pad) {
-    float x0 = g.min_pos[0] + (float)x * g.sp_cs - pad, x1 = x0 + g.sp_cs + 2.f * pad;
-    float y0 = g.min_pos[1] + (float)y * g.sp_cs - pad, y1 = y0 + g.sp_cs + 2.f * pad;
-    float z0 = g.min_pos[2] + (float)z * g.sp_cs - pad, z1 = z0 + g.sp_cs + 2.f * pad;
-    float dx = axis_gap(p.x, x0, x1), dy = axis_gap(p.y, y0, y1), dz = axis_gap(p.z, z0, z1);
-    return dx * dx + dy * dy + dz * dz;
-}
-
 // ---------------------------------------------------------------------------
 // density (calculationOfDensity): rho_i = sum_j sigma/h^3 (1 - (d/h)^2)^3, d < h,
 // over cells [c - e, c + e]; also stores m / rho into spos.w for the field.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
-                                                      const uint2* __restrict__ cell_info, float4* __restrict__ spos,
+__global__ void __launch_bounds__(kThreads, 8) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
+                                                      const uint32_t* __restrict__ cell_start, float4* __restrict__ spos,
                                                       float* __restrict__ rho, uint32_t n) {
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
     const float pad = 1e-4f * g.sp_cs;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float4 pi4 = spos[i];
-        float3 p = make_float3(pi4.x, pi4.y, pi4.z);
-        uint32_t key = skeys[i];
-        uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
+        const float4 pi4 = spos[i];
+        const float3 p = make_float3(pi4.x, pi4.y, pi4.z);
+        const uint32_t key = skeys[i];
+        const uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
         uint3 lo, hi;
         box_clamp(g, c, (uint32_t)g.spexpand, lo, hi);
+        hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
         float w = 0.f;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    if (cell_gap2(g, p, x, y, z, pad) >= ap.h_sq) continue;
-                    uint2 ci = cell_info[z * rxy + y * rx + x];
-                    uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        float4 q = spos[j];
-                        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                        float d2 = dx * dx + dy * dy + dz * dz;
-                        if (d2 < ap.h_sq) {
-                            float s = 1.f - d2 * ap.inv_h2;
-                            w += ap.kdens * s * s * s;
-                        }
-                    }
-                }
+        row_walk(g, p, lo, hi, ap.h_sq, pad, cell_start, [&](uint32_t j) {
+            const float4 q = __ldg(&spos[j]);
+            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float s = 1.f - d2 * ap.inv_h2;
+            w += (d2 < ap.h_sq) ? ap.kdens * s * s * s : 0.f;   // + 0 leaves the sum unchanged
+        });
         rho[i] = w;
     }
 }
 
+// m / rho into spos.w (0 for rho == 0: the field skips such particles), and the
+// isotropic kernel of every particle in the field's packed form,
+// G = I / h, h_s^2 = h^2, sigma * det(G) = sigma / h^3; the anisotropy pass
+// overwrites the surface particles' entries.
 __global__ void __launch_bounds__(kThreads) k_inv_density(float4* __restrict__ spos, const float* __restrict__ rho,
-                                                          float mass, uint32_t n) {
+                                                          float4* __restrict__ aniso, AnisoParams ap, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float r = rho[i];
-        spos[i].w = r == 0.f ? 0.f : mass / r;   // particles with rho == 0 are skipped by the field
+        const float r = rho[i];
+        spos[i].w = r == 0.f ? 0.f : ap.mass / r;
+        aniso[2 * (size_t)i + 0] = make_float4(ap.h_inv, 0.f, 0.f, ap.h_sq);
+        aniso[2 * (size_t)i + 1] = make_float4(ap.h_inv, 0.f, ap.h_inv, ap.kdens);
     }
 }
 
@@ -161,7 +148,7 @@ __device__ __forceinline__ void eig_sym3(T a[3][3], T e[3], T v[3][3], T tol) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 8) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
                                                       const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
-                                                      const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                      const uint32_t* __restrict__ cell_start, const float4* __restrict__ spos,
                                                       float4* __restrict__ mom) {
     const uint32_t ns = cnt->ns;
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
@@ -176,32 +163,24 @@ __global__ void __launch_bounds__(kThreads, 8) k_moments(KGrid g, AnisoParams ap
         const uint3 c = make_uint3(key % rx, (key / rx) % g.spres[1], key / rxy);
         uint3 lo, hi;
         box_clamp(g, c, 2u * (uint32_t)g.spexpand, lo, hi);
+        hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
         float s0 = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
         float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f, szz = 0.f;
         uint32_t nn = 0;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    if (cell_gap2(g, p, x, y, z, pad) >= r2h_sq) continue;
-                    const uint2 ci = __ldg(&cell_info[z * rxy + y * rx + x]);
-                    const uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        const float4 q = __ldg(&spos[j]);
-                        // |u| rounded operation by operation, as the reference's neighbour count sees it
-                        const float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
-                        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
-                        const float d = __fsqrt_rn(d2);
-                        nn += (d <= ap.h) ? 1u : 0u;
-                        if (d < ap.r2h) {
-                            const float t = d * inv_r2h;
-                            const float w = 1.f - t * t * t;
-                            const float wx = w * ux, wy = w * uy, wz = w * uz;
-                            s0 += w; sx += wx; sy += wy; sz += wz;
-                            sxx += wx * ux; sxy += wx * uy; sxz += wx * uz;
-                            syy += wy * uy; syz += wy * uz; szz += wz * uz;
-                        }
-                    }
-                }
+        row_walk(g, p, lo, hi, r2h_sq, pad, cell_start, [&](uint32_t j) {
+            const float4 q = __ldg(&spos[j]);
+            // |u| rounded operation by operation, as the reference's neighbour count sees it
+            const float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
+            const float d = __fsqrt_rn(d2);
+            nn += (d <= ap.h) ? 1u : 0u;
+            const float t = d * inv_r2h;
+            const float w = (d < ap.r2h) ? 1.f - t * t * t : 0.f;   // zero weight adds exactly nothing
+            const float wx = w * ux, wy = w * uy, wz = w * uz;
+            s0 += w; sx += wx; sy += wy; sz += wz;
+            sxx += wx * ux; sxy += wx * uy; sxz += wx * uz;
+            syy += wy * uy; syz += wy * uz; szz += wz * uz;
+        });
         mom[3 * (size_t)s + 0] = make_float4(s0, sx, sy, sz);
         mom[3 * (size_t)s + 1] = make_float4(sxx, sxy, sxz, syy);
         mom[3 * (size_t)s + 2] = make_float4(syz, szz, __uint_as_float(nn), 0.f);
@@ -311,13 +290,14 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     ap.cond_limit = ctx->cfg.fp64_svd_cond;
     Counters* cnt = ctx->counters.as<Counters>();
     k_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ap, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->rho.as<float>(), ctx->n);
+        g, ap, ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->rho.as<float>(), ctx->n);
     PMS_LAUNCHED(ctx);
-    k_inv_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(), P.mass, ctx->n);
+    k_inv_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(),
+                                                                           ctx->aniso.as<float4>(), ap, ctx->n);
     PMS_LAUNCHED(ctx);
     // ns is on the device; grids are sized by the particle count (an upper bound)
     k_moments<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->cell_info.as<uint2>(),
+        g, ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
         ctx->spos.as<float4>(), ctx->moments.as<float4>());
     PMS_LAUNCHED(ctx);
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->cell_rad.p, 0, sizeof(float) * (size_t)g.sp_size, ctx->stream));

@@ -84,6 +84,54 @@ __device__ __forceinline__ float from_ordered_bits(uint32_t u) {
     return __uint_as_float(b);
 }
 
+// Squared distance from p to the box of spatial cell (x, y, z), the box widened
+// by `pad` so particles whose key rounded into the cell from just outside are
+// still covered.
+__device__ __forceinline__ float cell_gap2(const KGrid& g, float3 p, uint32_t x, uint32_t y, uint32_t z, float pad) {
+    const float x0 = g.min_pos[0] + (float)x * g.sp_cs - pad, x1 = x0 + g.sp_cs + 2.f * pad;
+    const float y0 = g.min_pos[1] + (float)y * g.sp_cs - pad, y1 = y0 + g.sp_cs + 2.f * pad;
+    const float z0 = g.min_pos[2] + (float)z * g.sp_cs - pad, z1 = z0 + g.sp_cs + 2.f * pad;
+    const float dx = axis_gap(p.x, x0, x1), dy = axis_gap(p.y, y0, y1), dz = axis_gap(p.z, z0, z1);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// Row-segment neighbour walk of one point.  Cells are sorted by key and key =
+// (z * res_y + y) * res_x + x, so the cells x in [xa, xb) of one row hold the
+// contiguous particle range [cell_start[row + xa], cell_start[row + xb]).  For
+// each row (z, y) of the window [lo, hi) (hi exclusive) that comes within
+// sqrt(r2) of p, the x range is cut to the cells the sphere can reach
+// (conservatively: a spare cell costs only the per-particle test) and body(j)
+// runs over the range, in the reference's z, y, x, particle order.
+// cell_start must have sp_size + 1 entries.
+template <class Body>
+__device__ __forceinline__ void row_walk(const KGrid& g, float3 p, uint3 lo, uint3 hi, float r2, float pad,
+                                         const uint32_t* __restrict__ cell_start, Body&& body) {
+    const uint32_t srx = g.spres[0], srxy = g.spres[0] * g.spres[1];
+    const float cs = g.sp_cs, inv = 1.f / g.sp_cs;
+    for (uint32_t z = lo.z; z < hi.z; ++z) {
+        const float z0 = g.min_pos[2] + (float)z * cs;
+        const float gz0 = axis_gap(p.z, z0 - pad, z0 + cs + pad);
+        const float gz = gz0 * gz0;
+        if (gz >= r2) continue;
+        for (uint32_t y = lo.y; y < hi.y; ++y) {
+            const float y0 = g.min_pos[1] + (float)y * cs;
+            const float gy0 = axis_gap(p.y, y0 - pad, y0 + cs + pad);
+            const float gyz = gz + gy0 * gy0;
+            if (gyz >= r2) continue;
+            const float dx = sqrtf(r2 - gyz) + 2.f * pad;
+            int xa = (int)floorf((p.x - dx - g.min_pos[0]) * inv) - 1;
+            int xb = (int)floorf((p.x + dx - g.min_pos[0]) * inv) + 2;
+            xa = max(xa, (int)lo.x);
+            xb = min(xb, (int)hi.x);
+            if (xa >= xb) continue;
+            const uint32_t row = z * srxy + y * srx;
+            const uint32_t ja = __ldg(&cell_start[row + (uint32_t)xa]), jb = __ldg(&cell_start[row + (uint32_t)xb]);
+#pragma unroll 2
+            for (uint32_t j = ja; j < jb; ++j) body(j);
+        }
+    }
+}
+
 // rank of bit `id` among set bits of a bitmap with exclusive word prefix sums
 __device__ __forceinline__ uint32_t bit_rank(const uint32_t* bm, const uint32_t* wprefix, uint32_t id) {
     uint32_t w = id >> 5, b = id & 31u;

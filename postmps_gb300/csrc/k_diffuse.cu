@@ -95,34 +95,31 @@ __global__ void __launch_bounds__(256) k_df_freelist(const uint32_t* __restrict_
 
 // calculationofNormal: thread t < NumFree computes the normal of particle t
 __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
-                                                        const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
-                                                        uint32_t n, float4* __restrict__ nrm) {
+                                                        const uint32_t* __restrict__ cell_start,
+                                                        const float4* __restrict__ spos, uint32_t n,
+                                                        float4* __restrict__ nrm) {
     const uint32_t nf = min(cnt->n_free, n);
-    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    const float pad = 1e-4f * g.sp_cs, r2 = dp.hd_sq;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
-        const float4 p = spos[t];
+        const float4 p4 = spos[t];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
         uint3 lo, hi;
         diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
         float nx = 0.f, ny = 0.f, nz = 0.f;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    const uint2 ci = cell_info[z * rxy + y * rx + x];
-                    const uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        const float4 q = spos[j];
-                        const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
-                        const float mp2 = sx * sx + sy * sy + sz * sz;
-                        const float mp = sqrtf(mp2);
-                        const float qq = mp / dp.hd;
-                        if (qq > 0.f && qq < 1.f) {
-                            const float d = dp.hd_sq - mp2;
-                            const float derivative = d * d * 6.f;
-                            const float c = dp.coefficient / mp * derivative;
-                            nx += c * sx; ny += c * sy; nz += c * sz;
-                        }
-                    }
-                }
+        row_walk(g, p, lo, hi, r2, pad, cell_start, [&](uint32_t j) {
+            const float4 q = __ldg(&spos[j]);
+            const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
+            const float mp2 = sx * sx + sy * sy + sz * sz;
+            const float mp = sqrtf(mp2);
+            const float qq = mp / dp.hd;
+            if (qq > 0.f && qq < 1.f) {
+                const float d = dp.hd_sq - mp2;
+                const float derivative = d * d * 6.f;
+                const float c = dp.coefficient / mp * derivative;
+                nx += c * sx; ny += c * sy; nz += c * sz;
+            }
+        });
         const float mn2 = nx * nx + ny * ny + nz * nz;
         if ((double)mn2 < kEps) continue;              // keeps the previous normal
         const float inv = 1.f / sqrtf(mn2);
@@ -134,38 +131,34 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParam
 // potentials
 // ---------------------------------------------------------------------------
 // calculationofTrappedairpotential: every particle
-__global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffuseParams dp, const uint2* __restrict__ cell_info,
+__global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffuseParams dp, const uint32_t* __restrict__ cell_start,
                                                          const float4* __restrict__ spos, const float4* __restrict__ svel,
                                                          uint32_t n, float4* __restrict__ pot) {
-    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    const float pad = 1e-4f * g.sp_cs, r2 = dp.hd_sq;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 p = spos[i], v = svel[i];
+        const float4 p4 = spos[i], v = svel[i];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
         uint3 lo, hi;
         diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
         float ita = 0.f;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    const uint2 ci = cell_info[z * rxy + y * rx + x];
-                    const uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        const float4 q = spos[j];
-                        const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
-                        const float mp = sqrtf(sx * sx + sy * sy + sz * sz);
-                        if ((double)mp > kEps && mp <= dp.hd) {
-                            const float4 w = svel[j];
-                            const float ux = v.x - w.x, uy = v.y - w.y, uz = v.z - w.z;
-                            float mv = ux * ux + uy * uy + uz * uz;
-                            if ((double)mv > kEps) {
-                                mv = sqrtf(mv);
-                                const float qq = mp / dp.hd;
-                                const float e = 1.f - (ux / mv * (sx / mp) + uy / mv * (sy / mp) + uz / mv * (sz / mp));
-                                const float wgt = 1.f - qq;
-                                ita += mv * e * wgt;
-                            }
-                        }
-                    }
+        row_walk(g, p, lo, hi, r2, pad, cell_start, [&](uint32_t j) {
+            const float4 q = __ldg(&spos[j]);
+            const float4 w = __ldg(&svel[j]);
+            const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
+            const float mp = sqrtf(sx * sx + sy * sy + sz * sz);
+            if ((double)mp > kEps && mp <= dp.hd) {
+                const float ux = v.x - w.x, uy = v.y - w.y, uz = v.z - w.z;
+                float mv = ux * ux + uy * uy + uz * uz;
+                if ((double)mv > kEps) {
+                    mv = sqrtf(mv);
+                    const float qq = mp / dp.hd;
+                    const float e = 1.f - (ux / mv * (sx / mp) + uy / mv * (sy / mp) + uz / mv * (sz / mp));
+                    const float wgt = 1.f - qq;
+                    ita += mv * e * wgt;
                 }
+            }
+        });
         pot[i].y = ita;
         pot[i].z = (float)(0.5 * (double)dp.mass * (double)(v.x * v.x + v.y * v.y + v.z * v.z));
     }
@@ -173,14 +166,16 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
 
 // calculationofWavecrests: free-surface particles
 __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
-                                                        const uint32_t* __restrict__ freelist, const uint2* __restrict__ cell_info,
+                                                        const uint32_t* __restrict__ freelist,
+                                                        const uint32_t* __restrict__ cell_start,
                                                         const float4* __restrict__ spos, const float4* __restrict__ svel,
                                                         const float4* __restrict__ nrm, float4* __restrict__ pot) {
     const uint32_t nf = cnt->n_free;
-    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+    const float pad = 1e-4f * g.sp_cs, r2 = dp.hd_sq;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x) {
         const uint32_t i = freelist[t];
-        const float4 p = spos[i], v = svel[i], ni = nrm[i];
+        const float4 p4 = spos[i], v = svel[i], ni = nrm[i];
+        const float3 p = make_float3(p4.x, p4.y, p4.z);
         const float nn = dot_rn(ni.x, ni.y, ni.z, ni.x, ni.y, ni.z);
         const float vv = dot_rn(v.x, v.y, v.z, v.x, v.y, v.z);
         if ((double)nn <= kEps || (double)vv <= kEps || (double)dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < 0.6) {
@@ -189,31 +184,26 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
         }
         uint3 lo, hi;
         diffuse_box(g, p.x, p.y, p.z, lo, hi);
+        hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
         float wc = 0.f;
-        for (uint32_t z = lo.z; z <= hi.z; ++z)
-            for (uint32_t y = lo.y; y <= hi.y; ++y)
-                for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                    const uint2 ci = cell_info[z * rxy + y * rx + x];
-                    const uint32_t m = ci.y & 0x7fffffffu;
-                    for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                        const float4 nj = nrm[j];
-                        if ((double)dot_rn(nj.x, nj.y, nj.z, nj.x, nj.y, nj.z) <= kEps) continue;
-                        const float4 q = spos[j];
-                        // crests2p: x_ji = normalize(x_j - x_i); counts if x_ji . n_i < -eps
-                        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-                        const float l2 = dx * dx + dy * dy + dz * dz;
-                        if (l2 == 0.f) continue;                 // normalize(0) is NaN: contributes 0
-                        const float il = 1.f / sqrtf(l2);
-                        const float c = (dx * il) * ni.x + (dy * il) * ni.y + (dz * il) * ni.z;
-                        if ((double)c < -kEps) {
-                            // curvature2p: (1 - n_i . n_j) * Weend(x_i - x_j, h)
-                            const float e1 = 1.f - (ni.x * nj.x + ni.y * nj.y + ni.z * nj.z);
-                            const float mx = sqrtf(l2);
-                            const float w = (mx <= dp.hd && mx > 0.f) ? (float)(1.0 - (double)(mx / dp.hd)) : 0.f;
-                            wc += e1 * w;
-                        }
-                    }
-                }
+        row_walk(g, p, lo, hi, r2, pad, cell_start, [&](uint32_t j) {
+            const float4 nj = __ldg(&nrm[j]);
+            const float4 q = __ldg(&spos[j]);
+            if ((double)dot_rn(nj.x, nj.y, nj.z, nj.x, nj.y, nj.z) <= kEps) return;
+            // crests2p: x_ji = normalize(x_j - x_i); counts if x_ji . n_i < -eps
+            const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+            const float l2 = dx * dx + dy * dy + dz * dz;
+            if (l2 == 0.f) return;                      // normalize(0) is NaN: contributes 0
+            const float il = 1.f / sqrtf(l2);
+            const float c = (dx * il) * ni.x + (dy * il) * ni.y + (dz * il) * ni.z;
+            if ((double)c < -kEps) {
+                // curvature2p: (1 - n_i . n_j) * Weend(x_i - x_j, h)
+                const float e1 = 1.f - (ni.x * nj.x + ni.y * nj.y + ni.z * nj.z);
+                const float mx = sqrtf(l2);
+                const float w = (mx <= dp.hd && mx > 0.f) ? (float)(1.0 - (double)(mx / dp.hd)) : 0.f;
+                wc += e1 * w;
+            }
+        });
         pot[i].x = wc;
     }
 }
@@ -471,14 +461,14 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     k_df_freelist<<<gb, 256, 0, ctx->stream>>>(ctx->d_isfree.as<uint32_t>(), ctx->d_freescan.as<uint32_t>(), n,
                                                ctx->d_freelist.as<uint32_t>());
     PMS_LAUNCHED(ctx);
-    k_df_normal<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), n,
+    k_df_normal<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), n,
                                                   ctx->d_nrm_free.as<float4>());
     PMS_LAUNCHED(ctx);
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->d_pot.p, 0, 16 * N, ctx->stream));
-    k_df_trapped<<<gk, kThreads, 0, ctx->stream>>>(g, dp, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(),
+    k_df_trapped<<<gk, kThreads, 0, ctx->stream>>>(g, dp, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(),
                                                    ctx->svel.as<float4>(), n, ctx->d_pot.as<float4>());
     PMS_LAUNCHED(ctx);
-    k_df_crests<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->d_freelist.as<uint32_t>(), ctx->cell_info.as<uint2>(),
+    k_df_crests<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->d_freelist.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
                                                   ctx->spos.as<float4>(), ctx->svel.as<float4>(),
                                                   ctx->d_nrm_free.as<float4>(), ctx->d_pot.as<float4>());
     PMS_LAUNCHED(ctx);

@@ -177,7 +177,10 @@ pms_status launch_hash_sort(pms_ctx* ctx) {
     k_hash_count<<<gb, kThreads, 0, ctx->stream>>>(g, ctx->in_pos.as<float>(), n, ctx->keys.as<uint32_t>(),
                                                    ctx->slot.as<uint32_t>(), ctx->cell_count.as<uint32_t>(), cnt);
     PMS_LAUNCHED(ctx);
-    pms_status st = scan_u32(ctx, ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), g.sp_size, nullptr);
+    // cell_start[c + 1] - cell_start[c] is cell c's count for every c, and cell_start[sp_size] = n,
+    // so the cells of a row segment form one contiguous particle range
+    pms_status st = scan_u32(ctx, ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), g.sp_size,
+                             ctx->cell_start.as<uint32_t>() + g.sp_size);
     if (st != PMS_OK) return st;
     k_scatter<<<gb, kThreads, 0, ctx->stream>>>(ctx->keys.as<uint32_t>(), ctx->slot.as<uint32_t>(),
                                                 ctx->cell_start.as<uint32_t>(), n, ctx->order.as<uint32_t>());

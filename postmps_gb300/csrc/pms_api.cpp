@@ -144,7 +144,7 @@ static pms_status ensure_particles(pms_ctx* c, uint32_t n) {
 static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) {
     const size_t S = g.sp_size ? g.sp_size : 1;
     PMS_CUDA(c, c->cell_count.ensure(4 * S));
-    PMS_CUDA(c, c->cell_start.ensure(4 * S));
+    PMS_CUDA(c, c->cell_start.ensure(4 * (S + 1)));   // cell_start[S] = n
     PMS_CUDA(c, c->cell_info.ensure(8 * S));
     PMS_CUDA(c, c->surf_count.ensure(4 * S));
     PMS_CUDA(c, c->surf_start.ensure(4 * S));
