@@ -1,12 +1,26 @@
 """Benchmark: particles/s of the particle-to-surface pipeline on one GB300.
 
-Workload (default): the 2M-particle crown splash -- a 200x200x40 jittered
-pool slab (lattice 0.005) plus a seeded 400k-particle ring launched radially
-at N(1.5, 0.3) m/s and advected 0.05 s; h = 0.01, scalar-grid cell 0.0025,
-iso 0.5, synthetic (seeded) data.  A step is one frame: the inputs are copied
-into the context (device to device for `value`, pinned host to device for
-`e2e`), then hashing, anisotropy, narrow band, field and marching cubes run;
-e2e also reads the mesh back to the host.  L2 is flushed (a 256 MiB write)
+Workloads (seeded synthetic data; --workload):
+  crown    (default) the 2M-particle crown splash -- a 200x200x40 jittered pool
+           slab (lattice 0.005) plus a seeded 400k-particle ring launched
+           radially at N(1.5, 0.3) m/s and advected 0.05 s; h = 0.01, scalar
+           cell 0.0025, iso 0.5, diffuse generation on.  A step is one frame.
+  block    the 262,144-particle water block (64^3, spacing 0.01), diffuse off.
+  slosh16  16 sloshing-tank frames of 100k-1.5M particles (14.3M in all),
+           spacing 0.01, reconstructed by one pms_run_batch call (one CUDA
+           graph launch); a step is the whole batch.
+  dam      the 8M-particle dam break (400x100x200, spacing 0.005), diffuse off.
+
+Bands (--band): "learned" runs the learned narrow band with its exact
+border-check fallback, "plain" the reference's band; the default runs both on
+the same frames, reports the learned arm as the headline (when a trained model
+is present) and the plain arm beside it, and judges the learned mesh against
+the plain mesh (triangle-count delta, Hausdorff distance in units of h).
+
+`value` is measured with the inputs already on the device (device-to-device
+upload inside the step); `e2e` goes through the C ABI from pinned host
+buffers and reads the triangle soup (and live diffuse particles) back into
+pinned host memory inside the timed region.  L2 is flushed (a 256 MiB write)
 between timed steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pms|reference]
@@ -16,11 +30,12 @@ oracle, OpenMP over all host cores) on a bounded sample of the same frame:
 the reference itself has no CPU implementation of this path and its CUDA
 sources do not build with this toolchain.
 Multi-GPU runs (torchrun) are frame-level replicas: each rank reconstructs its
-own frame, no collective touches the data path ("scaling": "weak").
+own frames, no collective touches the data path ("scaling": "weak").
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -37,22 +52,36 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particles/s end-to-end, plain vs learned-band, at <=0.05h Hausdorff vs FP64"
 UNIT = "particles/s"
+STAGES = ("grid", "anisotropy", "band", "field", "marching_cubes", "diffuse")
 
 
 def workload(name: str):
+    """(frames, keys, description, diffuse): frames is a list of (pos, vel, rho)."""
     from postmps_gb300 import synth
     if name == "crown":
-        pos, vel, rho = synth.crown_splash()
+        frames = [synth.crown_splash()]
         keys = {"sim.particlespacing": 0.005}
-        desc = {"workload": "crown_splash_2M", "particles": int(len(pos)), "h": 0.01, "grid_cell": 0.0025,
+        desc = {"workload": "crown_splash_2M", "particles": int(len(frames[0][0])), "h": 0.01, "grid_cell": 0.0025,
                 "iso": 0.5, "clamp_ratio": 4}
-    elif name == "block":
-        pos, vel, rho = synth.water_block(64)
-        keys = {}
-        desc = {"workload": "water_block_262k", "particles": int(len(pos)), "h": 0.02, "grid_cell": 0.005, "iso": 0.5}
-    else:
-        raise SystemExit(f"unknown workload {name}")
-    return pos, vel, rho, keys, desc
+        return frames, keys, desc, True
+    if name == "block":
+        frames = [synth.water_block(64)]
+        desc = {"workload": "water_block_262k", "particles": int(len(frames[0][0])), "h": 0.02, "grid_cell": 0.005,
+                "iso": 0.5}
+        return frames, {}, desc, False
+    if name == "slosh16":
+        frames = [synth.sloshing_tank(k, 16) for k in range(16)]
+        ns = [len(f[0]) for f in frames]
+        desc = {"workload": "sloshing_tank_16_frames", "frames": 16, "particles": int(sum(ns)),
+                "particles_per_frame": [min(ns), max(ns)], "h": 0.02, "grid_cell": 0.005, "iso": 0.5}
+        return frames, {}, desc, False
+    if name == "dam":
+        frames = [synth.dam_break()]
+        keys = {"sim.particlespacing": 0.005}
+        desc = {"workload": "dam_break_8M", "particles": int(len(frames[0][0])), "h": 0.01, "grid_cell": 0.0025,
+                "iso": 0.5}
+        return frames, keys, desc, False
+    raise SystemExit(f"unknown workload {name}")
 
 
 def write_config(keys: dict) -> str:
@@ -66,14 +95,20 @@ def write_config(keys: dict) -> str:
 # ---------------------------------------------------------------------------
 # algorithmic bytes per stage, from the frame's own counts
 # ---------------------------------------------------------------------------
-def algorithmic_bytes(c: dict, g, diffuse: bool) -> dict:
+def algorithmic_bytes(c: dict, sp_size: int, sc_size: int, diffuse: bool, learned: bool) -> dict:
     N, Ns, Vs, Cv, M = c["n_particles"], c["n_surface_particles"], c["n_band_vertices"], c["n_valid_cubes"], \
         c["n_mesh_vertices"]
-    Ssp, Ssc = g.sp_size, g.sc_size
+    Ssp, Ssc = sp_size, sc_size
     P = max(1, -(-int(np.ceil(np.log2(max(Ssp, 2)))) // 8))
     grid = (16 * N + Ssp / 8) + 16 * N * P + (32 * N + (24 * N if diffuse else 0)) + (4 * N + 8 * Ssp)
     aniso = (Ssp / 8 + 8 * Ssp + 4 * Ns) + (16 * N + 68 * Ns) + 20 * N
-    band = 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
+    if learned:
+        coarse = Ssc / 8
+        # coarse counts (read positions, write counts), prediction (read counts, write
+        # cube bits), cube corners, vertex scan and list
+        band = (16 * N + 4 * coarse) + (4 * coarse + Ssc / 8) + 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
+    else:
+        band = 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
     field = 16 * N + 44 * Ns + 8 * Vs
     mc = (4 * Vs + Ssc / 8 + 9 * Vs) + (12 * 8 * Cv + 24 * M)
     dif = (64 * N + 44 * (c["n_generated_diffuse"] + c["n_diffuse"])) if diffuse else 0
@@ -133,6 +168,9 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ---------------------------------------------------------------------------
+# CPU legs (the float64 oracle)
+# ---------------------------------------------------------------------------
 def cpu_baseline(pos, keys: dict, frac: float = 0.25) -> dict:
     """Float64 oracle of the plain path on an x-slab holding `frac` of the frame."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -155,10 +193,12 @@ def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    pos, vel, rho, keys, desc = workload(args.workload)
+    frames, keys, desc, _ = workload(args.workload)
+    pos = frames[0][0]
     for _ in range(args.warmup):
         cpu_baseline(pos, keys, args.cpu_fraction)
     vals, dts = [], []
+    cb = {}
     for _ in range(args.steps):
         t = time.perf_counter()
         cb = cpu_baseline(pos, keys, args.cpu_fraction)
@@ -174,6 +214,148 @@ def run_reference(args) -> None:
     print(json.dumps(line))
 
 
+# ---------------------------------------------------------------------------
+# GPU arms
+# ---------------------------------------------------------------------------
+class Timer:
+    """CUDA-event timing of K steps on the context's stream, L2 flushed between
+    steps, max over ranks."""
+
+    def __init__(self, torch, stream, world):
+        self.torch, self.stream, self.world = torch, stream, world
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def __call__(self, fn, k, after=None):
+        torch = self.torch
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        if self.world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for i in range(k):
+            self.flush.zero_()
+            ev[i][0].record(self.stream)
+            fn()
+            ev[i][1].record(self.stream)
+            if after:
+                after()
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / k
+        if self.world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+
+def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse: bool, clocks=None) -> dict:
+    pos, vel, rho = frame
+    n = len(pos)
+    d_pos, d_vel, d_rho = (torch.from_numpy(a).cuda() for a in (pos, vel, rho))
+    h_pos, h_vel, h_rho = (torch.from_numpy(a).pin_memory() for a in (pos, vel, rho))
+    ctx.set_band_mode(learned)
+    host = {}
+
+    def step_device():
+        ctx.upload_device(d_pos.data_ptr(), d_vel.data_ptr(), d_rho.data_ptr(), n)
+        ctx.run_frame()
+
+    def step_e2e():
+        # the user's calls: upload from pinned host memory, reconstruct, read the
+        # triangle soup (and the live diffuse particles) back into pinned memory
+        ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
+        ctx.run_frame()
+        nv = C.c_uint64()
+        pms.lib().pms_download_mesh(ctx.handle, None, None, 0, C.byref(nv))
+        buf = host.get("mesh")
+        if buf is None or buf.numel() < 3 * nv.value:
+            buf = host["mesh"] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
+        ctx._call("pms_download_mesh", buf.data_ptr(), None, buf.numel() // 3, C.byref(nv))
+        if diffuse:
+            host["diffuse"] = ctx.diffuse_particles(-1)
+
+    stage_sum = {k: 0.0 for k in STAGES}
+
+    def collect():
+        for s, v in ctx.stage_times().items():
+            stage_sum[s] += v
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    counts = ctx.counts().as_dict()
+    grid = ctx.grid()
+    if clocks:
+        clocks.start()
+    l0 = ctx.launches
+    ms = timer(step_device, args.steps, collect)
+    launches = (ctx.launches - l0) // max(1, args.steps)
+    clk = clocks.stop() if clocks else None
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    ms_e2e = timer(step_e2e, args.steps)
+    return {"ms": ms, "ms_e2e": ms_e2e, "counts": counts, "sp_size": grid.sp_size, "sc_size": grid.sc_size,
+            "launches": launches, "clocks": clk, "stage_ms": {k: v / args.steps for k, v in stage_sum.items()},
+            "h2d": 28 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(counts["n_diffuse"])}
+
+
+def batch_arm(pms, ctx, frames, learned: bool, args, timer, torch, clocks=None) -> dict:
+    dev = [tuple(torch.from_numpy(a).cuda() for a in fr) for fr in frames]
+    pin = [tuple(torch.from_numpy(a).pin_memory() for a in fr) for fr in frames]
+    dframes = [(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0])) for (p, v, r), fr in zip(dev, frames)]
+    hframes = [(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0])) for (p, v, r), fr in zip(pin, frames)]
+    host = {}
+
+    def step_device():
+        ctx.run_batch(dframes, learned=learned)
+
+    def step_e2e():
+        ctx.run_batch(hframes, learned=learned)
+        for f in range(len(frames)):
+            nv = C.c_uint64()
+            pms.lib().pms_batch_mesh(ctx.handle, f, None, 0, C.byref(nv))
+            buf = host.get(f)
+            if buf is None or buf.numel() < 3 * nv.value:
+                buf = host[f] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
+            ctx._call("pms_batch_mesh", f, buf.data_ptr(), buf.numel() // 3, C.byref(nv))
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    if clocks:
+        clocks.start()
+    l0 = ctx.launches
+    ms = timer(step_device, args.steps)
+    launches = (ctx.launches - l0) // max(1, args.steps)
+    clk = clocks.stop() if clocks else None
+    per_frame = []
+    counts = []
+    for f in range(len(frames)):
+        c, fms = ctx.batch_frame(f)
+        per_frame.append(fms)
+        counts.append(c.as_dict())
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    ms_e2e = timer(step_e2e, args.steps)
+    mesh = sum(int(c["n_mesh_vertices"]) for c in counts)
+    return {"ms": ms, "ms_e2e": ms_e2e, "launches": launches, "clocks": clk, "frame_ms": per_frame,
+            "counts": counts, "info": ctx.batch_info(), "h2d": sum(28 * len(fr[0]) for fr in frames), "d2h": 12 * mesh}
+
+
+def unbatched_ms(ctx, frames, learned: bool, args, timer, torch) -> float:
+    """The same frames through pms_run_frame one by one (device-resident inputs)."""
+    dev = [tuple(torch.from_numpy(a).cuda() for a in fr) for fr in frames]
+    ctx.set_band_mode(learned)
+
+    def step():
+        for (p, v, r), fr in zip(dev, frames):
+            ctx.upload_device(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0]))
+            ctx.run_frame()
+
+    step()
+    torch.cuda.synchronize()
+    return timer(step, max(1, args.steps // 2))
+
+
 def run_pms(args) -> None:
     import torch
     rank = int(os.environ.get("RANK", "0"))
@@ -185,90 +367,51 @@ def run_pms(args) -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     else:
         torch.cuda.set_device(0)
-    from postmps_gb300 import pms
-    pos, vel, rho, keys, desc = workload(args.workload)
+    from postmps_gb300 import learned as LN, pms
+    frames, keys, desc, diffuse = workload(args.workload)
+    if args.no_diffuse:
+        diffuse = False
     cfg_path = write_config(keys)
     cfg = pms.load_config(cfg_path)
     os.unlink(cfg_path)
     cfg.is_surface = 1
-    cfg.is_diffuse = 0 if args.no_diffuse else 1
-    stream = torch.cuda.current_stream()
+    cfg.is_diffuse = 1 if diffuse else 0
+    h = float(pms.derive_params(cfg).h)
+    # one non-default stream for everything: libpms's work, the L2 flush and the
+    # timing events are ordered on it (a NULL handle would give the context its own stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = pms.Context(cfg, local)
     ctx.set_stream(stream.cuda_stream)
-    n = len(pos)
-    d_pos = torch.from_numpy(pos).cuda()
-    d_vel = torch.from_numpy(vel).cuda()
-    d_rho = torch.from_numpy(rho).cuda()
-    h_pos = torch.from_numpy(pos).pin_memory()
-    h_vel = torch.from_numpy(vel).pin_memory()
-    h_rho = torch.from_numpy(rho).pin_memory()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def step_device():
-        ctx.upload_device(d_pos.data_ptr(), d_vel.data_ptr(), d_rho.data_ptr(), n)
-        ctx.run_frame()
-
-    mesh_host = {}
-
-    def step_e2e():
-        # the user's calls: upload from pinned host memory, reconstruct, read the
-        # triangle soup (and the live diffuse particles) back into pinned memory
-        ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
-        ctx.run_frame()
-        import ctypes as C
-        nv = C.c_uint64()
-        pms.lib().pms_download_mesh(ctx.handle, None, None, 0, C.byref(nv))
-        buf = mesh_host.get("mesh")
-        if buf is None or buf.numel() < 3 * nv.value:
-            buf = mesh_host["mesh"] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
-        ctx._call("pms_download_mesh", buf.data_ptr(), None, buf.numel() // 3, C.byref(nv))
-        if cfg.is_diffuse:
-            mesh_host["diffuse"] = ctx.diffuse_particles(-1)
-
-    for _ in range(args.warmup):
-        step_device()
-    torch.cuda.synchronize()
-    counts = ctx.counts().as_dict()
-    grid = ctx.grid()
-    stage_sum = {k: 0.0 for k in ("grid", "anisotropy", "band", "field", "marching_cubes", "diffuse")}
-
-    def timed(fn, k):
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        for i in range(k):
-            flush.zero_()
-            ev[i][0].record(stream)
-            fn()
-            ev[i][1].record(stream)
-            if fn is step_device:
-                for s, v in ctx.stage_times().items():
-                    stage_sum[s] += v
-        torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in ev) / k
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
-
+    timer = Timer(torch, stream, world)
+    model = None
+    if args.band in ("both", "learned") and os.path.exists(args.model):
+        model = LN.load_model(args.model)
+        ctx.set_band_model(model)
+    arms = (["learned", "plain"] if model is not None else ["plain"]) if args.band == "both" else [args.band]
+    if "learned" in arms and model is None:
+        raise SystemExit(f"--band learned needs a model ({args.model})")
     clocks = ClockSampler(local)
-    clocks.start()
-    l0 = ctx.launches
-    ms = timed(step_device, args.steps)
-    launches = (ctx.launches - l0) // max(1, args.steps)
-    clk = clocks.stop()
-    for _ in range(max(1, args.warmup // 2)):
-        step_e2e()
-    ms_e2e = timed(step_e2e, args.steps)
-    m_vertices = int(counts["n_mesh_vertices"])
-
-    value = world * n / (ms / 1e3)
-    e2e_value = world * n / (ms_e2e / 1e3)
-    stage_ms = {k: v / args.steps for k, v in stage_sum.items()}
-    alg = algorithmic_bytes(counts, grid, diffuse=bool(cfg.is_diffuse))
-    dom = max(alg, key=lambda k: stage_ms.get(k, 0.0))
+    batched = args.workload == "slosh16"
+    tune = None
+    if not args.no_tune:
+        # autotune the launch shapes on the largest frame (outside the timed region)
+        big = max(frames, key=lambda fr: len(fr[0]))
+        ctx.upload(*big)
+        ctx.build_grid()
+        ctx.surface()
+        tune = ctx.autotune()
+    res = {}
+    for i, arm in enumerate(arms):
+        if batched:
+            res[arm] = batch_arm(pms, ctx, frames, arm == "learned", args, timer, torch, clocks if i == 0 else None)
+        else:
+            res[arm] = single_frame_arm(pms, ctx, frames[0], arm == "learned", args, timer, torch, diffuse,
+                                        clocks if i == 0 else None)
+    head = res[arms[0]]
+    n_total = sum(len(fr[0]) for fr in frames)
+    value = world * n_total / (head["ms"] / 1e3)
+    e2e_value = world * n_total / (head["ms_e2e"] / 1e3)
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -277,31 +420,69 @@ def run_pms(args) -> None:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else None
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", f"traffic_{desc['workload']}.json")
-    if os.path.exists(tfile):
-        with open(tfile) as f:
-            traffic = json.load(f).get(dom)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": dict(desc, path="surface + diffuse" if cfg.is_diffuse else "surface (diffuse off)", band="plain",
-                       l2="flushed (256 MiB write) between steps",
-                       parallelism=f"replicas x{world}"),
-        "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": ms_e2e, "h2d_bytes_per_step": 28 * n,
-                "d2h_bytes_per_step": 12 * m_vertices + 32 * int(counts["n_diffuse"])},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "algorithmic_bytes": alg[dom], "peak_source": peak_src},
-        "stage_ms": stage_ms,
-        "counts": counts,
-        "clocks": clk,
-        "gpu_launches": int(launches),
+        "config": dict(desc, path=("surface + diffuse" if diffuse else "surface (diffuse off)"), band=arms[0],
+                       l2="flushed (256 MiB write) between steps", parallelism=f"replicas x{world}",
+                       step=("one pms_run_batch call (one CUDA graph launch)" if batched else "one frame")),
+        "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": head["ms_e2e"], "h2d_bytes_per_step": head["h2d"],
+                "d2h_bytes_per_step": head["d2h"]},
+        "clocks": head["clocks"],
+        "gpu_launches": int(head["launches"]),
+        "tune": tune,
     }
+    for arm in arms:
+        r = res[arm]
+        line[arm] = {"value": world * n_total / (r["ms"] / 1e3), "e2e": world * n_total / (r["ms_e2e"] / 1e3),
+                     "ms_per_step": r["ms"], "ms_e2e": r["ms_e2e"]}
+        if batched:
+            line[arm].update({"frame_ms": r["frame_ms"], "graph": r["info"],
+                              "band_vertices": sum(c["n_band_vertices"] for c in r["counts"]),
+                              "triangles": sum(c["n_mesh_vertices"] for c in r["counts"]) // 3})
+        else:
+            line[arm].update({"stage_ms": r["stage_ms"], "counts": r["counts"]})
+    if batched:
+        line["unbatched_ms_per_step"] = unbatched_ms(ctx, frames, arms[0] == "learned", args, timer, torch)
+        # whole-path bytes of every frame over the whole batch time
+        tot = 0.0
+        for fr_c in res[arms[0]]["counts"]:
+            tot += sum(algorithmic_bytes(dict(fr_c, n_generated_diffuse=0, n_diffuse=0), fr_c["n_particles"],
+                                         fr_c["n_band_vertices"], False, arms[0] == "learned").values())
+        achieved = tot / (head["ms"] / 1e3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": "whole batch", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": None, "algorithmic_bytes": tot, "peak_source": peak_src}
+    else:
+        stage_ms = head["stage_ms"]
+        alg = algorithmic_bytes(head["counts"], head["sp_size"], head["sc_size"], diffuse, arms[0] == "learned")
+        dom = max(alg, key=lambda k: stage_ms.get(k, 0.0))
+        achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else None
+        traffic = None
+        tfile = os.path.join(ROOT, "profiles", f"traffic_{desc['workload']}.json")
+        if os.path.exists(tfile):
+            with open(tfile) as f:
+                tj = json.load(f)
+            traffic = tj.get(f"{arms[0]}:{dom}", tj.get(dom))
+        line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                            "algorithmic_bytes": alg[dom], "peak_source": peak_src}
+        line["stage_ms"] = stage_ms
+        line["counts"] = head["counts"]
+    if len(arms) == 2 and not batched and rank == 0 and not args.no_judge:
+        t0 = time.perf_counter()
+        pos, vel, rho = frames[0]
+        ctx.set_band_mode(False)
+        j = LN.compare(ctx, model, h, pos, vel, rho)
+        line["judge"] = {"hausdorff_h": j["hausdorff_h"], "hausdorff": j["hausdorff"],
+                         "triangle_delta": j["triangle_delta"], "cubes_only_plain": j["cubes_only_plain"],
+                         "cubes_only_learned": j["cubes_only_learned"],
+                         "fallback_cubes": j["learned"]["fallback_cubes"],
+                         "fallback_rounds": j["learned"]["fallback_rounds"],
+                         "plain_vs_fp64": "vertex positions within 1e-4 cell of the float64 oracle (parity tests)",
+                         "seconds": time.perf_counter() - t0}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(pos, keys, args.cpu_fraction)
+        line["cpu_baseline"] = cpu_baseline(frames[0][0], keys, args.cpu_fraction)
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
@@ -310,15 +491,20 @@ def run_pms(args) -> None:
 
 
 def main() -> None:
+    from postmps_gb300 import learned as LN
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pms", choices=["pms", "reference"])
-    ap.add_argument("--workload", default="crown", choices=["crown", "block"])
+    ap.add_argument("--workload", default="crown", choices=["crown", "block", "slosh16", "dam"])
+    ap.add_argument("--band", default="both", choices=["both", "learned", "plain"])
+    ap.add_argument("--model", default=LN.DEFAULT_MODEL)
     ap.add_argument("--cpu-fraction", type=float, default=0.25)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diffuse", action="store_true")
+    ap.add_argument("--no-judge", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -85,6 +85,7 @@ typedef struct pms_config {
     /* GB300 build additions (no reference counterpart) */
     double fp64_svd_cond;              /* covariances with condition number above this use the FP64 eigen solver (1e6) */
     uint64_t rng_seed;                 /* seed of the diffuse spawn uniforms (replaces std::random_device) */
+    char band_model[512];              /* [GB300] BandModel: learned-band model file; empty = plain band */
 } pms_config;
 
 /* Derived float32 parameters (SimParams, SurfaceParams, DiffuseParams, Define.h:85-139). */
@@ -127,6 +128,11 @@ typedef struct pms_counts {
     uint32_t n_diffuse;                /* OldNumDiffuseParticles after delete/append */
     uint32_t n_spray, n_foam, n_bubble;
     uint32_t n_fp64_svd;               /* covariances re-solved in FP64 */
+    /* learned band (pms_band_learned); zero after the plain band */
+    uint32_t n_band_candidates;        /* cubes the network evaluated */
+    uint32_t n_band_predicted;         /* cubes it predicted crossed */
+    uint32_t n_band_fallback;          /* cubes the border check added */
+    uint32_t n_band_iterations;        /* border-check rounds that added cubes */
 } pms_counts;
 
 typedef struct pms_ctx pms_ctx;
@@ -241,6 +247,117 @@ int pms_mc_tables(uint32_t* edge_flags /*256*/, int32_t* tri /*256*16*/, uint32_
  * each device looks up that array's device address (make it before any stream
  * capture).  Concurrent calls on the GPU share the scratch and race.
  * No counterpart in the reference (its scans allocate through thrust). */
+/* ---------------------------------------------------------------------------
+ * Learned narrow band.  No counterpart in the reference: it replaces the band
+ * marking of Anisotropic::processingOfVertices (Anisotropic.cu:43-50,
+ * estimationOfSurfaceVertices, Anisotropic_kernel.cuh:522-636) as the source
+ * of the vertices at which the field (Anisotropic_kernel.cuh:656-777) is
+ * evaluated.  A 64 -> 64 -> 1 ReLU MLP with BF16 weights reads, for each fine
+ * cube near the fluid boundary, a 4x4x4 patch of a coarse occupancy grid
+ * (cells of 2x2x2 fine cubes) and predicts whether the surface crosses the
+ * cube; the field is evaluated exactly at the corners of the predicted cubes;
+ * a border check then adds every cube that shares a crossed face with a valid
+ * cube but lacks field values, and repeats until none is missing.
+ * ------------------------------------------------------------------------- */
+#define PMS_BAND_MLP_INPUTS 64
+#define PMS_BAND_MLP_HIDDEN 64
+#define PMS_BAND_MLP_PARAMS 4225          /* W1 64x64, b1 64, w2 64, b2 */
+typedef struct pms_band_model {
+    uint16_t w1[PMS_BAND_MLP_INPUTS * PMS_BAND_MLP_HIDDEN];  /* bf16 bits, w1[i * 64 + j]: input i -> hidden j */
+    float b1[PMS_BAND_MLP_HIDDEN];
+    uint16_t w2[PMS_BAND_MLP_HIDDEN];    /* bf16 bits */
+    float b2;
+    float threshold;                     /* a cube is predicted when its logit exceeds this */
+} pms_band_model;
+
+pms_status pms_set_band_model(pms_ctx* ctx, const pms_band_model* model);
+/* Which band pms_run_frame uses: PMS_BAND_LEARNED needs a model.  A context
+ * created from a config naming [GB300] BandModel starts in PMS_BAND_LEARNED. */
+#define PMS_BAND_PLAIN 0
+#define PMS_BAND_LEARNED 1
+pms_status pms_set_band_mode(pms_ctx* ctx, int mode);
+/* Model files: "PMSBAND1", uint32 version 1, uint32 sizeof(pms_band_model),
+ * the struct (little-endian), uint32 length and that many bytes of JSON
+ * metadata (training provenance). */
+pms_status pms_save_band_model(const char* path, const pms_band_model* model, const char* meta_json);
+pms_status pms_load_band_model(const char* path, pms_band_model* out);
+/* Band and field in one: after pms_anisotropy; followed by pms_marching_cubes. */
+pms_status pms_band_learned(pms_ctx* ctx);
+/* pms_anisotropy + pms_band_learned + pms_marching_cubes. */
+pms_status pms_surface_learned(pms_ctx* ctx);
+
+/* Training data of the current frame, after a plain pms_surface: the coarse
+ * grid, the candidate cubes and the plain method's labels (valid cubes). */
+pms_status pms_learn_prepare(pms_ctx* ctx, uint32_t* n_candidates, uint32_t* n_valid_cubes);
+/* Candidate cubes (origin vertex ids) with the logits of the context's model
+ * and the plain labels; *n receives the count even when it exceeds cap. */
+pms_status pms_learn_candidates(pms_ctx* ctx, uint32_t* cube_ids, float* logits, uint8_t* labels, uint32_t cap,
+                                uint32_t* n);
+/* Features (bf16 bits, 64 per cube) of the given cubes, after pms_learn_prepare. */
+pms_status pms_learn_features(pms_ctx* ctx, const uint32_t* cube_ids, uint32_t n, uint16_t* x_bf16);
+
+/* Trainer: fp32 master weights, Adam state, and the bf16 model the forward
+ * pass reads; the forward and backward kernels run on the tensor cores. */
+typedef struct pms_trainer pms_trainer;
+pms_status pms_trainer_create(int device, uint64_t seed, pms_trainer** out);
+void       pms_trainer_destroy(pms_trainer* t);
+/* One Adam step on `batch` candidates sampled (by `seed`) from the frame that
+ * pms_learn_prepare set up in `data`; *loss receives the batch's mean loss. */
+pms_status pms_trainer_step(pms_trainer* t, pms_ctx* data, uint32_t batch, uint64_t seed, float lr, float pos_weight,
+                            float* loss);
+/* Gradient of the mean weighted cross-entropy over explicit samples, without
+ * an update (grad: PMS_BAND_MLP_PARAMS floats in the parameter layout). */
+pms_status pms_trainer_grad(pms_trainer* t, const uint16_t* x_bf16, const uint8_t* labels, uint32_t batch,
+                            float pos_weight, float* grad, float* loss);
+pms_status pms_trainer_get_params(pms_trainer* t, float* params);
+pms_status pms_trainer_set_params(pms_trainer* t, const float* params);
+/* The bf16 model of the current weights (threshold 0). */
+pms_status pms_trainer_get_model(pms_trainer* t, pms_band_model* out);
+
+/* ---------------------------------------------------------------------------
+ * Batched frames.  No counterpart in the reference, whose GPUPOST::runSimulation
+ * (GPUPOST.cpp:56-81) reconstructs one frame at a time with host round trips
+ * between stages.  pms_run_batch copies k frames (host or device pointers) into
+ * one device arena, finds their grids with one synchronisation, and runs the
+ * surface path of all of them in one CUDA graph launch (captured on first use
+ * and relaunched while the frames' grids stay the same).  Diffuse particles
+ * are not generated in a batch.  With PMS_BATCH_LEARNED the learned band is
+ * used; a frame whose border check finds missing cubes is re-run alone on the
+ * exact learned path, so results equal single-frame runs.
+ * ------------------------------------------------------------------------- */
+typedef struct pms_frame {
+    const float* pos_xyz;
+    const float* vel_xyz;   /* may be NULL */
+    const float* rhop;      /* may be NULL */
+    uint32_t n;
+} pms_frame;
+#define PMS_BATCH_LEARNED 1
+pms_status pms_run_batch(pms_ctx* ctx, const pms_frame* frames, uint32_t k, int flags);
+/* Counts of frame f of the last batch and its device time inside the graph
+ * (0 for a frame that was re-run alone). */
+pms_status pms_batch_frame(pms_ctx* ctx, uint32_t f, pms_counts* counts, float* ms);
+/* Triangle soup of frame f (positions, 3 vertices per triangle). */
+pms_status pms_batch_mesh(pms_ctx* ctx, uint32_t f, float* pos_xyz, uint64_t cap, uint64_t* n_vertices);
+/* Kernels per graph launch, graph captures so far, frames re-run alone so far. */
+pms_status pms_batch_info(pms_ctx* ctx, uint32_t* graph_kernels, uint32_t* captures, uint32_t* reruns);
+
+/* ---------------------------------------------------------------------------
+ * Autotuner.  No counterpart in the reference (fixed launch shapes).  After a
+ * reconstructed frame, pms_autotune times every candidate launch shape of the
+ * neighbour walks on that frame -- threads per block 64/128/256 for density,
+ * moments and field, and the field's cap of 1/2/4/8 resident waves of blocks --
+ * keeps the fastest in the context (results do not depend on the shape) and
+ * reports it.  pms_set_tune applies a shape chosen earlier (e.g. cached by
+ * the caller per workload); batches use the context's shape.
+ * ------------------------------------------------------------------------- */
+typedef struct pms_tune {
+    int field_threads, field_waves, density_threads, moments_threads;
+    float anisotropy_ms, field_ms;     /* the chosen shapes' times on the tuning frame */
+} pms_tune;
+pms_status pms_autotune(pms_ctx* ctx, pms_tune* out);
+pms_status pms_set_tune(pms_ctx* ctx, const pms_tune* t);
+pms_status pms_get_tune(pms_ctx* ctx, pms_tune* out);
+
 pms_status pms_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, uint32_t* d_total,
                                           void* cuda_stream);
 

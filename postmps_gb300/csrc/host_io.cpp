@@ -209,6 +209,7 @@ extern "C" pms_status pms_config_load(const char* path, pms_config* c) {
     // additions of this build (not in the reference): [GB300] section
     c->fp64_svd_cond = ini.real("GB300", "Fp64SvdCondition", 1e6);
     c->rng_seed = (uint64_t)ini.real("GB300", "RandomSeed", 4);
+    copy_str(c->band_model, sizeof(c->band_model), ini.get("GB300", "BandModel", ""));
     return PMS_OK;
 }
 

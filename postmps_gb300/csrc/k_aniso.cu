@@ -33,7 +33,8 @@ struct AnisoParams {
 // density (calculationOfDensity): rho_i = sum_j sigma/h^3 (1 - (d/h)^2)^3, d < h,
 // over cells [c - e, c + e]; also stores m / rho into spos.w for the field.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 8) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
+template <int BT>
+__global__ void __launch_bounds__(BT, 1024 / BT) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
                                                       const uint32_t* __restrict__ cell_start, float4* __restrict__ spos,
                                                       float* __restrict__ rho, uint32_t n) {
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
@@ -146,7 +147,8 @@ __device__ __forceinline__ void eig_sym3(T a[3][3], T e[3], T v[3][3], T tol) {
 // The reference's two passes (mean, then covariance about the mean) follow
 // from these: mean = x_i + S1/S0 and sum w (u - o)(u - o)^T = S2 - S1 S1^T / S0.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads, 8) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
+template <int BT>
+__global__ void __launch_bounds__(BT, 1024 / BT) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
                                                       const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
                                                       const uint32_t* __restrict__ cell_start, const float4* __restrict__ spos,
                                                       float4* __restrict__ mom) {
@@ -289,16 +291,29 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     ap.min_nn = P.min_num_neighbors;
     ap.cond_limit = ctx->cfg.fp64_svd_cond;
     Counters* cnt = ctx->counters.as<Counters>();
-    k_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ap, ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->rho.as<float>(), ctx->n);
+    // block sizes of the neighbour walks are autotuned (64, 128 or 256 threads)
+    const int bd = ctx->tune.density_threads, bm = ctx->tune.moments_threads;
+    auto dens = [&](auto kern) {
+        kern<<<grid_for(ctx->n, (unsigned)bd), bd, 0, ctx->stream>>>(g, ap, ctx->skeys.as<uint32_t>(),
+                                                                    ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(),
+                                                                    ctx->rho.as<float>(), ctx->n);
+    };
+    if (bd == 64) dens(k_density<64>);
+    else if (bd == 256) dens(k_density<256>);
+    else dens(k_density<128>);
     PMS_LAUNCHED(ctx);
     k_inv_density<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(ctx->spos.as<float4>(), ctx->rho.as<float>(),
                                                                            ctx->aniso.as<float4>(), ap, ctx->n);
     PMS_LAUNCHED(ctx);
     // ns is on the device; grids are sized by the particle count (an upper bound)
-    k_moments<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
-        ctx->spos.as<float4>(), ctx->moments.as<float4>());
+    auto mom = [&](auto kern) {
+        kern<<<grid_for(ctx->n, (unsigned)bm), bm, 0, ctx->stream>>>(g, ap, ctx->slist.as<uint32_t>(), cnt,
+                                                                    ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
+                                                                    ctx->spos.as<float4>(), ctx->moments.as<float4>());
+    };
+    if (bm == 64) mom(k_moments<64>);
+    else if (bm == 256) mom(k_moments<256>);
+    else mom(k_moments<128>);
     PMS_LAUNCHED(ctx);
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->cell_rad.p, 0, sizeof(float) * (size_t)g.sp_size, ctx->stream));
     k_eigen<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(

@@ -143,6 +143,13 @@ pms_status launch_band(pms_ctx* ctx) {
     return scan_u32(ctx, ctx->wcount.as<uint32_t>(), ctx->wprefix.as<uint32_t>(), nwords, &cnt->nv);
 }
 
+pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist) {
+    const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
+    k_band_list<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(bm, wprefix, nwords, vlist);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 pms_status launch_band_list(pms_ctx* ctx) {
     const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
     k_band_list<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(),

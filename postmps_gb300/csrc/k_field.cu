@@ -29,8 +29,6 @@
 
 namespace pms {
 
-static constexpr int kThreads = 128;
-
 struct FieldParams {
     float h;                  // isotropic support, the smallest culling radius of a cell
     float thr;                // 2 * iso: the early-exit threshold
@@ -66,11 +64,14 @@ __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float
     return sum;
 }
 
-__global__ void __launch_bounds__(kThreads, 8) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
+// BT threads per block (autotuned: 64, 128 or 256), 64 registers per thread at most
+template <int BT>
+__global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
+                                                    const uint32_t* __restrict__ n_dev,
                                                     const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
                                                     const float* __restrict__ cell_rad, const float4* __restrict__ spos,
                                                     const float4* __restrict__ aniso, float* __restrict__ field) {
-    const uint32_t nv = cnt->nv;
+    const uint32_t nv = *n_dev;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], srxy = g.spres[0] * g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_field(KGrid g, FieldParams fp, 
     }
 }
 
-pms_status launch_field(pms_ctx* ctx) {
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out) {
     const KGrid g = kgrid_of(ctx->grid);
     const pms_params& P = ctx->prm;
     FieldParams fp;
@@ -134,11 +135,22 @@ pms_status launch_field(pms_ctx* ctx) {
     fp.thr = 2.f * P.iso_value;
     fp.grow = 1.0001f;
     Counters* cnt = ctx->counters.as<Counters>();
-    k_field<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
-        g, fp, cnt, ctx->vlist.as<uint32_t>(), ctx->cell_start.as<uint32_t>(), ctx->cell_rad.as<float>(),
-        ctx->spos.as<float4>(), ctx->aniso.as<float4>(), ctx->field.as<float>());
+    const int bt = ctx->tune.field_threads;
+    const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1024u / (unsigned)bt));
+    auto go = [&](auto kern) {
+        kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
+                                             ctx->cell_rad.as<float>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out);
+    };
+    if (bt == 64) go(k_field<64>);
+    else if (bt == 256) go(k_field<256>);
+    else go(k_field<128>);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
+}
+
+pms_status launch_field(pms_ctx* ctx) {
+    Counters* cnt = ctx->counters.as<Counters>();
+    return launch_field_on(ctx, ctx->vlist.as<uint32_t>(), &cnt->nv, ctx->nv, ctx->field.as<float>());
 }
 
 }  // namespace pms

@@ -1,0 +1,764 @@
+// k_learn.cu -- learned narrow band: a 64 -> 64 -> 1 ReLU MLP (BF16 weights,
+// FP32 accumulate) that predicts which fine cubes of the scalar grid the
+// surface crosses, its training kernels, and the exact border-check fallback.
+// No counterpart in the reference: it replaces the band-vertex marking of
+// estimationOfSurfaceVertices (Anisotropic_kernel.cuh:522-636) as the source
+// of the vertices at which computationOfScalarFieldGrid
+// (Anisotropic_kernel.cuh:656-777) is evaluated; the field, the marching-cubes
+// classification and the triangle emission are the plain path's kernels.
+//
+// Features.  A coarse density grid has a vertex at every second scalar-grid
+// vertex (coarse vertex c sits on fine vertex 2c).  Every particle is splatted
+// onto the 8 coarse vertices around it with trilinear weights, accumulated in
+// 20-bit fixed point (integer atomics, so the sums do not depend on the order
+// of the additions).  Scaled by the particles a coarse cell holds at the
+// lattice spacing, a vertex inside the fluid reads about 1 (the trilinear
+// weights of a lattice sum to one) and a vertex in the air 0.  Fine cube c
+// (origin vertex x) lies in coarse cell k = x >> 1 with parity s = x & 1 per
+// axis; its 64 features are the densities of the 4 x 4 x 4 coarse vertices
+// nearest to it, k - 1 + d for s = 0 and k + 2 - d for s = 1 (d = 0..3): the
+// patch is reflected for odd cubes, so in the patch's own frame every cube
+// sits at offsets -2.5, -0.5, 1.5, 3.5 fine cells from the patch's vertices.
+// Feature index f = (dz * 4 + dy) * 4 + dx; value min(density, 64), rounded
+// to bf16.
+//
+// Candidates.  Only cubes of coarse cells whose 4 x 4 x 4 patch holds a vertex
+// above 0 and a vertex below 0.5 are evaluated (a uniformly full or uniformly
+// empty neighbourhood is deep inside or far outside the fluid).
+//
+// Network.  h = relu(x W1 + b1), z = h . w2 + b2; the cube is predicted when
+// z > threshold.  The first layer runs on the tensor cores, 16 cubes per warp
+// per mma.sync.m16n8k16 (bf16 inputs, fp32 accumulate), weights held in
+// registers as B fragments; the second layer is a quad shuffle reduction.
+//
+// Training.  Weighted binary cross-entropy on cubes the plain method labels
+// (valid marching cube = 1).  Forward as above; backward dz = sigmoid(z) (pw y
+// + 1 - y) - pw y (over the batch), dh = dz w2 [pre > 0], dW1 = X^T dh on the
+// tensor cores (dh rounded to bf16, fp32 accumulate), db1, dw2, db2 in fp32;
+// Adam on fp32 master weights, bf16 copies for the forward pass.
+#include "pms_internal.h"
+#include "k_common.cuh"
+#include "learn_internal.h"
+#include <cuda_bf16.h>
+
+namespace pms {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+__device__ __forceinline__ uint32_t pack_raw(uint16_t lo, uint16_t hi) { return (uint32_t)lo | ((uint32_t)hi << 16); }
+__device__ __forceinline__ float bf16_to_f(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
+
+// D = A (16x16 bf16, row) * B (16x8 bf16, col) + C, fp32
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+static constexpr float kFixScale = 1048576.f;        // 2^20: fixed point of the splat weights
+static constexpr float kFixInv = 1.f / 1048576.f;
+
+// scaled density of a coarse vertex from its fixed-point sum (before bf16 rounding)
+__device__ __forceinline__ float density_of(uint32_t sum, float inv_expected) {
+    return fminf(__fmul_rn(__fmul_rn((float)sum, kFixInv), inv_expected), 64.f);
+}
+__device__ __forceinline__ float feature_of(uint32_t sum, float inv_expected) {
+    return __bfloat162float(__float2bfloat16_rn(density_of(sum, inv_expected)));
+}
+
+// coarse vertex of canonical patch offset d (0..3) for a cube in coarse cell k
+// with parity s along one axis
+__device__ __forceinline__ int patch_cell(int k, int s, int d) { return s ? k + 2 - d : k - 1 + d; }
+
+// ---------------------------------------------------------------------------
+// coarse occupancy grid
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_coarse_count(KGrid g, LearnDims ld, const float4* __restrict__ spos, uint32_t n,
+                                                      uint32_t* __restrict__ counts) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = spos[i];
+        const float q[3] = {p.x, p.y, p.z};
+        int k[3];
+        float w1[3];
+        bool ok = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            // coarse coordinate: fine coordinate (p - min) / cell, halved
+            const float u = __fmul_rn(__fdiv_rn(__fsub_rn(q[a], g.scmin_pos[a]), g.sc_cs), 0.5f);
+            const float f0 = floorf(u);
+            ok = ok && f0 >= 0.f && f0 < (float)(ld.cres[a] - 1u);
+            k[a] = ok ? (int)f0 : 0;
+            w1[a] = __fsub_rn(u, f0);
+        }
+        if (!ok) continue;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float wx = (c & 1) ? w1[0] : __fsub_rn(1.f, w1[0]);
+            const float wy = (c & 2) ? w1[1] : __fsub_rn(1.f, w1[1]);
+            const float wz = (c & 4) ? w1[2] : __fsub_rn(1.f, w1[2]);
+            const uint32_t fix = __float2uint_rn(__fmul_rn(__fmul_rn(__fmul_rn(wx, wy), wz), kFixScale));
+            if (fix)
+                atomicAdd(&counts[((size_t)(k[2] + (c >> 2)) * ld.cres[1] + (k[1] + ((c >> 1) & 1))) * ld.cres[0] +
+                                  (k[0] + (c & 1))],
+                          fix);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// prediction over tiles of 4 x 4 x 4 coarse cells (8 x 8 x 8 fine cubes)
+// ---------------------------------------------------------------------------
+static constexpr int kTile = 4;                 // coarse cells per tile axis
+static constexpr int kHalo = 1;                 // patch vertices k - 1 .. k + 2 of the tile's cells k
+static constexpr int kSm = 8;                   // tile + halo = 7 coarse vertices per axis, padded
+static constexpr int kPredThreads = 128;
+
+struct PredictOut {
+    uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
+    uint32_t* cand;           // candidate cube ids; may be null
+    float* logit;             // their logits; may be null
+    uint32_t cand_cap;
+    uint32_t* n_cand;         // device counters
+    uint32_t* n_pred;
+};
+
+// W1 as B fragments: b[kk][nt][0..1] for k-step kk (features 16kk..16kk+15) and
+// n-tile nt (hidden 8nt..8nt+7)
+__device__ __forceinline__ void load_w1_frags(const DevModel* __restrict__ m, uint32_t (&b)[4][8][2], int lane) {
+    const uint16_t* w1 = m->w1;
+    const int kq = (lane & 3) * 2, n = lane >> 2;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int j = nt * 8 + n, i0 = kk * 16 + kq;
+            b[kk][nt][0] = pack_raw(w1[(i0 + 0) * kHid + j], w1[(i0 + 1) * kHid + j]);
+            b[kk][nt][1] = pack_raw(w1[(i0 + 8) * kHid + j], w1[(i0 + 9) * kHid + j]);
+        }
+}
+
+__global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDims ld, const uint32_t* __restrict__ counts,
+                                                                const DevModel* __restrict__ model, int use_model,
+                                                                PredictOut out) {
+    __shared__ float s_cnt[kSm][kSm][kSm];        // densities of the coarse vertices the tile's cubes read
+    __shared__ uint8_t s_mixed[kTile * kTile * kTile];
+    __shared__ uint16_t s_list[512];
+    __shared__ uint32_t s_n;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t tx = ld.tiles[0], ty = ld.tiles[1];
+    const uint32_t tile = blockIdx.x;
+    const int T0[3] = {(int)(tile % tx) * kTile, (int)((tile / tx) % ty) * kTile, (int)(tile / (tx * ty)) * kTile};
+    if (T0[2] >= (int)ld.cres[2]) return;
+    // load the coarse counts of the tile plus halo (outside the grid: empty)
+    int any = 0, all = 1;
+    for (int e = tid; e < kSm * kSm * kSm; e += kPredThreads) {
+        const int lx = e % kSm, ly = (e / kSm) % kSm, lz = e / (kSm * kSm);
+        const int cx = T0[0] - kHalo + lx, cy = T0[1] - kHalo + ly, cz = T0[2] - kHalo + lz;
+        uint32_t c = 0;
+        // the padding plane (index 7) lies beyond every patch: load it as empty without a read
+        if (lx < 7 && ly < 7 && lz < 7 && cx >= 0 && cy >= 0 && cz >= 0 && cx < (int)ld.cres[0] && cy < (int)ld.cres[1] &&
+            cz < (int)ld.cres[2])
+            c = __ldg(&counts[((size_t)cz * ld.cres[1] + cy) * ld.cres[0] + cx]);
+        const float d = density_of(c, ld.inv_expected);
+        s_cnt[lz][ly][lx] = d;
+        if (lx < 7 && ly < 7 && lz < 7) {
+            any |= d > 0.f;
+            all &= d >= 0.5f;
+        }
+    }
+    if (tid == 0) s_n = 0;
+    const int any_b = __syncthreads_or(any), all_b = __syncthreads_and(all);
+    if (!any_b || all_b) return;                 // uniformly empty or full: no candidates
+    // mixed flag of each coarse cell of the tile over its 4^3 patch vertices
+    if (tid < kTile * kTile * kTile) {
+        const int cx = tid % kTile, cy = (tid / kTile) % kTile, cz = tid / (kTile * kTile);
+        bool nz = false, lo = false;
+        for (int dz = 0; dz < 4; ++dz)
+            for (int dy = 0; dy < 4; ++dy)
+                for (int dx = 0; dx < 4; ++dx) {
+                    const float v = s_cnt[cz + dz][cy + dy][cx + dx];
+                    nz |= v > 0.f;
+                    lo |= v < 0.5f;
+                }
+        s_mixed[tid] = (nz && lo) ? 1 : 0;
+    }
+    __syncthreads();
+    // candidate cubes of the tile (local index q = (lz * 8 + ly) * 8 + lx)
+    for (int q = tid; q < 512; q += kPredThreads) {
+        const int lx = q & 7, ly = (q >> 3) & 7, lz = q >> 6;
+        const int fx = 2 * T0[0] + lx, fy = 2 * T0[1] + ly, fz = 2 * T0[2] + lz;
+        const bool in = fx < (int)g.scres[0] - 1 && fy < (int)g.scres[1] - 1 && fz < (int)g.scres[2] - 1;
+        if (in && s_mixed[((lz >> 1) * kTile + (ly >> 1)) * kTile + (lx >> 1)]) s_list[atomicAdd(&s_n, 1u)] = (uint16_t)q;
+    }
+    __syncthreads();
+    const uint32_t ncand = s_n;
+    if (ncand == 0) return;
+    if (tid == 0) atomicAdd(out.n_cand, ncand);
+    const uint32_t rxy = g.scres[0] * g.scres[1];
+    auto cube_id = [&](int q) -> uint32_t {
+        const int lx = q & 7, ly = (q >> 3) & 7, lz = q >> 6;
+        return (uint32_t)(2 * T0[2] + lz) * rxy + (uint32_t)(2 * T0[1] + ly) * g.scres[0] + (uint32_t)(2 * T0[0] + lx);
+    };
+    if (!use_model) {
+        // collect only
+        for (uint32_t e = tid; e < ncand; e += kPredThreads) {
+            const uint32_t slot = atomicAdd(out.n_pred, 1u);
+            if (out.cand && slot < out.cand_cap) out.cand[slot] = cube_id(s_list[e]);
+        }
+        return;
+    }
+    uint32_t b[4][8][2];
+    load_w1_frags(model, b, lane);
+    const int kq = (lane & 3) * 2;
+    float b1v[8][2], w2v[8][2];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = nt * 8 + kq + e;
+            b1v[nt][e] = model->b1[j];
+            w2v[nt][e] = bf16_to_f(model->w2[j]);
+        }
+    const float b2 = model->b2, thr = model->threshold;
+    const uint32_t ngroups = (ncand + 15) / 16;
+    for (uint32_t grp = warp; grp < ngroups; grp += kPredThreads / 32) {
+        const uint32_t e0 = grp * 16 + (lane >> 2), e1 = e0 + 8;
+        const int q0 = s_list[e0 < ncand ? e0 : ncand - 1], q1 = s_list[e1 < ncand ? e1 : ncand - 1];
+        // coarse index within smem (halo offset included) and parity of each row's cube
+        int k0[3], p0[3], k1[3], p1[3];
+        {
+            const int l0[3] = {q0 & 7, (q0 >> 3) & 7, q0 >> 6}, l1[3] = {q1 & 7, (q1 >> 3) & 7, q1 >> 6};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                k0[a] = (l0[a] >> 1) + kHalo; p0[a] = l0[a] & 1;
+                k1[a] = (l1[a] >> 1) + kHalo; p1[a] = l1[a] & 1;
+            }
+        }
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            // features (dz = kk, dy, dx) with c = dy * 4 + dx in {kq, kq + 1, kq + 8, kq + 9}
+            const int dy = kq >> 2, dx = kq & 3;
+            const int z0 = patch_cell(k0[2], p0[2], kk), z1 = patch_cell(k1[2], p1[2], kk);
+            const int y0a = patch_cell(k0[1], p0[1], dy), y0b = patch_cell(k0[1], p0[1], dy + 2);
+            const int y1a = patch_cell(k1[1], p1[1], dy), y1b = patch_cell(k1[1], p1[1], dy + 2);
+            const int x0a = patch_cell(k0[0], p0[0], dx), x0b = patch_cell(k0[0], p0[0], dx + 1);
+            const int x1a = patch_cell(k1[0], p1[0], dx), x1b = patch_cell(k1[0], p1[0], dx + 1);
+            uint32_t a[4];
+            a[0] = pack_bf16(s_cnt[z0][y0a][x0a], s_cnt[z0][y0a][x0b]);
+            a[1] = pack_bf16(s_cnt[z1][y1a][x1a], s_cnt[z1][y1a][x1b]);
+            a[2] = pack_bf16(s_cnt[z0][y0b][x0a], s_cnt[z0][y0b][x0b]);
+            a[3] = pack_bf16(s_cnt[z1][y1b][x1a], s_cnt[z1][y1b][x1b]);
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) mma_bf16(acc[nt], a, b[kk][nt][0], b[kk][nt][1]);
+        }
+        float z0s = 0.f, z1s = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                z0s += fmaxf(acc[nt][e] + b1v[nt][e], 0.f) * w2v[nt][e];
+                z1s += fmaxf(acc[nt][2 + e] + b1v[nt][e], 0.f) * w2v[nt][e];
+            }
+        z0s += __shfl_xor_sync(0xffffffffu, z0s, 1);
+        z0s += __shfl_xor_sync(0xffffffffu, z0s, 2);
+        z1s += __shfl_xor_sync(0xffffffffu, z1s, 1);
+        z1s += __shfl_xor_sync(0xffffffffu, z1s, 2);
+        if ((lane & 3) == 0) {
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const uint32_t e = r ? e1 : e0;
+                if (e >= ncand) continue;
+                const float z = (r ? z1s : z0s) + b2;
+                const uint32_t id = cube_id(r ? q1 : q0);
+                if (out.logit) {
+                    const uint32_t slot = atomicAdd(out.n_pred, 1u);
+                    if (slot < out.cand_cap) { out.cand[slot] = id; out.logit[slot] = z; }
+                } else if (z > thr) {
+                    atomicOr(&out.q[id >> 5], 1u << (id & 31u));
+                    atomicAdd(out.n_pred, 1u);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// vertex bitmaps from cube bitmaps: a cube marks its 8 corners
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t shifted(const uint32_t* __restrict__ b, uint64_t w, uint64_t s) {
+    const uint64_t q = s >> 5;
+    const uint32_t r = (uint32_t)(s & 31u);
+    if (w < q) return 0u;
+    const uint32_t hi = b[w - q];
+    if (r == 0) return hi;
+    const uint32_t lo = (w >= q + 1) ? b[w - q - 1] : 0u;
+    return (hi << r) | (lo >> (32u - r));
+}
+
+// out = corners(cubes) & ~exclude (exclude may be null); popcount per word
+__global__ void __launch_bounds__(256) k_cube_corners(const uint32_t* __restrict__ cubes, const uint32_t* __restrict__ exclude,
+                                                      uint32_t* __restrict__ out, uint32_t* __restrict__ wcount,
+                                                      uint64_t nwords, uint64_t nbits, uint64_t sy, uint64_t sz) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t v = cubes[w] | shifted(cubes, w, 1) | shifted(cubes, w, sy) | shifted(cubes, w, sy + 1) |
+                     shifted(cubes, w, sz) | shifted(cubes, w, sz + 1) | shifted(cubes, w, sz + sy) |
+                     shifted(cubes, w, sz + sy + 1);
+        if (w == nwords - 1 && (nbits & 31u)) v &= (1u << (nbits & 31u)) - 1u;
+        if (exclude) v &= ~exclude[w];
+        out[w] = v;
+        wcount[w] = __popc(v);
+    }
+}
+
+// a | b with popcount per word
+__global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                                                 uint32_t* __restrict__ out, uint32_t* __restrict__ wcount, uint64_t nwords) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = a[w] | b[w];
+        out[w] = v;
+        wcount[w] = __popc(v);
+    }
+}
+
+// Field of the merged vertex set: values of old vertices by rank in the old
+// set, of new ones by rank in the new set.
+__global__ void __launch_bounds__(256) k_field_merge(const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ n_dev,
+                                                     const uint32_t* __restrict__ bm_old, const uint32_t* __restrict__ wp_old,
+                                                     const float* __restrict__ f_old, const uint32_t* __restrict__ bm_new,
+                                                     const uint32_t* __restrict__ wp_new, const float* __restrict__ f_new,
+                                                     float* __restrict__ f_out) {
+    const uint32_t n = *n_dev;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t id = vlist[t];
+        const bool is_new = (bm_new[id >> 5] >> (id & 31u)) & 1u;
+        f_out[t] = is_new ? f_new[bit_rank(bm_new, wp_new, id)] : f_old[bit_rank(bm_old, wp_old, id)];
+    }
+}
+
+// Border check: a valid cube whose face has corners on both sides of the
+// iso-surface shares that crossing with the cube across the face, so the
+// neighbour is a valid cube too; if not all of the neighbour's corners have a
+// field value yet, the neighbour cube is queued.
+__global__ void __launch_bounds__(256) k_border(KGrid g, const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ vlist,
+                                                const uint32_t* __restrict__ mc_case,
+                                                const unsigned long long* __restrict__ mc_key,
+                                                const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
+                                                uint32_t* __restrict__ n_added) {
+    const uint32_t n = *n_dev;
+    const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
+    // face masks over the corner order {000,001,011,010,100,101,111,110} (x,y,z)
+    const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
+    const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        if (!mc_key[t]) continue;
+        const uint32_t cs = mc_case[t], id = vlist[t];
+        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const uint32_t m = cs & mask[f];
+            if (m == 0u || m == mask[f]) continue;
+            const int X = x + dxs[f], Y = y + dys[f], Z = z + dzs[f];
+            if (X < 0 || Y < 0 || Z < 0 || X > (int)rx - 2 || Y > (int)ry - 2 || Z > (int)rz - 2) continue;
+            const uint32_t nid = (uint32_t)Z * rxy + (uint32_t)Y * rx + (uint32_t)X;
+            // corners (x,y,z) + {0,1}^3
+            bool all = true;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
+                all = all && ((vbm[c >> 5] >> (c & 31u)) & 1u);
+            }
+            if (all) continue;
+            const uint32_t bit = 1u << (nid & 31u);
+            const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
+            if (!(old & bit)) atomicAdd(n_added, 1u);
+        }
+    }
+}
+
+// cube bitmap of the plain method's valid cubes (training labels)
+__global__ void __launch_bounds__(256) k_label_bits(const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ vlist,
+                                                    const unsigned long long* __restrict__ mc_key, uint32_t* __restrict__ lbm) {
+    const uint32_t n = *n_dev;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        if (mc_key[t]) atomicOr(&lbm[vlist[t] >> 5], 1u << (vlist[t] & 31u));
+}
+
+// features of explicit cubes (bf16 bits, 64 per cube), for checks against the oracle
+__global__ void __launch_bounds__(256) k_features(KGrid g, LearnDims ld, const uint32_t* __restrict__ counts,
+                                                  const uint32_t* __restrict__ cubes, uint32_t n, uint16_t* __restrict__ x) {
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < 64ull * n; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = (uint32_t)(e >> 6), f = (uint32_t)(e & 63u);
+        const uint32_t id = cubes[s];
+        const int c[3] = {(int)(id % rx), (int)((id / rx) % g.scres[1]), (int)(id / rxy)};
+        const int d[3] = {(int)(f & 3u), (int)((f >> 2) & 3u), (int)(f >> 4)};
+        int cc[3];
+        bool in = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            cc[a] = patch_cell(c[a] >> 1, c[a] & 1, d[a]);
+            in = in && cc[a] >= 0 && cc[a] < (int)ld.cres[a];
+        }
+        const uint32_t cnt = in ? counts[((size_t)cc[2] * ld.cres[1] + cc[1]) * ld.cres[0] + cc[0]] : 0u;
+        x[e] = __bfloat16_as_ushort(__float2bfloat16_rn(feature_of(cnt, ld.inv_expected)));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// training: one block = 128 samples (8 groups of 16), 4 warps
+// ---------------------------------------------------------------------------
+static constexpr int kTrainThreads = 128, kBlockSamples = 128;
+
+struct TrainIn {
+    // source A: sampled candidates of a frame
+    const uint32_t* cand; uint32_t n_cand; const uint32_t* labels; const uint32_t* counts;
+    // source B: explicit bf16 features and labels
+    const uint16_t* x; const uint8_t* y;
+    uint32_t batch; uint64_t seed; float pos_weight;
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(kTrainThreads) k_learn_train(KGrid g, LearnDims ld, TrainIn in,
+                                                               const DevModel* __restrict__ model, float* __restrict__ grad,
+                                                               float* __restrict__ loss_sum) {
+    __shared__ uint16_t s_x[kBlockSamples][kIn];
+    __shared__ uint16_t s_dh[kBlockSamples][kHid];
+    __shared__ float s_y[kBlockSamples];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t s_base = blockIdx.x * kBlockSamples;
+    const float inv_batch = 1.f / (float)in.batch;
+    // gather features and labels of the block's samples (invalid rows: zero, weight 0)
+    for (int e = tid; e < kBlockSamples * kIn; e += kTrainThreads) {
+        const int r = e / kIn, f = e % kIn;
+        const uint32_t s = s_base + r;
+        uint16_t v = 0;
+        float y = -1.f;                               // -1 marks a padding row
+        if (s < in.batch) {
+            if (in.x) {
+                v = in.x[(size_t)s * kIn + f];
+                y = in.y[s] ? 1.f : 0.f;
+            } else {
+                const uint32_t slot = (uint32_t)(mix64(in.seed ^ (0x9E3779B97F4A7C15ull * (s + 1))) % in.n_cand);
+                const uint32_t id = in.cand[slot];
+                const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+                const int c[3] = {(int)(id % rx), (int)((id / rx) % g.scres[1]), (int)(id / rxy)};
+                const int d[3] = {f & 3, (f >> 2) & 3, f >> 4};
+                int cc[3];
+                bool inside = true;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    cc[a] = patch_cell(c[a] >> 1, c[a] & 1, d[a]);
+                    inside = inside && cc[a] >= 0 && cc[a] < (int)ld.cres[a];
+                }
+                const uint32_t cnt = inside ? in.counts[((size_t)cc[2] * ld.cres[1] + cc[1]) * ld.cres[0] + cc[0]] : 0u;
+                v = __bfloat16_as_ushort(__float2bfloat16_rn(feature_of(cnt, ld.inv_expected)));
+                y = ((in.labels[id >> 5] >> (id & 31u)) & 1u) ? 1.f : 0.f;
+            }
+        }
+        s_x[r][f] = v;
+        if (f == 0) s_y[r] = y;
+    }
+    __syncthreads();
+    uint32_t b[4][8][2];
+    load_w1_frags(model, b, lane);
+    const int kq = (lane & 3) * 2;
+    float b1v[8][2], w2v[8][2], g_w2[8][2], g_b1[8][2];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int j = nt * 8 + kq + e;
+            b1v[nt][e] = model->b1[j];
+            w2v[nt][e] = bf16_to_f(model->w2[j]);
+            g_w2[nt][e] = g_b1[nt][e] = 0.f;
+        }
+    float g_b2 = 0.f, lsum = 0.f;
+    const float b2 = model->b2;
+    // phase 1: forward and the per-sample backward, two groups of 16 per warp
+    for (int grp = warp; grp < kBlockSamples / 16; grp += kTrainThreads / 32) {
+        const int r0 = grp * 16 + (lane >> 2), r1 = r0 + 8;
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+            const int c = kk * 16 + kq;
+            uint32_t a[4];
+            a[0] = pack_raw(s_x[r0][c], s_x[r0][c + 1]);
+            a[1] = pack_raw(s_x[r1][c], s_x[r1][c + 1]);
+            a[2] = pack_raw(s_x[r0][c + 8], s_x[r0][c + 9]);
+            a[3] = pack_raw(s_x[r1][c + 8], s_x[r1][c + 9]);
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) mma_bf16(acc[nt], a, b[kk][nt][0], b[kk][nt][1]);
+        }
+        float z0 = 0.f, z1 = 0.f;
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                acc[nt][e] += b1v[nt][e];
+                acc[nt][2 + e] += b1v[nt][e];
+                z0 += fmaxf(acc[nt][e], 0.f) * w2v[nt][e];
+                z1 += fmaxf(acc[nt][2 + e], 0.f) * w2v[nt][e];
+            }
+        z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
+        z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
+        z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
+        z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+        z0 += b2;
+        z1 += b2;
+        float dz[2];
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const float z = r ? z1 : z0, y = s_y[r ? r1 : r0];
+            if (y < 0.f) { dz[r] = 0.f; continue; }
+            const float p = 1.f / (1.f + expf(-z));
+            const float wy = in.pos_weight * y;
+            dz[r] = (p * (wy + 1.f - y) - wy) * inv_batch;
+            // softplus(-z) = -log sigmoid(z), softplus(z) = -log(1 - sigmoid(z))
+            const float sp_pos = fmaxf(-z, 0.f) + log1pf(expf(-fabsf(z)));
+            const float sp_neg = fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
+            if ((lane & 3) == 0) lsum += (wy * sp_pos + (1.f - y) * sp_neg) * inv_batch;
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int j = nt * 8 + kq + e;
+#pragma unroll
+                for (int r = 0; r < 2; ++r) {
+                    const float pre = acc[nt][2 * r + e];
+                    const float h = fmaxf(pre, 0.f);
+                    const float dh = pre > 0.f ? dz[r] * w2v[nt][e] : 0.f;
+                    g_w2[nt][e] += dz[r] * h;
+                    g_b1[nt][e] += dh;
+                    s_dh[r ? r1 : r0][j] = __bfloat16_as_ushort(__float2bfloat16_rn(dh));
+                }
+            }
+        if ((lane & 3) == 0) g_b2 += dz[0] + dz[1];
+    }
+    __syncthreads();
+    // phase 2: dW1 rows 16*warp .. 16*warp+15 = X^T dh over the block's 128 samples
+    {
+        float acc[8][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+        const int i0 = warp * 16 + (lane >> 2);
+        for (int ks = 0; ks < kBlockSamples / 16; ++ks) {
+            const int s0 = ks * 16 + kq;
+            uint32_t a[4];
+            a[0] = pack_raw(s_x[s0][i0], s_x[s0 + 1][i0]);
+            a[1] = pack_raw(s_x[s0][i0 + 8], s_x[s0 + 1][i0 + 8]);
+            a[2] = pack_raw(s_x[s0 + 8][i0], s_x[s0 + 9][i0]);
+            a[3] = pack_raw(s_x[s0 + 8][i0 + 8], s_x[s0 + 9][i0 + 8]);
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const int j = nt * 8 + (lane >> 2);
+                const uint32_t b0 = pack_raw(s_dh[s0][j], s_dh[s0 + 1][j]);
+                const uint32_t b1 = pack_raw(s_dh[s0 + 8][j], s_dh[s0 + 9][j]);
+                mma_bf16(acc[nt], a, b0, b1);
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int j = nt * 8 + kq + e;
+                atomicAdd(&grad[i0 * kHid + j], acc[nt][e]);
+                atomicAdd(&grad[(i0 + 8) * kHid + j], acc[nt][2 + e]);
+            }
+    }
+    // the per-column sums: lanes with equal (lane & 3) hold the same columns
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            float a = g_w2[nt][e], c = g_b1[nt][e];
+#pragma unroll
+            for (int o = 4; o < 32; o <<= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
+            }
+            if (lane < 4) {
+                const int j = nt * 8 + kq + e;
+                atomicAdd(&grad[kOffW2 + j], a);
+                atomicAdd(&grad[kOffB1 + j], c);
+            }
+        }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        g_b2 += __shfl_xor_sync(0xffffffffu, g_b2, o);
+        lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&grad[kOffB2], g_b2);
+        atomicAdd(loss_sum, lsum);
+    }
+}
+
+// Adam on the fp32 master parameters, then the bf16 / fp32 model copy
+__global__ void __launch_bounds__(256) k_adam(float* __restrict__ w, const float* __restrict__ grad, float* __restrict__ m,
+                                              float* __restrict__ v, AdamParams ap, DevModel* __restrict__ model) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kNumParams; i += gridDim.x * blockDim.x) {
+        if (ap.lr != 0.f) {
+            const float gi = grad[i];
+            const float mi = ap.beta1 * m[i] + (1.f - ap.beta1) * gi;
+            const float vi = ap.beta2 * v[i] + (1.f - ap.beta2) * gi * gi;
+            m[i] = mi;
+            v[i] = vi;
+            w[i] -= ap.lr * (mi * ap.inv_bc1) / (sqrtf(vi * ap.inv_bc2) + ap.eps);
+        }
+        const float wi = w[i];
+        if (i < kOffB1) model->w1[i] = __bfloat16_as_ushort(__float2bfloat16_rn(wi));
+        else if (i < kOffW2) model->b1[i - kOffB1] = wi;
+        else if (i < kOffB2) model->w2[i - kOffW2] = __bfloat16_as_ushort(__float2bfloat16_rn(wi));
+        else model->b2 = wi;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+LearnDims learn_dims(const pms_ctx* ctx) {
+    const pms_grid& g = ctx->grid;
+    LearnDims ld;
+    for (int a = 0; a < 3; ++a) {
+        ld.cres[a] = g.scres[a] / 2u + 2u;                        // coarse vertices per axis
+        ld.tiles[a] = ((g.scres[a] + 1u) / 2u + kTile - 1) / kTile;  // tiles over the coarse cells holding cubes
+    }
+    const double side = 2.0 * (double)g.sc_grid_size, sp = (double)ctx->prm.particle_spacing;
+    const double expected = (side / sp) * (side / sp) * (side / sp);
+    ld.inv_expected = (float)(expected > 0.0 ? 1.0 / expected : 1.0);
+    return ld;
+}
+
+pms_status launch_coarse_counts(pms_ctx* ctx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const LearnDims ld = learn_dims(ctx);
+    const size_t nc = (size_t)ld.cres[0] * ld.cres[1] * ld.cres[2];
+    PMS_CUDA(ctx, ctx->l_counts.ensure(4 * (nc ? nc : 1)));
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->l_counts.p, 0, 4 * nc, ctx->stream));
+    if (ctx->n) {
+        k_coarse_count<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(g, ld, ctx->spos.as<float4>(), ctx->n,
+                                                                         ctx->l_counts.as<uint32_t>());
+        PMS_LAUNCHED(ctx);
+    }
+    return PMS_OK;
+}
+
+pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* cand, float* logit, uint32_t cand_cap) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const LearnDims ld = learn_dims(ctx);
+    const uint64_t ntiles = (uint64_t)ld.tiles[0] * ld.tiles[1] * ld.tiles[2];
+    if (ntiles >= (1ull << 31)) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "coarse grid too large");
+    Counters* cnt = ctx->counters.as<Counters>();
+    PredictOut out;
+    out.q = q; out.cand = cand; out.logit = logit; out.cand_cap = cand_cap;
+    out.n_cand = &cnt->l_cand;
+    out.n_pred = &cnt->l_pred;
+    k_learn_predict<<<(unsigned)ntiles, kPredThreads, 0, ctx->stream>>>(g, ld, ctx->l_counts.as<uint32_t>(),
+                                                                       ctx->l_model.as<DevModel>(), use_model, out);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
+                               uint32_t* wcount) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
+    const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
+    k_cube_corners<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, exclude, out, wcount, nwords, nbits, sy, sz);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount) {
+    const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
+    k_bits_or<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(a, b, out, wcount, nwords);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
+
+pms_status launch_field_merge(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host,
+                              const uint32_t* bm_old, const uint32_t* wp_old, const float* f_old, const uint32_t* bm_new,
+                              const uint32_t* wp_new, const float* f_new, float* f_out) {
+    k_field_merge<<<grid_for(n_host, 256), 256, 0, ctx->stream>>>(vlist, n_dev, bm_old, wp_old, f_old, bm_new, wp_new,
+                                                                  f_new, f_out);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
+    const KGrid g = kgrid_of(ctx->grid);
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_border<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, &cnt->nv, ctx->vlist.as<uint32_t>(),
+                                                              ctx->mc_case.as<uint32_t>(),
+                                                              ctx->mc_key.as<unsigned long long>(), ctx->bm.as<uint32_t>(),
+                                                              qadd, &cnt->l_added);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm) {
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_label_bits<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(&cnt->nv, ctx->vlist.as<uint32_t>(),
+                                                                   ctx->mc_key.as<unsigned long long>(), lbm);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const LearnDims ld = learn_dims(ctx);
+    k_features<<<grid_for(64ull * n, 256), 256, 0, ctx->stream>>>(g, ld, ctx->l_counts.as<uint32_t>(), cubes, n, x);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,
+                         float* loss_sum) {
+    KGrid g = {};
+    LearnDims ld = {};
+    TrainIn in = {};
+    if (data) {
+        g = kgrid_of(data->grid);
+        ld = learn_dims(data);
+        in.cand = data->l_cand.as<uint32_t>();
+        in.n_cand = data->l_ncand;
+        in.labels = data->l_label.as<uint32_t>();
+        in.counts = data->l_counts.as<uint32_t>();
+    }
+    in.x = a.x;
+    in.y = a.y;
+    in.batch = a.batch;
+    in.seed = a.seed;
+    in.pos_weight = a.pos_weight;
+    const unsigned blocks = (a.batch + kBlockSamples - 1) / kBlockSamples;
+    k_learn_train<<<blocks, kTrainThreads, 0, stream>>>(g, ld, in, model, grad, loss_sum);
+    return cudaPeekAtLastError();
+}
+
+cudaError_t launch_adam(cudaStream_t stream, float* w, const float* grad, float* m, float* v, const AdamParams& ap,
+                        DevModel* model) {
+    k_adam<<<(kNumParams + 255) / 256, 256, 0, stream>>>(w, grad, m, v, ap, model);
+    return cudaPeekAtLastError();
+}
+
+}  // namespace pms

@@ -116,14 +116,18 @@ __device__ __forceinline__ float3 normalized(float3 v) {
 }
 
 // generateTriangles: one thread per valid cube
-__global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, const Counters* __restrict__ cnt,
+__global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counters* __restrict__ cnt,
                                                       const uint32_t* __restrict__ valid, const uint32_t* __restrict__ vlist,
                                                       const uint32_t* __restrict__ mc_case,
                                                       const unsigned long long* __restrict__ mc_off,
                                                       const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
                                                       const float* __restrict__ field, float* __restrict__ vert,
-                                                      float* __restrict__ vnorm) {
+                                                      float* __restrict__ vnorm,
+                                                      const unsigned long long* __restrict__ frame_base,
+                                                      unsigned long long cap) {
     const uint32_t nvalid = cnt->nvalid;
+    // batched frames write behind the earlier frames' vertices, within cap
+    const unsigned long long fb = frame_base ? *frame_base : 0ull;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const float sgn = (iso < 0.f) ? -1.f : 1.f;
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nvalid; k += gridDim.x * blockDim.x) {
@@ -161,11 +165,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, const 
             in[e] = make_float3(sgn * nn.x, sgn * nn.y, sgn * nn.z);
         }
         const uint32_t nvert = c_num_vertices[cs];
+        if (fb + base + nvert > cap) { atomicOr(&cnt->err, kErrCapacity); continue; }
         for (uint32_t v = 0; v < nvert; ++v) {
             const int e = c_tri[cs][v];
-            const size_t o = 3 * ((size_t)base + v);
+            const size_t o = 3 * ((size_t)fb + base + v);
             vert[o] = ip[e].x; vert[o + 1] = ip[e].y; vert[o + 2] = ip[e].z;
-            vnorm[o] = in[e].x; vnorm[o + 1] = in[e].y; vnorm[o + 2] = in[e].z;
+            if (vnorm) { vnorm[o] = in[e].x; vnorm[o + 1] = in[e].y; vnorm[o + 2] = in[e].z; }
         }
     }
 }
@@ -177,8 +182,9 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
         g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(),
         ctx->field.as<float>(), ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
     PMS_LAUNCHED(ctx);
+    // ctx->nv may be a bound (batched frames): the scan stops at the device count
     pms_status st = scan_u64(ctx, ctx->mc_key.as<unsigned long long>(), ctx->mc_off.as<unsigned long long>(), ctx->nv,
-                             ctx->tmp.as<unsigned long long>());
+                             ctx->tmp.as<unsigned long long>(), &cnt->nv);
     if (st != PMS_OK) return st;
     k_mc_totals<<<1, 1, 0, ctx->stream>>>(ctx->tmp.as<unsigned long long>(), cnt);
     PMS_LAUNCHED(ctx);
@@ -188,15 +194,34 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
     return PMS_OK;
 }
 
-pms_status launch_mc_emit(pms_ctx* ctx) {
+// batched frames: this frame's mesh starts where the earlier frames' meshes end
+__global__ void k_batch_base(const Counters* __restrict__ cnt, unsigned long long* __restrict__ running,
+                             unsigned long long* __restrict__ base) {
+    const unsigned long long b = *running;
+    *base = b;
+    *running = b + cnt->nmesh;
+}
+
+pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long long* running, unsigned long long* base) {
+    k_batch_base<<<1, 1, 0, ctx->stream>>>(cnt, running, base);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
+                             unsigned long long cap) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
         g, ctx->prm.iso_value, cnt, ctx->valid.as<uint32_t>(), ctx->vlist.as<uint32_t>(), ctx->mc_case.as<uint32_t>(),
         ctx->mc_off.as<unsigned long long>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(),
-        ctx->vert.as<float>(), ctx->vnorm.as<float>());
+        vert, vnorm, frame_base, cap);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
+}
+
+pms_status launch_mc_emit(pms_ctx* ctx) {
+    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull);
 }
 
 }  // namespace pms

@@ -84,6 +84,12 @@ extern "C" pms_status pms_create(const pms_config* cfg, int device, pms_ctx** ou
     cudaMemsetAsync(c->counters.p, 0, sizeof(Counters), c->stream);
     st = upload_mc_tables(c);
     if (st != PMS_OK) { pms_destroy(c); return st; }
+    if (cfg->band_model[0]) {
+        pms_band_model m;
+        if ((st = pms_load_band_model(cfg->band_model, &m)) != PMS_OK) { pms_destroy(c); return PMS_ERR_CONFIG; }
+        if ((st = pms_set_band_model(c, &m)) != PMS_OK) { pms_destroy(c); return st; }
+        c->band_mode = PMS_BAND_LEARNED;
+    }
     *out = c;
     return PMS_OK;
 }
@@ -92,6 +98,7 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    pms_batch_release(c);
     release_all(c);
     for (int i = 0; i <= kNumStages; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -118,7 +125,14 @@ extern "C" pms_status pms_set_stream(pms_ctx* c, void* s) {
 // ---------------------------------------------------------------------------
 // capacity
 // ---------------------------------------------------------------------------
-static pms_status ensure_particles(pms_ctx* c, uint32_t n) {
+namespace pms {
+pms_status ensure_particle_buffers(pms_ctx* c, uint32_t n);
+pms_status ensure_grid_buffers(pms_ctx* c, const pms_grid& g);
+}  // namespace pms
+static pms_status ensure_particles(pms_ctx* c, uint32_t n) { return pms::ensure_particle_buffers(c, n); }
+static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) { return pms::ensure_grid_buffers(c, g); }
+
+pms_status pms::ensure_particle_buffers(pms_ctx* c, uint32_t n) {
     const size_t N = n ? n : 1;
     PMS_CUDA(c, c->in_pos.ensure(12 * N));
     PMS_CUDA(c, c->in_vel.ensure(12 * N));
@@ -141,7 +155,7 @@ static pms_status ensure_particles(pms_ctx* c, uint32_t n) {
     return PMS_OK;
 }
 
-static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) {
+pms_status pms::ensure_grid_buffers(pms_ctx* c, const pms_grid& g) {
     const size_t S = g.sp_size ? g.sp_size : 1;
     PMS_CUDA(c, c->cell_count.ensure(4 * S));
     PMS_CUDA(c, c->cell_start.ensure(4 * (S + 1)));   // cell_start[S] = n
@@ -157,7 +171,12 @@ static pms_status ensure_grid(pms_ctx* c, const pms_grid& g) {
     return PMS_OK;
 }
 
-static pms_status ensure_band(pms_ctx* c, uint32_t nv) {
+namespace pms {
+pms_status ensure_band_buffers(pms_ctx* c, uint32_t nv);
+void mark_stage(pms_ctx* c, int boundary);
+}  // namespace pms
+
+pms_status pms::ensure_band_buffers(pms_ctx* c, uint32_t nv) {
     const size_t V = nv ? nv : 1;
     PMS_CUDA(c, c->vlist.ensure(4 * V));
     PMS_CUDA(c, c->field.ensure(4 * V));
@@ -203,7 +222,7 @@ static pms_status check_device_errors(pms_ctx* c) {
 
 // Stage timing: ev[0] opens a frame, ev[k + 1] closes stage k; a stage's time
 // runs from the most recent earlier event.
-static void mark(pms_ctx* c, int boundary) {
+void pms::mark_stage(pms_ctx* c, int boundary) {
     cudaEventRecord(c->ev[boundary], c->stream);
     if (boundary == 0) {
         c->last_event = 0;
@@ -214,6 +233,8 @@ static void mark(pms_ctx* c, int boundary) {
     c->ev_recorded[boundary - 1] = true;
     c->last_event = boundary;
 }
+static void mark(pms_ctx* c, int boundary) { mark_stage(c, boundary); }
+static pms_status ensure_band(pms_ctx* c, uint32_t nv) { return ensure_band_buffers(c, nv); }
 
 // ---------------------------------------------------------------------------
 // upload (FileData::loadFluidFile + GPUmemory::memAlcandCpy_fluid)
@@ -234,6 +255,8 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     c->n = n;
     c->have_particles = true;
     c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = false;
+    c->band_learned = c->mc_classified = false;
+    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     c->ns = c->nv = c->nvalid = 0;
     c->nmesh = 0;
     for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
@@ -299,6 +322,8 @@ extern "C" pms_status pms_band(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
     cudaSetDevice(c->device);
+    c->band_learned = c->mc_classified = false;
+    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
     pms_status st;
     if ((st = launch_band(c))) return st;
@@ -331,8 +356,9 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     c->nmesh = 0;
     if (c->nv) {
         pms_status st;
-        if ((st = launch_mc_classify(c))) return st;
-        if ((st = sync_counters(c))) return st;
+        // the learned band's last border check already classified the final vertex set
+        if (!c->mc_classified && (st = launch_mc_classify(c))) return st;
+        if (!c->mc_classified && (st = sync_counters(c))) return st;
         c->nvalid = c->h_counters->nvalid;
         c->nmesh = c->h_counters->nmesh;
         const size_t M = c->nmesh ? c->nmesh : 1;
@@ -368,7 +394,7 @@ extern "C" pms_status pms_run_frame(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     pms_status st;
     if ((st = pms_build_grid(c))) return st;
-    if (c->cfg.is_surface && (st = pms_surface(c))) return st;
+    if (c->cfg.is_surface && (st = c->band_mode == PMS_BAND_LEARNED ? pms_surface_learned(c) : pms_surface(c))) return st;
     if (c->cfg.is_diffuse && (st = pms_diffuse(c))) return st;
     c->frame_index++;
     return PMS_OK;
@@ -397,6 +423,12 @@ extern "C" pms_status pms_get_counts(pms_ctx* c, pms_counts* out) {
     out->n_spray = h.n_type[0];
     out->n_foam = h.n_type[1];
     out->n_bubble = h.n_type[2];
+    if (c->band_learned) {
+        out->n_band_candidates = c->l_ncand;
+        out->n_band_predicted = c->l_npred;
+        out->n_band_fallback = c->l_nadded;
+        out->n_band_iterations = c->l_iters;
+    }
     return check_device_errors(c);
 }
 

@@ -1,0 +1,372 @@
+// pms_batch.cpp -- many frames in one CUDA graph launch.  No counterpart in
+// the reference: GPUPOST::runSimulation (GPUPOST.cpp:56-81) runs one frame at
+// a time, synchronising with the host after almost every stage.
+//
+// A batch runs in two passes.  (1) All frames are copied into one device
+// arena and their bounding boxes are computed (one synchronisation for the
+// whole batch); the host derives each frame's grid from its box exactly as
+// for a single frame.  (2) Every stage of every frame is captured, in order,
+// into one CUDA graph whose kernels size their work from counts kept on the
+// device -- one Counters record per frame -- with host-side launch grids and
+// buffers sized by per-frame bounds, so nothing in the graph waits for the
+// host.  Frames run one after another on the context's buffers; meshes land
+// behind each other in one arena (the running offset lives on the device).
+// The graph is kept and relaunched while the frames' grids stay the same.
+//
+// With the learned band, the graph holds the prediction, the field at the
+// predicted corners and one border check per frame; a frame whose border
+// check finds missing cubes is re-run alone on the exact learned path
+// afterwards, so the batched result equals the single-frame result.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <utility>
+
+#include "pms_internal.h"
+#include "learn_internal.h"
+
+using namespace pms;
+
+namespace pms {
+pms_status ensure_band_buffers(pms_ctx* c, uint32_t nv);
+pms_status ensure_particle_buffers(pms_ctx* c, uint32_t n);
+pms_status ensure_grid_buffers(pms_ctx* c, const pms_grid& g);
+pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long long* running, unsigned long long* base);
+}  // namespace pms
+
+struct BatchState {
+    DBuf pos, vel, rho, cnt, base, mesh;
+    std::vector<uint32_t> n;
+    std::vector<uint64_t> off;
+    std::vector<pms_grid> grid;
+    std::vector<Counters> hcnt;
+    std::vector<unsigned long long> hbase;
+    std::vector<cudaEvent_t> ev;
+    std::vector<std::vector<float>> rerun_mesh;   // frames re-run alone (learned band fallback)
+    std::vector<char> rerun;
+    cudaGraphExec_t exec = nullptr;
+    int flags = -1;
+    uint64_t mesh_cap = 0;
+    uint32_t captures = 0, reruns = 0;
+    ~BatchState() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh}) b->release();
+    }
+};
+
+static BatchState* batch_of(pms_ctx* c) {
+    if (!c->batch) c->batch = new BatchState;
+    return static_cast<BatchState*>(c->batch);
+}
+
+void pms_batch_release(pms_ctx* c) {
+    delete static_cast<BatchState*>(c->batch);
+    c->batch = nullptr;
+}
+
+static bool same_grid(const pms_grid& a, const pms_grid& b) { return memcmp(&a, &b, sizeof(a)) == 0; }
+
+// Points the context at frame f of the arena (buffers borrowed, not owned).
+struct FrameView {
+    pms_ctx* c;
+    DBuf pos, vel, rho, cnt;
+    uint32_t n;
+    pms_grid grid;
+    explicit FrameView(pms_ctx* ctx) : c(ctx), pos(ctx->in_pos), vel(ctx->in_vel), rho(ctx->in_rho), cnt(ctx->counters),
+                                       n(ctx->n), grid(ctx->grid) {}
+    void point(BatchState* b, uint32_t f) {
+        c->in_pos.p = b->pos.as<char>() + 12 * b->off[f];
+        c->in_vel.p = b->vel.as<char>() + 12 * b->off[f];
+        c->in_rho.p = b->rho.as<char>() + 4 * b->off[f];
+        // borrowed: a capacity no request exceeds, so nothing frees or regrows them through the view
+        c->in_pos.cap = c->in_vel.cap = c->in_rho.cap = SIZE_MAX;
+        c->counters.p = b->cnt.as<Counters>() + f;
+        c->counters.cap = SIZE_MAX;
+        c->n = b->n[f];
+        c->grid = b->grid[f];
+    }
+    ~FrameView() {
+        c->in_pos = pos; c->in_vel = vel; c->in_rho = rho; c->counters = cnt;
+        c->n = n; c->grid = grid;
+    }
+};
+
+// Stages of one frame without host synchronisation (the context points at the frame).
+static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool learned) {
+    pms_status st;
+    Counters* cnt = c->counters.as<Counters>();
+    const pms_grid& g = c->grid;
+    const uint64_t W = ((uint64_t)g.sc_size + 31) / 32;
+    c->nv = g.sc_size;                       // bounds for launch grids; kernels read the device counts
+    c->nvalid = g.sc_size;
+    if ((st = launch_bbox(c))) return st;    // resets the frame's counters
+    if (c->n == 0) return PMS_OK;
+    if ((st = launch_hash_sort(c))) return st;
+    if ((st = launch_surface_cells(c))) return st;
+    if ((st = launch_density_aniso(c))) return st;
+    if (learned) {
+        if ((st = launch_coarse_counts(c))) return st;
+        PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
+        if ((st = launch_predict(c, 1, c->l_q.as<uint32_t>(), nullptr, nullptr, 0))) return st;
+        if ((st = launch_cube_corners(c, c->l_q.as<uint32_t>(), nullptr, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>())))
+            return st;
+        if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->wprefix.as<uint32_t>(), W, &cnt->nv))) return st;
+        if ((st = launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>())))
+            return st;
+        if ((st = launch_field(c))) return st;
+        if ((st = launch_mc_classify(c))) return st;
+        PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
+        if ((st = launch_border(c, c->l_qadd.as<uint32_t>()))) return st;   // counts into the frame's l_added
+    } else {
+        if ((st = launch_band(c))) return st;
+        if ((st = launch_band_list(c))) return st;
+        if ((st = launch_field(c))) return st;
+        if ((st = launch_mc_classify(c))) return st;
+    }
+    unsigned long long* base = b->base.as<unsigned long long>();
+    if ((st = launch_batch_base(c, cnt, base + b->n.size(), base + f))) return st;
+    return launch_mc_emit_to(c, b->mesh.as<float>(), nullptr, base + f, b->mesh_cap);
+}
+
+static pms_status capture(pms_ctx* c, BatchState* b, bool learned) {
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    const uint32_t k = (uint32_t)b->n.size();
+    cudaGraph_t graph = nullptr;
+    PMS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    pms_status st = PMS_OK;
+    {
+        FrameView view(c);
+        const uint64_t launches0 = c->launches;
+        cudaError_t e = cudaMemsetAsync(b->base.as<unsigned long long>() + k, 0, sizeof(unsigned long long), c->stream);
+        if (e != cudaSuccess) st = PMS_ERR_CUDA;
+        for (uint32_t f = 0; f < k && !st; ++f) {
+            view.point(b, f);
+            if (cudaEventRecord(b->ev[f], c->stream) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
+            st = capture_frame(c, b, f, learned);
+        }
+        if (!st && cudaEventRecord(b->ev[k], c->stream) != cudaSuccess) st = PMS_ERR_CUDA;
+        c->batch_launches = c->launches - launches0;
+        c->launches = launches0;             // counted when the graph runs
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (st) { if (graph) cudaGraphDestroy(graph); return st; }
+    if (e != cudaSuccess) return pms_fail(c, PMS_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { b->exec = nullptr; return pms_fail(c, PMS_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e)); }
+    b->captures++;
+    return PMS_OK;
+}
+
+static pms_status check_frame_errors(pms_ctx* c, const Counters& h, uint32_t f) {
+    if (h.err & kErrNonFinite) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: positions contain NaN or Inf", f);
+    if (h.err & kErrBigCell) return pms_fail(c, PMS_ERR_UNSUPPORTED, "frame %u: a spatial cell holds more than 4096 particles", f);
+    if (h.err & kErrKeyRange) return pms_fail(c, PMS_ERR_CUDA, "frame %u: internal: a cell key fell outside the grid", f);
+    return PMS_OK;
+}
+
+static inline float decode_ordered(uint32_t u) {
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_t k, int flags) {
+    if (!c || (k && !frames)) return PMS_ERR_INVALID_ARGUMENT;
+    const bool learned = (flags & PMS_BATCH_LEARNED) != 0;
+    if (learned && !c->have_model) return pms_fail(c, PMS_ERR_STATE, "learned batch without a model");
+    for (uint32_t f = 0; f < k; ++f)
+        if (frames[f].n && !frames[f].pos_xyz) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: no positions", f);
+    cudaSetDevice(c->device);
+    BatchState* b = batch_of(c);
+    if (k == 0) { b->n.clear(); b->hcnt.clear(); b->rerun.clear(); b->rerun_mesh.clear(); return PMS_OK; }
+    // ---- pass 1: arena, uploads, bounding boxes
+    uint64_t total = 0;
+    std::vector<uint64_t> off(k);
+    std::vector<uint32_t> n(k);
+    uint32_t nmax = 0;
+    for (uint32_t f = 0; f < k; ++f) { off[f] = total; n[f] = frames[f].n; total += n[f]; nmax = std::max(nmax, n[f]); }
+    const size_t T = total ? total : 1;
+    PMS_CUDA(c, b->pos.ensure(12 * T));
+    PMS_CUDA(c, b->vel.ensure(12 * T));
+    PMS_CUDA(c, b->rho.ensure(4 * T));
+    PMS_CUDA(c, b->cnt.ensure(sizeof(Counters) * (k ? k : 1)));
+    PMS_CUDA(c, b->base.ensure(sizeof(unsigned long long) * (k + 1)));
+    const bool shape_same = b->n == n && b->flags == flags;
+    for (uint32_t f = 0; f < k; ++f) {
+        const size_t m = n[f];
+        if (!m) continue;
+        PMS_CUDA(c, cudaMemcpyAsync(b->pos.as<char>() + 12 * off[f], frames[f].pos_xyz, 12 * m, cudaMemcpyDefault, c->stream));
+        if (frames[f].vel_xyz)
+            PMS_CUDA(c, cudaMemcpyAsync(b->vel.as<char>() + 12 * off[f], frames[f].vel_xyz, 12 * m, cudaMemcpyDefault, c->stream));
+        else
+            PMS_CUDA(c, cudaMemsetAsync(b->vel.as<char>() + 12 * off[f], 0, 12 * m, c->stream));
+        if (frames[f].rhop)
+            PMS_CUDA(c, cudaMemcpyAsync(b->rho.as<char>() + 4 * off[f], frames[f].rhop, 4 * m, cudaMemcpyDefault, c->stream));
+        else
+            PMS_CUDA(c, cudaMemsetAsync(b->rho.as<char>() + 4 * off[f], 0, 4 * m, c->stream));
+    }
+    b->n = n;
+    b->off = off;
+    b->flags = flags;
+    pms_status st;
+    {
+        FrameView view(c);
+        for (uint32_t f = 0; f < k; ++f) {
+            view.point(b, f);
+            if ((st = launch_bbox(c))) return st;
+        }
+    }
+    b->hcnt.resize(k);
+    if (k) PMS_CUDA(c, cudaMemcpyAsync(b->hcnt.data(), b->cnt.p, sizeof(Counters) * k, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<pms_grid> grid(k);
+    pms_grid gmax = {};
+    for (uint32_t f = 0; f < k; ++f) {
+        if ((st = check_frame_errors(c, b->hcnt[f], f))) return st;
+        if (!n[f]) { memset(&grid[f], 0, sizeof(pms_grid)); continue; }
+        float bmin[3], bmax[3];
+        for (int a = 0; a < 3; ++a) { bmin[a] = decode_ordered(b->hcnt[f].bbox_min[a]); bmax[a] = decode_ordered(b->hcnt[f].bbox_max[a]); }
+        if ((st = pms_grid_from_bbox(&c->prm, bmin, bmax, &grid[f]))) return pms_fail(c, st, "frame %u: grid too large", f);
+        gmax.sp_size = std::max(gmax.sp_size, grid[f].sp_size);
+        gmax.sc_size = std::max(gmax.sc_size, grid[f].sc_size);
+    }
+    bool grids_same = shape_same && b->grid.size() == k;
+    for (uint32_t f = 0; grids_same && f < k; ++f) grids_same = same_grid(b->grid[f], grid[f]);
+    b->grid = grid;
+    // ---- capacities for the largest frame (nothing may allocate inside the graph)
+    if ((st = ensure_particle_buffers(c, nmax))) return st;
+    if ((st = ensure_grid_buffers(c, gmax))) return st;
+    if ((st = ensure_band_buffers(c, gmax.sc_size))) return st;
+    PMS_CUDA(c, c->scan.partial.ensure(sizeof(unsigned long long) * 1024));
+    if (learned) {
+        const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
+        PMS_CUDA(c, c->l_q.ensure(4 * (W + 1)));
+        PMS_CUDA(c, c->l_qadd.ensure(4 * (W + 1)));
+        size_t ncoarse = 1;
+        for (uint32_t f = 0; f < k; ++f) {
+            const size_t m = (size_t)(grid[f].scres[0] / 2 + 2) * (grid[f].scres[1] / 2 + 2) * (grid[f].scres[2] / 2 + 2);
+            ncoarse = std::max(ncoarse, m);
+        }
+        PMS_CUDA(c, c->l_counts.ensure(4 * ncoarse));
+    }
+    uint64_t want_cap = 0;
+    for (uint32_t f = 0; f < k; ++f) {
+        const uint64_t sx = grid[f].scres[0], sy = grid[f].scres[1], sz = grid[f].scres[2];
+        want_cap += std::min<uint64_t>(15ull * grid[f].sc_size, std::max<uint64_t>(1u << 20, 24ull * (sx * sy + sy * sz + sx * sz)));
+    }
+    if (want_cap > b->mesh_cap) { b->mesh_cap = want_cap; grids_same = false; }
+    PMS_CUDA(c, b->mesh.ensure(12 * (b->mesh_cap ? b->mesh_cap : 1)));
+    while (b->ev.size() < k + 1) {
+        cudaEvent_t e;
+        PMS_CUDA(c, cudaEventCreate(&e));
+        b->ev.push_back(e);
+    }
+    // ---- pass 2: the graph (captured again when the frames' grids changed)
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        if (!grids_same || !b->exec) {
+            if ((st = capture(c, b, learned))) return st;
+            grids_same = true;
+        }
+        PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
+        c->launches += c->batch_launches;
+        b->hbase.resize(k + 1);
+        if (k) PMS_CUDA(c, cudaMemcpyAsync(b->hcnt.data(), b->cnt.p, sizeof(Counters) * k, cudaMemcpyDeviceToHost, c->stream));
+        PMS_CUDA(c, cudaMemcpyAsync(b->hbase.data(), b->base.p, sizeof(unsigned long long) * (k + 1), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+        bool overflow = false;
+        for (uint32_t f = 0; f < k; ++f) {
+            if ((st = check_frame_errors(c, b->hcnt[f], f))) return st;
+            overflow |= (b->hcnt[f].err & kErrCapacity) != 0;
+        }
+        if (!overflow) break;
+        b->mesh_cap = std::max<uint64_t>(2 * b->mesh_cap, b->hbase[k] + (b->hbase[k] >> 2));
+        PMS_CUDA(c, b->mesh.ensure(12 * b->mesh_cap));
+        grids_same = false;
+        if (attempt == 2) return pms_fail(c, PMS_ERR_CAPACITY, "batch mesh arena overflow");
+    }
+    // ---- learned band: frames whose border check found missing cubes run alone on the exact path
+    b->rerun.assign(k, 0);
+    b->rerun_mesh.assign(k, {});
+    if (learned) {
+        for (uint32_t f = 0; f < k; ++f) {
+            if (b->hcnt[f].l_added == 0) continue;
+            b->rerun[f] = 1;
+            b->reruns++;
+            if ((st = pms_upload_particles_device(c, b->pos.as<float>() + 3 * off[f], b->vel.as<float>() + 3 * off[f],
+                                                  b->rho.as<float>() + off[f], n[f])))
+                return st;
+            if ((st = pms_build_grid(c)) || (st = pms_surface_learned(c))) return st;
+            uint64_t nv = 0;
+            pms_download_mesh(c, nullptr, nullptr, 0, &nv);
+            b->rerun_mesh[f].resize(3 * nv);
+            if (nv && (st = pms_download_mesh(c, b->rerun_mesh[f].data(), nullptr, nv, &nv))) return st;
+            PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+            pms::Counters h = *c->h_counters;
+            h.l_added = 0;
+            b->hcnt[f] = h;
+            b->hcnt[f].nmesh = nv;
+        }
+    }
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_frame(pms_ctx* c, uint32_t f, pms_counts* out, float* ms) {
+    if (!c || !c->batch) return PMS_ERR_INVALID_ARGUMENT;
+    BatchState* b = static_cast<BatchState*>(c->batch);
+    if (f >= b->n.size()) return PMS_ERR_INVALID_ARGUMENT;
+    const Counters& h = b->hcnt[f];
+    if (out) {
+        memset(out, 0, sizeof(*out));
+        out->n_particles = b->n[f];
+        out->n_surface_particles = h.ns;
+        out->n_band_vertices = h.nv;
+        out->n_valid_cubes = h.nvalid;
+        out->n_mesh_vertices = h.nmesh;
+        out->n_fp64_svd = h.n_fp64;
+        if (b->flags & PMS_BATCH_LEARNED) {
+            out->n_band_candidates = h.l_cand;
+            out->n_band_predicted = h.l_pred;
+            out->n_band_iterations = b->rerun[f] ? 1u : 0u;
+        }
+    }
+    if (ms) {
+        *ms = 0.f;
+        if (!b->rerun[f]) cudaEventElapsedTime(ms, b->ev[f], b->ev[f + 1]);
+    }
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_mesh(pms_ctx* c, uint32_t f, float* pos, uint64_t cap, uint64_t* n_out) {
+    if (!c || !c->batch || !n_out) return PMS_ERR_INVALID_ARGUMENT;
+    BatchState* b = static_cast<BatchState*>(c->batch);
+    if (f >= b->n.size()) return PMS_ERR_INVALID_ARGUMENT;
+    if (b->rerun[f]) {
+        const uint64_t m = b->rerun_mesh[f].size() / 3;
+        *n_out = m;
+        if (!pos) return PMS_OK;
+        if (cap < m) return PMS_ERR_CAPACITY;
+        memcpy(pos, b->rerun_mesh[f].data(), 12 * m);
+        return PMS_OK;
+    }
+    const uint64_t m = b->hcnt[f].nmesh;
+    *n_out = m;
+    if (!pos) return PMS_OK;
+    if (cap < m) return PMS_ERR_CAPACITY;
+    cudaSetDevice(c->device);
+    if (m) PMS_CUDA(c, cudaMemcpyAsync(pos, b->mesh.as<float>() + 3 * b->hbase[f], 12 * m, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_info(pms_ctx* c, uint32_t* graph_kernels, uint32_t* captures, uint32_t* reruns) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    BatchState* b = static_cast<BatchState*>(c->batch);
+    if (graph_kernels) *graph_kernels = (uint32_t)c->batch_launches;
+    if (captures) *captures = b ? b->captures : 0;
+    if (reruns) *reruns = b ? b->reruns : 0;
+    return PMS_OK;
+}

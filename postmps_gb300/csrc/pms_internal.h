@@ -51,7 +51,11 @@ struct Counters {
     uint32_t n_live;        // after delete/append
     uint32_t n_type[4];     // spray, foam, bubble, deleted
     uint32_t rad_max_bits;  // largest anisotropic support maxvalue * h (float bits)
-    uint32_t pad[1];
+    // learned band
+    uint32_t l_cand;        // candidate cubes evaluated by the network
+    uint32_t l_pred;        // predicted cubes (or candidate slots written)
+    uint32_t l_added;       // cubes the last border check queued
+    uint32_t l_nnew;        // vertices those cubes add
 };
 
 enum : uint32_t {
@@ -76,6 +80,12 @@ const char* mc_tables_origin();
 // Scan workspace.
 struct ScanTemp {
     DBuf partial;           // per-block partial sums (u64 capable)
+};
+
+// Launch shapes chosen by the autotuner (pms_autotune): threads per block of
+// the neighbour walks and the field's resident-block cap (blocks per SM).
+struct Tune {
+    int field_threads = 128, field_waves = 8, density_threads = 128, moments_threads = 128;
 };
 
 // Stage timing events.
@@ -117,6 +127,16 @@ struct pms_ctx {
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
+    // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
+    pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
+              l_field_new, l_vlist_m, l_field_m, l_cand, l_logit, l_label;
+    bool have_model = false, band_learned = false, mc_classified = false;
+    int band_mode = PMS_BAND_PLAIN;
+    pms::Tune tune;
+    // batched frames (pms_batch.cpp)
+    void* batch = nullptr;
+    uint64_t batch_launches = 0;         // kernels in the batch graph
+    uint32_t l_ncand = 0, l_npred = 0, l_nadded = 0, l_iters = 0;
     uint32_t diffuse_old = 0;    // live diffuse particles carried to the next frame
     uint32_t frame_index = 0;
 
@@ -162,10 +182,12 @@ inline unsigned grid_for(uint64_t n, unsigned block, unsigned max_blocks = 152u 
 }
 
 // scans (scan.cu): exclusive prefix sums of n elements; *total_dev receives the
-// sum (may be null).  All asynchronous on the stream.
-pms_status scan_u32(pms_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev);
+// sum (may be null); with n_dev, elements at and past *n_dev count as zero
+// (n is then a bound).  All asynchronous on the stream.
+pms_status scan_u32(pms_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev,
+                    const uint32_t* n_dev = nullptr);
 pms_status scan_u64(pms_ctx* ctx, const unsigned long long* in, unsigned long long* out, uint64_t n,
-                    unsigned long long* total_dev);
+                    unsigned long long* total_dev, const uint32_t* n_dev = nullptr);
 
 // stage launchers (one .cu each)
 pms_status launch_bbox(pms_ctx* ctx);
@@ -175,13 +197,23 @@ pms_status launch_density_aniso(pms_ctx* ctx);
 pms_status launch_band(pms_ctx* ctx);
 pms_status launch_band_list(pms_ctx* ctx);
 pms_status launch_field(pms_ctx* ctx);
+// field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid)
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
+// ascending list of the set bits of a bitmap over the scalar grid
+pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 pms_status launch_mc_classify(pms_ctx* ctx);
 pms_status launch_mc_emit(pms_ctx* ctx);
+// triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
+pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
+                             unsigned long long cap);
 pms_status launch_diffuse(pms_ctx* ctx);
 pms_status upload_mc_tables(pms_ctx* ctx);
 
 // host utilities
 pms_status sync_counters(pms_ctx* ctx);
+}  // namespace pms
+void pms_batch_release(pms_ctx* c);   // pms_batch.cpp
+namespace pms {
 // diffuse results (k_diffuse.cu)
 pms_status diffuse_debug(pms_ctx* ctx, int array_id, std::vector<uint8_t>& out);
 pms_status write_diffuse_frame(pms_ctx* ctx, const pms_config& cfg, int frame);

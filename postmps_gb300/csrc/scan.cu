@@ -47,12 +47,13 @@ __device__ __forceinline__ T block_excl_scan(T v, T* smem_warp, T& total) {
 
 template <class T>
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const T* __restrict__ in, uint64_t n, uint64_t chunk,
-                                                              T* __restrict__ partial) {
+                                                              T* __restrict__ partial, const uint32_t* __restrict__ n_dev) {
     __shared__ T warp_sums[kScanThreads / 32];
     uint64_t b0 = (uint64_t)blockIdx.x * chunk;
     uint64_t b1 = b0 + chunk < n ? b0 + chunk : n;
+    const uint64_t nn = n_dev && (uint64_t)*n_dev < n ? (uint64_t)*n_dev : n;   // elements past nn count as 0
     T acc = 0;
-    for (uint64_t i = b0 + threadIdx.x; i < b1; i += kScanThreads) acc += in[i];
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += kScanThreads) acc += i < nn ? in[i] : T(0);
     T total;
     block_excl_scan<T>(acc, warp_sums, total);
     if (threadIdx.x == 0) partial[blockIdx.x] = total;
@@ -75,17 +76,19 @@ __global__ void __launch_bounds__(1024) k_scan_partials(T* __restrict__ partial,
 
 template <class T>
 __global__ void __launch_bounds__(kScanThreads) k_scan_down(const T* __restrict__ in, T* __restrict__ out, uint64_t n,
-                                                             uint64_t chunk, const T* __restrict__ partial) {
+                                                             uint64_t chunk, const T* __restrict__ partial,
+                                                             const uint32_t* __restrict__ n_dev) {
     __shared__ T tile[kScanTile];
     __shared__ T warp_sums[kScanThreads / 32];
     uint64_t b0 = (uint64_t)blockIdx.x * chunk;
     uint64_t b1 = b0 + chunk < n ? b0 + chunk : n;
+    const uint64_t nn = n_dev && (uint64_t)*n_dev < n ? (uint64_t)*n_dev : n;
     T carry = partial[blockIdx.x];
     for (uint64_t t0 = b0; t0 < b1; t0 += kScanTile) {
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             uint64_t i = t0 + k * kScanThreads + threadIdx.x;
-            tile[k * kScanThreads + threadIdx.x] = i < b1 ? in[i] : T(0);
+            tile[k * kScanThreads + threadIdx.x] = i < nn && i < b1 ? in[i] : T(0);
         }
         __syncthreads();
         T loc[kScanItems];
@@ -108,7 +111,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_down(const T* __restrict_
 }
 
 template <class T>
-static pms_status scan_impl(pms_ctx* ctx, const T* in, T* out, uint64_t n, T* total_dev) {
+static pms_status scan_impl(pms_ctx* ctx, const T* in, T* out, uint64_t n, T* total_dev, const uint32_t* n_dev) {
     if (n == 0) {
         if (total_dev) PMS_CUDA(ctx, cudaMemsetAsync(total_dev, 0, sizeof(T), ctx->stream));
         return PMS_OK;
@@ -119,21 +122,22 @@ static pms_status scan_impl(pms_ctx* ctx, const T* in, T* out, uint64_t n, T* to
     nb = (int)((n + chunk - 1) / chunk);
     PMS_CUDA(ctx, ctx->scan.partial.ensure(sizeof(unsigned long long) * kScanMaxBlocks));
     T* partial = ctx->scan.partial.as<T>();
-    k_scan_reduce<T><<<nb, kScanThreads, 0, ctx->stream>>>(in, n, chunk, partial);
+    k_scan_reduce<T><<<nb, kScanThreads, 0, ctx->stream>>>(in, n, chunk, partial, n_dev);
     PMS_LAUNCHED(ctx);
     k_scan_partials<T><<<1, 1024, 0, ctx->stream>>>(partial, nb, total_dev);
     PMS_LAUNCHED(ctx);
-    k_scan_down<T><<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n, chunk, partial);
+    k_scan_down<T><<<nb, kScanThreads, 0, ctx->stream>>>(in, out, n, chunk, partial, n_dev);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
-pms_status scan_u32(pms_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev) {
-    return scan_impl<uint32_t>(ctx, in, out, n, total_dev);
+pms_status scan_u32(pms_ctx* ctx, const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* total_dev,
+                    const uint32_t* n_dev) {
+    return scan_impl<uint32_t>(ctx, in, out, n, total_dev, n_dev);
 }
 pms_status scan_u64(pms_ctx* ctx, const unsigned long long* in, unsigned long long* out, uint64_t n,
-                    unsigned long long* total_dev) {
-    return scan_impl<unsigned long long>(ctx, in, out, n, total_dev);
+                    unsigned long long* total_dev, const uint32_t* n_dev) {
+    return scan_impl<unsigned long long>(ctx, in, out, n, total_dev, n_dev);
 }
 
 }  // namespace pms

@@ -57,7 +57,7 @@ class Config(C.Structure):
         ("fluid_path", C.c_char * 512), ("fluid_prefix", C.c_char * 128),
         ("surface_path", C.c_char * 512), ("surface_prefix", C.c_char * 128),
         ("diffuse_path", C.c_char * 512), ("diffuse_prefix", C.c_char * 128),
-        ("fp64_svd_cond", C.c_double), ("rng_seed", C.c_uint64),
+        ("fp64_svd_cond", C.c_double), ("rng_seed", C.c_uint64), ("band_model", C.c_char * 512),
     ]
 
 
@@ -94,10 +94,52 @@ class Counts(C.Structure):
         ("n_valid_cubes", C.c_uint32), ("n_mesh_vertices", C.c_uint64), ("n_free_surface", C.c_uint32),
         ("n_generated_diffuse", C.c_uint32), ("n_spawning", C.c_uint32), ("n_diffuse", C.c_uint32),
         ("n_spray", C.c_uint32), ("n_foam", C.c_uint32), ("n_bubble", C.c_uint32), ("n_fp64_svd", C.c_uint32),
+        ("n_band_candidates", C.c_uint32), ("n_band_predicted", C.c_uint32), ("n_band_fallback", C.c_uint32),
+        ("n_band_iterations", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tune(C.Structure):
+    """pms_tune: launch shapes of the neighbour walks."""
+    _fields_ = [("field_threads", C.c_int), ("field_waves", C.c_int), ("density_threads", C.c_int),
+                ("moments_threads", C.c_int), ("anisotropy_ms", C.c_float), ("field_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Frame(C.Structure):
+    """pms_frame: one frame of a batch (host or device pointers)."""
+    _fields_ = [("pos_xyz", C.c_void_p), ("vel_xyz", C.c_void_p), ("rhop", C.c_void_p), ("n", C.c_uint32)]
+
+
+BATCH_LEARNED = 1
+MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 64, 64, 4225
+
+
+class BandModel(C.Structure):
+    """pms_band_model: bf16 weights (as uint16 bits), fp32 biases, logit threshold."""
+    _fields_ = [
+        ("w1", C.c_uint16 * (MLP_INPUTS * MLP_HIDDEN)), ("b1", C.c_float * MLP_HIDDEN),
+        ("w2", C.c_uint16 * MLP_HIDDEN), ("b2", C.c_float), ("threshold", C.c_float),
+    ]
+
+    def arrays(self) -> dict:
+        return {"w1": np.ctypeslib.as_array(self.w1).copy(), "b1": np.ctypeslib.as_array(self.b1).copy(),
+                "w2": np.ctypeslib.as_array(self.w2).copy(), "b2": float(self.b2), "threshold": float(self.threshold)}
+
+    @classmethod
+    def from_arrays(cls, d: dict) -> "BandModel":
+        m = cls()
+        np.ctypeslib.as_array(m.w1)[:] = np.asarray(d["w1"], np.uint16).reshape(-1)
+        np.ctypeslib.as_array(m.b1)[:] = np.asarray(d["b1"], np.float32).reshape(-1)
+        np.ctypeslib.as_array(m.w2)[:] = np.asarray(d["w2"], np.uint16).reshape(-1)
+        m.b2 = float(d["b2"])
+        m.threshold = float(d["threshold"])
+        return m
 
 
 _lib = None
@@ -149,6 +191,30 @@ def lib() -> C.CDLL:
         L.pms_free_host.restype = None
         L.pms_run_config.argtypes = [C.c_char_p, C.c_int]
         L.pms_mc_tables.argtypes = [_u32p, _i32p, _u32p, _u32p, C.c_int]
+        L.pms_set_band_model.argtypes = [vp, C.POINTER(BandModel)]
+        L.pms_set_band_mode.argtypes = [vp, C.c_int]
+        L.pms_run_batch.argtypes = [vp, C.POINTER(Frame), C.c_uint32, C.c_int]
+        L.pms_autotune.argtypes = [vp, C.POINTER(Tune)]
+        L.pms_set_tune.argtypes = [vp, C.POINTER(Tune)]
+        L.pms_get_tune.argtypes = [vp, C.POINTER(Tune)]
+        L.pms_batch_frame.argtypes = [vp, C.c_uint32, C.POINTER(Counts), C.POINTER(C.c_float)]
+        L.pms_batch_mesh.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.pms_batch_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.pms_save_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel), C.c_char_p]
+        L.pms_load_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel)]
+        L.pms_band_learned.argtypes = [vp]
+        L.pms_surface_learned.argtypes = [vp]
+        L.pms_learn_prepare.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.pms_learn_candidates.argtypes = [vp, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32)]
+        L.pms_learn_features.argtypes = [vp, vp, C.c_uint32, vp]
+        L.pms_trainer_create.argtypes = [C.c_int, C.c_uint64, C.POINTER(vp)]
+        L.pms_trainer_destroy.argtypes = [vp]
+        L.pms_trainer_destroy.restype = None
+        L.pms_trainer_step.argtypes = [vp, vp, C.c_uint32, C.c_uint64, C.c_float, C.c_float, C.POINTER(C.c_float)]
+        L.pms_trainer_grad.argtypes = [vp, vp, vp, C.c_uint32, C.c_float, vp, C.POINTER(C.c_float)]
+        L.pms_trainer_get_params.argtypes = [vp, vp]
+        L.pms_trainer_set_params.argtypes = [vp, vp]
+        L.pms_trainer_get_model.argtypes = [vp, C.POINTER(BandModel)]
         _lib = L
     return _lib
 
@@ -290,6 +356,91 @@ class Context:
     def diffuse(self): self._call("pms_diffuse")
     def run_frame(self): self._call("pms_run_frame")
 
+    # learned band
+    def set_band_model(self, model: BandModel) -> None:
+        self._call("pms_set_band_model", C.byref(model))
+
+    def set_band_mode(self, learned: bool) -> None:
+        self._call("pms_set_band_mode", 1 if learned else 0)
+
+    def band_learned(self): self._call("pms_band_learned")
+    def surface_learned(self): self._call("pms_surface_learned")
+
+    def learn_prepare(self) -> tuple[int, int]:
+        nc, nv = C.c_uint32(), C.c_uint32()
+        self._call("pms_learn_prepare", C.byref(nc), C.byref(nv))
+        return nc.value, nv.value
+
+    def learn_candidates(self, logits: bool = True) -> dict:
+        n = C.c_uint32()
+        st = lib().pms_learn_candidates(self._h, None, None, None, 0, C.byref(n))
+        if st not in (0, 4):
+            _check(st, self._h)
+        m = n.value
+        ids = np.zeros(m, np.uint32)
+        lg = np.zeros(m, np.float32) if logits else None
+        lab = np.zeros(m, np.uint8)
+        self._call("pms_learn_candidates", _ptr(ids), _ptr(lg), _ptr(lab), m, C.byref(n))
+        return {"cube": ids, "logit": lg, "label": lab}
+
+    # autotuner
+    def autotune(self) -> dict:
+        t = Tune()
+        self._call("pms_autotune", C.byref(t))
+        return t.as_dict()
+
+    def set_tune(self, d: dict) -> None:
+        t = Tune(**{k: d[k] for k in ("field_threads", "field_waves", "density_threads", "moments_threads")})
+        self._call("pms_set_tune", C.byref(t))
+
+    def get_tune(self) -> dict:
+        t = Tune()
+        self._call("pms_get_tune", C.byref(t))
+        return t.as_dict()
+
+    # batched frames
+    def run_batch(self, frames, learned: bool = False) -> None:
+        """frames: sequence of (pos, vel, rho) numpy arrays (vel / rho may be None),
+        or of pms_frame-like (pos_ptr, vel_ptr, rho_ptr, n) tuples of raw pointers."""
+        arr = (Frame * max(1, len(frames)))()
+        self._keep = []
+        for i, fr in enumerate(frames):
+            if len(fr) == 4:
+                arr[i] = Frame(fr[0], fr[1], fr[2], fr[3])
+                continue
+            pos, vel, rho = fr
+            pos = np.ascontiguousarray(pos, np.float32)
+            vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+            rho = None if rho is None else np.ascontiguousarray(rho, np.float32)
+            self._keep += [pos, vel, rho]
+            arr[i] = Frame(_ptr(pos), _ptr(vel), _ptr(rho), len(pos))
+        self._call("pms_run_batch", arr, len(frames), BATCH_LEARNED if learned else 0)
+
+    def batch_frame(self, f: int) -> tuple[Counts, float]:
+        c = Counts()
+        ms = C.c_float()
+        self._call("pms_batch_frame", f, C.byref(c), C.byref(ms))
+        return c, float(ms.value)
+
+    def batch_mesh(self, f: int) -> np.ndarray:
+        n = C.c_uint64()
+        self._call("pms_batch_mesh", f, None, 0, C.byref(n))
+        out = np.zeros((n.value, 3), np.float32)
+        if n.value:
+            self._call("pms_batch_mesh", f, _ptr(out), n.value, C.byref(n))
+        return out
+
+    def batch_info(self) -> dict:
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._call("pms_batch_info", C.byref(a), C.byref(b), C.byref(c))
+        return {"graph_kernels": a.value, "captures": b.value, "reruns": c.value}
+
+    def learn_features(self, cubes) -> np.ndarray:
+        cubes = np.ascontiguousarray(cubes, np.uint32)
+        x = np.zeros((len(cubes), MLP_INPUTS), np.uint16)
+        self._call("pms_learn_features", _ptr(cubes), len(cubes), _ptr(x))
+        return x
+
     # results
     def counts(self) -> Counts:
         c = Counts()
@@ -349,3 +500,62 @@ class Context:
     @property
     def launches(self) -> int:
         return int(lib().pms_kernel_launches(self._h))
+
+
+def save_band_model(path: str, model: BandModel, meta: str = "") -> None:
+    _check(lib().pms_save_band_model(path.encode(), C.byref(model), meta.encode()))
+
+
+def load_band_model(path: str) -> BandModel:
+    m = BandModel()
+    _check(lib().pms_load_band_model(path.encode(), C.byref(m)))
+    return m
+
+
+class Trainer:
+    """pms_trainer: fp32 master weights and Adam state of the band MLP; the
+    forward and backward passes run in libpms's BF16 tensor-core kernels."""
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        h = C.c_void_p()
+        _check(lib().pms_trainer_create(device, seed, C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().pms_trainer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, ctx: "Context", batch: int, seed: int, lr: float, pos_weight: float) -> float:
+        loss = C.c_float()
+        _check(lib().pms_trainer_step(self._h, ctx.handle, batch, seed, lr, pos_weight, C.byref(loss)), ctx.handle)
+        return float(loss.value)
+
+    def grad(self, x_bf16: np.ndarray, y: np.ndarray, pos_weight: float) -> tuple[np.ndarray, float]:
+        x = np.ascontiguousarray(x_bf16, np.uint16)
+        yy = np.ascontiguousarray(y, np.uint8)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = C.c_float()
+        _check(lib().pms_trainer_grad(self._h, _ptr(x), _ptr(yy), len(yy), pos_weight, _ptr(g), C.byref(loss)))
+        return g, float(loss.value)
+
+    def params(self) -> np.ndarray:
+        w = np.zeros(MLP_PARAMS, np.float32)
+        _check(lib().pms_trainer_get_params(self._h, _ptr(w)))
+        return w
+
+    def set_params(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, np.float32)
+        _check(lib().pms_trainer_set_params(self._h, _ptr(w)))
+
+    def model(self, threshold: float = 0.0) -> BandModel:
+        m = BandModel()
+        _check(lib().pms_trainer_get_model(self._h, C.byref(m)))
+        m.threshold = threshold
+        return m

@@ -110,14 +110,15 @@ def crown_splash(n_slab=(200, 200, 40), spacing: float = 0.005, n_ring: int = 40
     return pos, vel, rho
 
 
-def sloshing_tank(frame: int, n_frames: int = 16, spacing: float = 0.01, length: float = 1.0, width: float = 0.3,
-                  depth0: float = 0.3, amp: float = 0.05, seed: int = 5):
+def sloshing_tank(frame: int, n_frames: int = 16, spacing: float = 0.01, length: float = 2.0, width: float = 1.0,
+                  depth_min: float = 0.05, depth_max: float = 0.75, amp: float = 0.05, seed: int = 5):
     """Frame k of a sloshing tank: particles fill z <= z0 + A sin(2 pi t) cos(pi x / L),
-    t = k / n_frames seconds, with a seeded fill level so that counts vary
-    between frames (seeded inflow/outflow)."""
+    t = k / n_frames seconds, with a seeded fill level z0 in [depth_min,
+    depth_max] (seeded inflow/outflow), so that at the default sizes the
+    particle count varies between about 100k and 1.5M per frame."""
     t = frame / float(n_frames)
     level = uniform(seed + frame, 7, 1)[0]
-    z0 = depth0 * (0.25 + 1.75 * level)
+    z0 = depth_min + (depth_max - depth_min) * level
     nx, ny = int(round(length / spacing)), int(round(width / spacing))
     nz = int(np.ceil((z0 + amp) / spacing)) + 1
     pos = lattice(nx, ny, nz, spacing, 0.1 * spacing, seed + frame)
@@ -224,3 +225,19 @@ def keys_of(**overrides) -> dict:
     for k, v in overrides.items():
         keys[k.lower()] = v
     return keys
+
+
+def crown_variant(seed: int, spacing: float = 0.005, scale: float = 1.0):
+    """A seeded crown splash of 1-2M particles (at scale 1): slab footprint,
+    depth, ring size, ring radius and flight time drawn from `seed`.  Used as
+    training (seeds 100-149) and held-out (seeds 200-209) frames of the
+    learned band; `scale` shrinks every particle count for quick runs."""
+    u = uniform(seed, 11, 6).astype(np.float64)
+    s = scale ** (1.0 / 3.0)
+    nx = int(round((170 + 30 * u[0]) * s))
+    ny = int(round((170 + 30 * u[1]) * s))
+    nz = int(round((30 + 10 * u[2]) * s))
+    n_ring = int(round((200_000 + 300_000 * u[3]) * scale))
+    radius = (0.18 + 0.12 * u[4]) * s
+    t = 0.02 + 0.06 * u[5]
+    return crown_splash((nx, ny, nz), spacing, n_ring, seed=seed, ring_seed=seed + 1000, t=t, radius=radius)

@@ -1,0 +1,118 @@
+"""Batched frames in one CUDA graph (GPU): every frame of a batch gives the
+same counts and the same triangle soup, bit for bit, as the frame run alone;
+the graph is captured once and relaunched while the frames' grids stay the
+same and captured again when they change; the learned band in a batch equals
+the learned band frame by frame."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def _frames(k, spacing=0.02):
+    from postmps_gb300 import synth
+    # smaller tank and coarser spacing: a few 10k particles per frame
+    return [synth.sloshing_tank(f, n_frames=k, spacing=spacing, length=1.0, width=0.4, depth_min=0.05, depth_max=0.4)
+            for f in range(k)]
+
+
+def _ctx(pms, spacing):
+    from postmps_gb300 import synth
+    import os
+    import tempfile
+    fd, path = tempfile.mkstemp(suffix=".txt")
+    with os.fdopen(fd, "w") as f:
+        f.write(synth.config_text(**{"sim.particlespacing": spacing}))
+    cfg = pms.load_config(path)
+    os.unlink(path)
+    return pms.Context(cfg, 0)
+
+
+def _single(ctx, fr, learned=False):
+    ctx.upload(*fr)
+    ctx.build_grid()
+    if learned:
+        ctx.surface_learned()
+    else:
+        ctx.surface()
+    return ctx.counts(), ctx.mesh(normals=False)[0]
+
+
+@pytest.mark.gpu
+def test_batch_equals_single_frames(pms_lib):
+    pms = pms_lib
+    frames = _frames(5)
+    frames.insert(2, (np.zeros((0, 3), np.float32), None, None))     # an empty frame in the middle
+    with _ctx(pms, 0.02) as ctx:
+        ctx.run_batch(frames)
+        got = [(ctx.batch_frame(f), ctx.batch_mesh(f)) for f in range(len(frames))]
+        info = ctx.batch_info()
+        assert info["captures"] == 1 and info["graph_kernels"] > 10 * len(frames)
+        for f, fr in enumerate(frames):
+            (cb, ms), mb = got[f]
+            if len(fr[0]) == 0:
+                assert cb.n_particles == 0 and len(mb) == 0
+                continue
+            cs, ms_ = _single(ctx, fr)
+            assert (cb.n_surface_particles, cb.n_band_vertices, cb.n_valid_cubes, cb.n_mesh_vertices) == \
+                   (cs.n_surface_particles, cs.n_band_vertices, cs.n_valid_cubes, cs.n_mesh_vertices)
+            assert np.array_equal(mb, ms_), f
+            assert ms > 0.0
+        # the same frames again: no new capture; changed frames: captured again
+        ctx.run_batch(frames)
+        assert ctx.batch_info()["captures"] == 1
+        assert np.array_equal(ctx.batch_mesh(1), got[1][1])
+        moved = [(fr[0] + np.float32(0.013), fr[1], fr[2]) if len(fr[0]) else fr for fr in frames]
+        ctx.run_batch(moved)
+        assert ctx.batch_info()["captures"] == 2
+        cs, ms_ = _single(ctx, moved[0])
+        assert np.array_equal(ctx.batch_mesh(0), ms_)
+
+
+@pytest.mark.gpu
+def test_learned_batch_equals_learned_single_frames(pms_lib):
+    pms = pms_lib
+    frames = _frames(4)
+    with _ctx(pms, 0.02) as ctx:
+        # a quickly trained model on the first frame is enough: the fallback makes results exact
+        ctx.upload(*frames[0])
+        ctx.build_grid()
+        ctx.surface()
+        ctx.learn_prepare()
+        t = pms.Trainer(0, 9)
+        for k in range(60):
+            t.step(ctx, 4096, k, 3e-3, 4.0)
+        ctx.set_band_model(t.model(0.0))
+        ctx.run_batch(frames, learned=True)
+        got = [ctx.batch_mesh(f) for f in range(len(frames))]
+        for f, fr in enumerate(frames):
+            cs, ms_ = _single(ctx, fr, learned=True)
+            assert np.array_equal(got[f], ms_), f
+        t.close()
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_results_and_shapes_agree(pms_lib):
+    """Every launch shape gives the same field; tuning leaves the frame's results as they were."""
+    pms = pms_lib
+    frames = _frames(2)
+    with _ctx(pms, 0.02) as ctx:
+        ctx.upload(*frames[1])
+        ctx.build_grid()
+        ctx.surface()
+        ref_field = ctx.debug("field").copy()
+        ref_counts = ctx.counts().as_dict()
+        ref_mesh = ctx.mesh(normals=False)[0]
+        t = ctx.autotune()
+        assert t["field_threads"] in (64, 128, 256) and t["field_waves"] in (1, 2, 4, 8)
+        assert t["density_threads"] in (64, 128, 256) and t["moments_threads"] in (64, 128, 256)
+        assert t["field_ms"] > 0 and t["anisotropy_ms"] > 0
+        assert np.array_equal(ctx.debug("field"), ref_field)
+        assert ctx.counts().as_dict() == ref_counts
+        for shape in ({"field_threads": 64, "field_waves": 1, "density_threads": 256, "moments_threads": 64},
+                      {"field_threads": 256, "field_waves": 8, "density_threads": 64, "moments_threads": 256}):
+            ctx.set_tune(shape)
+            cs, mesh = _single(ctx, frames[1])
+            assert np.array_equal(mesh, ref_mesh)
+        with pytest.raises(pms.PmsError):
+            ctx.set_tune({"field_threads": 96, "field_waves": 1, "density_threads": 64, "moments_threads": 64})
