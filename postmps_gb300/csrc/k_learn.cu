@@ -385,6 +385,58 @@ __global__ void __launch_bounds__(256) k_border(KGrid g, const uint32_t* __restr
     }
 }
 
+// Border check of a list of cubes whose corners all have field values (the
+// cubes the last round queued): their cases are computed here from the field
+// (bit k set when corner k lies at or below iso, the corner order of
+// detectValidSurfaceCubes) and the crossed faces are checked as in k_border.
+__global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes, uint32_t n,
+                                                     const uint32_t* __restrict__ vbm, const uint32_t* __restrict__ wp,
+                                                     const float* __restrict__ field, uint32_t* __restrict__ qadd,
+                                                     uint32_t* __restrict__ n_added) {
+    const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
+    const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
+    const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
+    // corner order {000,001,011,010,100,101,111,110} as (x, y, z) offsets
+    const uint32_t cx[8] = {0, 0, 0, 0, 1, 1, 1, 1}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 1, 1, 0, 0, 1, 1, 0};
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t id = cubes[t];
+        uint32_t cs = 0;
+        bool all = true;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t c = id + cx[k] + cy[k] * rx + cz[k] * rxy;
+            if (!((vbm[c >> 5] >> (c & 31u)) & 1u)) { all = false; break; }
+            cs |= (field[bit_rank(vbm, wp, c)] <= iso ? 1u : 0u) << k;
+        }
+        if (!all || cs == 0u || cs == 255u) continue;
+        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
+#pragma unroll
+        for (int f = 0; f < 6; ++f) {
+            const uint32_t m = cs & mask[f];
+            if (m == 0u || m == mask[f]) continue;
+            const int X = x + dxs[f], Y = y + dys[f], Z = z + dzs[f];
+            if (X < 0 || Y < 0 || Z < 0 || X > (int)rx - 2 || Y > (int)ry - 2 || Z > (int)rz - 2) continue;
+            const uint32_t nid = (uint32_t)Z * rxy + (uint32_t)Y * rx + (uint32_t)X;
+            bool have = true;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
+                have = have && ((vbm[c >> 5] >> (c & 31u)) & 1u);
+            }
+            if (have) continue;
+            const uint32_t bit = 1u << (nid & 31u);
+            const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
+            if (!(old & bit)) atomicAdd(n_added, 1u);
+        }
+    }
+}
+
+// popcount per word of a bitmap
+__global__ void __launch_bounds__(256) k_popc(const uint32_t* __restrict__ b, uint32_t* __restrict__ wcount, uint64_t nwords) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x)
+        wcount[w] = __popc(b[w]);
+}
+
 // cube bitmap of the plain method's valid cubes (training labels)
 __global__ void __launch_bounds__(256) k_label_bits(const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ vlist,
                                                     const unsigned long long* __restrict__ mc_key, uint32_t* __restrict__ lbm) {
@@ -712,6 +764,23 @@ pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
                                                               ctx->mc_case.as<uint32_t>(),
                                                               ctx->mc_key.as<unsigned long long>(), ctx->bm.as<uint32_t>(),
                                                               qadd, &cnt->l_added);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd) {
+    const KGrid g = kgrid_of(ctx->grid);
+    Counters* cnt = ctx->counters.as<Counters>();
+    k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, ctx->bm.as<uint32_t>(),
+                                                              ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(), qadd,
+                                                              &cnt->l_added);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount) {
+    const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
+    k_popc<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(b, wcount, nwords);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -75,7 +75,8 @@ struct FrameView {
     pms_grid grid;
     explicit FrameView(pms_ctx* ctx) : c(ctx), pos(ctx->in_pos), vel(ctx->in_vel), rho(ctx->in_rho), cnt(ctx->counters),
                                        n(ctx->n), grid(ctx->grid) {}
-    void point(BatchState* b, uint32_t f) {
+    // the frame's grid is known only after the bounding-box pass (with_grid false there)
+    void point(BatchState* b, uint32_t f, bool with_grid = true) {
         c->in_pos.p = b->pos.as<char>() + 12 * b->off[f];
         c->in_vel.p = b->vel.as<char>() + 12 * b->off[f];
         c->in_rho.p = b->rho.as<char>() + 4 * b->off[f];
@@ -84,7 +85,7 @@ struct FrameView {
         c->counters.p = b->cnt.as<Counters>() + f;
         c->counters.cap = SIZE_MAX;
         c->n = b->n[f];
-        c->grid = b->grid[f];
+        if (with_grid) c->grid = b->grid[f];
     }
     ~FrameView() {
         c->in_pos = pos; c->in_vel = vel; c->in_rho = rho; c->counters = cnt;
@@ -215,7 +216,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     {
         FrameView view(c);
         for (uint32_t f = 0; f < k; ++f) {
-            view.point(b, f);
+            view.point(b, f, false);
             if ((st = launch_bbox(c))) return st;
         }
     }

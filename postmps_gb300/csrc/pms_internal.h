@@ -129,7 +129,7 @@ struct pms_ctx {
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
     // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
     pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
-              l_field_new, l_vlist_m, l_field_m, l_cand, l_logit, l_label;
+              l_field_new, l_vlist_m, l_field_m, l_cand, l_logit, l_label, l_qlist, l_wp_q;
     bool have_model = false, band_learned = false, mc_classified = false;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;

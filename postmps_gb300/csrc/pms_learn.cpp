@@ -116,48 +116,60 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     c->l_npred = c->h_counters->l_pred;
     c->have_band = true;
     mark_stage(c, kStageBand + 1);
-    // exact field at those vertices, then the border check until no cube is missing
+    // exact field at those vertices, then the border check until no cube is missing:
+    // a full check over every valid cube, then rounds that evaluate the queued cubes'
+    // new corners and check only those cubes; one synchronisation per round
     if (c->nv && (st = launch_field(c))) return st;
-    for (uint32_t round = 0; c->nv && round < kMaxBorderRounds; ++round) {
-        if ((st = launch_mc_classify(c))) return st;
+    uint64_t nv_bound = c->nv;                 // host bound on the vertex count while rounds run
+    uint32_t added = 0;
+    auto full_check = [&]() -> pms_status {
+        pms_status s2;
+        c->nv = (uint32_t)nv_bound;
+        if ((s2 = launch_mc_classify(c))) return s2;
         PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
         PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-        if ((st = launch_border(c, c->l_qadd.as<uint32_t>()))) return st;
-        if ((st = sync_counters(c))) return st;
-        const uint32_t added = c->h_counters->l_added;
-        if (added == 0) { c->mc_classified = true; break; }
+        if ((s2 = launch_border(c, c->l_qadd.as<uint32_t>()))) return s2;
+        if ((s2 = sync_counters(c))) return s2;
+        added = c->h_counters->l_added;
+        c->nv = c->h_counters->nv;
+        nv_bound = c->nv;
+        return PMS_OK;
+    };
+    if (c->nv && (st = full_check())) return st;
+    for (uint32_t round = 0; added && round < kMaxBorderRounds; ++round) {
         c->l_nadded += added;
         c->l_iters++;
-        // vertices the added cubes bring, and their field
+        // the queued cubes as a list
+        if ((st = launch_popc(c, c->l_qadd.as<uint32_t>(), c->l_wc_new.as<uint32_t>()))) return st;
+        PMS_CUDA(c, c->l_wp_q.ensure(4 * (W + 1)));
+        if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), W, nullptr))) return st;
+        PMS_CUDA(c, c->l_qlist.ensure(4 * (size_t)added));
+        if ((st = launch_bits_list(c, c->l_qadd.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), c->l_qlist.as<uint32_t>())))
+            return st;
+        // their corners without a value yet, and the field there
         if ((st = launch_cube_corners(c, c->l_qadd.as<uint32_t>(), c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(),
                                       c->l_wc_new.as<uint32_t>())))
             return st;
         if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
-        if ((st = sync_counters(c))) return st;
-        const uint32_t nnew = c->h_counters->l_nnew;
-        const size_t NN = nnew ? nnew : 1;
-        PMS_CUDA(c, c->l_vlist_new.ensure(4 * NN));
-        PMS_CUDA(c, c->l_field_new.ensure(4 * NN));
-        if (nnew) {
-            if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(),
-                                       c->l_vlist_new.as<uint32_t>())))
-                return st;
-            if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, nnew, c->l_field_new.as<float>())))
-                return st;
-        }
+        const uint64_t nnew_bound = std::min<uint64_t>(8ull * added, (uint64_t)c->grid.sc_size);
+        PMS_CUDA(c, c->l_vlist_new.ensure(4 * (nnew_bound + 1)));
+        PMS_CUDA(c, c->l_field_new.ensure(4 * (nnew_bound + 1)));
+        if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
+            return st;
+        if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, (uint32_t)nnew_bound,
+                                  c->l_field_new.as<float>())))
+            return st;
         // merged vertex set: bitmap, ranks, list, field
         if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
                                  c->wcount.as<uint32_t>())))
             return st;
         if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
-        if ((st = sync_counters(c))) return st;
-        const uint32_t nv_m = c->h_counters->nv;
-        const size_t NM = nv_m ? nv_m : 1;
-        PMS_CUDA(c, c->l_vlist_m.ensure(4 * NM));
-        PMS_CUDA(c, c->l_field_m.ensure(4 * NM));
+        nv_bound = std::min<uint64_t>(nv_bound + nnew_bound, (uint64_t)c->grid.sc_size);
+        PMS_CUDA(c, c->l_vlist_m.ensure(4 * (nv_bound + 1)));
+        PMS_CUDA(c, c->l_field_m.ensure(4 * (nv_bound + 1)));
         if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
             return st;
-        if ((st = launch_field_merge(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, nv_m, c->bm.as<uint32_t>(),
+        if ((st = launch_field_merge(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, (uint32_t)nv_bound, c->bm.as<uint32_t>(),
                                      c->wprefix.as<uint32_t>(), c->field.as<float>(), c->l_bm_new.as<uint32_t>(),
                                      c->l_wp_new.as<uint32_t>(), c->l_field_new.as<float>(), c->l_field_m.as<float>())))
             return st;
@@ -165,9 +177,23 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
         std::swap(c->wprefix, c->l_wp_m);
         std::swap(c->vlist, c->l_vlist_m);
         std::swap(c->field, c->l_field_m);
-        c->nv = nv_m;
-        if ((st = ensure_band_buffers(c, c->nv))) return st;
+        // border check of the queued cubes, now evaluated; the next queue goes into l_q
+        PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
+        PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
+        if ((st = launch_border_list(c, c->l_qlist.as<uint32_t>(), added, c->l_q.as<uint32_t>()))) return st;
+        std::swap(c->l_q, c->l_qadd);
+        if ((st = sync_counters(c))) return st;
+        added = c->h_counters->l_added;
+        if (!added) {
+            // cubes whose corners were completed by other cubes' rounds: one full check
+            if ((st = ensure_band_buffers(c, (uint32_t)c->h_counters->nv))) return st;
+            nv_bound = c->h_counters->nv;
+            if ((st = full_check())) return st;
+        }
     }
+    c->nv = c->h_counters->nv;
+    if ((st = ensure_band_buffers(c, c->nv))) return st;
+    c->mc_classified = (added == 0);           // the last full check classified the final vertex set
     c->have_field = true;
     mark_stage(c, kStageField + 1);
     return PMS_OK;
