@@ -821,13 +821,13 @@ cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainAr
     in.pos_weight = a.pos_weight;
     const unsigned blocks = (a.batch + kBlockSamples - 1) / kBlockSamples;
     k_learn_train<<<blocks, kTrainThreads, 0, stream>>>(g, ld, in, model, grad, loss_sum);
-    return cudaPeekAtLastError();
+    return cudaGetLastError();
 }
 
 cudaError_t launch_adam(cudaStream_t stream, float* w, const float* grad, float* m, float* v, const AdamParams& ap,
                         DevModel* model) {
     k_adam<<<(kNumParams + 255) / 256, 256, 0, stream>>>(w, grad, m, v, ap, model);
-    return cudaPeekAtLastError();
+    return cudaGetLastError();
 }
 
 }  // namespace pms

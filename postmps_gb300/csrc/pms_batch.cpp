@@ -143,10 +143,14 @@ static pms_status capture(pms_ctx* c, BatchState* b, bool learned) {
         if (e != cudaSuccess) st = PMS_ERR_CUDA;
         for (uint32_t f = 0; f < k && !st; ++f) {
             view.point(b, f);
-            if (cudaEventRecord(b->ev[f], c->stream) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
+            // external: recorded when the graph runs (a plain record inside a capture only orders work)
+            if (cudaEventRecordWithFlags(b->ev[f], c->stream, cudaEventRecordExternal) != cudaSuccess) {
+                st = PMS_ERR_CUDA;
+                break;
+            }
             st = capture_frame(c, b, f, learned);
         }
-        if (!st && cudaEventRecord(b->ev[k], c->stream) != cudaSuccess) st = PMS_ERR_CUDA;
+        if (!st && cudaEventRecordWithFlags(b->ev[k], c->stream, cudaEventRecordExternal) != cudaSuccess) st = PMS_ERR_CUDA;
         c->batch_launches = c->launches - launches0;
         c->launches = launches0;             // counted when the graph runs
     }
@@ -242,6 +246,13 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     if ((st = ensure_grid_buffers(c, gmax))) return st;
     if ((st = ensure_band_buffers(c, gmax.sc_size))) return st;
     PMS_CUDA(c, c->scan.partial.ensure(sizeof(unsigned long long) * 1024));
+    {
+        uint64_t pt = 1, vt = 1;
+        for (uint32_t f = 0; f < k; ++f) { pt = std::max(pt, particle_tiles(grid[f])); vt = std::max(vt, vertex_tiles(grid[f])); }
+        if ((st = ensure_order(c, c->porder, nmax, pt)) || (st = ensure_order(c, c->sorder, nmax, pt)) ||
+            (st = ensure_order(c, c->vorder, gmax.sc_size, vt)))
+            return st;
+    }
     if (learned) {
         const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
         PMS_CUDA(c, c->l_q.ensure(4 * (W + 1)));
@@ -336,7 +347,10 @@ extern "C" pms_status pms_batch_frame(pms_ctx* c, uint32_t f, pms_counts* out, f
     }
     if (ms) {
         *ms = 0.f;
-        if (!b->rerun[f]) cudaEventElapsedTime(ms, b->ev[f], b->ev[f + 1]);
+        if (!b->rerun[f] && cudaEventElapsedTime(ms, b->ev[f], b->ev[f + 1]) != cudaSuccess) {
+            *ms = 0.f;
+            cudaGetLastError();                      // a missing time is not a failure of later calls
+        }
     }
     return PMS_OK;
 }

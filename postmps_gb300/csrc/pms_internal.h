@@ -82,6 +82,11 @@ struct ScanTemp {
     DBuf partial;           // per-block partial sums (u64 capable)
 };
 
+// A processing order with 3D locality (k_order.cu): perm lists item indices tile by tile.
+struct OrderBufs {
+    DBuf perm, tid_of, slot, tile_count, tile_start;
+};
+
 // Launch shapes chosen by the autotuner (pms_autotune): threads per block of
 // the neighbour walks and the field's resident-block cap (blocks per SM).
 struct Tune {
@@ -133,6 +138,7 @@ struct pms_ctx {
     bool have_model = false, band_learned = false, mc_classified = false;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;
+    pms::OrderBufs vorder, porder, sorder;   // band vertices, particles, surface particles
     // batched frames (pms_batch.cpp)
     void* batch = nullptr;
     uint64_t batch_launches = 0;         // kernels in the batch graph
@@ -166,7 +172,7 @@ pms_status pms_fail(pms_ctx* ctx, pms_status s, const char* fmt, ...);
 #define PMS_LAUNCHED(ctx)                                                                      \
     do {                                                                                       \
         (ctx)->launches++;                                                                     \
-        cudaError_t e__ = cudaPeekAtLastError();                                               \
+        cudaError_t e__ = cudaGetLastError();                                                  \
         if (e__ != cudaSuccess)                                                                \
             return pms_fail((ctx), PMS_ERR_CUDA, "kernel launch: %s (%s:%d)",                  \
                             cudaGetErrorString(e__), __FILE__, __LINE__);                      \
@@ -198,7 +204,15 @@ pms_status launch_band(pms_ctx* ctx);
 pms_status launch_band_list(pms_ctx* ctx);
 pms_status launch_field(pms_ctx* ctx);
 // field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid)
-pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out,
+                           bool ordered = false);
+// tile orders (k_order.cu)
+pms_status launch_vertex_order(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host);
+pms_status launch_particle_order(pms_ctx* ctx);
+pms_status launch_surface_order(pms_ctx* ctx);
+pms_status ensure_order(pms_ctx* ctx, OrderBufs& ob, uint64_t items, uint64_t ntiles);
+uint64_t vertex_tiles(const pms_grid& g);
+uint64_t particle_tiles(const pms_grid& g);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 pms_status launch_mc_classify(pms_ctx* ctx);
