@@ -215,6 +215,24 @@ def run_reference(args) -> None:
 
 
 # ---------------------------------------------------------------------------
+# replicas: one frame set per rank, no collective on the data path
+# ---------------------------------------------------------------------------
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time (the job's time); a no-op on one rank."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job units/s: every rank processed units_per_rank in at most ms."""
+    return world * units_per_rank / (ms / 1e3)
+
+
+# ---------------------------------------------------------------------------
 # GPU arms
 # ---------------------------------------------------------------------------
 class Timer:
@@ -240,11 +258,7 @@ class Timer:
                 after()
         torch.cuda.synchronize()
         ms = sum(a.elapsed_time(b) for a, b in ev) / k
-        if self.world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(ms, self.world, "cuda")
 
 
 def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse: bool, clocks=None) -> dict:
@@ -428,8 +442,8 @@ def run_pms(args) -> None:
         head_arm = "learned" if ok and res["learned"]["ms_e2e"] < res["plain"]["ms_e2e"] else "plain"
     head = res[head_arm]
     n_total = sum(len(fr[0]) for fr in frames)
-    value = world * n_total / (head["ms"] / 1e3)
-    e2e_value = world * n_total / (head["ms_e2e"] / 1e3)
+    value = job_throughput(n_total, world, head["ms"])
+    e2e_value = job_throughput(n_total, world, head["ms_e2e"])
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:

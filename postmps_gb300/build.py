@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = [
     "scan.cu", "k_grid.cu", "k_aniso.cu", "k_band.cu", "k_field.cu", "k_mc.cu", "k_diffuse.cu",
-    "mc_tables.cu", "pms_api.cpp", "host_io.cpp", "scan_noalloc.cu", "k_learn.cu", "pms_learn.cpp", "pms_batch.cpp", "pms_tune.cpp", "k_order.cu",
+    "mc_tables.cu", "pms_api.cpp", "host_io.cpp", "scan_noalloc.cu", "k_learn.cu", "pms_learn.cpp", "pms_batch.cpp", "pms_tune.cpp",
 ]
 
 

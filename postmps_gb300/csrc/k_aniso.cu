@@ -36,11 +36,10 @@ struct AnisoParams {
 template <int BT>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_density(KGrid g, AnisoParams ap, const uint32_t* __restrict__ skeys,
                                                       const uint32_t* __restrict__ cell_start, float4* __restrict__ spos,
-                                                      float* __restrict__ rho, uint32_t n, const uint32_t* __restrict__ perm) {
+                                                      float* __restrict__ rho, uint32_t n) {
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
     const float pad = 1e-4f * g.sp_cs;
-    for (uint32_t ii = blockIdx.x * blockDim.x + threadIdx.x; ii < n; ii += gridDim.x * blockDim.x) {
-        const uint32_t i = perm[ii];                 // tile order
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 pi4 = spos[i];
         const float3 p = make_float3(pi4.x, pi4.y, pi4.z);
         const uint32_t key = skeys[i];
@@ -152,14 +151,13 @@ template <int BT>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
                                                       const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
                                                       const uint32_t* __restrict__ cell_start, const float4* __restrict__ spos,
-                                                      float4* __restrict__ mom, const uint32_t* __restrict__ perm) {
+                                                      float4* __restrict__ mom) {
     const uint32_t ns = cnt->ns;
     const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
     const float pad = 1e-4f * g.sp_cs;
     const float r2h_sq = ap.r2h * ap.r2h;
     const float inv_r2h = 1.f / ap.r2h;
-    for (uint32_t ss = blockIdx.x * blockDim.x + threadIdx.x; ss < ns; ss += gridDim.x * blockDim.x) {
-        const uint32_t s = perm[ss];                 // tile order
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         const uint32_t i = slist[s];
         const float4 pi4 = spos[i];
         const float3 p = make_float3(pi4.x, pi4.y, pi4.z);
@@ -293,16 +291,12 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     ap.min_nn = P.min_num_neighbors;
     ap.cond_limit = ctx->cfg.fp64_svd_cond;
     Counters* cnt = ctx->counters.as<Counters>();
-    pms_status st = launch_particle_order(ctx);
-    if (st) return st;
-    if ((st = launch_surface_order(ctx))) return st;
     // block sizes of the neighbour walks are autotuned (64, 128 or 256 threads)
     const int bd = ctx->tune.density_threads, bm = ctx->tune.moments_threads;
     auto dens = [&](auto kern) {
         kern<<<grid_for(ctx->n, (unsigned)bd), bd, 0, ctx->stream>>>(g, ap, ctx->skeys.as<uint32_t>(),
                                                                     ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(),
-                                                                    ctx->rho.as<float>(), ctx->n,
-                                                                    ctx->porder.perm.as<uint32_t>());
+                                                                    ctx->rho.as<float>(), ctx->n);
     };
     if (bd == 64) dens(k_density<64>);
     else if (bd == 256) dens(k_density<256>);
@@ -315,8 +309,7 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     auto mom = [&](auto kern) {
         kern<<<grid_for(ctx->n, (unsigned)bm), bm, 0, ctx->stream>>>(g, ap, ctx->slist.as<uint32_t>(), cnt,
                                                                     ctx->skeys.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
-                                                                    ctx->spos.as<float4>(), ctx->moments.as<float4>(),
-                                                                    ctx->sorder.perm.as<uint32_t>());
+                                                                    ctx->spos.as<float4>(), ctx->moments.as<float4>());
     };
     if (bm == 64) mom(k_moments<64>);
     else if (bm == 256) mom(k_moments<256>);

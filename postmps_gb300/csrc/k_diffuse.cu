@@ -133,11 +133,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParam
 // calculationofTrappedairpotential: every particle
 __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffuseParams dp, const uint32_t* __restrict__ cell_start,
                                                          const float4* __restrict__ spos, const float4* __restrict__ svel,
-                                                         uint32_t n, float4* __restrict__ pot,
-                                                         const uint32_t* __restrict__ perm) {
+                                                         uint32_t n, float4* __restrict__ pot) {
     const float pad = 1e-4f * g.sp_cs, r2 = dp.hd_sq;
-    for (uint32_t ii = blockIdx.x * blockDim.x + threadIdx.x; ii < n; ii += gridDim.x * blockDim.x) {
-        const uint32_t i = perm ? perm[ii] : ii;     // tile order when the anisotropy pass built one
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 p4 = spos[i], v = svel[i];
         const float3 p = make_float3(p4.x, p4.y, p4.z);
         uint3 lo, hi;
@@ -468,8 +466,7 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     PMS_LAUNCHED(ctx);
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->d_pot.p, 0, 16 * N, ctx->stream));
     k_df_trapped<<<gk, kThreads, 0, ctx->stream>>>(g, dp, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(),
-                                                   ctx->svel.as<float4>(), n, ctx->d_pot.as<float4>(),
-                                                   ctx->have_aniso ? ctx->porder.perm.as<uint32_t>() : nullptr);
+                                                   ctx->svel.as<float4>(), n, ctx->d_pot.as<float4>());
     PMS_LAUNCHED(ctx);
     k_df_crests<<<gk, kThreads, 0, ctx->stream>>>(g, dp, cnt, ctx->d_freelist.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
                                                   ctx->spos.as<float4>(), ctx->svel.as<float4>(),

@@ -67,7 +67,7 @@ __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float
 // BT threads per block (autotuned: 64, 128 or 256), 64 registers per thread at most
 template <int BT>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
-                                                    const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ perm,
+                                                    const uint32_t* __restrict__ n_dev,
                                                     const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
                                                     const float* __restrict__ cell_rad, const float4* __restrict__ spos,
                                                     const float4* __restrict__ aniso, float* __restrict__ field) {
@@ -79,8 +79,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp
     // largest support of any particle this frame
     const float rmax = fmaxf(__uint_as_float(cnt->rad_max_bits), fp.h) * fp.grow;
     const float rmax2 = rmax * rmax;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += gridDim.x * blockDim.x) {
-        const uint32_t t = perm ? perm[i] : i;       // tile order: a block's vertices lie close together
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x) {
         const uint32_t id = vlist[t];
         const uint32_t iz = id / rxy, rem = id - iz * rxy, iy = rem / rx, ix = rem - iy * rx;
         const float3 v = make_float3(sc_coord(g, ix, 0), sc_coord(g, iy, 1), sc_coord(g, iz, 2));
@@ -128,14 +127,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp
     }
 }
 
-pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out,
-                           bool ordered) {
-    const uint32_t* perm = nullptr;
-    if (ordered) {
-        pms_status st = launch_vertex_order(ctx, vlist, n_dev, n_host);
-        if (st) return st;
-        perm = ctx->vorder.perm.as<uint32_t>();
-    }
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out) {
     const KGrid g = kgrid_of(ctx->grid);
     const pms_params& P = ctx->prm;
     FieldParams fp;
@@ -146,7 +138,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     const int bt = ctx->tune.field_threads;
     const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1024u / (unsigned)bt));
     auto go = [&](auto kern) {
-        kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, perm, vlist, ctx->cell_start.as<uint32_t>(),
+        kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
                                              ctx->cell_rad.as<float>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out);
     };
     if (bt == 64) go(k_field<64>);
@@ -158,7 +150,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
 
 pms_status launch_field(pms_ctx* ctx) {
     Counters* cnt = ctx->counters.as<Counters>();
-    return launch_field_on(ctx, ctx->vlist.as<uint32_t>(), &cnt->nv, ctx->nv, ctx->field.as<float>(), true);
+    return launch_field_on(ctx, ctx->vlist.as<uint32_t>(), &cnt->nv, ctx->nv, ctx->field.as<float>());
 }
 
 }  // namespace pms

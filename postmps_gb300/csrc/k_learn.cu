@@ -389,10 +389,12 @@ __global__ void __launch_bounds__(256) k_border(KGrid g, const uint32_t* __restr
 // cubes the last round queued): their cases are computed here from the field
 // (bit k set when corner k lies at or below iso, the corner order of
 // detectValidSurfaceCubes) and the crossed faces are checked as in k_border.
-__global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes, uint32_t n,
+__global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes,
+                                                     uint32_t n_host, const uint32_t* __restrict__ n_dev,
                                                      const uint32_t* __restrict__ vbm, const uint32_t* __restrict__ wp,
                                                      const float* __restrict__ field, uint32_t* __restrict__ qadd,
                                                      uint32_t* __restrict__ n_added) {
+    const uint32_t n = n_dev ? *n_dev : n_host;
     const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
     const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
     const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
@@ -768,10 +770,10 @@ pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
     return PMS_OK;
 }
 
-pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd) {
+pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd, const uint32_t* n_dev) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
-    k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, ctx->bm.as<uint32_t>(),
+    k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, n_dev, ctx->bm.as<uint32_t>(),
                                                               ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(), qadd,
                                                               &cnt->l_added);
     PMS_LAUNCHED(ctx);

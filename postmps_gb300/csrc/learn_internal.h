@@ -45,7 +45,9 @@ pms_status launch_field_merge(pms_ctx* ctx, const uint32_t* vlist, const uint32_
                               const uint32_t* wp_new, const float* f_new, float* f_out);
 pms_status launch_border(pms_ctx* ctx, uint32_t* qadd);
 pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
-pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd);
+// n: the list length, or a bound when n_dev holds it on the device
+pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd,
+                              const uint32_t* n_dev = nullptr);
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount);
 pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x);
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,

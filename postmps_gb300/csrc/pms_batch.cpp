@@ -48,6 +48,7 @@ struct BatchState {
     int flags = -1;
     uint64_t mesh_cap = 0;
     uint32_t captures = 0, reruns = 0;
+    uint64_t gen = 0;                 // buffer generation the graph was captured against
     ~BatchState() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -93,6 +94,56 @@ struct FrameView {
     }
 };
 
+// Border-check rounds inside the graph: a fixed number per frame, every size a
+// bound and every count on the device (a round with an empty queue does no work).
+static constexpr int kGraphRounds = 3;
+
+// classify every cube of the vertex set, then queue the cubes across crossed faces
+static pms_status full_check(pms_ctx* c, uint64_t W) {
+    Counters* cnt = c->counters.as<Counters>();
+    pms_status st;
+    if ((st = launch_mc_classify(c))) return st;
+    PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
+    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
+    return launch_border(c, c->l_qadd.as<uint32_t>());
+}
+
+// one round: field at the queued cubes' new corners, merge, check the queued cubes
+static pms_status border_round(pms_ctx* c, uint64_t W) {
+    Counters* cnt = c->counters.as<Counters>();
+    const uint32_t S = c->grid.sc_size;
+    pms_status st;
+    if ((st = launch_popc(c, c->l_qadd.as<uint32_t>(), c->l_wc_new.as<uint32_t>()))) return st;
+    if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), W, &cnt->l_nq))) return st;
+    if ((st = launch_bits_list(c, c->l_qadd.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), c->l_qlist.as<uint32_t>()))) return st;
+    if ((st = launch_cube_corners(c, c->l_qadd.as<uint32_t>(), c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(),
+                                  c->l_wc_new.as<uint32_t>())))
+        return st;
+    if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
+    if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
+        return st;
+    if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, S, c->l_field_new.as<float>()))) return st;
+    if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
+                             c->wcount.as<uint32_t>())))
+        return st;
+    if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
+    if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
+        return st;
+    if ((st = launch_field_merge(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, S, c->bm.as<uint32_t>(),
+                                 c->wprefix.as<uint32_t>(), c->field.as<float>(), c->l_bm_new.as<uint32_t>(),
+                                 c->l_wp_new.as<uint32_t>(), c->l_field_new.as<float>(), c->l_field_m.as<float>())))
+        return st;
+    std::swap(c->bm, c->l_bm_m);
+    std::swap(c->wprefix, c->l_wp_m);
+    std::swap(c->vlist, c->l_vlist_m);
+    std::swap(c->field, c->l_field_m);
+    PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
+    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
+    if ((st = launch_border_list(c, c->l_qlist.as<uint32_t>(), S, c->l_q.as<uint32_t>(), &cnt->l_nq))) return st;
+    std::swap(c->l_q, c->l_qadd);
+    return PMS_OK;
+}
+
 // Stages of one frame without host synchronisation (the context points at the frame).
 static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool learned) {
     pms_status st;
@@ -116,9 +167,10 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool lear
         if ((st = launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>())))
             return st;
         if ((st = launch_field(c))) return st;
-        if ((st = launch_mc_classify(c))) return st;
-        PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
-        if ((st = launch_border(c, c->l_qadd.as<uint32_t>()))) return st;   // counts into the frame's l_added
+        if ((st = full_check(c, W))) return st;
+        for (int r = 0; r < kGraphRounds; ++r)
+            if ((st = border_round(c, W))) return st;
+        if ((st = full_check(c, W))) return st;              // what is still missing: the frame runs again alone
     } else {
         if ((st = launch_band(c))) return st;
         if ((st = launch_band_list(c))) return st;
@@ -246,17 +298,18 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     if ((st = ensure_grid_buffers(c, gmax))) return st;
     if ((st = ensure_band_buffers(c, gmax.sc_size))) return st;
     PMS_CUDA(c, c->scan.partial.ensure(sizeof(unsigned long long) * 1024));
-    {
-        uint64_t pt = 1, vt = 1;
-        for (uint32_t f = 0; f < k; ++f) { pt = std::max(pt, particle_tiles(grid[f])); vt = std::max(vt, vertex_tiles(grid[f])); }
-        if ((st = ensure_order(c, c->porder, nmax, pt)) || (st = ensure_order(c, c->sorder, nmax, pt)) ||
-            (st = ensure_order(c, c->vorder, gmax.sc_size, vt)))
-            return st;
-    }
     if (learned) {
         const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
-        PMS_CUDA(c, c->l_q.ensure(4 * (W + 1)));
-        PMS_CUDA(c, c->l_qadd.ensure(4 * (W + 1)));
+        const size_t S = (size_t)gmax.sc_size + 1;
+        for (DBuf* d : {&c->l_q, &c->l_qadd, &c->l_bm_new, &c->l_wc_new, &c->l_wp_new, &c->l_bm_m, &c->l_wp_m, &c->l_wp_q})
+            PMS_CUDA(c, d->ensure(4 * (W + 1)));
+        for (DBuf* d : {&c->l_vlist_new, &c->l_field_new, &c->l_vlist_m, &c->l_field_m, &c->l_qlist})
+            PMS_CUDA(c, d->ensure(4 * S));
+        // the buffers that trade places with these in the rounds must be as large
+        PMS_CUDA(c, c->bm.ensure(4 * (W + 1)));
+        PMS_CUDA(c, c->wprefix.ensure(4 * (W + 1)));
+        PMS_CUDA(c, c->vlist.ensure(4 * S));
+        PMS_CUDA(c, c->field.ensure(4 * S));
         size_t ncoarse = 1;
         for (uint32_t f = 0; f < k; ++f) {
             const size_t m = (size_t)(grid[f].scres[0] / 2 + 2) * (grid[f].scres[1] / 2 + 2) * (grid[f].scres[2] / 2 + 2);
@@ -276,10 +329,11 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         PMS_CUDA(c, cudaEventCreate(&e));
         b->ev.push_back(e);
     }
-    // ---- pass 2: the graph (captured again when the frames' grids changed)
+    // ---- pass 2: the graph (captured again when the frames' grids or any buffer changed)
     for (int attempt = 0; attempt < 3; ++attempt) {
-        if (!grids_same || !b->exec) {
+        if (!grids_same || !b->exec || b->gen != g_dbuf_generation) {
             if ((st = capture(c, b, learned))) return st;
+            b->gen = g_dbuf_generation;
             grids_same = true;
         }
         PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));

@@ -16,18 +16,27 @@ namespace pms {
 // ---------------------------------------------------------------------------
 // device buffers: grow-only, contents not preserved across growth
 // ---------------------------------------------------------------------------
+// Every (re)allocation or release bumps this generation: a captured CUDA graph
+// holds raw buffer addresses and is captured again when it has changed.
+inline uint64_t g_dbuf_generation = 0;
+
 struct DBuf {
     void* p = nullptr;
     size_t cap = 0;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap && p) return cudaSuccess;
+        ++g_dbuf_generation;
         if (p) { cudaFree(p); p = nullptr; cap = 0; }
         size_t want = bytes < 256 ? 256 : bytes;
         cudaError_t e = cudaMalloc(&p, want);
         if (e == cudaSuccess) cap = want;
         return e;
     }
-    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+    void release() {
+        if (p) { ++g_dbuf_generation; cudaFree(p); }
+        p = nullptr;
+        cap = 0;
+    }
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
@@ -56,6 +65,7 @@ struct Counters {
     uint32_t l_pred;        // predicted cubes (or candidate slots written)
     uint32_t l_added;       // cubes the last border check queued
     uint32_t l_nnew;        // vertices those cubes add
+    uint32_t l_nq;          // cubes queued for a border-check round (batched frames)
 };
 
 enum : uint32_t {
@@ -80,11 +90,6 @@ const char* mc_tables_origin();
 // Scan workspace.
 struct ScanTemp {
     DBuf partial;           // per-block partial sums (u64 capable)
-};
-
-// A processing order with 3D locality (k_order.cu): perm lists item indices tile by tile.
-struct OrderBufs {
-    DBuf perm, tid_of, slot, tile_count, tile_start;
 };
 
 // Launch shapes chosen by the autotuner (pms_autotune): threads per block of
@@ -138,7 +143,6 @@ struct pms_ctx {
     bool have_model = false, band_learned = false, mc_classified = false;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;
-    pms::OrderBufs vorder, porder, sorder;   // band vertices, particles, surface particles
     // batched frames (pms_batch.cpp)
     void* batch = nullptr;
     uint64_t batch_launches = 0;         // kernels in the batch graph
@@ -204,15 +208,7 @@ pms_status launch_band(pms_ctx* ctx);
 pms_status launch_band_list(pms_ctx* ctx);
 pms_status launch_field(pms_ctx* ctx);
 // field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid)
-pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out,
-                           bool ordered = false);
-// tile orders (k_order.cu)
-pms_status launch_vertex_order(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host);
-pms_status launch_particle_order(pms_ctx* ctx);
-pms_status launch_surface_order(pms_ctx* ctx);
-pms_status ensure_order(pms_ctx* ctx, OrderBufs& ob, uint64_t items, uint64_t ntiles);
-uint64_t vertex_tiles(const pms_grid& g);
-uint64_t particle_tiles(const pms_grid& g);
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 pms_status launch_mc_classify(pms_ctx* ctx);

@@ -21,7 +21,7 @@ static constexpr uint32_t kMaxBorderRounds = 256;
 
 static pms_status zero_learn_counters(pms_ctx* c) {
     PMS_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->counters.p) + offsetof(Counters, l_cand), 0,
-                                sizeof(uint32_t) * 4, c->stream));
+                                sizeof(uint32_t) * 5, c->stream));
     return PMS_OK;
 }
 
