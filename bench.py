@@ -423,16 +423,18 @@ def run_pms(args) -> None:
                                         ClockSampler(local))
     # the judge: learned mesh against the plain mesh of the same frame (outside the timed region)
     judge = None
-    if len(arms) == 2 and not batched and not args.no_judge:
+    if len(arms) == 2 and not args.no_judge:
+        # every frame of the workload (a batch gives each frame the single-frame result)
         t0 = time.perf_counter()
-        pos, vel, rho = frames[0]
         ctx.set_band_mode(False)
-        j = LN.compare(ctx, model, h, pos, vel, rho)
-        judge = {"hausdorff_h": j["hausdorff_h"], "hausdorff": j["hausdorff"],
-                 "triangle_delta": j["triangle_delta"], "cubes_only_plain": j["cubes_only_plain"],
-                 "cubes_only_learned": j["cubes_only_learned"],
-                 "fallback_cubes": j["learned"]["fallback_cubes"],
-                 "fallback_rounds": j["learned"]["fallback_rounds"],
+        js = [LN.compare(ctx, model, h, *fr) for fr in frames if len(fr[0])]
+        worst = max(js, key=lambda j: j["hausdorff"])
+        judge = {"hausdorff_h": worst["hausdorff_h"], "hausdorff": worst["hausdorff"],
+                 "frames": len(js), "triangle_delta": sum(j["triangle_delta"] for j in js),
+                 "cubes_only_plain": sum(j["cubes_only_plain"] for j in js),
+                 "cubes_only_learned": sum(j["cubes_only_learned"] for j in js),
+                 "fallback_cubes": sum(j["learned"]["fallback_cubes"] for j in js),
+                 "fallback_rounds": max(j["learned"]["fallback_rounds"] for j in js),
                  "plain_vs_fp64": "vertex positions within 1e-4 cell of the float64 oracle (parity tests)",
                  "seconds": time.perf_counter() - t0}
     # headline: the learned band only when the judge passes it (<= 0.05 h) and it is faster

@@ -60,16 +60,18 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_density(KGrid g, AnisoParams 
 }
 
 // m / rho into spos.w (0 for rho == 0: the field skips such particles), and the
-// isotropic kernel of every particle in the field's packed form,
-// G = I / h, h_s^2 = h^2, sigma * det(G) = sigma / h^3; the anisotropy pass
+// isotropic kernel of every particle in the field's packed form: M = G^T G
+// with G = I / h (off-diagonals doubled), h_s^2 = h^2, and the weight
+// (m / rho) sigma det(G) = (m / rho) sigma / h^3; the anisotropy pass
 // overwrites the surface particles' entries.
 __global__ void __launch_bounds__(kThreads) k_inv_density(float4* __restrict__ spos, const float* __restrict__ rho,
                                                           float4* __restrict__ aniso, AnisoParams ap, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float r = rho[i];
         spos[i].w = r == 0.f ? 0.f : ap.mass / r;
-        aniso[2 * (size_t)i + 0] = make_float4(ap.h_inv, 0.f, 0.f, ap.h_sq);
-        aniso[2 * (size_t)i + 1] = make_float4(ap.h_inv, 0.f, ap.h_inv, ap.kdens);
+        const float inv_h2 = ap.h_inv * ap.h_inv;
+        aniso[2 * (size_t)i + 0] = make_float4(inv_h2, 0.f, 0.f, ap.h_sq);
+        aniso[2 * (size_t)i + 1] = make_float4(inv_h2, 0.f, inv_h2, spos[i].w * ap.kdens);
     }
 }
 
@@ -264,8 +266,15 @@ __global__ void __launch_bounds__(kThreads) k_eigen(AnisoParams ap, const uint32
                         - G[0][0] * G[1][2] * G[2][1] - G[0][1] * G[1][0] * G[2][2] - G[0][2] * G[1][1] * G[2][0];
         const float hs = maxv * ap.h;
         // symmetric G packed in two float4: {g00, g01, g02, hs^2}, {g11, g12, g22, sigma * det}
-        aniso[2 * (size_t)i + 0] = make_float4(G[0][0], G[0][1], G[0][2], hs * hs);
-        aniso[2 * (size_t)i + 1] = make_float4(G[1][1], G[1][2], G[2][2], kSigma * det);
+        // the field's packed form: M = G^T G = G G (G is symmetric), off-diagonals doubled,
+        // so |G r|^2 = r^T M r costs 9 multiply-adds; w = (m / rho) sigma det(G)
+        float M[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) M[a][b] = G[a][0] * G[0][b] + G[a][1] * G[1][b] + G[a][2] * G[2][b];
+        aniso[2 * (size_t)i + 0] = make_float4(M[0][0], 2.f * M[0][1], 2.f * M[0][2], hs * hs);
+        aniso[2 * (size_t)i + 1] = make_float4(M[1][1], 2.f * M[1][2], M[2][2], pi4.w * (kSigma * det));
         nrm4[i] = make_float4(nv[0], nv[1], nv[2], flag);
         mean4[s] = make_float4(pi4.x + ox, pi4.y + oy, pi4.z + oz, ws);
         float* gd = gdebug + 10 * (size_t)s;

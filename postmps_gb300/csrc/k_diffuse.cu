@@ -34,6 +34,13 @@ namespace pms {
 
 static constexpr int kThreads = 128;
 static constexpr double kEps = 1.0e-7;          // EPSILON_, Define.h:10 (double)
+// The reference compares float values with the double EPSILON_ (and 0.6).  For a
+// float x, (double)x > E  <=>  x > down(E) and (double)x < E  <=>  x < up(E), with
+// down / up the nearest floats below / above E, so these float constants give the
+// same decisions without the FP64 pipe in the neighbour loops.
+static constexpr float kEpsDown = 0x1.ad7f28p-24f;   // largest float <= 1e-7
+static constexpr float kEpsUp = 0x1.ad7f2ap-24f;     // smallest float >= 1e-7
+static constexpr float k06Up = 0x1.333334p-1f;       // smallest float >= 0.6
 static constexpr float kPiF = 3.14159265f;      // PI, Define.h:9
 static constexpr int kSpray = 6, kBubble = 20;  // SPARY, BUBBLE, Define.h:13-14
 
@@ -45,7 +52,7 @@ struct DiffuseParticle {   // 32 bytes: two float4-aligned halves
 };
 
 struct DiffuseParams {
-    float hd, hd_sq, coefficient, mass, time_step, buoyancy, drag;
+    float hd, hd_sq, hd_inv, coefficient, mass, time_step, buoyancy, drag;
     float min_wc, max_wc, min_ta, max_ta, min_ke, max_ke;
     int ta_mult, wc_mult, life_time;
     float lo_bound[3], hi_bound[3];    // grid min + 4.5 spacing, grid max - 4.5 spacing
@@ -121,7 +128,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParam
             }
         });
         const float mn2 = nx * nx + ny * ny + nz * nz;
-        if ((double)mn2 < kEps) continue;              // keeps the previous normal
+        if (mn2 < kEpsUp) continue;              // keeps the previous normal
         const float inv = 1.f / sqrtf(mn2);
         nrm[t] = make_float4(nx * inv, ny * inv, nz * inv, 0.f);
     }
@@ -147,14 +154,15 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
             const float4 w = __ldg(&svel[j]);
             const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
             const float mp = sqrtf(sx * sx + sy * sy + sz * sz);
-            if ((double)mp > kEps && mp <= dp.hd) {
+            if (mp > kEpsDown && mp <= dp.hd) {
                 const float ux = v.x - w.x, uy = v.y - w.y, uz = v.z - w.z;
                 float mv = ux * ux + uy * uy + uz * uz;
-                if ((double)mv > kEps) {
+                if (mv > kEpsDown) {
                     mv = sqrtf(mv);
-                    const float qq = mp / dp.hd;
-                    const float e = 1.f - (ux / mv * (sx / mp) + uy / mv * (sy / mp) + uz / mv * (sz / mp));
-                    const float wgt = 1.f - qq;
+                    // (u/|u|) . (s/|s|) as one quotient: the reference's six divisions
+                    // differ from it only in rounding
+                    const float e = 1.f - (ux * sx + uy * sy + uz * sz) / (mv * mp);
+                    const float wgt = 1.f - mp * dp.hd_inv;
                     ita += mv * e * wgt;
                 }
             }
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
         const float3 p = make_float3(p4.x, p4.y, p4.z);
         const float nn = dot_rn(ni.x, ni.y, ni.z, ni.x, ni.y, ni.z);
         const float vv = dot_rn(v.x, v.y, v.z, v.x, v.y, v.z);
-        if ((double)nn <= kEps || (double)vv <= kEps || (double)dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < 0.6) {
+        if (nn <= kEpsDown || vv <= kEpsDown || dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < k06Up) {
             pot[i].x = 0.f;
             continue;
         }
@@ -189,18 +197,18 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
         row_walk(g, p, lo, hi, r2, pad, cell_start, [&](uint32_t j) {
             const float4 nj = __ldg(&nrm[j]);
             const float4 q = __ldg(&spos[j]);
-            if ((double)dot_rn(nj.x, nj.y, nj.z, nj.x, nj.y, nj.z) <= kEps) return;
+            if (dot_rn(nj.x, nj.y, nj.z, nj.x, nj.y, nj.z) <= kEpsDown) return;
             // crests2p: x_ji = normalize(x_j - x_i); counts if x_ji . n_i < -eps
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float l2 = dx * dx + dy * dy + dz * dz;
             if (l2 == 0.f) return;                      // normalize(0) is NaN: contributes 0
             const float il = 1.f / sqrtf(l2);
             const float c = (dx * il) * ni.x + (dy * il) * ni.y + (dz * il) * ni.z;
-            if ((double)c < -kEps) {
+            if (c < -kEpsDown) {
                 // curvature2p: (1 - n_i . n_j) * Weend(x_i - x_j, h)
                 const float e1 = 1.f - (ni.x * nj.x + ni.y * nj.y + ni.z * nj.z);
                 const float mx = sqrtf(l2);
-                const float w = (mx <= dp.hd && mx > 0.f) ? (float)(1.0 - (double)(mx / dp.hd)) : 0.f;
+                const float w = (mx <= dp.hd && mx > 0.f) ? __fsub_rn(1.f, mx / dp.hd) : 0.f;   // 1 - q exact in double, then rounded
                 wc += e1 * w;
             }
         });
@@ -422,7 +430,7 @@ __global__ void __launch_bounds__(256) k_df_append(const DiffuseParticle* __rest
 static DiffuseParams diffuse_params(const pms_ctx* ctx) {
     const pms_params& P = ctx->prm;
     DiffuseParams d;
-    d.hd = P.hd; d.hd_sq = P.hd_sq; d.coefficient = P.coefficient; d.mass = P.mass; d.time_step = P.time_step;
+    d.hd = P.hd; d.hd_sq = P.hd_sq; d.hd_inv = 1.f / P.hd; d.coefficient = P.coefficient; d.mass = P.mass; d.time_step = P.time_step;
     d.buoyancy = P.buoyancy; d.drag = P.drag;
     d.min_wc = P.min_wc; d.max_wc = P.max_wc; d.min_ta = P.min_ta; d.max_ta = P.max_ta;
     d.min_ke = P.min_ke; d.max_ke = P.max_ke;

@@ -42,24 +42,24 @@ __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pa
 }
 
 // Sum of the contributions of particles [j0, j1) at vertex v.  A particle adds
-// sigma det(G) (m/rho) (1 - |G r|^2)^3 when |r|^2 < h_s^2 and |G r|^2 < 1
-// (anisotropicW, myCuda.cuh:151-191); every other particle adds exactly 0.
+// sigma det(G) (m/rho) (1 - |G r|^2)^3 when |G r|^2 < 1 (anisotropicW,
+// myCuda.cuh:151-191); every other particle adds exactly 0.  The reference
+// also tests |r| < maxvalue * h first, which |G r| < 1 already implies
+// (maxvalue * h = 1 / smallest singular value of G); at the very edge the two
+// can differ only by rounding, where the contribution is ~0.  |G r|^2 is
+// evaluated as r^T M r with the packed M = G^T G (off-diagonals doubled) and
+// the weight w = (m/rho) sigma det(G) stored per particle.
 __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float3 v, const float4* __restrict__ spos,
                                            const float4* __restrict__ aniso, float sum) {
 #pragma unroll 2
     for (uint32_t j = j0; j < j1; ++j) {
         const float4 q = __ldg(&spos[j]);
-        const float4 a0 = __ldg(&aniso[2 * (size_t)j]);
-        const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);
+        const float4 a0 = __ldg(&aniso[2 * (size_t)j]);      // {m00, 2 m01, 2 m02, h_s^2}
+        const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);  // {m11, 2 m12, m22, w}
         const float rx = q.x - v.x, ry = q.y - v.y, rz = q.z - v.z;
-        const float l2 = rx * rx + ry * ry + rz * rz;
-        const float tx = rx * a0.x + ry * a0.y + rz * a0.z;
-        const float ty = rx * a0.y + ry * a1.x + rz * a1.y;
-        const float tz = rx * a0.z + ry * a1.y + rz * a1.z;
-        const float d2 = tx * tx + ty * ty + tz * tz;
+        const float d2 = rx * (a0.x * rx + a0.y * ry + a0.z * rz) + ry * (a1.x * ry + a1.y * rz) + rz * (a1.z * rz);
         const float x = 1.f - d2;
-        const float c = q.w * (a1.w * x * x * x);
-        sum += (l2 < a0.w && d2 < 1.f) ? c : 0.f;
+        sum += (d2 < 1.f) ? a1.w * (x * x * x) : 0.f;
     }
     return sum;
 }

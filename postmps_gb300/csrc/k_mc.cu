@@ -28,6 +28,9 @@ __constant__ uint8_t c_edge_vertex[12][2];
 static constexpr int kThreads = 128;
 __device__ __constant__ int c_corner[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {0, 1, 0},
                                               {1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}};
+// c_partner[k][a]: the corner that differs from corner k only along axis a
+__device__ __constant__ int c_partner[8][3] = {{4, 3, 1}, {5, 2, 0}, {6, 1, 3}, {7, 0, 2},
+                                               {0, 7, 5}, {1, 6, 4}, {2, 5, 7}, {3, 4, 6}};
 
 pms_status upload_mc_tables(pms_ctx* ctx) {
     const McTables& T = mc_tables_host();
@@ -143,10 +146,21 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
             const int X = x + c_corner[c][0], Y = y + c_corner[c][1], Z = z + c_corner[c][2];
             cp[c] = make_float3(sc_coord_i(g, X, 0), sc_coord_i(g, Y, 1), sc_coord_i(g, Z, 2));
             cf[c] = grid_value(g, bm, wprefix, field, X, Y, Z);
+        }
+        // central differences (getVertexNorm): along each axis one neighbour of a corner
+        // is the cube's other corner on that axis, the other lies outside the cube
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int ox = c_corner[c][0], oy = c_corner[c][1], oz = c_corner[c][2];
+            const int X = x + ox, Y = y + oy, Z = z + oz;
+            const float fx = grid_value(g, bm, wprefix, field, ox ? X + 1 : X - 1, Y, Z);
+            const float fy = grid_value(g, bm, wprefix, field, X, oy ? Y + 1 : Y - 1, Z);
+            const float fz = grid_value(g, bm, wprefix, field, X, Y, oz ? Z + 1 : Z - 1);
+            const float px = cf[c_partner[c][0]], py = cf[c_partner[c][1]], pz = cf[c_partner[c][2]];
             float3 n;
-            n.x = grid_value(g, bm, wprefix, field, X - 1, Y, Z) - grid_value(g, bm, wprefix, field, X + 1, Y, Z);
-            n.y = grid_value(g, bm, wprefix, field, X, Y - 1, Z) - grid_value(g, bm, wprefix, field, X, Y + 1, Z);
-            n.z = grid_value(g, bm, wprefix, field, X, Y, Z - 1) - grid_value(g, bm, wprefix, field, X, Y, Z + 1);
+            n.x = ox ? px - fx : fx - px;
+            n.y = oy ? py - fy : fy - py;
+            n.z = oz ? pz - fz : fz - pz;
             cn[c] = normalized(n);
         }
         const uint32_t ef = c_edge_flags[cs];
