@@ -208,12 +208,11 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
     return PMS_OK;
 }
 
-// batched frames: this frame's mesh starts where the earlier frames' meshes end
+// batched frames: this frame's mesh takes the next free stretch of the arena
+// (frames of different lanes run concurrently, so the claim is atomic)
 __global__ void k_batch_base(const Counters* __restrict__ cnt, unsigned long long* __restrict__ running,
                              unsigned long long* __restrict__ base) {
-    const unsigned long long b = *running;
-    *base = b;
-    *running = b + cnt->nmesh;
+    *base = atomicAdd(running, (unsigned long long)cnt->nmesh);
 }
 
 pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long long* running, unsigned long long* base) {

@@ -12,6 +12,10 @@
 // host.  Frames run one after another on the context's buffers; meshes land
 // behind each other in one arena (the running offset lives on the device).
 // The graph is kept and relaunched while the frames' grids stay the same.
+// Frames are spread over lanes -- the context and up to three sub-contexts,
+// each with its own buffers and stream -- that fork from and join the
+// capture stream, so independent frames overlap on the GPU; a frame's mesh
+// claims its stretch of the arena with an atomic add.
 //
 // With the learned band, the graph holds the prediction, the field at the
 // predicted corners and one border check per frame; a frame whose border
@@ -41,7 +45,10 @@ struct BatchState {
     std::vector<pms_grid> grid;
     std::vector<Counters> hcnt;
     std::vector<unsigned long long> hbase;
-    std::vector<cudaEvent_t> ev;
+    std::vector<cudaEvent_t> ev, ev_end;         // per-frame start / end, recorded inside the graph
+    std::vector<pms_ctx*> lanes;                 // sub-contexts (lane 0 is the context itself)
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr;
     std::vector<std::vector<float>> rerun_mesh;   // frames re-run alone (learned band fallback)
     std::vector<char> rerun;
     cudaGraphExec_t exec = nullptr;
@@ -49,9 +56,14 @@ struct BatchState {
     uint64_t mesh_cap = 0;
     uint32_t captures = 0, reruns = 0;
     uint64_t gen = 0;                 // buffer generation the graph was captured against
+    uint32_t nlanes_captured = 0;
     ~BatchState() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_end) cudaEventDestroy(e);
+        for (cudaEvent_t e : join) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        for (pms_ctx* l : lanes) pms_destroy(l);
         for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh}) b->release();
     }
 };
@@ -182,37 +194,104 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool lear
     return launch_mc_emit_to(c, b->mesh.as<float>(), nullptr, base + f, b->mesh_cap);
 }
 
-static pms_status capture(pms_ctx* c, BatchState* b, bool learned) {
+static constexpr uint32_t kBatchLanes = 4;
+
+// lane l of the batch: the context itself for l = 0, else a sub-context
+static pms_ctx* lane_ctx(pms_ctx* c, BatchState* b, uint32_t l) { return l == 0 ? c : b->lanes[l - 1]; }
+
+static pms_status capture(pms_ctx* c, BatchState* b, bool learned, uint32_t nlanes) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     const uint32_t k = (uint32_t)b->n.size();
+    // frames to lanes, largest first onto the least loaded lane
+    std::vector<uint32_t> order(k), lane_of(k);
+    for (uint32_t f = 0; f < k; ++f) order[f] = f;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return b->n[x] > b->n[y]; });
+    std::vector<uint64_t> load(nlanes, 0);
+    for (uint32_t f : order) {
+        const uint32_t l = (uint32_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        lane_of[f] = l;
+        load[l] += b->n[f] + 1;
+    }
     cudaGraph_t graph = nullptr;
+    std::vector<uint64_t> launches0(nlanes);
+    for (uint32_t l = 0; l < nlanes; ++l) launches0[l] = lane_ctx(c, b, l)->launches;
     PMS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
     pms_status st = PMS_OK;
-    {
-        FrameView view(c);
-        const uint64_t launches0 = c->launches;
-        cudaError_t e = cudaMemsetAsync(b->base.as<unsigned long long>() + k, 0, sizeof(unsigned long long), c->stream);
-        if (e != cudaSuccess) st = PMS_ERR_CUDA;
+    cudaError_t e = cudaMemsetAsync(b->base.as<unsigned long long>() + k, 0, sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b->fork, c->stream);
+    for (uint32_t l = 1; l < nlanes && e == cudaSuccess; ++l) e = cudaStreamWaitEvent(lane_ctx(c, b, l)->stream, b->fork, 0);
+    if (e != cudaSuccess) st = PMS_ERR_CUDA;
+    for (uint32_t l = 0; l < nlanes && !st; ++l) {
+        pms_ctx* lc = lane_ctx(c, b, l);
+        FrameView view(lc);
         for (uint32_t f = 0; f < k && !st; ++f) {
+            if (lane_of[f] != l) continue;
             view.point(b, f);
             // external: recorded when the graph runs (a plain record inside a capture only orders work)
-            if (cudaEventRecordWithFlags(b->ev[f], c->stream, cudaEventRecordExternal) != cudaSuccess) {
-                st = PMS_ERR_CUDA;
-                break;
-            }
-            st = capture_frame(c, b, f, learned);
+            if (cudaEventRecordWithFlags(b->ev[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
+            if ((st = capture_frame(lc, b, f, learned))) break;
+            if (cudaEventRecordWithFlags(b->ev_end[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) st = PMS_ERR_CUDA;
         }
-        if (!st && cudaEventRecordWithFlags(b->ev[k], c->stream, cudaEventRecordExternal) != cudaSuccess) st = PMS_ERR_CUDA;
-        c->batch_launches = c->launches - launches0;
-        c->launches = launches0;             // counted when the graph runs
     }
-    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
-    if (st) { if (graph) cudaGraphDestroy(graph); return st; }
+    for (uint32_t l = 1; l < nlanes && !st; ++l) {
+        if (cudaEventRecord(b->join[l - 1], lane_ctx(c, b, l)->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(c->stream, b->join[l - 1], 0) != cudaSuccess)
+            st = PMS_ERR_CUDA;
+    }
+    c->batch_launches = 0;
+    for (uint32_t l = 0; l < nlanes; ++l) {
+        pms_ctx* lc = lane_ctx(c, b, l);
+        c->batch_launches += lc->launches - launches0[l];
+        lc->launches = launches0[l];          // counted when the graph runs
+    }
+    e = cudaStreamEndCapture(c->stream, &graph);
+    if (st) {
+        if (graph) cudaGraphDestroy(graph);
+        // a lane's failure message lives on the lane
+        for (uint32_t l = 1; l < nlanes; ++l)
+            if (!lane_ctx(c, b, l)->last_error.empty()) c->last_error = lane_ctx(c, b, l)->last_error;
+        return st;
+    }
     if (e != cudaSuccess) return pms_fail(c, PMS_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
     e = cudaGraphInstantiate(&b->exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) { b->exec = nullptr; return pms_fail(c, PMS_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e)); }
     b->captures++;
+    return PMS_OK;
+}
+
+// every buffer a lane's frames need, sized for the largest frame (nothing may allocate inside the graph)
+static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_grid& gmax,
+                              const std::vector<pms_grid>& grid, bool learned) {
+    pms_status st;
+    if ((st = ensure_particle_buffers(lc, nmax))) return st;
+    if ((st = ensure_grid_buffers(lc, gmax))) return st;
+    if ((st = ensure_band_buffers(lc, gmax.sc_size))) return st;
+    PMS_CUDA(lc, lc->scan.partial.ensure(sizeof(unsigned long long) * 1024));
+    lc->tune = c->tune;
+    if (!learned) return PMS_OK;
+    const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
+    const size_t S = (size_t)gmax.sc_size + 1;
+    for (DBuf* d : {&lc->l_q, &lc->l_qadd, &lc->l_bm_new, &lc->l_wc_new, &lc->l_wp_new, &lc->l_bm_m, &lc->l_wp_m, &lc->l_wp_q})
+        PMS_CUDA(lc, d->ensure(4 * (W + 1)));
+    for (DBuf* d : {&lc->l_vlist_new, &lc->l_field_new, &lc->l_vlist_m, &lc->l_field_m, &lc->l_qlist})
+        PMS_CUDA(lc, d->ensure(4 * S));
+    // the buffers that trade places with these in the rounds must be as large
+    PMS_CUDA(lc, lc->bm.ensure(4 * (W + 1)));
+    PMS_CUDA(lc, lc->wprefix.ensure(4 * (W + 1)));
+    PMS_CUDA(lc, lc->vlist.ensure(4 * S));
+    PMS_CUDA(lc, lc->field.ensure(4 * S));
+    size_t ncoarse = 1;
+    for (const pms_grid& g : grid)
+        ncoarse = std::max(ncoarse, (size_t)(g.scres[0] / 2 + 2) * (g.scres[1] / 2 + 2) * (g.scres[2] / 2 + 2));
+    PMS_CUDA(lc, lc->l_counts.ensure(4 * ncoarse));
+    if (lc != c) {
+        // the lane reads the context's model
+        PMS_CUDA(lc, lc->l_model.ensure(sizeof(pms_band_model)));
+        PMS_CUDA(lc, cudaMemcpyAsync(lc->l_model.p, c->l_model.p, sizeof(pms_band_model), cudaMemcpyDeviceToDevice, c->stream));
+        PMS_CUDA(lc, cudaStreamSynchronize(c->stream));
+        lc->have_model = true;
+    }
     return PMS_OK;
 }
 
@@ -293,30 +372,22 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     bool grids_same = shape_same && b->grid.size() == k;
     for (uint32_t f = 0; grids_same && f < k; ++f) grids_same = same_grid(b->grid[f], grid[f]);
     b->grid = grid;
-    // ---- capacities for the largest frame (nothing may allocate inside the graph)
-    if ((st = ensure_particle_buffers(c, nmax))) return st;
-    if ((st = ensure_grid_buffers(c, gmax))) return st;
-    if ((st = ensure_band_buffers(c, gmax.sc_size))) return st;
-    PMS_CUDA(c, c->scan.partial.ensure(sizeof(unsigned long long) * 1024));
-    if (learned) {
-        const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
-        const size_t S = (size_t)gmax.sc_size + 1;
-        for (DBuf* d : {&c->l_q, &c->l_qadd, &c->l_bm_new, &c->l_wc_new, &c->l_wp_new, &c->l_bm_m, &c->l_wp_m, &c->l_wp_q})
-            PMS_CUDA(c, d->ensure(4 * (W + 1)));
-        for (DBuf* d : {&c->l_vlist_new, &c->l_field_new, &c->l_vlist_m, &c->l_field_m, &c->l_qlist})
-            PMS_CUDA(c, d->ensure(4 * S));
-        // the buffers that trade places with these in the rounds must be as large
-        PMS_CUDA(c, c->bm.ensure(4 * (W + 1)));
-        PMS_CUDA(c, c->wprefix.ensure(4 * (W + 1)));
-        PMS_CUDA(c, c->vlist.ensure(4 * S));
-        PMS_CUDA(c, c->field.ensure(4 * S));
-        size_t ncoarse = 1;
-        for (uint32_t f = 0; f < k; ++f) {
-            const size_t m = (size_t)(grid[f].scres[0] / 2 + 2) * (grid[f].scres[1] / 2 + 2) * (grid[f].scres[2] / 2 + 2);
-            ncoarse = std::max(ncoarse, m);
-        }
-        PMS_CUDA(c, c->l_counts.ensure(4 * ncoarse));
+    // ---- lanes and their capacities (nothing may allocate inside the graph)
+    const uint32_t nlanes = std::min<uint32_t>(kBatchLanes, k);
+    while (b->lanes.size() + 1 < nlanes) {
+        pms_ctx* lc = nullptr;
+        pms_config lcfg = c->cfg;
+        lcfg.band_model[0] = 0;
+        if ((st = pms_create(&lcfg, c->device, &lc))) return pms_fail(c, st, "batch lane context");
+        b->lanes.push_back(lc);
+        cudaEvent_t e;
+        PMS_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        b->join.push_back(e);
     }
+    if (!b->fork) PMS_CUDA(c, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    for (uint32_t l = 0; l < nlanes; ++l)
+        if ((st = ensure_lane(lane_ctx(c, b, l), c, nmax, gmax, grid, learned))) return st;
+    if (nlanes != b->nlanes_captured) grids_same = false;
     uint64_t want_cap = 0;
     for (uint32_t f = 0; f < k; ++f) {
         const uint64_t sx = grid[f].scres[0], sy = grid[f].scres[1], sz = grid[f].scres[2];
@@ -325,15 +396,18 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     if (want_cap > b->mesh_cap) { b->mesh_cap = want_cap; grids_same = false; }
     PMS_CUDA(c, b->mesh.ensure(12 * (b->mesh_cap ? b->mesh_cap : 1)));
     while (b->ev.size() < k + 1) {
-        cudaEvent_t e;
-        PMS_CUDA(c, cudaEventCreate(&e));
-        b->ev.push_back(e);
+        cudaEvent_t e0, e1;
+        PMS_CUDA(c, cudaEventCreate(&e0));
+        PMS_CUDA(c, cudaEventCreate(&e1));
+        b->ev.push_back(e0);
+        b->ev_end.push_back(e1);
     }
     // ---- pass 2: the graph (captured again when the frames' grids or any buffer changed)
     for (int attempt = 0; attempt < 3; ++attempt) {
         if (!grids_same || !b->exec || b->gen != g_dbuf_generation) {
-            if ((st = capture(c, b, learned))) return st;
+            if ((st = capture(c, b, learned, nlanes))) return st;
             b->gen = g_dbuf_generation;
+            b->nlanes_captured = nlanes;
             grids_same = true;
         }
         PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
@@ -401,7 +475,7 @@ extern "C" pms_status pms_batch_frame(pms_ctx* c, uint32_t f, pms_counts* out, f
     }
     if (ms) {
         *ms = 0.f;
-        if (!b->rerun[f] && cudaEventElapsedTime(ms, b->ev[f], b->ev[f + 1]) != cudaSuccess) {
+        if (!b->rerun[f] && cudaEventElapsedTime(ms, b->ev[f], b->ev_end[f]) != cudaSuccess) {
             *ms = 0.f;
             cudaGetLastError();                      // a missing time is not a failure of later calls
         }
