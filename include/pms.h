@@ -183,6 +183,13 @@ pms_status pms_surface(pms_ctx* ctx);           /* SurfaceReconstruction::runsim
 pms_status pms_diffuse(pms_ctx* ctx);           /* DiffuseGeneration::runsimulation, DiffuseGeneration.cu:89-104 */
 pms_status pms_run_frame(pms_ctx* ctx);         /* one iteration of GPUPOST::runSimulation, GPUPOST.cpp:56-81 */
 
+/* Density and velocity at every mesh vertex: MarchingCube::scalarvalue /
+ * estimationOfScalarValue (MarchingCube.cu:153-163, MarchingCube_kernel.cuh:161-233),
+ * which the reference runs after the triangles; here on request (the reference
+ * only writes them from FileData::saveSurfaceVTKfile, which its frame loop does
+ * not call).  After pms_marching_cubes. */
+pms_status pms_scalar_values(pms_ctx* ctx);
+
 /* Results (synchronise the stream). */
 pms_status pms_get_counts(pms_ctx* ctx, pms_counts* out);
 pms_status pms_get_grid(pms_ctx* ctx, pms_grid* out);
@@ -191,6 +198,10 @@ pms_status pms_get_grid(pms_ctx* ctx, pms_grid* out);
  * (FileData.cpp:1297-1300).  *n_vertices receives the count even on PMS_ERR_CAPACITY. */
 pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices,
                              uint64_t* n_vertices);
+/* The scalar values of the mesh vertices (any array may be NULL): velocity xyz,
+ * its length and the density (the reference's ScalarValue). */
+pms_status pms_download_scalar_values(pms_ctx* ctx, float* vel_xyz, float* vel_len, float* rhop, uint64_t cap,
+                                      uint64_t* n_vertices);
 /* Live diffuse particles of one type (0 spray, 1 foam, 2 bubble, -1 all), in the
  * reference's generated-then-old order (DiffuseGeneration.cu:760-867).  Any of
  * the arrays may be NULL; ttl is int32, energies are float32. */
@@ -371,6 +382,10 @@ pms_status pms_read_vtk_particles(const char* path, float** pos_xyz, float** vel
 /* Writes particles as BINARY legacy VTK polydata with Vel and Rhop arrays. */
 pms_status pms_write_vtk_particles(const char* path, const float* pos_xyz, const float* vel_xyz,
                                    const float* rhop, uint32_t n);
+/* Surface mesh with Normal (negated, as the reference writes it), Rhop, VelLength and
+ * Vel point arrays, BINARY legacy VTK (FileData::saveSurfaceVTKfile, FileData.cpp:677-773). */
+pms_status pms_write_surface_vtk(const char* path, const float* pos_xyz, const float* nrm_xyz, const float* vel_xyz,
+                                 const float* vel_len, const float* rhop, uint64_t n_vertices);
 /* ASCII PLY triangle soup in tinyply 2.3's layout (FileData.cpp:1277-1332). */
 pms_status pms_write_ply(const char* path, const float* pos_xyz, uint64_t n_vertices);
 /* Diffuse particles as BINARY legacy VTK with Velocity, Size, energy, Ita and

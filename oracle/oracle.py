@@ -105,6 +105,8 @@ def lib():
         L.orc_exclusive_scan_u32.restype = C.c_uint64
         L.orc_surface_list.argtypes = [C.POINTER(Grid), _u32p, _u32p, _u32p, _u32p]
         L.orc_density.argtypes = [C.POINTER(Params), C.POINTER(Grid), _f32p, C.c_uint32, _u32p, _u32p, _f64p]
+        L.orc_scalar_values.argtypes = [C.POINTER(Params), C.POINTER(Grid), _f32p, _f32p, _f64p, _u32p, _u32p, _f32p,
+                                        C.c_uint64, _f64p]
         L.orc_anisotropy.argtypes = [C.POINTER(Params), C.POINTER(Grid), _f32p, C.c_uint32, _u32p, _u32p,
                                      _u32p, C.c_uint32, _f64p, _f64p, _f64p, _f64p, _u8p, _u32p]
         L.orc_band_bitmap.argtypes = [C.POINTER(Grid), C.c_float, _f32p, _u32p, C.c_uint32, _f32p, _u8p, _u32p]
@@ -328,6 +330,17 @@ def mc_emit(g: Grid, iso: float, bm, band, field64, cases, nvert):
     return vpos[: 3 * m].reshape(-1, 3), vnrm[: 3 * m].reshape(-1, 3)
 
 
+def scalar_values(p: Params, g: Grid, spos, svel, rho, start, end, verts) -> np.ndarray:
+    """estimationOfScalarValue at mesh vertices, float64: (m, 5) {vel xyz, |vel|, rhop}."""
+    verts = np.ascontiguousarray(verts, np.float32).reshape(-1)
+    m = verts.size // 3
+    out = np.zeros(5 * max(m, 1))
+    lib().orc_scalar_values(C.byref(p), C.byref(g), np.ascontiguousarray(spos, np.float32).reshape(-1),
+                            np.ascontiguousarray(svel, np.float32).reshape(-1), np.ascontiguousarray(rho, np.float64),
+                            np.ascontiguousarray(start, np.uint32), np.ascontiguousarray(end, np.uint32), verts, m, out)
+    return out[: 5 * m].reshape(-1, 5)
+
+
 def run_surface(p: Params, pos: np.ndarray, g: Grid | None = None) -> SurfaceResult:
     """FP64 oracle of the plain surface path on one frame."""
     L = lib()
@@ -378,7 +391,7 @@ class RefResult(C.Structure):
         ("surf_list", C.POINTER(C.c_uint32)), ("mean", C.POINTER(C.c_float)), ("G", C.POINTER(C.c_float)),
         ("band_flags", C.POINTER(C.c_uint32)), ("band_list", C.POINTER(C.c_uint32)), ("field", C.POINTER(C.c_float)),
         ("cube_flag", C.POINTER(C.c_uint32)), ("nvert", C.POINTER(C.c_uint32)),
-        ("vpos", C.POINTER(C.c_float)), ("vnrm", C.POINTER(C.c_float)),
+        ("vpos", C.POINTER(C.c_float)), ("vnrm", C.POINTER(C.c_float)), ("sval", C.POINTER(C.c_float)),
     ]
 
 
@@ -430,6 +443,7 @@ def ref_surface_run(config_path: str, pos, vel=None, rhop=None) -> dict:
     out["nvert"] = _arr(res.nvert, nb, np.uint32)
     out["vpos"] = _arr(res.vpos, 3 * nm, np.float32).reshape(-1, 3)
     out["vnrm"] = _arr(res.vnrm, 3 * nm, np.float32).reshape(-1, 3)
+    out["sval"] = _arr(res.sval, 5 * nm, np.float32).reshape(-1, 5) if res.sval else np.zeros((0, 5), np.float32)
     R.ref_free(C.byref(res))
     return out
 

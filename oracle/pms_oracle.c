@@ -787,3 +787,48 @@ double orc_hausdorff_vertices_to_mesh(const double* a, uint64_t na, const double
     free(items); free(fill); free(cnt);
     return worst;
 }
+
+/* ------------------------------------------------------------------------ */
+/* MarchingCube_kernel.cuh:161-233  estimationOfScalarValue (float64)        */
+/* For mesh vertex v in spatial cell c: over cells [c - e, c + e) (clamped,  */
+/* the upper bound exclusive as in the reference), w = 1 - (d/h)^3 for       */
+/* d < h; rhop = sum w rho_j / sum w, vel = sum w vel_j / sum w (zero when   */
+/* no particle is within h).  out: 5 per vertex {vel xyz, |vel|, rhop}.      */
+/* ------------------------------------------------------------------------ */
+void orc_scalar_values(const orc_params* p, const orc_grid* g, const float* spos, const float* svel,
+                       const double* rho, const uint32_t* start, const uint32_t* end, const float* verts,
+                       uint64_t m, double* out)
+{
+    const double h = p->h;
+    #pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t t = 0; t < (int64_t)m; ++t) {
+        const float* v = verts + 3 * t;
+        uint32_t c[3], lo[3], hi[3];
+        cell_of(g, v, c);
+        box_incl(g, c, (uint32_t)g->spexpand, lo, hi);
+        double ws = 0.0, rh = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
+        for (uint32_t z = lo[2]; z < hi[2]; ++z)
+            for (uint32_t y = lo[1]; y < hi[1]; ++y)
+                for (uint32_t x = lo[0]; x < hi[0]; ++x) {
+                    const uint32_t q = lin3(x, y, z, g->spres);
+                    for (uint32_t j = start[q]; j < end[q]; ++j) {
+                        const float* pj = spos + 3 * (size_t)j;
+                        const double dx = (double)v[0] - pj[0], dy = (double)v[1] - pj[1], dz = (double)v[2] - pj[2];
+                        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+                        if (d >= h) continue;
+                        const double s = d / h, w = 1.0 - s * s * s;
+                        rh += w * rho[j];
+                        vx += w * svel[3 * (size_t)j]; vy += w * svel[3 * (size_t)j + 1]; vz += w * svel[3 * (size_t)j + 2];
+                        ws += w;
+                    }
+                }
+        double* o = out + 5 * t;
+        if (ws > 0.0) {
+            vx /= ws; vy /= ws; vz /= ws;
+            o[0] = vx; o[1] = vy; o[2] = vz; o[3] = sqrt(vx * vx + vy * vy + vz * vz); o[4] = rh / ws;
+        } else {
+            o[0] = o[1] = o[2] = o[3] = o[4] = 0.0;
+        }
+    }
+}
+

@@ -95,6 +95,10 @@ void orc_surface_list(const orc_grid* g, const uint32_t* surf_count, const uint3
                       const uint32_t* start, uint32_t* list);
 
 /* ---- anisotropy (float64) ---------------------------------------------------- */
+/* estimationOfScalarValue at mesh vertices (float64); out 5 per vertex {vel xyz, |vel|, rhop} */
+void orc_scalar_values(const orc_params* p, const orc_grid* g, const float* spos, const float* svel,
+                       const double* rho, const uint32_t* start, const uint32_t* end, const float* verts,
+                       uint64_t m, double* out);
 void orc_density(const orc_params* p, const orc_grid* g, const float* spos, uint32_t n,
                  const uint32_t* start, const uint32_t* end, double* rho);
 /* Per surface particle s (list[s] = sorted index):

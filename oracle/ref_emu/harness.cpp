@@ -109,13 +109,14 @@ struct ref_result {
     uint32_t* nvert;         /* n_band */
     float* vpos;             /* 3 n_mesh */
     float* vnrm;             /* 3 n_mesh */
+    float* sval;             /* 5 n_mesh: ScalarValue {vel xyz, |vel|, rhop} (estimationOfScalarValue) */
 };
 
 void ref_free(ref_result* r)
 {
     void* ptrs[] = {r->keys_sorted, r->perm, r->pos_sorted, r->rho, r->nrm, r->flag, r->cell_start, r->cell_end,
                     r->surf_count, r->surf_list, r->mean, r->G, r->band_flags, r->band_list, r->field,
-                    r->cube_flag, r->nvert, r->vpos, r->vnrm};
+                    r->cube_flag, r->nvert, r->vpos, r->vnrm, r->sval};
     for (void* p : ptrs) std::free(p);
     std::memset(r, 0, sizeof(*r));
 }
@@ -306,6 +307,12 @@ int ref_surface_run(const char* config_path, const float* pos, const float* vel,
     out->vnrm = (float*)std::malloc(12 * (size_t)NumMesh);
     std::memcpy(out->vpos, vert.data(), 12 * (size_t)NumMesh);
     std::memcpy(out->vnrm, norm.data(), 12 * (size_t)NumMesh);
+    /* MarchingCube.cu:50-52, 153-163: scalar values at the mesh vertices */
+    std::vector<ScalarValue> sv(NumMesh);
+    std::memset(sv.data(), 0, sizeof(ScalarValue) * NumMesh);
+    launch(NumMesh, [&] { estimationOfScalarValue(vert.data(), P, range.data(), sv.data()); });
+    out->sval = (float*)std::malloc(sizeof(ScalarValue) * (size_t)NumMesh);
+    std::memcpy(out->sval, sv.data(), sizeof(ScalarValue) * (size_t)NumMesh);
     return 0;
 }
 

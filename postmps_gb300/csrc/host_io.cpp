@@ -18,6 +18,7 @@
 #include <map>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 #include <algorithm>
 
@@ -523,10 +524,74 @@ extern "C" pms_status pms_write_vtk_particles(const char* path, const float* pos
     return f ? PMS_OK : PMS_ERR_IO;
 }
 
+// Surface mesh with the scalar values, legacy VTK polydata (the arrays of
+// FileData::saveSurfaceVTKfile, FileData.cpp:677-773: points, triangles
+// (i, i+1, i+2), Normal = -normal, Rhop, VelLength, Vel).  The reference writes
+// it through VTK in ASCII; this writer is BINARY (big-endian), which VTK reads the same.
+extern "C" pms_status pms_write_surface_vtk(const char* path, const float* pos, const float* nrm, const float* vel,
+                                            const float* vel_len, const float* rhop, uint64_t nv) {
+    if (!path || (nv && !pos) || nv >= (1ull << 31)) return PMS_ERR_INVALID_ARGUMENT;
+    const uint64_t nt = nv / 3;
+    std::string s;
+    s.reserve(64ull * nv + 1024);
+    s += "# vtk DataFile Version 3.0\nsurface\nBINARY\nDATASET POLYDATA\n";
+    s += "POINTS " + std::to_string(nv) + " float\n";
+    for (size_t i = 0; i < 3ull * nv; ++i) put_be32(s, &pos[i]);
+    s += "\nPOLYGONS " + std::to_string(nt) + " " + std::to_string(4ull * nt) + "\n";
+    for (uint64_t t = 0; t < nt; ++t) {
+        const int32_t k = 3, a = (int32_t)(3 * t), b = a + 1, c = a + 2;
+        put_be32(s, &k); put_be32(s, &a); put_be32(s, &b); put_be32(s, &c);
+    }
+    s += "\nPOINT_DATA " + std::to_string(nv) + "\nFIELD FieldData 4\n";
+    s += "Normal 3 " + std::to_string(nv) + " float\n";
+    for (size_t i = 0; i < 3ull * nv; ++i) { float v = nrm ? -nrm[i] : 0.f; put_be32(s, &v); }
+    s += "\nRhop 1 " + std::to_string(nv) + " float\n";
+    for (size_t i = 0; i < nv; ++i) { float v = rhop ? rhop[i] : 0.f; put_be32(s, &v); }
+    s += "\nVelLength 1 " + std::to_string(nv) + " float\n";
+    for (size_t i = 0; i < nv; ++i) { float v = vel_len ? vel_len[i] : 0.f; put_be32(s, &v); }
+    s += "\nVel 3 " + std::to_string(nv) + " float\n";
+    for (size_t i = 0; i < 3ull * nv; ++i) { float v = vel ? vel[i] : 0.f; put_be32(s, &v); }
+    s += "\n";
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return PMS_ERR_IO;
+    f.write(s.data(), (std::streamsize)s.size());
+    return f ? PMS_OK : PMS_ERR_IO;
+}
+
 // ---------------------------------------------------------------------------
 // PLY, ASCII, in tinyply 2.3's layout: header, then "x y z \n" per vertex with
 // the stream's default float formatting (printf %g), then "3 a b c \n" per face.
 // ---------------------------------------------------------------------------
+// Text of vertex lines [v0, v1) ("%g %g %g \n", tinyply's ASCII layout) and face
+// lines [t0, t1) ("3 i i+1 i+2 \n") into out.
+static void ply_lines(const float* pos, uint64_t v0, uint64_t v1, uint64_t t0, uint64_t t1, std::string& out) {
+    char tmp[128];
+    out.clear();
+    out.reserve((size_t)((v1 - v0) * 36 + (t1 - t0) * 32));
+    for (uint64_t i = v0; i < v1; ++i) {
+        const int k = snprintf(tmp, sizeof(tmp), "%g %g %g \n", (double)pos[3 * i], (double)pos[3 * i + 1], (double)pos[3 * i + 2]);
+        out.append(tmp, (size_t)k);
+    }
+    for (uint64_t t = t0; t < t1; ++t) {
+        // decimal digits by hand: the same text as "3 %u %u %u \n"
+        char* p = tmp;
+        *p++ = '3';
+        for (int c = 0; c < 3; ++c) {
+            *p++ = ' ';
+            uint32_t v = (uint32_t)(3 * t + c);
+            char d[12];
+            int nd = 0;
+            do { d[nd++] = (char)('0' + v % 10); v /= 10; } while (v);
+            while (nd) *p++ = d[--nd];
+        }
+        *p++ = ' ';
+        *p++ = '\n';
+        out.append(tmp, (size_t)(p - tmp));
+    }
+}
+
+// The text is formatted in parallel chunks (one per hardware thread) and written in order, so
+// the file is the same byte for byte as a serial writer's.
 extern "C" pms_status pms_write_ply(const char* path, const float* pos, uint64_t nv) {
     if (!path || (nv && !pos)) return PMS_ERR_INVALID_ARGUMENT;
     FILE* f = fopen(path, "wb");
@@ -535,25 +600,22 @@ extern "C" pms_status pms_write_ply(const char* path, const float* pos, uint64_t
     fprintf(f, "ply\nformat ascii 1.0\ncomment generated by tinyply 2.3\n");
     fprintf(f, "element vertex %llu\nproperty float x\nproperty float y\nproperty float z\n", (unsigned long long)nv);
     fprintf(f, "element face %llu\nproperty list uchar uint vertex_indices\nend_header\n", (unsigned long long)nf);
-    std::vector<char> buf(1 << 20);
-    size_t used = 0;
-    auto flush = [&]() { if (used) fwrite(buf.data(), 1, used, f); used = 0; };
-    char tmp[128];
-    for (uint64_t i = 0; i < nv; ++i) {
-        int k = snprintf(tmp, sizeof(tmp), "%g %g %g \n", (double)pos[3 * i], (double)pos[3 * i + 1], (double)pos[3 * i + 2]);
-        if (used + (size_t)k > buf.size()) flush();
-        memcpy(buf.data() + used, tmp, (size_t)k);
-        used += (size_t)k;
-    }
-    for (uint64_t t = 0; t < nf; ++t) {
-        int k = snprintf(tmp, sizeof(tmp), "3 %u %u %u \n", (unsigned)(3 * t), (unsigned)(3 * t + 1), (unsigned)(3 * t + 2));
-        if (used + (size_t)k > buf.size()) flush();
-        memcpy(buf.data() + used, tmp, (size_t)k);
-        used += (size_t)k;
-    }
-    flush();
-    bool ok = ferror(f) == 0;
-    fclose(f);
+    unsigned hw = std::thread::hardware_concurrency();
+    const uint64_t T = std::max<uint64_t>(1, std::min<uint64_t>(hw ? hw : 1, (nv + nf) / 65536 + 1));
+    // chunks: vertex lines first, then face lines, each split into T pieces; written in order
+    std::vector<std::string> vtext(T), ftext(T);
+    std::vector<std::thread> th;
+    for (uint64_t c = 0; c < T; ++c)
+        th.emplace_back([&, c]() {
+            ply_lines(pos, nv * c / T, nv * (c + 1) / T, 0, 0, vtext[c]);
+            ply_lines(pos, 0, 0, nf * c / T, nf * (c + 1) / T, ftext[c]);
+        });
+    for (std::thread& t : th) t.join();
+    bool ok = true;
+    for (const std::string& sv : vtext) ok = ok && fwrite(sv.data(), 1, sv.size(), f) == sv.size();
+    for (const std::string& sf : ftext) ok = ok && fwrite(sf.data(), 1, sf.size(), f) == sf.size();
+    ok = ferror(f) == 0 && ok;
+    ok = fclose(f) == 0 && ok;
     return ok ? PMS_OK : PMS_ERR_IO;
 }
 

@@ -208,6 +208,61 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
     return PMS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// estimationOfScalarValue (MarchingCube_kernel.cuh:161-233, called after the
+// triangles by MarchingCube::triangulation, MarchingCube.cu:50-52): density
+// and velocity at every mesh vertex, averaged over the particles within h of
+// it with w = 1 - (d/h)^3, over the cells [c - e, c + e) of the vertex's
+// spatial cell (upper bound exclusive, as the reference).  Out: 5 floats per
+// vertex {vel xyz, |vel|, rhop}, the reference's ScalarValue; zero where no
+// particle is within h.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_scalar_values(KGrid g, float h, const Counters* __restrict__ cnt,
+                                                            const float* __restrict__ vert,
+                                                            const uint32_t* __restrict__ cell_start,
+                                                            const float4* __restrict__ spos, const float4* __restrict__ svel,
+                                                            const float* __restrict__ rho, float* __restrict__ out) {
+    const unsigned long long m = cnt->nmesh;
+    const float pad = 1e-4f * g.sp_cs;
+    for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < m;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const float3 v = make_float3(vert[3 * t], vert[3 * t + 1], vert[3 * t + 2]);
+        const uint3 c = sp_cell(g, v.x, v.y, v.z);
+        uint3 lo, hi;
+        box_clamp(g, c, (uint32_t)g.spexpand, lo, hi);   // loops run to hi exclusive, as the reference's
+        float ws = 0.f, rh = 0.f, vx = 0.f, vy = 0.f, vz = 0.f;
+        row_walk(g, v, lo, hi, h * h, pad, cell_start, [&](uint32_t j) {
+            const float4 q = __ldg(&spos[j]);
+            const float dx = v.x - q.x, dy = v.y - q.y, dz = v.z - q.z;
+            const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+            if (dist < h) {
+                const float s = dist / h;
+                const float w = 1.f - s * s * s;
+                const float4 u = __ldg(&svel[j]);
+                rh += w * __ldg(&rho[j]);
+                vx += w * u.x; vy += w * u.y; vz += w * u.z;
+                ws += w;
+            }
+        });
+        float* o = out + 5 * t;
+        if (ws > 0.f) {
+            rh /= ws; vx /= ws; vy /= ws; vz /= ws;
+            o[0] = vx; o[1] = vy; o[2] = vz; o[3] = sqrtf(vx * vx + vy * vy + vz * vz); o[4] = rh;
+        } else {
+            o[0] = o[1] = o[2] = o[3] = o[4] = 0.f;
+        }
+    }
+}
+
+pms_status launch_scalar_values(pms_ctx* ctx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    k_scalar_values<<<grid_for(ctx->nmesh, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ctx->prm.h, ctx->counters.as<Counters>(), ctx->vert.as<float>(), ctx->cell_start.as<uint32_t>(),
+        ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->rho.as<float>(), ctx->sval.as<float>());
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 // batched frames: this frame's mesh takes the next free stretch of the arena
 // (frames of different lanes run concurrently, so the claim is atomic)
 __global__ void k_batch_base(const Counters* __restrict__ cnt, unsigned long long* __restrict__ running,

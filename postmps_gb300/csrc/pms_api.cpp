@@ -52,7 +52,7 @@ static void release_all(pms_ctx* c) {
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
                     &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
                     &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
-                    &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->d_isfree, &c->d_freescan,
+                    &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
                     &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp};
@@ -254,7 +254,7 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     }
     c->n = n;
     c->have_particles = true;
-    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = false;
+    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = false;
     c->band_learned = c->mc_classified = false;
     c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     c->ns = c->nv = c->nvalid = 0;
@@ -368,6 +368,36 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     }
     c->have_mc = true;
     mark(c, kStageMc + 1);
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_scalar_values(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_mc) return pms_fail(c, PMS_ERR_STATE, "pms_scalar_values before pms_marching_cubes");
+    cudaSetDevice(c->device);
+    PMS_CUDA(c, c->sval.ensure(20 * (size_t)(c->nmesh ? c->nmesh : 1)));
+    if (c->nmesh) { pms_status st = launch_scalar_values(c); if (st) return st; }
+    c->have_values = true;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_download_scalar_values(pms_ctx* c, float* vel_xyz, float* vel_len, float* rhop, uint64_t cap,
+                                                 uint64_t* n_out) {
+    if (!c || !n_out) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_values) return pms_fail(c, PMS_ERR_STATE, "pms_download_scalar_values before pms_scalar_values");
+    cudaSetDevice(c->device);
+    const uint64_t m = c->nmesh;
+    *n_out = m;
+    if (!vel_xyz && !vel_len && !rhop) return PMS_OK;
+    if (cap < m) return PMS_ERR_CAPACITY;
+    std::vector<float> sv(5 * (size_t)m);
+    if (m) PMS_CUDA(c, cudaMemcpyAsync(sv.data(), c->sval.p, 20 * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (uint64_t i = 0; i < m; ++i) {
+        if (vel_xyz) { vel_xyz[3 * i] = sv[5 * i]; vel_xyz[3 * i + 1] = sv[5 * i + 1]; vel_xyz[3 * i + 2] = sv[5 * i + 2]; }
+        if (vel_len) vel_len[i] = sv[5 * i + 3];
+        if (rhop) rhop[i] = sv[5 * i + 4];
+    }
     return PMS_OK;
 }
 

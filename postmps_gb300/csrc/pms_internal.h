@@ -133,7 +133,8 @@ struct pms_ctx {
     // band
     pms::DBuf bm0, bm, wcount, wprefix, vlist;
     // field and marching cubes
-    pms::DBuf field, mc_case, mc_key, mc_off, valid, vert, vnorm;
+    pms::DBuf field, mc_case, mc_key, mc_off, valid, vert, vnorm, sval;
+    bool have_values = false;
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
@@ -213,6 +214,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 pms_status launch_mc_classify(pms_ctx* ctx);
 pms_status launch_mc_emit(pms_ctx* ctx);
+pms_status launch_scalar_values(pms_ctx* ctx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
                              unsigned long long cap);

@@ -191,6 +191,9 @@ def lib() -> C.CDLL:
         L.pms_free_host.restype = None
         L.pms_run_config.argtypes = [C.c_char_p, C.c_int]
         L.pms_mc_tables.argtypes = [_u32p, _i32p, _u32p, _u32p, C.c_int]
+        L.pms_scalar_values.argtypes = [vp]
+        L.pms_download_scalar_values.argtypes = [vp, vp, vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.pms_write_surface_vtk.argtypes = [C.c_char_p, vp, vp, vp, vp, vp, C.c_uint64]
         L.pms_set_band_model.argtypes = [vp, C.POINTER(BandModel)]
         L.pms_set_band_mode.argtypes = [vp, C.c_int]
         L.pms_run_batch.argtypes = [vp, C.POINTER(Frame), C.c_uint32, C.c_int]
@@ -286,6 +289,11 @@ def write_vtk(path: str, pos, vel=None, rho=None) -> None:
     _check(lib().pms_write_vtk_particles(str(path).encode(), _ptr(pos), _ptr(vel), _ptr(rho), len(pos)))
 
 
+def write_surface_vtk(path: str, verts, normals=None, vel=None, vel_len=None, rhop=None) -> None:
+    arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (verts, normals, vel, vel_len, rhop)]
+    _check(lib().pms_write_surface_vtk(path.encode(), *[_ptr(a) for a in arrs], len(arrs[0])))
+
+
 def write_ply(path: str, verts) -> None:
     v = np.ascontiguousarray(verts, np.float32)
     _check(lib().pms_write_ply(str(path).encode(), _ptr(v), len(v)))
@@ -355,6 +363,18 @@ class Context:
     def surface(self): self._call("pms_surface")
     def diffuse(self): self._call("pms_diffuse")
     def run_frame(self): self._call("pms_run_frame")
+
+    # density and velocity at the mesh vertices
+    def scalar_values(self) -> dict:
+        self._call("pms_scalar_values")
+        n = C.c_uint64()
+        self._call("pms_download_scalar_values", None, None, None, 0, C.byref(n))
+        m = n.value
+        out = {"vel": np.zeros((m, 3), np.float32), "vel_len": np.zeros(m, np.float32), "rhop": np.zeros(m, np.float32)}
+        if m:
+            self._call("pms_download_scalar_values", _ptr(out["vel"]), _ptr(out["vel_len"]), _ptr(out["rhop"]), m,
+                       C.byref(n))
+        return out
 
     # learned band
     def set_band_model(self, model: BandModel) -> None:

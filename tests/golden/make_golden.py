@@ -79,7 +79,7 @@ def make(name: str) -> str:
         iso=np.float32(R["iso"]), keys_sorted=R["keys_sorted"], perm=R["perm"], cell_start=R["cell_start"],
         cell_end=R["cell_end"], surf_count=R["surf_count"], surf_list=sl, rho=R["rho"], mean=R["mean"], G=R["G"],
         nrm=R["nrm"][sl], flag=(R["flag"][sl] != 0).astype(np.uint8), band_list=R["band_list"], field=R["field"],
-        cube_flag=R["cube_flag"], nvert=R["nvert"], vpos=R["vpos"], vnrm=R["vnrm"],
+        cube_flag=R["cube_flag"], nvert=R["nvert"], vpos=R["vpos"], vnrm=R["vnrm"], sval=R["sval"],
         n_surface=np.uint32(R["n_surface"]), n_band=np.uint32(R["n_band"]), n_valid=np.uint32(R["n_valid"]),
         n_mesh=np.uint32(R["n_mesh"]), mc_tables_sha256=np.array(tables_digest()),
     )

@@ -183,3 +183,38 @@ def test_stage_order_enforced(pms_lib, tmp_config):
         with pytest.raises(pms_lib.PmsError) as ei:
             ctx.field()
         assert ei.value.status == 7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["drops_sheet", "block12_ratio4"])
+def test_scalar_values_match_oracle(pms_lib, oracle, tmp_config, tmp_path, case):
+    """estimationOfScalarValue on the GPU against the float64 oracle at the GPU's
+    own mesh vertices, with the GPU's sorted particles and densities (the
+    oracle itself is pinned to the reference's kernel by the CPU tests)."""
+    pms = pms_lib
+    d = load_golden(case)
+    cfg = pms.load_config(tmp_config(d["config"]))
+    with pms.Context(cfg, 0) as ctx:
+        ctx.upload(d["pos"], d["vel"], d["rho_in"])
+        ctx.build_grid()
+        ctx.surface()
+        sv = ctx.scalar_values()
+        verts, nrm = ctx.mesh()
+        spos = ctx.debug("pos_sorted")
+        perm = ctx.debug("perm")
+        rho = ctx.debug("density").astype(np.float64)
+        start, end = ctx.debug("cell_start"), ctx.debug("cell_end")
+        g = ctx.grid()
+    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(d["config"])))
+    og = oracle.grid_from_positions(p, d["pos"])
+    ref = oracle.scalar_values(p, og, spos, d["vel"][perm], rho, start, end, verts)
+    assert len(ref) == len(verts) == len(sv["rhop"]) > 0
+    scale = max(1.0, float(np.abs(ref[:, 4]).max()))
+    assert float(np.abs(sv["rhop"] - ref[:, 4]).max()) <= 1e-5 * scale
+    vs = max(1e-6, float(np.abs(ref[:, :4]).max()))
+    assert float(np.abs(sv["vel"] - ref[:, :3]).max()) <= 1e-5 * vs
+    assert float(np.abs(sv["vel_len"] - ref[:, 3]).max()) <= 1e-5 * vs
+    path = str(tmp_path / "surface.vtk")
+    pms.write_surface_vtk(path, verts, nrm, sv["vel"], sv["vel_len"], sv["rhop"])
+    head = open(path, "rb").read(200)
+    assert head.startswith(b"# vtk DataFile Version 3.0\nsurface\nBINARY\nDATASET POLYDATA\nPOINTS ")

@@ -145,3 +145,21 @@ def test_hausdorff_helper(oracle):
     pts = np.array([[0.25, 0.25, 0.5], [2.0, 0.0, 0.0]], np.float64).reshape(-1)
     h = oracle.lib().orc_hausdorff_vertices_to_mesh(pts, 2, tri, 3, 0.3)
     assert abs(h - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_scalar_values_given_reference_mesh(oracle, case):
+    """estimationOfScalarValue (MarchingCube_kernel.cuh:161-233): the float64
+    restatement at the reference's own mesh vertices, with the reference's
+    densities, against the reference's float32 values."""
+    d = load_golden(case)
+    p, g = setup(oracle, d)
+    spos = np.ascontiguousarray(d["pos"][d["perm"]])
+    svel = np.ascontiguousarray(d["vel"][d["perm"]])
+    sv = oracle.scalar_values(p, g, spos, svel, d["rho"].astype(np.float64), d["cell_start"], d["cell_end"], d["vpos"])
+    ref = d["sval"].astype(np.float64)                   # {vel xyz, |vel|, rhop}
+    assert sv.shape == ref.shape
+    scale_r = max(1.0, float(np.abs(ref[:, 4]).max()))
+    assert float(np.abs(sv[:, 4] - ref[:, 4]).max()) <= 1e-5 * scale_r
+    scale_v = max(1e-6, float(np.abs(ref[:, :4]).max()))
+    assert float(np.abs(sv[:, :4] - ref[:, :4]).max()) <= 1e-5 * scale_v
