@@ -26,6 +26,7 @@ static constexpr float kSigma = 1.56668147f;      // Define.h:11, 315/(64 pi)
 struct AnisoParams {
     float h, h_sq, h_inv, r2h, mass, kdens, inv_h2;
     int min_nn;
+    uint32_t sp_size, spres_x;   // where the per-row radii start; cells per row
     double cond_limit;
 };
 
@@ -194,7 +195,8 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_moments(KGrid g, AnisoParams 
 // ---------------------------------------------------------------------------
 // anisotropy, pass 2: covariance, eigen decomposition, clamp, G, normal, flag
 // (Anisotropic_kernel.cuh:431-518) from the moments; also the per-cell
-// support radius max(maxvalue * h) that lets the field skip far cells.
+// and per-row support radius max(maxvalue * h) that lets the field skip far
+// rows and cells.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_eigen(AnisoParams ap, const uint32_t* __restrict__ slist,
                                                     const Counters* __restrict__ cnt, const uint32_t* __restrict__ skeys,
@@ -284,9 +286,39 @@ __global__ void __launch_bounds__(kThreads) k_eigen(AnisoParams ap, const uint32
             for (int b = 0; b < 3; ++b) gd[3 * a + b] = G[a][b];
         gd[9] = maxv;
         nnb[s] = nn;
-        // per-cell and global support radius (positive floats order like their bits)
-        atomicMax(reinterpret_cast<unsigned int*>(&cell_rad[skeys[i]]), __float_as_uint(hs));
+        // per-cell, per-row and global support radius (positive floats order like their bits)
+        const uint32_t key = skeys[i];
+        atomicMax(reinterpret_cast<unsigned int*>(&cell_rad[key]), __float_as_uint(hs));
+        atomicMax(reinterpret_cast<unsigned int*>(&cell_rad[ap.sp_size + key / ap.spres_x]), __float_as_uint(hs));
         atomicMax(&cnt_w->rad_max_bits, __float_as_uint(hs));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-cell culling record for the field: the bounding box of the cell's
+// particles and the square of the largest support among them (h, or the
+// cell's largest maxvalue * h), grown by kSupportGrow.  A vertex farther than
+// that from the box gets exactly 0 from every particle of the cell.  Only
+// non-empty cells are written (the field reads no record of an empty cell).
+// rec[2c] = {min x, min y, min z, r^2}, rec[2c + 1] = {max x, max y, max z, 0}.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_cell_records(const uint32_t* __restrict__ cell_start,
+                                                           const float4* __restrict__ spos,
+                                                           const float* __restrict__ cell_rad, float h, uint32_t S,
+                                                           float4* __restrict__ rec) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < S; c += gridDim.x * blockDim.x) {
+        const uint32_t j0 = cell_start[c], j1 = cell_start[c + 1];
+        if (j0 == j1) continue;
+        const float4 q = spos[j0];
+        float lx = q.x, ly = q.y, lz = q.z, hx = q.x, hy = q.y, hz = q.z;
+        for (uint32_t j = j0 + 1; j < j1; ++j) {
+            const float4 p = spos[j];
+            lx = fminf(lx, p.x); ly = fminf(ly, p.y); lz = fminf(lz, p.z);
+            hx = fmaxf(hx, p.x); hy = fmaxf(hy, p.y); hz = fmaxf(hz, p.z);
+        }
+        const float r = fmaxf(cell_rad[c], h) * kSupportGrow;
+        rec[2 * (size_t)c] = make_float4(lx, ly, lz, r * r);
+        rec[2 * (size_t)c + 1] = make_float4(hx, hy, hz, 0.f);
     }
 }
 
@@ -299,6 +331,8 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     ap.inv_h2 = 1.f / (P.h * P.h);
     ap.min_nn = P.min_num_neighbors;
     ap.cond_limit = ctx->cfg.fp64_svd_cond;
+    ap.sp_size = g.sp_size;
+    ap.spres_x = g.spres[0];
     Counters* cnt = ctx->counters.as<Counters>();
     // block sizes of the neighbour walks are autotuned (64, 128 or 256 threads)
     const int bd = ctx->tune.density_threads, bm = ctx->tune.moments_threads;
@@ -324,11 +358,16 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     else if (bm == 256) mom(k_moments<256>);
     else mom(k_moments<128>);
     PMS_LAUNCHED(ctx);
-    PMS_CUDA(ctx, cudaMemsetAsync(ctx->cell_rad.p, 0, sizeof(float) * (size_t)g.sp_size, ctx->stream));
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->cell_rad.p, 0,
+                                  sizeof(float) * ((size_t)g.sp_size + (size_t)g.spres[1] * g.spres[2]), ctx->stream));
     k_eigen<<<grid_for(ctx->n, kThreads), kThreads, 0, ctx->stream>>>(
         ap, ctx->slist.as<uint32_t>(), cnt, ctx->skeys.as<uint32_t>(), ctx->spos.as<float4>(), ctx->moments.as<float4>(),
         ctx->aniso.as<float4>(), ctx->nrm4.as<float4>(), ctx->mean4.as<float4>(), ctx->gdebug.as<float>(),
         ctx->nnb.as<uint32_t>(), ctx->cell_rad.as<float>(), cnt);
+    PMS_LAUNCHED(ctx);
+    k_cell_records<<<grid_for(g.sp_size, kThreads), kThreads, 0, ctx->stream>>>(
+        ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->cell_rad.as<float>(), P.h, g.sp_size,
+        ctx->cell_rec.as<float4>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

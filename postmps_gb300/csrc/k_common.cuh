@@ -95,36 +95,56 @@ __device__ __forceinline__ float cell_gap2(const KGrid& g, float3 p, uint32_t x,
     return dx * dx + dy * dy + dz * dz;
 }
 
+// Margin, in cells, added to every range that the neighbour walks cut from a
+// support radius.  The ranges are computed from the point's position in cell
+// units, u = (p - min) / cell, whose rounding error (like that of a particle's
+// own key) stays below 1e-3 cells on grids of up to 8000 cells per axis; a cell
+// left out by the cut therefore holds no particle within the support, and the
+// cut changes no sum.
+constexpr float kRangeMargin = 0.01f;
+
+// Relative margin on support radii used for culling: a particle's kernel is
+// non-zero only within its support (|G r| < 1 implies |r| < maxvalue * h), and
+// float rounding of |G r|^2 moves that edge by ~1e-6 relative at most.
+constexpr float kSupportGrow = 1.0001f;
+
+// First and one-past-last cell of [u - rc, u + rc] along one axis, clipped to [lo, hi).
+__device__ __forceinline__ void cell_range(float u, float rc, uint32_t lo, uint32_t hi, int& a, int& b) {
+    a = max((int)floorf(u - rc), (int)lo);
+    b = min((int)floorf(u + rc) + 1, (int)hi);
+}
+
 // Row-segment neighbour walk of one point.  Cells are sorted by key and key =
 // (z * res_y + y) * res_x + x, so the cells x in [xa, xb) of one row hold the
-// contiguous particle range [cell_start[row + xa], cell_start[row + xb]).  For
-// each row (z, y) of the window [lo, hi) (hi exclusive) that comes within
-// sqrt(r2) of p, the x range is cut to the cells the sphere can reach
-// (conservatively: a spare cell costs only the per-particle test) and body(j)
-// runs over the range, in the reference's z, y, x, particle order.
-// cell_start must have sp_size + 1 entries.
+// contiguous particle range [cell_start[row + xa], cell_start[row + xb]).  The
+// walk visits only the slabs z and rows y of the window [lo, hi) (hi
+// exclusive) that come within sqrt(r2) of p, each row cut to the cells the
+// sphere reaches, and body(j) runs over the particle ranges in the reference's
+// z, y, x, particle order.  cell_start must have sp_size + 1 entries.
 template <class Body>
 __device__ __forceinline__ void row_walk(const KGrid& g, float3 p, uint3 lo, uint3 hi, float r2, float pad,
                                          const uint32_t* __restrict__ cell_start, Body&& body) {
     const uint32_t srx = g.spres[0], srxy = g.spres[0] * g.spres[1];
     const float cs = g.sp_cs, inv = 1.f / g.sp_cs;
-    for (uint32_t z = lo.z; z < hi.z; ++z) {
+    const float ux = (p.x - g.min_pos[0]) * inv, uy = (p.y - g.min_pos[1]) * inv, uz = (p.z - g.min_pos[2]) * inv;
+    int za, zb;
+    cell_range(uz, sqrtf(r2) * inv + kRangeMargin, lo.z, hi.z, za, zb);
+    for (int z = za; z < zb; ++z) {
         const float z0 = g.min_pos[2] + (float)z * cs;
         const float gz0 = axis_gap(p.z, z0 - pad, z0 + cs + pad);
         const float gz = gz0 * gz0;
         if (gz >= r2) continue;
-        for (uint32_t y = lo.y; y < hi.y; ++y) {
+        int ya, yb;
+        cell_range(uy, sqrtf(r2 - gz) * inv + kRangeMargin, lo.y, hi.y, ya, yb);
+        for (int y = ya; y < yb; ++y) {
             const float y0 = g.min_pos[1] + (float)y * cs;
             const float gy0 = axis_gap(p.y, y0 - pad, y0 + cs + pad);
             const float gyz = gz + gy0 * gy0;
             if (gyz >= r2) continue;
-            const float dx = sqrtf(r2 - gyz) + 2.f * pad;
-            int xa = (int)floorf((p.x - dx - g.min_pos[0]) * inv) - 1;
-            int xb = (int)floorf((p.x + dx - g.min_pos[0]) * inv) + 2;
-            xa = max(xa, (int)lo.x);
-            xb = min(xb, (int)hi.x);
+            int xa, xb;
+            cell_range(ux, sqrtf(r2 - gyz) * inv + kRangeMargin, lo.x, hi.x, xa, xb);
             if (xa >= xb) continue;
-            const uint32_t row = z * srxy + y * srx;
+            const uint32_t row = (uint32_t)z * srxy + (uint32_t)y * srx;
             const uint32_t ja = __ldg(&cell_start[row + (uint32_t)xa]), jb = __ldg(&cell_start[row + (uint32_t)xb]);
 #pragma unroll 2
             for (uint32_t j = ja; j < jb; ++j) body(j);

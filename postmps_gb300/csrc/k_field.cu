@@ -18,12 +18,14 @@
 // non-surface cells -- so one branch-free formula serves both kinds and the
 // loads of consecutive particles overlap.  The cells x in [xa, xb) of a row are
 // the contiguous particle range [cell_start[row + xa], cell_start[row + xb]);
-// each row is cut to the cells the largest support can reach, and a cell whose
+// slabs and rows are cut to those the largest support can reach, each row to
+// the cells its own largest support reaches, and a cell whose particles' bounding
 // box lies beyond the support of every particle in it (h, or the cell's largest
 // maxvalue * h recorded by the anisotropy pass) contributes exactly zero and is
-// skipped.  Adding a zero contribution leaves the sum unchanged, so neither
-// cut changes the reference's sum or its early exit: the threshold test after
-// a skipped cell sees the same sum as the test before it.
+// skipped.
+// Adding a zero contribution leaves the sum unchanged, so no cut changes the
+// reference's sum or its early exit: the threshold test after a skipped cell
+// sees the same sum as the test before it.
 #include "pms_internal.h"
 #include "k_common.cuh"
 
@@ -39,6 +41,16 @@ __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pa
     float a = lo - pad, b = lo + cs + pad;
     float d = fmaxf(a - p, p - b);
     return d > 0.f ? d * d : 0.f;
+}
+
+// true when vertex v is within the culling radius of cell c's particle box
+// (cell records: {min xyz, r^2}, {max xyz, 0})
+__device__ __forceinline__ bool cell_reaches(const float4* __restrict__ rec, uint32_t c, const float3 v) {
+    const float4 b0 = __ldg(&rec[2 * (size_t)c]), b1 = __ldg(&rec[2 * (size_t)c + 1]);
+    const float dx = fmaxf(fmaxf(b0.x - v.x, v.x - b1.x), 0.f);
+    const float dy = fmaxf(fmaxf(b0.y - v.y, v.y - b1.y), 0.f);
+    const float dz = fmaxf(fmaxf(b0.z - v.z, v.z - b1.z), 0.f);
+    return dx * dx + dy * dy + dz * dz < b0.w;
 }
 
 // Sum of the contributions of particles [j0, j1) at vertex v.  A particle adds
@@ -64,18 +76,25 @@ __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float
     return sum;
 }
 
-// BT threads per block (autotuned: 64, 128 or 256), 64 registers per thread at most
+// BT threads per block (autotuned: 64, 128 or 256), 64 registers per thread at most.
+// cell_rad holds sp_size per-cell support radii followed by one radius per row
+// (z, y): the largest maxvalue * h of the row's particles (0 where none is
+// anisotropic).  The z and y ranges are cut from the largest support of the
+// frame, each row's x range from the row's own radius, and each non-empty cell
+// by its record: the bounding box of its particles and its largest support.
 template <int BT>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
                                                     const uint32_t* __restrict__ n_dev,
                                                     const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
-                                                    const float* __restrict__ cell_rad, const float4* __restrict__ spos,
-                                                    const float4* __restrict__ aniso, float* __restrict__ field) {
+                                                    const float* __restrict__ cell_rad, const float4* __restrict__ rec,
+                                                    const float4* __restrict__ spos, const float4* __restrict__ aniso,
+                                                    float* __restrict__ field) {
     const uint32_t nv = *n_dev;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
-    const uint32_t srx = g.spres[0], srxy = g.spres[0] * g.spres[1];
+    const uint32_t srx = g.spres[0], sry = g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
     const float pad = 1e-4f * g.sp_cs, inv_cs = 1.f / g.sp_cs;
+    const float* __restrict__ row_rad = cell_rad + g.sp_size;
     // largest support of any particle this frame
     const float rmax = fmaxf(__uint_as_float(cnt->rad_max_bits), fp.h) * fp.grow;
     const float rmax2 = rmax * rmax;
@@ -86,38 +105,39 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp
         const uint3 c = sp_cell(g, v.x, v.y, v.z);
         uint3 lo, hi;
         box_clamp(g, c, e2, lo, hi);             // the reference's loops run to hi exclusive
+        const float ux = (v.x - g.min_pos[0]) * inv_cs, uy = (v.y - g.min_pos[1]) * inv_cs,
+                    uz = (v.z - g.min_pos[2]) * inv_cs;
         float sum = 0.f;
-        for (uint32_t z = lo.z; z < hi.z; ++z) {
+        int za, zb;
+        cell_range(uz, rmax * inv_cs + kRangeMargin, lo.z, hi.z, za, zb);
+        for (int z = za; z < zb; ++z) {
             const float gz = gap2_axis(v.z, g.min_pos[2] + (float)z * g.sp_cs, g.sp_cs, pad);
             if (gz >= rmax2) continue;
-            for (uint32_t y = lo.y; y < hi.y; ++y) {
+            int ya, yb;
+            cell_range(uy, sqrtf(rmax2 - gz) * inv_cs + kRangeMargin, lo.y, hi.y, ya, yb);
+            for (int y = ya; y < yb; ++y) {
                 const float gyz = gz + gap2_axis(v.y, g.min_pos[1] + (float)y * g.sp_cs, g.sp_cs, pad);
-                if (gyz >= rmax2) continue;
-                const uint32_t row = z * srxy + y * srx;
+                const uint32_t rowi = (uint32_t)z * sry + (uint32_t)y;
+                const float rr = fmaxf(__ldg(&row_rad[rowi]), fp.h) * fp.grow;
+                const float rr2 = rr * rr;
+                if (gyz >= rr2) continue;           // every cell of the row adds 0
+                const uint32_t row = rowi * srx;
                 if (sum > fp.thr) {
                     // threshold crossed: the reference adds this row's first cell, then breaks
                     if (lo.x < hi.x) {
-                        const float gx = gyz + gap2_axis(v.x, g.min_pos[0] + (float)lo.x * g.sp_cs, g.sp_cs, pad);
-                        if (gx < rmax2)
-                            sum = range_sum(__ldg(&cell_start[row + lo.x]), __ldg(&cell_start[row + lo.x + 1]), v, spos,
-                                            aniso, sum);
+                        const uint32_t j0 = __ldg(&cell_start[row + lo.x]), j1 = __ldg(&cell_start[row + lo.x + 1]);
+                        if (j0 != j1 && cell_reaches(rec, row + lo.x, v)) sum = range_sum(j0, j1, v, spos, aniso, sum);
                     }
                     continue;
                 }
-                // cells of the row the largest support can reach
-                const float dx = sqrtf(rmax2 - gyz) + 2.f * pad;
-                int xa = (int)floorf((v.x - dx - g.min_pos[0]) * inv_cs) - 1;
-                int xb = (int)floorf((v.x + dx - g.min_pos[0]) * inv_cs) + 2;
-                xa = max(xa, (int)lo.x);
-                xb = min(xb, (int)hi.x);
+                // cells of the row the row's largest support can reach
+                int xa, xb;
+                cell_range(ux, sqrtf(rr2 - gyz) * inv_cs + kRangeMargin, lo.x, hi.x, xa, xb);
                 uint32_t jn = xa < xb ? __ldg(&cell_start[row + (uint32_t)xa]) : 0u;
                 for (int x = xa; x < xb; ++x) {
                     const uint32_t j0 = jn;
                     jn = __ldg(&cell_start[row + (uint32_t)x + 1u]);
-                    if (j0 == jn) continue;
-                    const float gx = gyz + gap2_axis(v.x, g.min_pos[0] + (float)x * g.sp_cs, g.sp_cs, pad);
-                    const float r = fmaxf(__ldg(&cell_rad[row + (uint32_t)x]), fp.h) * fp.grow;
-                    if (gx >= r * r) continue;
+                    if (j0 == jn || !cell_reaches(rec, row + (uint32_t)x, v)) continue;
                     sum = range_sum(j0, jn, v, spos, aniso, sum);
                     if (sum > fp.thr) break;
                 }
@@ -133,13 +153,14 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     FieldParams fp;
     fp.h = P.h;
     fp.thr = 2.f * P.iso_value;
-    fp.grow = 1.0001f;
+    fp.grow = kSupportGrow;
     Counters* cnt = ctx->counters.as<Counters>();
     const int bt = ctx->tune.field_threads;
     const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1024u / (unsigned)bt));
     auto go = [&](auto kern) {
         kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
-                                             ctx->cell_rad.as<float>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out);
+                                             ctx->cell_rad.as<float>(), ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(),
+                                             ctx->aniso.as<float4>(), out);
     };
     if (bt == 64) go(k_field<64>);
     else if (bt == 256) go(k_field<256>);

@@ -50,7 +50,7 @@ extern "C" uint64_t pms_kernel_launches(const pms_ctx* ctx) { return ctx ? ctx->
 static void release_all(pms_ctx* c) {
     DBuf* bufs[] = {&c->in_pos, &c->in_vel, &c->in_rho, &c->keys, &c->slot, &c->order, &c->skeys, &c->spos,
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
-                    &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
+                    &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->cell_rec, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
                     &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
                     &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
@@ -162,7 +162,8 @@ pms_status pms::ensure_grid_buffers(pms_ctx* c, const pms_grid& g) {
     PMS_CUDA(c, c->cell_info.ensure(8 * S));
     PMS_CUDA(c, c->surf_count.ensure(4 * S));
     PMS_CUDA(c, c->surf_start.ensure(4 * S));
-    PMS_CUDA(c, c->cell_rad.ensure(4 * S));
+    PMS_CUDA(c, c->cell_rad.ensure(4 * (S + (size_t)g.spres[1] * g.spres[2])));   // per cell, then per row
+    PMS_CUDA(c, c->cell_rec.ensure(32 * S));   // two float4 per cell
     const size_t W = ((uint64_t)g.sc_size + 31) / 32 + 1;
     PMS_CUDA(c, c->bm0.ensure(4 * W));
     PMS_CUDA(c, c->bm.ensure(4 * W));

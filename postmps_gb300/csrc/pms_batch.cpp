@@ -368,6 +368,9 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         if ((st = pms_grid_from_bbox(&c->prm, bmin, bmax, &grid[f]))) return pms_fail(c, st, "frame %u: grid too large", f);
         gmax.sp_size = std::max(gmax.sp_size, grid[f].sp_size);
         gmax.sc_size = std::max(gmax.sc_size, grid[f].sc_size);
+        // rows of the largest frame (the per-row radii follow the per-cell ones)
+        gmax.spres[1] = 1;
+        gmax.spres[2] = std::max(gmax.spres[2], grid[f].spres[1] * grid[f].spres[2]);
     }
     bool grids_same = shape_same && b->grid.size() == k;
     for (uint32_t f = 0; grids_same && f < k; ++f) grids_same = same_grid(b->grid[f], grid[f]);

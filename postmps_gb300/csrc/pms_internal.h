@@ -129,7 +129,7 @@ struct pms_ctx {
     pms::DBuf keys, slot, order, skeys, spos, svel, rho;
     pms::DBuf cell_count, cell_start, cell_info, surf_count, surf_start, big_cells;
     // anisotropy
-    pms::DBuf slist, moments, aniso, nrm4, mean4, gdebug, nnb, cell_rad;
+    pms::DBuf slist, moments, aniso, nrm4, mean4, gdebug, nnb, cell_rad, cell_rec;
     // band
     pms::DBuf bm0, bm, wcount, wprefix, vlist;
     // field and marching cubes
