@@ -298,8 +298,8 @@ __global__ void __launch_bounds__(kThreads) k_eigen(AnisoParams ap, const uint32
 // per-cell culling record for the field: the bounding box of the cell's
 // particles and the square of the largest support among them (h, or the
 // cell's largest maxvalue * h), grown by kSupportGrow.  A vertex farther than
-// that from the box gets exactly 0 from every particle of the cell.  Only
-// non-empty cells are written (the field reads no record of an empty cell).
+// that from the box gets exactly 0 from every particle of the cell.  An empty
+// cell gets r^2 = -1, which no vertex reaches.
 // rec[2c] = {min x, min y, min z, r^2}, rec[2c + 1] = {max x, max y, max z, 0}.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_cell_records(const uint32_t* __restrict__ cell_start,
@@ -308,7 +308,10 @@ __global__ void __launch_bounds__(kThreads) k_cell_records(const uint32_t* __res
                                                            float4* __restrict__ rec) {
     for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < S; c += gridDim.x * blockDim.x) {
         const uint32_t j0 = cell_start[c], j1 = cell_start[c + 1];
-        if (j0 == j1) continue;
+        if (j0 == j1) {
+            rec[2 * (size_t)c] = make_float4(0.f, 0.f, 0.f, -1.f);
+            continue;
+        }
         const float4 q = spos[j0];
         float lx = q.x, ly = q.y, lz = q.z, hx = q.x, hy = q.y, hz = q.z;
         for (uint32_t j = j0 + 1; j < j1; ++j) {

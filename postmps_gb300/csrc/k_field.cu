@@ -44,7 +44,7 @@ __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pa
 }
 
 // true when vertex v is within the culling radius of cell c's particle box
-// (cell records: {min xyz, r^2}, {max xyz, 0})
+// (cell records: {min xyz, r^2}, {max xyz, 0}; r^2 = -1 for an empty cell)
 __device__ __forceinline__ bool cell_reaches(const float4* __restrict__ rec, uint32_t c, const float3 v) {
     const float4 b0 = __ldg(&rec[2 * (size_t)c]), b1 = __ldg(&rec[2 * (size_t)c + 1]);
     const float dx = fmaxf(fmaxf(b0.x - v.x, v.x - b1.x), 0.f);
@@ -76,14 +76,15 @@ __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float
     return sum;
 }
 
-// BT threads per block (autotuned: 64, 128 or 256), 64 registers per thread at most.
+// BT threads per block (autotuned: 64, 128 or 256), 48 registers per thread at most
+// (40 resident warps per SM).
 // cell_rad holds sp_size per-cell support radii followed by one radius per row
 // (z, y): the largest maxvalue * h of the row's particles (0 where none is
 // anisotropic).  The z and y ranges are cut from the largest support of the
 // frame, each row's x range from the row's own radius, and each non-empty cell
 // by its record: the bounding box of its particles and its largest support.
 template <int BT>
-__global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
+__global__ void __launch_bounds__(BT, 1280 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
                                                     const uint32_t* __restrict__ n_dev,
                                                     const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
                                                     const float* __restrict__ cell_rad, const float4* __restrict__ rec,
@@ -124,21 +125,27 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_field(KGrid g, FieldParams fp
                 const uint32_t row = rowi * srx;
                 if (sum > fp.thr) {
                     // threshold crossed: the reference adds this row's first cell, then breaks
-                    if (lo.x < hi.x) {
-                        const uint32_t j0 = __ldg(&cell_start[row + lo.x]), j1 = __ldg(&cell_start[row + lo.x + 1]);
-                        if (j0 != j1 && cell_reaches(rec, row + lo.x, v)) sum = range_sum(j0, j1, v, spos, aniso, sum);
-                    }
+                    if (lo.x < hi.x && cell_reaches(rec, row + lo.x, v))
+                        sum = range_sum(__ldg(&cell_start[row + lo.x]), __ldg(&cell_start[row + lo.x + 1]), v, spos,
+                                        aniso, sum);
                     continue;
                 }
-                // cells of the row the row's largest support can reach
+                // cells of the row the row's largest support can reach, 32 at a time:
+                // first the cells whose record the vertex reaches (independent loads),
+                // then their particles in x order until the threshold is crossed
                 int xa, xb;
                 cell_range(ux, sqrtf(rr2 - gyz) * inv_cs + kRangeMargin, lo.x, hi.x, xa, xb);
-                uint32_t jn = xa < xb ? __ldg(&cell_start[row + (uint32_t)xa]) : 0u;
-                for (int x = xa; x < xb; ++x) {
-                    const uint32_t j0 = jn;
-                    jn = __ldg(&cell_start[row + (uint32_t)x + 1u]);
-                    if (j0 == jn || !cell_reaches(rec, row + (uint32_t)x, v)) continue;
-                    sum = range_sum(j0, jn, v, spos, aniso, sum);
+                for (int x0 = xa; x0 < xb; x0 += 32) {
+                    const int nx = min(xb - x0, 32);
+                    uint32_t reach = 0u;
+                    for (int k = 0; k < nx; ++k)
+                        reach |= (cell_reaches(rec, row + (uint32_t)(x0 + k), v) ? 1u : 0u) << k;
+                    while (reach) {
+                        const uint32_t cell = row + (uint32_t)(x0 + __ffs(reach) - 1);
+                        reach &= reach - 1u;
+                        sum = range_sum(__ldg(&cell_start[cell]), __ldg(&cell_start[cell + 1u]), v, spos, aniso, sum);
+                        if (sum > fp.thr) break;
+                    }
                     if (sum > fp.thr) break;
                 }
             }
@@ -156,7 +163,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     fp.grow = kSupportGrow;
     Counters* cnt = ctx->counters.as<Counters>();
     const int bt = ctx->tune.field_threads;
-    const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1024u / (unsigned)bt));
+    const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1280u / (unsigned)bt));
     auto go = [&](auto kern) {
         kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
                                              ctx->cell_rad.as<float>(), ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(),
