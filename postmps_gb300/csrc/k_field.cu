@@ -83,13 +83,15 @@ __device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float
 // anisotropic).  The z and y ranges are cut from the largest support of the
 // frame, each row's x range from the row's own radius, and each non-empty cell
 // by its record: the bounding box of its particles and its largest support.
+// The value goes to field[t] (band order; skipped when field is null) and to
+// fdense[id] (the whole scalar grid).
 template <int BT>
 __global__ void __launch_bounds__(BT, 1280 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
                                                     const uint32_t* __restrict__ n_dev,
                                                     const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
                                                     const float* __restrict__ cell_rad, const float4* __restrict__ rec,
                                                     const float4* __restrict__ spos, const float4* __restrict__ aniso,
-                                                    float* __restrict__ field) {
+                                                    float* __restrict__ field, float* __restrict__ fdense) {
     const uint32_t nv = *n_dev;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], sry = g.spres[1];
@@ -150,7 +152,8 @@ __global__ void __launch_bounds__(BT, 1280 / BT) k_field(KGrid g, FieldParams fp
                 }
             }
         }
-        field[t] = sum;
+        if (field) field[t] = sum;
+        fdense[id] = sum;
     }
 }
 
@@ -167,7 +170,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     auto go = [&](auto kern) {
         kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
                                              ctx->cell_rad.as<float>(), ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(),
-                                             ctx->aniso.as<float4>(), out);
+                                             ctx->aniso.as<float4>(), out, ctx->fdense.as<float>());
     };
     if (bt == 64) go(k_field<64>);
     else if (bt == 256) go(k_field<256>);
@@ -176,9 +179,25 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     return PMS_OK;
 }
 
+// the frame's first field evaluation: the dense field starts at 0 everywhere
 pms_status launch_field(pms_ctx* ctx) {
     Counters* cnt = ctx->counters.as<Counters>();
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->fdense.p, 0, 4 * (size_t)ctx->grid.sc_size, ctx->stream));
     return launch_field_on(ctx, ctx->vlist.as<uint32_t>(), &cnt->nv, ctx->nv, ctx->field.as<float>());
+}
+
+// field[t] = fdense[vlist[t]]: the band-order field of a vertex list whose values are all computed
+__global__ void __launch_bounds__(256) k_field_gather(const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ n_dev,
+                                                      const float* __restrict__ fdense, float* __restrict__ field) {
+    const uint32_t n = *n_dev;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        field[t] = __ldg(&fdense[__ldg(&vlist[t])]);
+}
+
+pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out) {
+    k_field_gather<<<grid_for(n_host, 256), 256, 0, ctx->stream>>>(vlist, n_dev, ctx->fdense.as<float>(), out);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
 }
 
 }  // namespace pms

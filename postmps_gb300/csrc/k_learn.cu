@@ -330,21 +330,6 @@ __global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a,
     }
 }
 
-// Field of the merged vertex set: values of old vertices by rank in the old
-// set, of new ones by rank in the new set.
-__global__ void __launch_bounds__(256) k_field_merge(const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ bm_old, const uint32_t* __restrict__ wp_old,
-                                                     const float* __restrict__ f_old, const uint32_t* __restrict__ bm_new,
-                                                     const uint32_t* __restrict__ wp_new, const float* __restrict__ f_new,
-                                                     float* __restrict__ f_out) {
-    const uint32_t n = *n_dev;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint32_t id = vlist[t];
-        const bool is_new = (bm_new[id >> 5] >> (id & 31u)) & 1u;
-        f_out[t] = is_new ? f_new[bit_rank(bm_new, wp_new, id)] : f_old[bit_rank(bm_old, wp_old, id)];
-    }
-}
-
 // Border check: a valid cube whose face has corners on both sides of the
 // iso-surface shares that crossing with the cube across the face, so the
 // neighbour is a valid cube too; if not all of the neighbour's corners have a
@@ -391,9 +376,8 @@ __global__ void __launch_bounds__(256) k_border(KGrid g, const uint32_t* __restr
 // detectValidSurfaceCubes) and the crossed faces are checked as in k_border.
 __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes,
                                                      uint32_t n_host, const uint32_t* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ vbm, const uint32_t* __restrict__ wp,
-                                                     const float* __restrict__ field, uint32_t* __restrict__ qadd,
-                                                     uint32_t* __restrict__ n_added) {
+                                                     const uint32_t* __restrict__ vbm, const float* __restrict__ fdense,
+                                                     uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added) {
     const uint32_t n = n_dev ? *n_dev : n_host;
     const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
     const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
@@ -408,7 +392,7 @@ __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const u
         for (int k = 0; k < 8; ++k) {
             const uint32_t c = id + cx[k] + cy[k] * rx + cz[k] * rxy;
             if (!((vbm[c >> 5] >> (c & 31u)) & 1u)) { all = false; break; }
-            cs |= (field[bit_rank(vbm, wp, c)] <= iso ? 1u : 0u) << k;
+            cs |= (__ldg(&fdense[c]) <= iso ? 1u : 0u) << k;
         }
         if (!all || cs == 0u || cs == 255u) continue;
         const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
@@ -750,15 +734,6 @@ pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, ui
 
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 
-pms_status launch_field_merge(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host,
-                              const uint32_t* bm_old, const uint32_t* wp_old, const float* f_old, const uint32_t* bm_new,
-                              const uint32_t* wp_new, const float* f_new, float* f_out) {
-    k_field_merge<<<grid_for(n_host, 256), 256, 0, ctx->stream>>>(vlist, n_dev, bm_old, wp_old, f_old, bm_new, wp_new,
-                                                                  f_new, f_out);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
 pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
@@ -774,8 +749,7 @@ pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, u
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, n_dev, ctx->bm.as<uint32_t>(),
-                                                              ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(), qadd,
-                                                              &cnt->l_added);
+                                                              ctx->fdense.as<float>(), qadd, &cnt->l_added);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

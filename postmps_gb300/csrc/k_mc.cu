@@ -11,9 +11,15 @@
 // differences of the field, zero outside the grid and outside the band,
 // myCuda.cuh:259-289) and writes the triangle soup in table order.
 //
-// GB300 design: the field lives compactly in band order; a vertex's value is
-// found through the band bitmap (rank = word prefix + popcount).  One scan
-// over packed 64-bit keys (valid << 32 | nvert) yields both offsets.  Tables
+// GB300 design: the field is read from the dense scalar-grid copy the field
+// kernel writes (0 off the band, so a normal's out-of-band neighbour reads 0
+// as in the reference); band membership comes from the band bitmap.  One scan
+// over packed 64-bit keys (valid << 32 | nvert) yields both offsets; the
+// compaction writes one 16-byte record per valid cube {vertex id, case, first
+// mesh vertex}, so the emission reads its inputs coalesced.  Each warp emits
+// 32 consecutive valid cubes: their mesh vertices are contiguous, so the warp
+// stages them in shared memory and writes whole lines (scattered 4-byte stores
+// from each cube would leave partial sectors for the memory to merge).  Tables
 // sit in constant memory.
 #include "pms_internal.h"
 #include "k_common.cuh"
@@ -49,18 +55,11 @@ pms_status upload_mc_tables(pms_ctx* ctx) {
     return PMS_OK;
 }
 
-__device__ __forceinline__ bool band_value(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
-                                           const float* __restrict__ field, uint64_t nbits, uint64_t id, float& f) {
-    if (!bit_get(bm, nbits, id)) return false;
-    f = __ldg(&field[bit_rank(bm, wprefix, (uint32_t)id)]);
-    return true;
-}
-
 // detectValidSurfaceCubes (6-argument version)
 __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, const Counters* __restrict__ cnt,
                                                           const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ bm,
-                                                          const uint32_t* __restrict__ wprefix, const float* __restrict__ field,
-                                                          uint32_t* __restrict__ mc_case, unsigned long long* __restrict__ mc_key) {
+                                                          const float* __restrict__ fdense, uint32_t* __restrict__ mc_case,
+                                                          unsigned long long* __restrict__ mc_key) {
     const uint32_t nv = cnt->nv;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint64_t nbits = g.sc_size;
@@ -69,18 +68,16 @@ __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, co
         const uint32_t z = id / rxy, rem = id - z * rxy, y = rem / rx, x = rem - y * rx;
         uint32_t cs = 0, nvert = 0;
         bool all = true;
-        float f[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             // uint32 corner index as getCornerIndex1Ds computes it
             const uint32_t cid = (z + c_corner[k][2]) * rxy + (y + c_corner[k][1]) * rx + (x + c_corner[k][0]);
-            if (!band_value(bm, wprefix, field, nbits, cid, f[k])) { all = false; }
+            const bool in = bit_get(bm, nbits, cid);
+            all = all && in;
+            if (in) cs |= (__ldg(&fdense[cid]) <= iso ? 1u : 0u) << k;
         }
-        if (all) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) cs |= (f[k] <= iso ? 1u : 0u) << k;
-            nvert = c_num_vertices[cs];
-        }
+        if (all) nvert = c_num_vertices[cs];
+        else cs = 0;
         mc_case[t] = cs;
         mc_key[t] = nvert ? ((1ull << 32) | nvert) : 0ull;
     }
@@ -93,24 +90,27 @@ __global__ void k_mc_totals(const unsigned long long* __restrict__ total, Counte
     cnt->nmesh = t & 0xffffffffull;
 }
 
+// compactValidSurfaceCubes, plus the emission's per-cube record
 __global__ void __launch_bounds__(256) k_mc_compact(const Counters* __restrict__ cnt,
                                                     const unsigned long long* __restrict__ mc_key,
                                                     const unsigned long long* __restrict__ mc_off,
-                                                    uint32_t* __restrict__ valid) {
+                                                    const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ mc_case,
+                                                    uint32_t* __restrict__ valid, uint4* __restrict__ cube) {
     const uint32_t nv = cnt->nv;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x)
-        if (mc_key[t]) valid[(uint32_t)(mc_off[t] >> 32)] = t;
+        if (mc_key[t]) {
+            const unsigned long long off = mc_off[t];
+            const uint32_t k = (uint32_t)(off >> 32);
+            valid[k] = t;
+            cube[k] = make_uint4(vlist[t], mc_case[t], (uint32_t)(off & 0xffffffffull), 0u);
+        }
 }
 
-__device__ __forceinline__ float grid_value(const KGrid& g, const uint32_t* __restrict__ bm,
-                                            const uint32_t* __restrict__ wprefix, const float* __restrict__ field,
-                                            int x, int y, int z) {
+// field at scalar-grid vertex (x, y, z): 0 outside the grid and off the band
+__device__ __forceinline__ float grid_value(const KGrid& g, const float* __restrict__ fdense, int x, int y, int z) {
     if (x < 0 || y < 0 || z < 0 || (uint32_t)x >= g.scres[0] || (uint32_t)y >= g.scres[1] || (uint32_t)z >= g.scres[2])
         return 0.f;
-    const uint64_t id = (uint64_t)z * g.scres[0] * g.scres[1] + (uint64_t)y * g.scres[0] + (uint64_t)x;
-    float f = 0.f;
-    band_value(bm, wprefix, field, g.sc_size, id, f);
-    return f;
+    return __ldg(&fdense[((size_t)z * g.scres[1] + (size_t)y) * g.scres[0] + (size_t)x]);
 }
 
 __device__ __forceinline__ float3 normalized(float3 v) {
@@ -118,73 +118,96 @@ __device__ __forceinline__ float3 normalized(float3 v) {
     return make_float3(v.x * inv, v.y * inv, v.z * inv);
 }
 
-// generateTriangles: one thread per valid cube
+// generateTriangles: one thread per valid cube, a warp per 32 consecutive cubes
+static constexpr int kEmitWarps = kThreads / 32;
+static constexpr int kEmitStage = 32 * 15 * 3;     // floats: 32 cubes x 15 mesh vertices x 3
+
 __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counters* __restrict__ cnt,
-                                                      const uint32_t* __restrict__ valid, const uint32_t* __restrict__ vlist,
-                                                      const uint32_t* __restrict__ mc_case,
-                                                      const unsigned long long* __restrict__ mc_off,
-                                                      const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
-                                                      const float* __restrict__ field, float* __restrict__ vert,
-                                                      float* __restrict__ vnorm,
+                                                      const uint4* __restrict__ cube, const float* __restrict__ fdense,
+                                                      float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
                                                       unsigned long long cap) {
+    __shared__ float stage[kEmitWarps][kEmitStage];
     const uint32_t nvalid = cnt->nvalid;
     // batched frames write behind the earlier frames' vertices, within cap
     const unsigned long long fb = frame_base ? *frame_base : 0ull;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const float sgn = (iso < 0.f) ? -1.f : 1.f;
-    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nvalid; k += gridDim.x * blockDim.x) {
-        const uint32_t t = valid[k];
-        const uint32_t id = vlist[t];
-        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-        const uint32_t cs = mc_case[t];
-        const uint32_t base = (uint32_t)(mc_off[t] & 0xffffffffull);
-        float3 cp[8], cn[8];
-        float cf[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int X = x + c_corner[c][0], Y = y + c_corner[c][1], Z = z + c_corner[c][2];
-            cp[c] = make_float3(sc_coord_i(g, X, 0), sc_coord_i(g, Y, 1), sc_coord_i(g, Z, 2));
-            cf[c] = grid_value(g, bm, wprefix, field, X, Y, Z);
-        }
-        // central differences (getVertexNorm): along each axis one neighbour of a corner
-        // is the cube's other corner on that axis, the other lies outside the cube
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const int ox = c_corner[c][0], oy = c_corner[c][1], oz = c_corner[c][2];
-            const int X = x + ox, Y = y + oy, Z = z + oz;
-            const float fx = grid_value(g, bm, wprefix, field, ox ? X + 1 : X - 1, Y, Z);
-            const float fy = grid_value(g, bm, wprefix, field, X, oy ? Y + 1 : Y - 1, Z);
-            const float fz = grid_value(g, bm, wprefix, field, X, Y, oz ? Z + 1 : Z - 1);
-            const float px = cf[c_partner[c][0]], py = cf[c_partner[c][1]], pz = cf[c_partner[c][2]];
-            float3 n;
-            n.x = ox ? px - fx : fx - px;
-            n.y = oy ? py - fy : fy - py;
-            n.z = oz ? pz - fz : fz - pz;
-            cn[c] = normalized(n);
-        }
-        const uint32_t ef = c_edge_flags[cs];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* st = stage[warp];
+    for (uint32_t k0 = (blockIdx.x * kEmitWarps + warp) * 32u; k0 < nvalid; k0 += gridDim.x * kEmitWarps * 32u) {
+        const uint32_t k = k0 + (uint32_t)lane;
+        const bool active = k < nvalid;
+        const uint4 cr = active ? __ldg(&cube[k]) : make_uint4(0u, 0u, 0u, 0u);
+        const uint32_t id = cr.x, cs = cr.y, base = cr.z;
+        const uint32_t nvert = active ? (uint32_t)c_num_vertices[cs] : 0u;
+        // the warp's mesh vertices are [base0, base0 + total)
+        const int last = (int)min(31u, nvalid - 1u - k0);
+        const uint32_t base0 = __shfl_sync(0xffffffffu, base, 0);
+        const uint32_t total = __shfl_sync(0xffffffffu, base + nvert, last) - base0;
+        const unsigned long long w0 = fb + base0;
+        const uint32_t room = w0 >= cap ? 0u : (cap - w0 < (unsigned long long)total ? (uint32_t)(cap - w0) : total);
+        if (room < total && lane == 0) atomicOr(&cnt->err, kErrCapacity);
         float3 ip[12], in[12];
+        if (nvert) {
+            const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
+            float3 cp[8], cn[8];
+            float cf[8];
 #pragma unroll
-        for (int e = 0; e < 12; ++e) {
-            if (!(ef & (1u << e))) continue;
-            const int a = c_edge_vertex[e][0], b = c_edge_vertex[e][1];
-            const float d = cf[b] - cf[a];
-            // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5
-            const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
-            ip[e] = make_float3(cp[a].x + tt * (cp[b].x - cp[a].x), cp[a].y + tt * (cp[b].y - cp[a].y),
-                                cp[a].z + tt * (cp[b].z - cp[a].z));
-            const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x), cn[a].y + tt * (cn[b].y - cn[a].y),
-                                                     cn[a].z + tt * (cn[b].z - cn[a].z)));
-            in[e] = make_float3(sgn * nn.x, sgn * nn.y, sgn * nn.z);
+            for (int c = 0; c < 8; ++c) {
+                const int X = x + c_corner[c][0], Y = y + c_corner[c][1], Z = z + c_corner[c][2];
+                cp[c] = make_float3(sc_coord_i(g, X, 0), sc_coord_i(g, Y, 1), sc_coord_i(g, Z, 2));
+                cf[c] = __ldg(&fdense[(size_t)Z * rxy + (size_t)Y * rx + (size_t)X]);   // a band vertex
+            }
+            // central differences (getVertexNorm): along each axis one neighbour of a corner
+            // is the cube's other corner on that axis, the other lies outside the cube
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const int ox = c_corner[c][0], oy = c_corner[c][1], oz = c_corner[c][2];
+                const int X = x + ox, Y = y + oy, Z = z + oz;
+                const float fx = grid_value(g, fdense, ox ? X + 1 : X - 1, Y, Z);
+                const float fy = grid_value(g, fdense, X, oy ? Y + 1 : Y - 1, Z);
+                const float fz = grid_value(g, fdense, X, Y, oz ? Z + 1 : Z - 1);
+                const float px = cf[c_partner[c][0]], py = cf[c_partner[c][1]], pz = cf[c_partner[c][2]];
+                float3 n;
+                n.x = ox ? px - fx : fx - px;
+                n.y = oy ? py - fy : fy - py;
+                n.z = oz ? pz - fz : fz - pz;
+                cn[c] = normalized(n);
+            }
+            const uint32_t ef = c_edge_flags[cs];
+#pragma unroll
+            for (int e = 0; e < 12; ++e) {
+                if (!(ef & (1u << e))) continue;
+                const int a = c_edge_vertex[e][0], b = c_edge_vertex[e][1];
+                const float d = cf[b] - cf[a];
+                // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5
+                const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
+                ip[e] = make_float3(cp[a].x + tt * (cp[b].x - cp[a].x), cp[a].y + tt * (cp[b].y - cp[a].y),
+                                    cp[a].z + tt * (cp[b].z - cp[a].z));
+                const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x),
+                                                         cn[a].y + tt * (cn[b].y - cn[a].y),
+                                                         cn[a].z + tt * (cn[b].z - cn[a].z)));
+                in[e] = make_float3(sgn * nn.x, sgn * nn.y, sgn * nn.z);
+            }
         }
-        const uint32_t nvert = c_num_vertices[cs];
-        if (fb + base + nvert > cap) { atomicOr(&cnt->err, kErrCapacity); continue; }
+        // positions, then normals: stage the warp's vertices in order, write whole lines
+        const uint32_t o = base - base0;
         for (uint32_t v = 0; v < nvert; ++v) {
-            const int e = c_tri[cs][v];
-            const size_t o = 3 * ((size_t)fb + base + v);
-            vert[o] = ip[e].x; vert[o + 1] = ip[e].y; vert[o + 2] = ip[e].z;
-            if (vnorm) { vnorm[o] = in[e].x; vnorm[o + 1] = in[e].y; vnorm[o + 2] = in[e].z; }
+            const float3 p = ip[c_tri[cs][v]];
+            st[3 * (o + v)] = p.x; st[3 * (o + v) + 1] = p.y; st[3 * (o + v) + 2] = p.z;
+        }
+        __syncwarp();
+        for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) vert[3 * (size_t)w0 + i] = st[i];
+        __syncwarp();
+        if (vnorm) {
+            for (uint32_t v = 0; v < nvert; ++v) {
+                const float3 q = in[c_tri[cs][v]];
+                st[3 * (o + v)] = q.x; st[3 * (o + v) + 1] = q.y; st[3 * (o + v) + 2] = q.z;
+            }
+            __syncwarp();
+            for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) vnorm[3 * (size_t)w0 + i] = st[i];
+            __syncwarp();
         }
     }
 }
@@ -193,8 +216,8 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_classify<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(),
-        ctx->field.as<float>(), ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
+        g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(),
+        ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
     PMS_LAUNCHED(ctx);
     // ctx->nv may be a bound (batched frames): the scan stops at the device count
     pms_status st = scan_u64(ctx, ctx->mc_key.as<unsigned long long>(), ctx->mc_off.as<unsigned long long>(), ctx->nv,
@@ -202,8 +225,9 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
     if (st != PMS_OK) return st;
     k_mc_totals<<<1, 1, 0, ctx->stream>>>(ctx->tmp.as<unsigned long long>(), cnt);
     PMS_LAUNCHED(ctx);
-    k_mc_compact<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(cnt, ctx->mc_key.as<unsigned long long>(),
-                                                                  ctx->mc_off.as<unsigned long long>(), ctx->valid.as<uint32_t>());
+    k_mc_compact<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(
+        cnt, ctx->mc_key.as<unsigned long long>(), ctx->mc_off.as<unsigned long long>(), ctx->vlist.as<uint32_t>(),
+        ctx->mc_case.as<uint32_t>(), ctx->valid.as<uint32_t>(), ctx->cube.as<uint4>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
@@ -281,9 +305,7 @@ pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsi
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->valid.as<uint32_t>(), ctx->vlist.as<uint32_t>(), ctx->mc_case.as<uint32_t>(),
-        ctx->mc_off.as<unsigned long long>(), ctx->bm.as<uint32_t>(), ctx->wprefix.as<uint32_t>(), ctx->field.as<float>(),
-        vert, vnorm, frame_base, cap);
+        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

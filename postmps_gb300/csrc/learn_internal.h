@@ -40,9 +40,6 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
 pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
                                uint32_t* wcount);
 pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount);
-pms_status launch_field_merge(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host,
-                              const uint32_t* bm_old, const uint32_t* wp_old, const float* f_old, const uint32_t* bm_new,
-                              const uint32_t* wp_new, const float* f_new, float* f_out);
 pms_status launch_border(pms_ctx* ctx, uint32_t* qadd);
 pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
 // n: the list length, or a bound when n_dev holds it on the device

@@ -52,7 +52,7 @@ static void release_all(pms_ctx* c) {
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
                     &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->cell_rec, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
                     &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
-                    &c->mc_key, &c->mc_off, &c->valid, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
+                    &c->mc_key, &c->mc_off, &c->valid, &c->fdense, &c->cube, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
                     &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp};
@@ -164,6 +164,7 @@ pms_status pms::ensure_grid_buffers(pms_ctx* c, const pms_grid& g) {
     PMS_CUDA(c, c->surf_start.ensure(4 * S));
     PMS_CUDA(c, c->cell_rad.ensure(4 * (S + (size_t)g.spres[1] * g.spres[2])));   // per cell, then per row
     PMS_CUDA(c, c->cell_rec.ensure(32 * S));   // two float4 per cell
+    PMS_CUDA(c, c->fdense.ensure(4 * ((size_t)g.sc_size + 1)));
     const size_t W = ((uint64_t)g.sc_size + 31) / 32 + 1;
     PMS_CUDA(c, c->bm0.ensure(4 * W));
     PMS_CUDA(c, c->bm.ensure(4 * W));
@@ -185,6 +186,7 @@ pms_status pms::ensure_band_buffers(pms_ctx* c, uint32_t nv) {
     PMS_CUDA(c, c->mc_key.ensure(8 * V));
     PMS_CUDA(c, c->mc_off.ensure(8 * V));
     PMS_CUDA(c, c->valid.ensure(4 * V));
+    PMS_CUDA(c, c->cube.ensure(16 * V));
     return PMS_OK;
 }
 

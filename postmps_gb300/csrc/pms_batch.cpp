@@ -120,7 +120,7 @@ static pms_status full_check(pms_ctx* c, uint64_t W) {
     return launch_border(c, c->l_qadd.as<uint32_t>());
 }
 
-// one round: field at the queued cubes' new corners, merge, check the queued cubes
+// one round: field at the queued cubes' new corners, merged vertex set, check the queued cubes
 static pms_status border_round(pms_ctx* c, uint64_t W) {
     Counters* cnt = c->counters.as<Counters>();
     const uint32_t S = c->grid.sc_size;
@@ -134,17 +134,14 @@ static pms_status border_round(pms_ctx* c, uint64_t W) {
     if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
     if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
         return st;
-    if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, S, c->l_field_new.as<float>()))) return st;
+    if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, S, nullptr))) return st;
     if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
                              c->wcount.as<uint32_t>())))
         return st;
     if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
     if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
         return st;
-    if ((st = launch_field_merge(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, S, c->bm.as<uint32_t>(),
-                                 c->wprefix.as<uint32_t>(), c->field.as<float>(), c->l_bm_new.as<uint32_t>(),
-                                 c->l_wp_new.as<uint32_t>(), c->l_field_new.as<float>(), c->l_field_m.as<float>())))
-        return st;
+    if ((st = launch_field_gather(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, S, c->l_field_m.as<float>()))) return st;
     std::swap(c->bm, c->l_bm_m);
     std::swap(c->wprefix, c->l_wp_m);
     std::swap(c->vlist, c->l_vlist_m);
@@ -274,7 +271,7 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
     const size_t S = (size_t)gmax.sc_size + 1;
     for (DBuf* d : {&lc->l_q, &lc->l_qadd, &lc->l_bm_new, &lc->l_wc_new, &lc->l_wp_new, &lc->l_bm_m, &lc->l_wp_m, &lc->l_wp_q})
         PMS_CUDA(lc, d->ensure(4 * (W + 1)));
-    for (DBuf* d : {&lc->l_vlist_new, &lc->l_field_new, &lc->l_vlist_m, &lc->l_field_m, &lc->l_qlist})
+    for (DBuf* d : {&lc->l_vlist_new, &lc->l_vlist_m, &lc->l_field_m, &lc->l_qlist})
         PMS_CUDA(lc, d->ensure(4 * S));
     // the buffers that trade places with these in the rounds must be as large
     PMS_CUDA(lc, lc->bm.ensure(4 * (W + 1)));

@@ -134,6 +134,9 @@ struct pms_ctx {
     pms::DBuf bm0, bm, wcount, wprefix, vlist;
     // field and marching cubes
     pms::DBuf field, mc_case, mc_key, mc_off, valid, vert, vnorm, sval;
+    // the field over the whole scalar grid, 0 off the band (the marching cubes' lookups);
+    // per valid cube {vertex id, case, first mesh vertex, 0}
+    pms::DBuf fdense, cube;
     bool have_values = false;
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
@@ -210,6 +213,7 @@ pms_status launch_band_list(pms_ctx* ctx);
 pms_status launch_field(pms_ctx* ctx);
 // field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid)
 pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
+pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 pms_status launch_mc_classify(pms_ctx* ctx);

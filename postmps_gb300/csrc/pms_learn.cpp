@@ -153,11 +153,9 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
         if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
         const uint64_t nnew_bound = std::min<uint64_t>(8ull * added, (uint64_t)c->grid.sc_size);
         PMS_CUDA(c, c->l_vlist_new.ensure(4 * (nnew_bound + 1)));
-        PMS_CUDA(c, c->l_field_new.ensure(4 * (nnew_bound + 1)));
         if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
             return st;
-        if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, (uint32_t)nnew_bound,
-                                  c->l_field_new.as<float>())))
+        if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, (uint32_t)nnew_bound, nullptr)))
             return st;
         // merged vertex set: bitmap, ranks, list, field
         if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
@@ -169,9 +167,7 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
         PMS_CUDA(c, c->l_field_m.ensure(4 * (nv_bound + 1)));
         if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
             return st;
-        if ((st = launch_field_merge(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, (uint32_t)nv_bound, c->bm.as<uint32_t>(),
-                                     c->wprefix.as<uint32_t>(), c->field.as<float>(), c->l_bm_new.as<uint32_t>(),
-                                     c->l_wp_new.as<uint32_t>(), c->l_field_new.as<float>(), c->l_field_m.as<float>())))
+        if ((st = launch_field_gather(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, (uint32_t)nv_bound, c->l_field_m.as<float>())))
             return st;
         std::swap(c->bm, c->l_bm_m);
         std::swap(c->wprefix, c->l_wp_m);
