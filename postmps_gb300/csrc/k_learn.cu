@@ -113,52 +113,63 @@ __global__ void __launch_bounds__(256) k_coarse_count(KGrid g, LearnDims ld, con
 }
 
 // ---------------------------------------------------------------------------
-// prediction over tiles of 4 x 4 x 4 coarse cells (8 x 8 x 8 fine cubes)
+// Densities as bf16 feature pairs over the coarse grid padded by one plane on
+// the low side of every axis (patch vertex -1 lies there and reads 0):
+// padded vertex p = ((cz + 1) * P1 + cy + 1) * P0 + cx + 1 with P = cres + 1,
+// and dens2[p] = bf16(d(p)) | bf16(d(p + 1)) << 16, d = min(density, 64).
+// ---------------------------------------------------------------------------
+struct PadDims {
+    uint32_t p0, p1, p2;
+    size_t np;                // p0 * p1 * p2
+};
+__host__ __device__ inline PadDims pad_dims(const LearnDims& ld) {
+    PadDims d;
+    d.p0 = ld.cres[0] + 1; d.p1 = ld.cres[1] + 1; d.p2 = ld.cres[2] + 1;
+    d.np = (size_t)d.p0 * d.p1 * d.p2;
+    return d;
+}
+
+__device__ __forceinline__ uint32_t padded_feature(const uint32_t* __restrict__ counts, const LearnDims& ld,
+                                                   const PadDims& pd, size_t p) {
+    if (p >= pd.np) return 0u;
+    const uint32_t px = (uint32_t)(p % pd.p0), py = (uint32_t)((p / pd.p0) % pd.p1), pz = (uint32_t)(p / ((size_t)pd.p0 * pd.p1));
+    if (px == 0 || py == 0 || pz == 0) return 0u;
+    const size_t c = ((size_t)(pz - 1) * ld.cres[1] + (py - 1)) * ld.cres[0] + (px - 1);
+    return __bfloat16_as_ushort(__float2bfloat16_rn(density_of(counts[c], ld.inv_expected)));
+}
+
+__global__ void __launch_bounds__(256) k_coarse_dens(const uint32_t* __restrict__ counts, LearnDims ld,
+                                                     uint32_t* __restrict__ dens2) {
+    const PadDims pd = pad_dims(ld);
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < pd.np; p += (size_t)gridDim.x * blockDim.x)
+        dens2[p] = padded_feature(counts, ld, pd, p) | (padded_feature(counts, ld, pd, p + 1) << 16);
+}
+
+// ---------------------------------------------------------------------------
+// candidates over tiles of 4 x 4 x 4 coarse cells (8 x 8 x 8 fine cubes):
+// each tile lists its candidate cubes and appends them to one list
 // ---------------------------------------------------------------------------
 static constexpr int kTile = 4;                 // coarse cells per tile axis
 static constexpr int kHalo = 1;                 // patch vertices k - 1 .. k + 2 of the tile's cells k
 static constexpr int kSm = 8;                   // tile + halo = 7 coarse vertices per axis, padded
-static constexpr int kPredThreads = 128;
+static constexpr int kCandThreads = 128;
 
-struct PredictOut {
-    uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
-    uint32_t* cand;           // candidate cube ids; may be null
-    float* logit;             // their logits; may be null
-    uint32_t cand_cap;
-    uint32_t* n_cand;         // device counters
-    uint32_t* n_pred;
-};
-
-// W1 as B fragments: b[kk][nt][0..1] for k-step kk (features 16kk..16kk+15) and
-// n-tile nt (hidden 8nt..8nt+7)
-__device__ __forceinline__ void load_w1_frags(const DevModel* __restrict__ m, uint32_t (&b)[4][8][2], int lane) {
-    const uint16_t* w1 = m->w1;
-    const int kq = (lane & 3) * 2, n = lane >> 2;
-#pragma unroll
-    for (int kk = 0; kk < 4; ++kk)
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const int j = nt * 8 + n, i0 = kk * 16 + kq;
-            b[kk][nt][0] = pack_raw(w1[(i0 + 0) * kHid + j], w1[(i0 + 1) * kHid + j]);
-            b[kk][nt][1] = pack_raw(w1[(i0 + 8) * kHid + j], w1[(i0 + 9) * kHid + j]);
-        }
-}
-
-__global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDims ld, const uint32_t* __restrict__ counts,
-                                                                const DevModel* __restrict__ model, int use_model,
-                                                                PredictOut out) {
+// clist[i] = {cube id, padded coarse vertex of the cube's coarse cell | parity
+// x << 29 | parity y << 30 | parity z << 31}
+__global__ void __launch_bounds__(kCandThreads) k_learn_cand(KGrid g, LearnDims ld, const uint32_t* __restrict__ counts,
+                                                             uint2* __restrict__ clist, uint32_t* __restrict__ n_cand) {
     __shared__ float s_cnt[kSm][kSm][kSm];        // densities of the coarse vertices the tile's cubes read
     __shared__ uint8_t s_mixed[kTile * kTile * kTile];
     __shared__ uint16_t s_list[512];
-    __shared__ uint32_t s_n;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ uint32_t s_n, s_base;
+    const int tid = threadIdx.x;
     const uint32_t tx = ld.tiles[0], ty = ld.tiles[1];
     const uint32_t tile = blockIdx.x;
     const int T0[3] = {(int)(tile % tx) * kTile, (int)((tile / tx) % ty) * kTile, (int)(tile / (tx * ty)) * kTile};
     if (T0[2] >= (int)ld.cres[2]) return;
-    // load the coarse counts of the tile plus halo (outside the grid: empty)
+    // the coarse densities of the tile plus halo (outside the grid: empty)
     int any = 0, all = 1;
-    for (int e = tid; e < kSm * kSm * kSm; e += kPredThreads) {
+    for (int e = tid; e < kSm * kSm * kSm; e += kCandThreads) {
         const int lx = e % kSm, ly = (e / kSm) % kSm, lz = e / (kSm * kSm);
         const int cx = T0[0] - kHalo + lx, cy = T0[1] - kHalo + ly, cz = T0[2] - kHalo + lz;
         uint32_t c = 0;
@@ -191,7 +202,8 @@ __global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDi
     }
     __syncthreads();
     // candidate cubes of the tile (local index q = (lz * 8 + ly) * 8 + lx)
-    for (int q = tid; q < 512; q += kPredThreads) {
+    const uint32_t rxy = g.scres[0] * g.scres[1];
+    for (int q = tid; q < 512; q += kCandThreads) {
         const int lx = q & 7, ly = (q >> 3) & 7, lz = q >> 6;
         const int fx = 2 * T0[0] + lx, fy = 2 * T0[1] + ly, fz = 2 * T0[2] + lz;
         const bool in = fx < (int)g.scres[0] - 1 && fy < (int)g.scres[1] - 1 && fz < (int)g.scres[2] - 1;
@@ -200,20 +212,93 @@ __global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDi
     __syncthreads();
     const uint32_t ncand = s_n;
     if (ncand == 0) return;
-    if (tid == 0) atomicAdd(out.n_cand, ncand);
-    const uint32_t rxy = g.scres[0] * g.scres[1];
-    auto cube_id = [&](int q) -> uint32_t {
+    if (tid == 0) s_base = atomicAdd(n_cand, ncand);
+    __syncthreads();
+    const PadDims pd = pad_dims(ld);
+    for (uint32_t e = tid; e < ncand; e += kCandThreads) {
+        const int q = s_list[e];
         const int lx = q & 7, ly = (q >> 3) & 7, lz = q >> 6;
-        return (uint32_t)(2 * T0[2] + lz) * rxy + (uint32_t)(2 * T0[1] + ly) * g.scres[0] + (uint32_t)(2 * T0[0] + lx);
-    };
+        const uint32_t fx = 2 * T0[0] + lx, fy = 2 * T0[1] + ly, fz = 2 * T0[2] + lz;
+        const uint32_t pv = (((fz >> 1) + 1) * pd.p1 + (fy >> 1) + 1) * pd.p0 + (fx >> 1) + 1;
+        clist[s_base + e] = make_uint2(fz * rxy + fy * g.scres[0] + fx,
+                                       pv | ((fx & 1u) << 29) | ((fy & 1u) << 30) | ((fz & 1u) << 31));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the network over the candidate list: a persistent kernel, 16 candidates per
+// warp per step
+// ---------------------------------------------------------------------------
+static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 3;
+
+struct PredictOut {
+    uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
+    uint32_t* cand;           // candidate cube ids; may be null
+    float* logit;             // their logits; may be null
+    uint32_t cand_cap;
+    uint32_t* n_pred;         // device counter
+};
+
+// W1 as B fragments: b[kk][nt][0..1] for k-step kk (features 16kk..16kk+15) and
+// n-tile nt (hidden 8nt..8nt+7)
+__device__ __forceinline__ void load_w1_frags(const DevModel* __restrict__ m, uint32_t (&b)[4][8][2], int lane) {
+    const uint16_t* w1 = m->w1;
+    const int kq = (lane & 3) * 2, n = lane >> 2;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            const int i0 = kk * 16 + kq, j = nt * 8 + n;
+            b[kk][nt][0] = pack_raw(w1[(i0 + 0) * kHid + j], w1[(i0 + 1) * kHid + j]);
+            b[kk][nt][1] = pack_raw(w1[(i0 + 8) * kHid + j], w1[(i0 + 9) * kHid + j]);
+        }
+}
+
+// The A-fragment registers of one cube for a lane: features (dz, dy, dx) with
+// dx in {dx0, dx0 + 1} (one dens2 pair) and dy in {dy0, dy0 + 2}, for dz = kk.
+// Patch offset d of a cube with parity s lies at coarse offset d - 1 (s = 0)
+// or 2 - d (s = 1) from its coarse cell: for s = 1 the pair runs backwards
+// and its halves are swapped.
+struct PatchRow {
+    uint32_t base;            // padded index of the pair (dx0, dz = 0, dy = dy0)
+    int dz, dy2;              // padded index steps for dz + 1 and dy + 2
+    bool swap;
+};
+
+__device__ __forceinline__ void patch_row(uint32_t rec, int dx0, int dy0, uint32_t p0, uint32_t p01, PatchRow& r) {
+    const int sx = (rec >> 29) & 1, sy = (rec >> 30) & 1, sz = (rec >> 31) & 1;
+    const int pv = (int)(rec & 0x1fffffffu);
+    const int xo = sx ? 1 - dx0 : dx0 - 1;
+    const int yo = sy ? 2 - dy0 : dy0 - 1;
+    const int zo = sz ? 2 : -1;
+    r.base = (uint32_t)(pv + zo * (int)p01 + yo * (int)p0 + xo);
+    r.dz = sz ? -(int)p01 : (int)p01;
+    r.dy2 = sy ? -2 * (int)p0 : 2 * (int)p0;
+    r.swap = sx;
+}
+
+__device__ __forceinline__ uint32_t patch_pair(const uint32_t* __restrict__ dens2, const PatchRow& r, int kk, int yi) {
+    const uint32_t v = __ldg(&dens2[(int)r.base + kk * r.dz + yi * r.dy2]);
+    return r.swap ? __byte_perm(v, 0u, 0x1032) : v;
+}
+
+__global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(LearnDims ld, const uint32_t* __restrict__ dens2,
+                                                           const uint2* __restrict__ clist,
+                                                           const uint32_t* __restrict__ n_dev,
+                                                           const DevModel* __restrict__ model, int use_model,
+                                                           PredictOut out) {
+    const uint32_t n = *n_dev;
     if (!use_model) {
         // collect only
-        for (uint32_t e = tid; e < ncand; e += kPredThreads) {
-            const uint32_t slot = atomicAdd(out.n_pred, 1u);
-            if (out.cand && slot < out.cand_cap) out.cand[slot] = cube_id(s_list[e]);
-        }
+        for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n && e < out.cand_cap; e += gridDim.x * blockDim.x)
+            out.cand[e] = clist[e].x;
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(out.n_pred, n);
         return;
     }
+    const int lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t ngroups = (n + 15) / 16;
+    if (gw >= ngroups) return;
     uint32_t b[4][8][2];
     load_w1_frags(model, b, lane);
     const int kq = (lane & 3) * 2;
@@ -227,37 +312,28 @@ __global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDi
             w2v[nt][e] = bf16_to_f(model->w2[j]);
         }
     const float b2 = model->b2, thr = model->threshold;
-    const uint32_t ngroups = (ncand + 15) / 16;
-    for (uint32_t grp = warp; grp < ngroups; grp += kPredThreads / 32) {
+    // features (dz = kk, dy, dx) with c = dy * 4 + dx in {kq, kq + 1, kq + 8, kq + 9}
+    const int dx0 = kq & 3, dy0 = kq >> 2;
+    const PadDims pd = pad_dims(ld);
+    const uint32_t p01 = pd.p0 * pd.p1;
+    uint32_t npred = 0;
+    for (uint32_t grp = gw; grp < ngroups; grp += nw) {
         const uint32_t e0 = grp * 16 + (lane >> 2), e1 = e0 + 8;
-        const int q0 = s_list[e0 < ncand ? e0 : ncand - 1], q1 = s_list[e1 < ncand ? e1 : ncand - 1];
-        // coarse index within smem (halo offset included) and parity of each row's cube
-        int k0[3], p0[3], k1[3], p1[3];
-        {
-            const int l0[3] = {q0 & 7, (q0 >> 3) & 7, q0 >> 6}, l1[3] = {q1 & 7, (q1 >> 3) & 7, q1 >> 6};
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                k0[a] = (l0[a] >> 1) + kHalo; p0[a] = l0[a] & 1;
-                k1[a] = (l1[a] >> 1) + kHalo; p1[a] = l1[a] & 1;
-            }
-        }
+        const uint2 c0 = __ldg(&clist[min(e0, n - 1)]), c1 = __ldg(&clist[min(e1, n - 1)]);
+        const uint32_t id0 = c0.x, id1 = c1.x;
+        PatchRow r0, r1;
+        patch_row(c0.y, dx0, dy0, pd.p0, p01, r0);
+        patch_row(c1.y, dx0, dy0, pd.p0, p01, r1);
         float acc[8][4];
 #pragma unroll
         for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
-            // features (dz = kk, dy, dx) with c = dy * 4 + dx in {kq, kq + 1, kq + 8, kq + 9}
-            const int dy = kq >> 2, dx = kq & 3;
-            const int z0 = patch_cell(k0[2], p0[2], kk), z1 = patch_cell(k1[2], p1[2], kk);
-            const int y0a = patch_cell(k0[1], p0[1], dy), y0b = patch_cell(k0[1], p0[1], dy + 2);
-            const int y1a = patch_cell(k1[1], p1[1], dy), y1b = patch_cell(k1[1], p1[1], dy + 2);
-            const int x0a = patch_cell(k0[0], p0[0], dx), x0b = patch_cell(k0[0], p0[0], dx + 1);
-            const int x1a = patch_cell(k1[0], p1[0], dx), x1b = patch_cell(k1[0], p1[0], dx + 1);
             uint32_t a[4];
-            a[0] = pack_bf16(s_cnt[z0][y0a][x0a], s_cnt[z0][y0a][x0b]);
-            a[1] = pack_bf16(s_cnt[z1][y1a][x1a], s_cnt[z1][y1a][x1b]);
-            a[2] = pack_bf16(s_cnt[z0][y0b][x0a], s_cnt[z0][y0b][x0b]);
-            a[3] = pack_bf16(s_cnt[z1][y1b][x1a], s_cnt[z1][y1b][x1b]);
+            a[0] = patch_pair(dens2, r0, kk, 0);
+            a[1] = patch_pair(dens2, r1, kk, 0);
+            a[2] = patch_pair(dens2, r0, kk, 1);
+            a[3] = patch_pair(dens2, r1, kk, 1);
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt) mma_bf16(acc[nt], a, b[kk][nt][0], b[kk][nt][1]);
         }
@@ -275,21 +351,25 @@ __global__ void __launch_bounds__(kPredThreads) k_learn_predict(KGrid g, LearnDi
         z1s += __shfl_xor_sync(0xffffffffu, z1s, 2);
         if ((lane & 3) == 0) {
 #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const uint32_t e = r ? e1 : e0;
-                if (e >= ncand) continue;
-                const float z = (r ? z1s : z0s) + b2;
-                const uint32_t id = cube_id(r ? q1 : q0);
+            for (int rr = 0; rr < 2; ++rr) {
+                const uint32_t e = rr ? e1 : e0;
+                if (e >= n) continue;
+                const float z = (rr ? z1s : z0s) + b2;
+                const uint32_t id = rr ? id1 : id0;
                 if (out.logit) {
-                    const uint32_t slot = atomicAdd(out.n_pred, 1u);
-                    if (slot < out.cand_cap) { out.cand[slot] = id; out.logit[slot] = z; }
+                    if (e < out.cand_cap) { out.cand[e] = id; out.logit[e] = z; }
+                    ++npred;
                 } else if (z > thr) {
                     atomicOr(&out.q[id >> 5], 1u << (id & 31u));
-                    atomicAdd(out.n_pred, 1u);
+                    ++npred;
                 }
             }
         }
     }
+    // one count per warp
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) npred += __shfl_xor_sync(0xffffffffu, npred, o);
+    if (lane == 0 && npred) atomicAdd(out.n_pred, npred);
 }
 
 // ---------------------------------------------------------------------------
@@ -690,12 +770,17 @@ pms_status launch_coarse_counts(pms_ctx* ctx) {
     const LearnDims ld = learn_dims(ctx);
     const size_t nc = (size_t)ld.cres[0] * ld.cres[1] * ld.cres[2];
     PMS_CUDA(ctx, ctx->l_counts.ensure(4 * (nc ? nc : 1)));
+    const PadDims pd = pad_dims(ld);
+    if (pd.np >= (1ull << 29)) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "coarse grid too large");
+    PMS_CUDA(ctx, ctx->l_dens.ensure(4 * pd.np));
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->l_counts.p, 0, 4 * nc, ctx->stream));
     if (ctx->n) {
         k_coarse_count<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(g, ld, ctx->spos.as<float4>(), ctx->n,
                                                                          ctx->l_counts.as<uint32_t>());
         PMS_LAUNCHED(ctx);
     }
+    k_coarse_dens<<<grid_for(pd.np, 256), 256, 0, ctx->stream>>>(ctx->l_counts.as<uint32_t>(), ld, ctx->l_dens.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
@@ -705,12 +790,17 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
     const uint64_t ntiles = (uint64_t)ld.tiles[0] * ld.tiles[1] * ld.tiles[2];
     if (ntiles >= (1ull << 31)) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "coarse grid too large");
     Counters* cnt = ctx->counters.as<Counters>();
+    // candidates are distinct cubes: at most one per scalar-grid vertex
+    PMS_CUDA(ctx, ctx->l_clist.ensure(8 * ((size_t)g.sc_size + 1)));
+    k_learn_cand<<<(unsigned)ntiles, kCandThreads, 0, ctx->stream>>>(g, ld, ctx->l_counts.as<uint32_t>(),
+                                                                    ctx->l_clist.as<uint2>(), &cnt->l_cand);
+    PMS_LAUNCHED(ctx);
     PredictOut out;
     out.q = q; out.cand = cand; out.logit = logit; out.cand_cap = cand_cap;
-    out.n_cand = &cnt->l_cand;
     out.n_pred = &cnt->l_pred;
-    k_learn_predict<<<(unsigned)ntiles, kPredThreads, 0, ctx->stream>>>(g, ld, ctx->l_counts.as<uint32_t>(),
-                                                                       ctx->l_model.as<DevModel>(), use_model, out);
+    k_learn_mlp<<<152u * kMlpBlocksPerSm, kMlpThreads, 0, ctx->stream>>>(
+        ld, ctx->l_dens.as<uint32_t>(), ctx->l_clist.as<uint2>(), &cnt->l_cand,
+        ctx->l_model.as<DevModel>(), use_model, out);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -26,32 +26,50 @@
 
 namespace pms {
 
-__constant__ uint32_t c_edge_flags[256];
-__constant__ int8_t c_tri[256][16];
-__constant__ uint8_t c_num_vertices[256];
-__constant__ uint8_t c_edge_vertex[12][2];
+// Case tables in global memory: lanes of a warp look up different cases, which
+// constant memory would serialise.  g_case[c] = edge flags (bits 0-11) | number
+// of mesh vertices << 16; g_slots[c][e] = the mesh vertices (bit v) of case c
+// that lie on edge e.
+__device__ uint32_t g_case[256];
+__device__ uint16_t g_slots[256][12];
 
 static constexpr int kThreads = 128;
-__device__ __constant__ int c_corner[8][3] = {{0, 0, 0}, {0, 0, 1}, {0, 1, 1}, {0, 1, 0},
-                                              {1, 0, 0}, {1, 0, 1}, {1, 1, 1}, {1, 1, 0}};
-// c_partner[k][a]: the corner that differs from corner k only along axis a
-__device__ __constant__ int c_partner[8][3] = {{4, 3, 1}, {5, 2, 0}, {6, 1, 3}, {7, 0, 2},
-                                               {0, 7, 5}, {1, 6, 4}, {2, 5, 7}, {3, 4, 6}};
+
+// Corner c's offset along axis a, for the corner order {000, 001, 011, 010,
+// 100, 101, 111, 110} in (x, y, z) (myCuda.cuh:205-216); the corner that
+// differs from c only along axis a; the end corners of edge e
+// (vertexIndexesOfEdge: the four edges of the x = 0 face, of the x = 1 face,
+// then the four along x).  The emission is compiled for this edge numbering
+// and the table upload checks that the active tables use it.
+__host__ __device__ constexpr int corner_off(int c, int a) {
+    return a == 0 ? (c >> 2) : a == 1 ? ((c >> 1) & 1) : ((c & 1) ^ ((c >> 1) & 1));
+}
+__host__ __device__ constexpr int corner_at(int x, int y, int z) { return 4 * x + 2 * y + (y ^ z); }
+__host__ __device__ constexpr int corner_partner(int c, int a) {
+    return corner_at(corner_off(c, 0) ^ (a == 0), corner_off(c, 1) ^ (a == 1), corner_off(c, 2) ^ (a == 2));
+}
+__host__ __device__ constexpr int edge_end(int e, int i) {
+    return e < 8 ? (i == 0 ? e : (e & 4) + ((e + 1) & 3)) : (i == 0 ? e - 8 : e - 4);
+}
 
 pms_status upload_mc_tables(pms_ctx* ctx) {
     const McTables& T = mc_tables_host();
-    int8_t tri[256][16];
-    uint8_t nv[256];
-    uint8_t ev[12][2];
+    for (int e = 0; e < 12; ++e)
+        if ((int)T.edge_vertex[e][0] != edge_end(e, 0) || (int)T.edge_vertex[e][1] != edge_end(e, 1))
+            return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "marching-cubes tables number the cube edges differently");
+    uint32_t cs[256];
+    uint16_t slots[256][12];
     for (int c = 0; c < 256; ++c) {
-        nv[c] = (uint8_t)T.num_vertices[c];
-        for (int k = 0; k < 16; ++k) tri[c][k] = (int8_t)T.tri[c][k];
+        cs[c] = (T.edge_flags[c] & 0xfffu) | (T.num_vertices[c] << 16);
+        for (int e = 0; e < 12; ++e) slots[c][e] = 0;
+        for (uint32_t v = 0; v < T.num_vertices[c] && v < 16; ++v) {
+            const int e = T.tri[c][v];
+            if (e < 0 || e >= 12) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "marching-cubes table: edge %d in case %d", e, c);
+            slots[c][e] |= (uint16_t)(1u << v);
+        }
     }
-    for (int e = 0; e < 12; ++e) { ev[e][0] = (uint8_t)T.edge_vertex[e][0]; ev[e][1] = (uint8_t)T.edge_vertex[e][1]; }
-    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_edge_flags, T.edge_flags, sizeof(T.edge_flags)));
-    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_tri, tri, sizeof(tri)));
-    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_num_vertices, nv, sizeof(nv)));
-    PMS_CUDA(ctx, cudaMemcpyToSymbol(c_edge_vertex, ev, sizeof(ev)));
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(g_case, cs, sizeof(cs)));
+    PMS_CUDA(ctx, cudaMemcpyToSymbol(g_slots, slots, sizeof(slots)));
     return PMS_OK;
 }
 
@@ -71,12 +89,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, co
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             // uint32 corner index as getCornerIndex1Ds computes it
-            const uint32_t cid = (z + c_corner[k][2]) * rxy + (y + c_corner[k][1]) * rx + (x + c_corner[k][0]);
+            const uint32_t cid = (z + corner_off(k, 2)) * rxy + (y + corner_off(k, 1)) * rx + (x + corner_off(k, 0));
             const bool in = bit_get(bm, nbits, cid);
             all = all && in;
             if (in) cs |= (__ldg(&fdense[cid]) <= iso ? 1u : 0u) << k;
         }
-        if (all) nvert = c_num_vertices[cs];
+        if (all) nvert = __ldg(&g_case[cs]) >> 16;
         else cs = 0;
         mc_case[t] = cs;
         mc_key[t] = nvert ? ((1ull << 32) | nvert) : 0ull;
@@ -118,9 +136,11 @@ __device__ __forceinline__ float3 normalized(float3 v) {
     return make_float3(v.x * inv, v.y * inv, v.z * inv);
 }
 
-// generateTriangles: one thread per valid cube, a warp per 32 consecutive cubes
+// generateTriangles: one thread per valid cube, a warp per 32 consecutive cubes.
+// Every edge's point and normal go straight to the mesh vertices of the case
+// that use it (g_slots), staged per warp as {position, normal}.
 static constexpr int kEmitWarps = kThreads / 32;
-static constexpr int kEmitStage = 32 * 15 * 3;     // floats: 32 cubes x 15 mesh vertices x 3
+static constexpr int kEmitStage = 32 * 15 * 6;     // floats: 32 cubes x 15 mesh vertices x {p, n}
 
 __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counters* __restrict__ cnt,
                                                       const uint4* __restrict__ cube, const float* __restrict__ fdense,
@@ -140,7 +160,8 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
         const bool active = k < nvalid;
         const uint4 cr = active ? __ldg(&cube[k]) : make_uint4(0u, 0u, 0u, 0u);
         const uint32_t id = cr.x, cs = cr.y, base = cr.z;
-        const uint32_t nvert = active ? (uint32_t)c_num_vertices[cs] : 0u;
+        const uint32_t info = __ldg(&g_case[cs]);
+        const uint32_t nvert = active ? info >> 16 : 0u, ef = active ? info & 0xfffu : 0u;
         // the warp's mesh vertices are [base0, base0 + total)
         const int last = (int)min(31u, nvalid - 1u - k0);
         const uint32_t base0 = __shfl_sync(0xffffffffu, base, 0);
@@ -148,67 +169,64 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
         const unsigned long long w0 = fb + base0;
         const uint32_t room = w0 >= cap ? 0u : (cap - w0 < (unsigned long long)total ? (uint32_t)(cap - w0) : total);
         if (room < total && lane == 0) atomicOr(&cnt->err, kErrCapacity);
-        float3 ip[12], in[12];
         if (nvert) {
             const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-            float3 cp[8], cn[8];
+            // corner coordinates: axis value of offset 0 and 1
+            const float px[2] = {sc_coord_i(g, x, 0), sc_coord_i(g, x + 1, 0)};
+            const float py[2] = {sc_coord_i(g, y, 1), sc_coord_i(g, y + 1, 1)};
+            const float pz[2] = {sc_coord_i(g, z, 2), sc_coord_i(g, z + 1, 2)};
             float cf[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                const int X = x + c_corner[c][0], Y = y + c_corner[c][1], Z = z + c_corner[c][2];
-                cp[c] = make_float3(sc_coord_i(g, X, 0), sc_coord_i(g, Y, 1), sc_coord_i(g, Z, 2));
-                cf[c] = __ldg(&fdense[(size_t)Z * rxy + (size_t)Y * rx + (size_t)X]);   // a band vertex
-            }
+            for (int c = 0; c < 8; ++c)    // band vertices: the uint32 index the classification used
+                cf[c] = __ldg(&fdense[(uint32_t)(z + corner_off(c, 2)) * rxy + (uint32_t)(y + corner_off(c, 1)) * rx +
+                                      (uint32_t)(x + corner_off(c, 0))]);
             // central differences (getVertexNorm): along each axis one neighbour of a corner
             // is the cube's other corner on that axis, the other lies outside the cube
+            float3 cn[8];
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
-                const int ox = c_corner[c][0], oy = c_corner[c][1], oz = c_corner[c][2];
+                const int ox = corner_off(c, 0), oy = corner_off(c, 1), oz = corner_off(c, 2);
                 const int X = x + ox, Y = y + oy, Z = z + oz;
                 const float fx = grid_value(g, fdense, ox ? X + 1 : X - 1, Y, Z);
                 const float fy = grid_value(g, fdense, X, oy ? Y + 1 : Y - 1, Z);
                 const float fz = grid_value(g, fdense, X, Y, oz ? Z + 1 : Z - 1);
-                const float px = cf[c_partner[c][0]], py = cf[c_partner[c][1]], pz = cf[c_partner[c][2]];
-                float3 n;
-                n.x = ox ? px - fx : fx - px;
-                n.y = oy ? py - fy : fy - py;
-                n.z = oz ? pz - fz : fz - pz;
-                cn[c] = normalized(n);
+                const float qx = cf[corner_partner(c, 0)], qy = cf[corner_partner(c, 1)], qz = cf[corner_partner(c, 2)];
+                cn[c] = normalized(make_float3(ox ? qx - fx : fx - qx, oy ? qy - fy : fy - qy, oz ? qz - fz : fz - qz));
             }
-            const uint32_t ef = c_edge_flags[cs];
+            const uint32_t o = base - base0;
+            const uint16_t* slots = g_slots[cs];
 #pragma unroll
             for (int e = 0; e < 12; ++e) {
                 if (!(ef & (1u << e))) continue;
-                const int a = c_edge_vertex[e][0], b = c_edge_vertex[e][1];
+                const int a = edge_end(e, 0), b = edge_end(e, 1);
                 const float d = cf[b] - cf[a];
                 // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5
                 const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
-                ip[e] = make_float3(cp[a].x + tt * (cp[b].x - cp[a].x), cp[a].y + tt * (cp[b].y - cp[a].y),
-                                    cp[a].z + tt * (cp[b].z - cp[a].z));
-                const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x),
-                                                         cn[a].y + tt * (cn[b].y - cn[a].y),
+                const float ax = px[corner_off(a, 0)], ay = py[corner_off(a, 1)], az = pz[corner_off(a, 2)];
+                const float bx = px[corner_off(b, 0)], by = py[corner_off(b, 1)], bz = pz[corner_off(b, 2)];
+                const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x), cn[a].y + tt * (cn[b].y - cn[a].y),
                                                          cn[a].z + tt * (cn[b].z - cn[a].z)));
-                in[e] = make_float3(sgn * nn.x, sgn * nn.y, sgn * nn.z);
+                const float q[6] = {ax + tt * (bx - ax), ay + tt * (by - ay), az + tt * (bz - az),
+                                    sgn * nn.x, sgn * nn.y, sgn * nn.z};
+                for (uint32_t m = __ldg(&slots[e]); m; m &= m - 1u) {
+                    float* dst = st + 6 * (o + (uint32_t)(__ffs(m) - 1));
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) dst[c] = q[c];
+                }
             }
         }
-        // positions, then normals: stage the warp's vertices in order, write whole lines
-        const uint32_t o = base - base0;
-        for (uint32_t v = 0; v < nvert; ++v) {
-            const float3 p = ip[c_tri[cs][v]];
-            st[3 * (o + v)] = p.x; st[3 * (o + v) + 1] = p.y; st[3 * (o + v) + 2] = p.z;
+        __syncwarp();
+        // whole lines: positions, then normals
+        for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
+            const uint32_t v = i / 3u, c = i - 3u * v;
+            vert[3 * (size_t)w0 + i] = st[6 * v + c];
         }
-        __syncwarp();
-        for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) vert[3 * (size_t)w0 + i] = st[i];
-        __syncwarp();
-        if (vnorm) {
-            for (uint32_t v = 0; v < nvert; ++v) {
-                const float3 q = in[c_tri[cs][v]];
-                st[3 * (o + v)] = q.x; st[3 * (o + v) + 1] = q.y; st[3 * (o + v) + 2] = q.z;
+        if (vnorm)
+            for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
+                const uint32_t v = i / 3u, c = i - 3u * v;
+                vnorm[3 * (size_t)w0 + i] = st[6 * v + 3 + c];
             }
-            __syncwarp();
-            for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) vnorm[3 * (size_t)w0 + i] = st[i];
-            __syncwarp();
-        }
+        __syncwarp();
     }
 }
 

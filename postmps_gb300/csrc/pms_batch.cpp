@@ -282,6 +282,11 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
     for (const pms_grid& g : grid)
         ncoarse = std::max(ncoarse, (size_t)(g.scres[0] / 2 + 2) * (g.scres[1] / 2 + 2) * (g.scres[2] / 2 + 2));
     PMS_CUDA(lc, lc->l_counts.ensure(4 * ncoarse));
+    size_t npad = 1;
+    for (const pms_grid& g : grid)
+        npad = std::max(npad, (size_t)(g.scres[0] / 2 + 3) * (g.scres[1] / 2 + 3) * (g.scres[2] / 2 + 3));
+    PMS_CUDA(lc, lc->l_dens.ensure(4 * npad));    // padded coarse grid: cres + 1 per axis
+    PMS_CUDA(lc, lc->l_clist.ensure(8 * S));
     if (lc != c) {
         // the lane reads the context's model
         PMS_CUDA(lc, lc->l_model.ensure(sizeof(pms_band_model)));

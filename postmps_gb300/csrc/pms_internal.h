@@ -142,6 +142,7 @@ struct pms_ctx {
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
     // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
+    pms::DBuf l_dens, l_clist;   // bf16 coarse density pairs (padded grid), candidate cube records
     pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
               l_field_new, l_vlist_m, l_field_m, l_cand, l_logit, l_label, l_qlist, l_wp_q;
     bool have_model = false, band_learned = false, mc_classified = false;
