@@ -363,6 +363,7 @@ pms_status pms_batch_info(pms_ctx* ctx, uint32_t* graph_kernels, uint32_t* captu
  * ------------------------------------------------------------------------- */
 typedef struct pms_tune {
     int field_threads, field_waves, density_threads, moments_threads;
+    int field_vpt;                     /* band vertices per field work item: 1, 2 or 4 (x-neighbours) */
     float anisotropy_ms, field_ms;     /* the chosen shapes' times on the tuning frame */
 } pms_tune;
 pms_status pms_autotune(pms_ctx* ctx, pms_tune* out);

@@ -26,6 +26,8 @@
 // Adding a zero contribution leaves the sum unchanged, so no cut changes the
 // reference's sum or its early exit: the threshold test after a skipped cell
 // sees the same sum as the test before it.
+#include <type_traits>
+
 #include "pms_internal.h"
 #include "k_common.cuh"
 
@@ -43,56 +45,37 @@ __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pa
     return d > 0.f ? d * d : 0.f;
 }
 
-// true when vertex v is within the culling radius of cell c's particle box
-// (cell records: {min xyz, r^2}, {max xyz, 0}; r^2 = -1 for an empty cell)
-__device__ __forceinline__ bool cell_reaches(const float4* __restrict__ rec, uint32_t c, const float3 v) {
-    const float4 b0 = __ldg(&rec[2 * (size_t)c]), b1 = __ldg(&rec[2 * (size_t)c + 1]);
-    const float dx = fmaxf(fmaxf(b0.x - v.x, v.x - b1.x), 0.f);
-    const float dy = fmaxf(fmaxf(b0.y - v.y, v.y - b1.y), 0.f);
-    const float dz = fmaxf(fmaxf(b0.z - v.z, v.z - b1.z), 0.f);
-    return dx * dx + dy * dy + dz * dz < b0.w;
-}
+// A particle adds sigma det(G) (m/rho) (1 - |G r|^2)^3 when |G r|^2 < 1
+// (anisotropicW, myCuda.cuh:151-191); every other particle adds exactly 0.
+// The reference also tests |r| < maxvalue * h first, which |G r| < 1 already
+// implies (maxvalue * h = 1 / smallest singular value of G); at the very edge
+// the two can differ only by rounding, where the contribution is ~0.  |G r|^2
+// is evaluated as r^T M r with the packed M = G^T G (off-diagonals doubled)
+// and the weight w = (m/rho) sigma det(G) stored per particle.
+// A work item is a run of up to K band vertices that are neighbours along x
+// (ids id0, id0 + 1, ...; one row of the scalar grid): item = first band index
+// t0 | (count - 1) << 29.  The run shares the slabs and rows of its walk (same
+// y and z), each cell's bounds and record loads and each particle's loads;
+// every vertex keeps its own window, x range, sum and early exit, and adds its
+// contributions in the reference's order, so each value is the one a walk of
+// that vertex alone gives.
+static constexpr uint32_t kItemShift = 29;
 
-// Sum of the contributions of particles [j0, j1) at vertex v.  A particle adds
-// sigma det(G) (m/rho) (1 - |G r|^2)^3 when |G r|^2 < 1 (anisotropicW,
-// myCuda.cuh:151-191); every other particle adds exactly 0.  The reference
-// also tests |r| < maxvalue * h first, which |G r| < 1 already implies
-// (maxvalue * h = 1 / smallest singular value of G); at the very edge the two
-// can differ only by rounding, where the contribution is ~0.  |G r|^2 is
-// evaluated as r^T M r with the packed M = G^T G (off-diagonals doubled) and
-// the weight w = (m/rho) sigma det(G) stored per particle.
-__device__ __forceinline__ float range_sum(uint32_t j0, uint32_t j1, const float3 v, const float4* __restrict__ spos,
-                                           const float4* __restrict__ aniso, float sum) {
-#pragma unroll 2
-    for (uint32_t j = j0; j < j1; ++j) {
-        const float4 q = __ldg(&spos[j]);
-        const float4 a0 = __ldg(&aniso[2 * (size_t)j]);      // {m00, 2 m01, 2 m02, h_s^2}
-        const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);  // {m11, 2 m12, m22, w}
-        const float rx = q.x - v.x, ry = q.y - v.y, rz = q.z - v.z;
-        const float d2 = rx * (a0.x * rx + a0.y * ry + a0.z * rz) + ry * (a1.x * ry + a1.y * rz) + rz * (a1.z * rz);
-        const float x = 1.f - d2;
-        sum += (d2 < 1.f) ? a1.w * (x * x * x) : 0.f;
-    }
-    return sum;
-}
-
-// BT threads per block (autotuned: 64, 128 or 256), 48 registers per thread at most
-// (40 resident warps per SM).
-// cell_rad holds sp_size per-cell support radii followed by one radius per row
-// (z, y): the largest maxvalue * h of the row's particles (0 where none is
-// anisotropic).  The z and y ranges are cut from the largest support of the
-// frame, each row's x range from the row's own radius, and each non-empty cell
-// by its record: the bounding box of its particles and its largest support.
-// The value goes to field[t] (band order; skipped when field is null) and to
-// fdense[id] (the whole scalar grid).
-template <int BT>
-__global__ void __launch_bounds__(BT, 1280 / BT) k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt,
-                                                    const uint32_t* __restrict__ n_dev,
-                                                    const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
-                                                    const float* __restrict__ cell_rad, const float4* __restrict__ rec,
-                                                    const float4* __restrict__ spos, const float4* __restrict__ aniso,
-                                                    float* __restrict__ field, float* __restrict__ fdense) {
-    const uint32_t nv = *n_dev;
+// BT threads per block (autotuned: 64, 128 or 256), K vertices per item (1, 2
+// or 4, autotuned).  cell_rad holds sp_size per-cell support radii followed by
+// one radius per row (z, y): the largest maxvalue * h of the row's particles
+// (0 where none is anisotropic).  The z and y ranges are cut from the largest
+// support of the frame, each row's x range from the row's own radius, and each
+// non-empty cell by its record: the bounding box of its particles and its
+// largest support.  The value goes to field[t] (band order; skipped when field
+// is null) and to fdense[id] (the whole scalar grid).
+template <int BT, int K>
+__global__ void __launch_bounds__(BT, (K == 1 ? 1280 : 1024) / BT)
+k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_t* __restrict__ n_items_dev,
+        const uint32_t* __restrict__ items, const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
+        const float* __restrict__ cell_rad, const float4* __restrict__ rec, const float4* __restrict__ spos,
+        const float4* __restrict__ aniso, float* __restrict__ field, float* __restrict__ fdense) {
+    const uint32_t n_items = *n_items_dev;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], sry = g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
@@ -101,59 +84,158 @@ __global__ void __launch_bounds__(BT, 1280 / BT) k_field(KGrid g, FieldParams fp
     // largest support of any particle this frame
     const float rmax = fmaxf(__uint_as_float(cnt->rad_max_bits), fp.h) * fp.grow;
     const float rmax2 = rmax * rmax;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nv; t += gridDim.x * blockDim.x) {
-        const uint32_t id = vlist[t];
+    for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
+        const uint32_t item = items[it];
+        const uint32_t t0 = item & ((1u << kItemShift) - 1u);
+        const int m = (int)(item >> kItemShift) + 1;
+        const uint32_t id = vlist[t0];
         const uint32_t iz = id / rxy, rem = id - iz * rxy, iy = rem / rx, ix = rem - iy * rx;
-        const float3 v = make_float3(sc_coord(g, ix, 0), sc_coord(g, iy, 1), sc_coord(g, iz, 2));
-        const uint3 c = sp_cell(g, v.x, v.y, v.z);
+        const float vy = sc_coord(g, iy, 1), vz = sc_coord(g, iz, 2);
+        float vx[K], ux[K], sum[K];
+        int wlo[K], whi[K];                          // the vertices' x windows [c - 2e, c + 2e) (clamped)
         uint3 lo, hi;
-        box_clamp(g, c, e2, lo, hi);             // the reference's loops run to hi exclusive
-        const float ux = (v.x - g.min_pos[0]) * inv_cs, uy = (v.y - g.min_pos[1]) * inv_cs,
-                    uz = (v.z - g.min_pos[2]) * inv_cs;
-        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            vx[k] = sc_coord(g, ix + (uint32_t)k, 0);
+            const uint3 c = sp_cell(g, vx[k], vy, vz);
+            box_clamp(g, c, e2, lo, hi);             // y and z bounds agree for all vertices of the run
+            wlo[k] = (int)lo.x;
+            whi[k] = k < m ? (int)hi.x : (int)lo.x;  // vertices past the run: empty windows
+            ux[k] = (vx[k] - g.min_pos[0]) * inv_cs;
+            sum[k] = 0.f;
+        }
+        const float uy = (vy - g.min_pos[1]) * inv_cs, uz = (vz - g.min_pos[2]) * inv_cs;
         int za, zb;
         cell_range(uz, rmax * inv_cs + kRangeMargin, lo.z, hi.z, za, zb);
         for (int z = za; z < zb; ++z) {
-            const float gz = gap2_axis(v.z, g.min_pos[2] + (float)z * g.sp_cs, g.sp_cs, pad);
+            const float gz = gap2_axis(vz, g.min_pos[2] + (float)z * g.sp_cs, g.sp_cs, pad);
             if (gz >= rmax2) continue;
             int ya, yb;
             cell_range(uy, sqrtf(rmax2 - gz) * inv_cs + kRangeMargin, lo.y, hi.y, ya, yb);
             for (int y = ya; y < yb; ++y) {
-                const float gyz = gz + gap2_axis(v.y, g.min_pos[1] + (float)y * g.sp_cs, g.sp_cs, pad);
+                const float gyz = gz + gap2_axis(vy, g.min_pos[1] + (float)y * g.sp_cs, g.sp_cs, pad);
                 const uint32_t rowi = (uint32_t)z * sry + (uint32_t)y;
                 const float rr = fmaxf(__ldg(&row_rad[rowi]), fp.h) * fp.grow;
                 const float rr2 = rr * rr;
                 if (gyz >= rr2) continue;           // every cell of the row adds 0
                 const uint32_t row = rowi * srx;
-                if (sum > fp.thr) {
-                    // threshold crossed: the reference adds this row's first cell, then breaks
-                    if (lo.x < hi.x && cell_reaches(rec, row + lo.x, v))
-                        sum = range_sum(__ldg(&cell_start[row + lo.x]), __ldg(&cell_start[row + lo.x + 1]), v, spos,
-                                        aniso, sum);
-                    continue;
-                }
-                // cells of the row the row's largest support can reach, 32 at a time:
-                // first the cells whose record the vertex reaches (independent loads),
-                // then their particles in x order until the threshold is crossed
-                int xa, xb;
-                cell_range(ux, sqrtf(rr2 - gyz) * inv_cs + kRangeMargin, lo.x, hi.x, xa, xb);
-                for (int x0 = xa; x0 < xb; x0 += 32) {
-                    const int nx = min(xb - x0, 32);
-                    uint32_t reach = 0u;
-                    for (int k = 0; k < nx; ++k)
-                        reach |= (cell_reaches(rec, row + (uint32_t)(x0 + k), v) ? 1u : 0u) << k;
-                    while (reach) {
-                        const uint32_t cell = row + (uint32_t)(x0 + __ffs(reach) - 1);
-                        reach &= reach - 1u;
-                        sum = range_sum(__ldg(&cell_start[cell]), __ldg(&cell_start[cell + 1u]), v, spos, aniso, sum);
-                        if (sum > fp.thr) break;
+                // each vertex's cells of this row: past the threshold, only the window's
+                // first cell (the reference adds it, then breaks); else those the row's
+                // largest support reaches
+                const float rxc = sqrtf(rr2 - gyz) * inv_cs + kRangeMargin;
+                int xs[K], xe[K];
+                bool live[K];
+                int X0 = 0x7fffffff, X1 = -1;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    if (sum[k] > fp.thr) {
+                        xs[k] = wlo[k];
+                        xe[k] = min(wlo[k] + 1, whi[k]);
+                    } else {
+                        cell_range(ux[k], rxc, (uint32_t)wlo[k], (uint32_t)whi[k], xs[k], xe[k]);
                     }
-                    if (sum > fp.thr) break;
+                    live[k] = xs[k] < xe[k];
+                    if (live[k]) { X0 = min(X0, xs[k]); X1 = max(X1, xe[k]); }
+                }
+                for (int x0 = X0; x0 < X1; x0 += 32) {
+                    const int nx = min(X1 - x0, 32);
+                    // cells whose record each vertex reaches (independent loads)
+                    uint32_t reach[K];
+#pragma unroll
+                    for (int k = 0; k < K; ++k) reach[k] = 0u;
+                    for (int i = 0; i < nx; ++i) {
+                        const int x = x0 + i;
+                        const uint32_t c = row + (uint32_t)x;
+                        const float4 b0 = __ldg(&rec[2 * (size_t)c]), b1 = __ldg(&rec[2 * (size_t)c + 1]);
+                        const float dy = fmaxf(fmaxf(b0.y - vy, vy - b1.y), 0.f);
+                        const float dz = fmaxf(fmaxf(b0.z - vz, vz - b1.z), 0.f);
+                        const float dyz = dy * dy + dz * dz;
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            const float dx = fmaxf(fmaxf(b0.x - vx[k], vx[k] - b1.x), 0.f);
+                            const bool in = live[k] && x >= xs[k] && x < xe[k] && dx * dx + dyz < b0.w;
+                            reach[k] |= (in ? 1u : 0u) << i;
+                        }
+                    }
+                    uint32_t any = 0u;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) any |= reach[k];
+                    // the reached cells in x order; a vertex stops for the row once its
+                    // sum passes the threshold after one of its cells
+                    while (any) {
+                        const int i = __ffs(any) - 1;
+                        const uint32_t bit = 1u << i;
+                        const uint32_t c = row + (uint32_t)(x0 + i);
+                        bool use[K];
+#pragma unroll
+                        for (int k = 0; k < K; ++k) use[k] = (reach[k] & bit) != 0u;
+                        const uint32_t j1 = __ldg(&cell_start[c + 1u]);
+#pragma unroll 2
+                        for (uint32_t j = __ldg(&cell_start[c]); j < j1; ++j) {
+                            const float4 q = __ldg(&spos[j]);
+                            const float4 a0 = __ldg(&aniso[2 * (size_t)j]);      // {m00, 2 m01, 2 m02, h_s^2}
+                            const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);  // {m11, 2 m12, m22, w}
+                            // r^T M r with every rounding spelled out, so that the value does
+                            // not depend on how many vertices share the loads
+                            const float ry = __fsub_rn(q.y, vy), rz = __fsub_rn(q.z, vz);
+                            const float pyz = __fmaf_rn(rz, __fmul_rn(a1.z, rz), __fmul_rn(ry, __fmaf_rn(a1.x, ry, __fmul_rn(a1.y, rz))));
+                            const float cyz = __fmaf_rn(a0.y, ry, __fmul_rn(a0.z, rz));
+#pragma unroll
+                            for (int k = 0; k < K; ++k) {
+                                const float rxk = __fsub_rn(q.x, vx[k]);
+                                const float d2 = __fmaf_rn(rxk, __fmaf_rn(a0.x, rxk, cyz), pyz);
+                                const float xx = __fsub_rn(1.f, d2);
+                                const float w = (d2 < 1.f) ? __fmul_rn(a1.w, __fmul_rn(__fmul_rn(xx, xx), xx)) : 0.f;
+                                if (use[k]) sum[k] = __fadd_rn(sum[k], w);
+                            }
+                        }
+                        uint32_t still = 0u;
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            if (use[k] && sum[k] > fp.thr) { reach[k] = 0u; live[k] = false; }
+                            still |= reach[k];
+                        }
+                        any = still & ~((bit << 1) - 1u);   // i = 31: bit << 1 = 0, nothing left
+                    }
+                    bool more = false;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) more |= live[k] && xe[k] > x0 + nx;
+                    if (!more) break;
                 }
             }
         }
-        if (field) field[t] = sum;
-        fdense[id] = sum;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (k < m) {
+                if (field) field[t0 + k] = sum[k];
+                fdense[id + k] = sum[k];
+            }
+    }
+}
+
+// Work items over vlist[0 .. *n_dev): group g = entries [g K, g K + K) splits
+// into its runs of x-neighbours (id + 1 in the same row); count, then write.
+__global__ void __launch_bounds__(256) k_field_items(const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ n_dev,
+                                                     uint32_t ngroups, uint32_t K, uint32_t rx,
+                                                     const uint32_t* __restrict__ offs, uint32_t* __restrict__ out) {
+    const uint32_t n = *n_dev;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += gridDim.x * blockDim.x) {
+        const uint32_t t0 = g * K, t1 = min(t0 + K, n);
+        uint32_t runs = 0, start = t0, o = offs ? offs[g] : 0u;
+        for (uint32_t t = t0; t < t1; ++t) {
+            const uint32_t id = __ldg(&vlist[t]);
+            const bool join = t > t0 && id == __ldg(&vlist[t - 1]) + 1u && id % rx != 0u;
+            if (t > t0 && !join) {
+                if (offs) out[o + runs] = start | ((t - start - 1u) << kItemShift);
+                ++runs;
+                start = t;
+            }
+        }
+        if (t0 < t1) {
+            if (offs) out[o + runs] = start | ((t1 - start - 1u) << kItemShift);
+            ++runs;
+        }
+        if (!offs) out[g] = runs;
     }
 }
 
@@ -165,16 +247,38 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
     fp.thr = 2.f * P.iso_value;
     fp.grow = kSupportGrow;
     Counters* cnt = ctx->counters.as<Counters>();
+    if ((uint64_t)n_host >= (1ull << kItemShift)) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "band above 2^29 vertices");
+    const uint32_t K = (uint32_t)ctx->tune.field_vpt;
+    const uint32_t ngroups = (n_host + K - 1u) / K;
+    PMS_CUDA(ctx, ctx->fitem_cnt.ensure(4 * ((size_t)ngroups + 1)));
+    PMS_CUDA(ctx, ctx->fitem_off.ensure(4 * ((size_t)ngroups + 1)));
+    PMS_CUDA(ctx, ctx->fitems.ensure(4 * ((size_t)n_host + 1)));
+    const unsigned gb = grid_for(ngroups, 256);
+    k_field_items<<<gb, 256, 0, ctx->stream>>>(vlist, n_dev, ngroups, K, g.scres[0], nullptr, ctx->fitem_cnt.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    pms_status st = scan_u32(ctx, ctx->fitem_cnt.as<uint32_t>(), ctx->fitem_off.as<uint32_t>(), ngroups, &cnt->n_items);
+    if (st != PMS_OK) return st;
+    k_field_items<<<gb, 256, 0, ctx->stream>>>(vlist, n_dev, ngroups, K, g.scres[0], ctx->fitem_off.as<uint32_t>(),
+                                               ctx->fitems.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
     const int bt = ctx->tune.field_threads;
-    const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * (1280u / (unsigned)bt));
+    const unsigned per_sm = (K == 1 ? 1280u : 1024u) / (unsigned)bt;
+    const unsigned blocks = grid_for(n_host, (unsigned)bt, 152u * (unsigned)ctx->tune.field_waves * per_sm);
     auto go = [&](auto kern) {
-        kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, n_dev, vlist, ctx->cell_start.as<uint32_t>(),
-                                             ctx->cell_rad.as<float>(), ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(),
-                                             ctx->aniso.as<float4>(), out, ctx->fdense.as<float>());
+        kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, &cnt->n_items, ctx->fitems.as<uint32_t>(), vlist,
+                                             ctx->cell_start.as<uint32_t>(), ctx->cell_rad.as<float>(),
+                                             ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out,
+                                             ctx->fdense.as<float>());
     };
-    if (bt == 64) go(k_field<64>);
-    else if (bt == 256) go(k_field<256>);
-    else go(k_field<128>);
+    auto by_vpt = [&](auto bt_tag) {
+        constexpr int B = decltype(bt_tag)::value;
+        if (K == 1) go(k_field<B, 1>);
+        else if (K == 4) go(k_field<B, 4>);
+        else go(k_field<B, 2>);
+    };
+    if (bt == 64) by_vpt(std::integral_constant<int, 64>());
+    else if (bt == 256) by_vpt(std::integral_constant<int, 256>());
+    else by_vpt(std::integral_constant<int, 128>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -413,20 +413,19 @@ __global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a,
 // Border check: a valid cube whose face has corners on both sides of the
 // iso-surface shares that crossing with the cube across the face, so the
 // neighbour is a valid cube too; if not all of the neighbour's corners have a
-// field value yet, the neighbour cube is queued.
-__global__ void __launch_bounds__(256) k_border(KGrid g, const uint32_t* __restrict__ n_dev, const uint32_t* __restrict__ vlist,
-                                                const uint32_t* __restrict__ mc_case,
-                                                const unsigned long long* __restrict__ mc_key,
+// field value yet, the neighbour cube is queued.  One thread per valid cube
+// of the classification ({vertex id, case} records of the compaction).
+__global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
                                                 const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
                                                 uint32_t* __restrict__ n_added) {
-    const uint32_t n = *n_dev;
+    const uint32_t n = cnt->nvalid;
     const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
     // face masks over the corner order {000,001,011,010,100,101,111,110} (x,y,z)
     const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
     const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        if (!mc_key[t]) continue;
-        const uint32_t cs = mc_case[t], id = vlist[t];
+        const uint4 cr = __ldg(&cube[t]);
+        const uint32_t cs = cr.y, id = cr.x;
         const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
@@ -827,10 +826,9 @@ pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wp
 pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
-    k_border<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, &cnt->nv, ctx->vlist.as<uint32_t>(),
-                                                              ctx->mc_case.as<uint32_t>(),
-                                                              ctx->mc_key.as<unsigned long long>(), ctx->bm.as<uint32_t>(),
-                                                              qadd, &cnt->l_added);
+    // ctx->nv bounds the valid cubes; the kernel reads their count
+    k_border<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), ctx->bm.as<uint32_t>(), qadd,
+                                                              &cnt->l_added);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -52,7 +52,7 @@ static void release_all(pms_ctx* c) {
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
                     &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->cell_rec, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
                     &c->nnb, &c->bm0, &c->bm, &c->wcount, &c->wprefix, &c->vlist, &c->field, &c->mc_case,
-                    &c->mc_key, &c->mc_off, &c->valid, &c->fdense, &c->cube, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
+                    &c->mc_key, &c->mc_off, &c->valid, &c->fdense, &c->cube, &c->fitems, &c->fitem_cnt, &c->fitem_off, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
                     &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp};
@@ -187,6 +187,9 @@ pms_status pms::ensure_band_buffers(pms_ctx* c, uint32_t nv) {
     PMS_CUDA(c, c->mc_off.ensure(8 * V));
     PMS_CUDA(c, c->valid.ensure(4 * V));
     PMS_CUDA(c, c->cube.ensure(16 * V));
+    PMS_CUDA(c, c->fitems.ensure(4 * (V + 1)));
+    PMS_CUDA(c, c->fitem_cnt.ensure(4 * (V + 1)));
+    PMS_CUDA(c, c->fitem_off.ensure(4 * (V + 1)));
     return PMS_OK;
 }
 

@@ -66,6 +66,7 @@ struct Counters {
     uint32_t l_added;       // cubes the last border check queued
     uint32_t l_nnew;        // vertices those cubes add
     uint32_t l_nq;          // cubes queued for a border-check round (batched frames)
+    uint32_t n_items;       // work items of the last field launch
 };
 
 enum : uint32_t {
@@ -95,7 +96,7 @@ struct ScanTemp {
 // Launch shapes chosen by the autotuner (pms_autotune): threads per block of
 // the neighbour walks and the field's resident-block cap (blocks per SM).
 struct Tune {
-    int field_threads = 128, field_waves = 8, density_threads = 128, moments_threads = 128;
+    int field_threads = 128, field_waves = 8, density_threads = 128, moments_threads = 128, field_vpt = 2;
 };
 
 // Stage timing events.
@@ -137,6 +138,8 @@ struct pms_ctx {
     // the field over the whole scalar grid, 0 off the band (the marching cubes' lookups);
     // per valid cube {vertex id, case, first mesh vertex, 0}
     pms::DBuf fdense, cube;
+    // field work items (runs of x-neighbouring band vertices)
+    pms::DBuf fitems, fitem_cnt, fitem_off;
     bool have_values = false;
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,

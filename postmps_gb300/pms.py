@@ -105,7 +105,8 @@ class Counts(C.Structure):
 class Tune(C.Structure):
     """pms_tune: launch shapes of the neighbour walks."""
     _fields_ = [("field_threads", C.c_int), ("field_waves", C.c_int), ("density_threads", C.c_int),
-                ("moments_threads", C.c_int), ("anisotropy_ms", C.c_float), ("field_ms", C.c_float)]
+                ("moments_threads", C.c_int), ("field_vpt", C.c_int), ("anisotropy_ms", C.c_float),
+                ("field_ms", C.c_float)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -410,7 +411,8 @@ class Context:
         return t.as_dict()
 
     def set_tune(self, d: dict) -> None:
-        t = Tune(**{k: d[k] for k in ("field_threads", "field_waves", "density_threads", "moments_threads")})
+        t = Tune(**{k: d[k] for k in ("field_threads", "field_waves", "density_threads", "moments_threads")},
+                 field_vpt=d.get("field_vpt", 2))
         self._call("pms_set_tune", C.byref(t))
 
     def get_tune(self) -> dict:

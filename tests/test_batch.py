@@ -105,13 +105,14 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
         ref_counts = ctx.counts().as_dict()
         ref_mesh = ctx.mesh(normals=False)[0]
         t = ctx.autotune()
-        assert t["field_threads"] in (64, 128, 256) and t["field_waves"] in (1, 2, 4, 8)
+        assert t["field_threads"] in (64, 128, 256) and t["field_waves"] in (1, 2, 4, 8) and t["field_vpt"] in (1, 2, 4)
         assert t["density_threads"] in (64, 128, 256) and t["moments_threads"] in (64, 128, 256)
         assert t["field_ms"] > 0 and t["anisotropy_ms"] > 0
         assert np.array_equal(ctx.debug("field"), ref_field)
         assert ctx.counts().as_dict() == ref_counts
-        for shape in ({"field_threads": 64, "field_waves": 1, "density_threads": 256, "moments_threads": 64},
-                      {"field_threads": 256, "field_waves": 8, "density_threads": 64, "moments_threads": 256}):
+        for shape in ({"field_threads": 64, "field_waves": 1, "density_threads": 256, "moments_threads": 64, "field_vpt": 1},
+                      {"field_threads": 256, "field_waves": 8, "density_threads": 64, "moments_threads": 256, "field_vpt": 4},
+                      {"field_threads": 128, "field_waves": 2, "density_threads": 128, "moments_threads": 128, "field_vpt": 2}):
             ctx.set_tune(shape)
             cs, mesh = _single(ctx, frames[1])
             assert np.array_equal(mesh, ref_mesh)
