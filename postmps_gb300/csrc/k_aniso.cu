@@ -15,6 +15,8 @@
 // with exact rotations runs in float32, and covariances whose condition
 // number exceeds cfg.fp64_svd_cond are re-solved in float64.  Sums are
 // accumulated relative to the particle's own position for accuracy.
+#include <cmath>
+
 #include "pms_internal.h"
 #include "k_common.cuh"
 
@@ -25,6 +27,8 @@ static constexpr float kSigma = 1.56668147f;      // Define.h:11, 315/(64 pi)
 
 struct AnisoParams {
     float h, h_sq, h_inv, r2h, mass, kdens, inv_h2;
+    float nn_d2;     // |u| <= h      <=>  |u|^2 <= nn_d2  (|u| = sqrt of |u|^2, rounded)
+    float w_d2;      // |u| < 2h      <=>  |u|^2 <= w_d2
     int min_nn;
     uint32_t sp_size, spres_x;   // where the per-row radii start; cells per row
     double cond_limit;
@@ -149,6 +153,9 @@ __device__ __forceinline__ void eig_sym3(T a[3][3], T e[3], T v[3][3], T tol) {
 //   S0 = sum w, S1 = sum w u, S2 = sum w u u^T, J = #{|u| <= h}.
 // The reference's two passes (mean, then covariance about the mean) follow
 // from these: mean = x_i + S1/S0 and sum w (u - o)(u - o)^T = S2 - S1 S1^T / S0.
+// The count and the support test compare |u|^2 with the exact bounds of the
+// rounded square root (the same decisions as comparing |u|); the weight uses
+// the hardware reciprocal square root (a few ulp, inside the weight's rounding).
 // ---------------------------------------------------------------------------
 template <int BT>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_moments(KGrid g, AnisoParams ap, const uint32_t* __restrict__ slist,
@@ -177,10 +184,9 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_moments(KGrid g, AnisoParams 
             // |u| rounded operation by operation, as the reference's neighbour count sees it
             const float ux = __fsub_rn(q.x, p.x), uy = __fsub_rn(q.y, p.y), uz = __fsub_rn(q.z, p.z);
             const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(ux, ux), __fmul_rn(uy, uy)), __fmul_rn(uz, uz));
-            const float d = __fsqrt_rn(d2);
-            nn += (d <= ap.h) ? 1u : 0u;
-            const float t = d * inv_r2h;
-            const float w = (d < ap.r2h) ? 1.f - t * t * t : 0.f;   // zero weight adds exactly nothing
+            nn += (d2 <= ap.nn_d2) ? 1u : 0u;
+            const float t = d2 * rsqrtf(d2) * inv_r2h;               // d2 = 0 gives NaN, selected away
+            const float w = (d2 <= ap.w_d2 && d2 > 0.f) ? 1.f - t * t * t : (d2 > 0.f ? 0.f : 1.f);
             const float wx = w * ux, wy = w * uy, wz = w * uz;
             s0 += w; sx += wx; sy += wy; sz += wz;
             sxx += wx * ux; sxy += wx * uy; sxz += wx * uz;
@@ -325,6 +331,17 @@ __global__ void __launch_bounds__(kThreads) k_cell_records(const uint32_t* __res
     }
 }
 
+// Largest float x >= 0 with sqrt(x) <= r (inclusive) or sqrt(x) < r (strict),
+// sqrt correctly rounded: the rounded square root is non-decreasing, so
+// sqrt(x) <= r exactly when x <= that bound.
+static float sqrt_bound(float r, bool inclusive) {
+    auto ok = [&](float x) { const float s = std::sqrt(x); return inclusive ? s <= r : s < r; };
+    float x = r * r;
+    while (x > 0.f && !ok(x)) x = std::nextafter(x, 0.f);
+    while (ok(std::nextafter(x, INFINITY))) x = std::nextafter(x, INFINITY);
+    return x;
+}
+
 pms_status launch_density_aniso(pms_ctx* ctx) {
     const KGrid g = kgrid_of(ctx->grid);
     const pms_params& P = ctx->prm;
@@ -334,6 +351,8 @@ pms_status launch_density_aniso(pms_ctx* ctx) {
     ap.inv_h2 = 1.f / (P.h * P.h);
     ap.min_nn = P.min_num_neighbors;
     ap.cond_limit = ctx->cfg.fp64_svd_cond;
+    ap.nn_d2 = sqrt_bound(P.h, true);
+    ap.w_d2 = sqrt_bound(P.aniso_radius, false);
     ap.sp_size = g.sp_size;
     ap.spres_x = g.spres[0];
     Counters* cnt = ctx->counters.as<Counters>();

@@ -120,7 +120,8 @@ static pms_status full_check(pms_ctx* c, uint64_t W) {
     return launch_border(c, c->l_qadd.as<uint32_t>());
 }
 
-// one round: field at the queued cubes' new corners, merged vertex set, check the queued cubes
+// one round: field at the queued cubes' new corners (into the dense field), merged vertex set,
+// check the queued cubes
 static pms_status border_round(pms_ctx* c, uint64_t W) {
     Counters* cnt = c->counters.as<Counters>();
     const uint32_t S = c->grid.sc_size;
@@ -141,11 +142,9 @@ static pms_status border_round(pms_ctx* c, uint64_t W) {
     if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
     if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
         return st;
-    if ((st = launch_field_gather(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, S, c->l_field_m.as<float>()))) return st;
     std::swap(c->bm, c->l_bm_m);
     std::swap(c->wprefix, c->l_wp_m);
     std::swap(c->vlist, c->l_vlist_m);
-    std::swap(c->field, c->l_field_m);
     PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
     PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
     if ((st = launch_border_list(c, c->l_qlist.as<uint32_t>(), S, c->l_q.as<uint32_t>(), &cnt->l_nq))) return st;
@@ -179,6 +178,8 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool lear
         if ((st = full_check(c, W))) return st;
         for (int r = 0; r < kGraphRounds; ++r)
             if ((st = border_round(c, W))) return st;
+        // the band-order field of the final vertex set (the rounds work on the dense field)
+        if ((st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, g.sc_size, c->field.as<float>()))) return st;
         if ((st = full_check(c, W))) return st;              // what is still missing: the frame runs again alone
     } else {
         if ((st = launch_band(c))) return st;
@@ -271,7 +272,7 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
     const size_t S = (size_t)gmax.sc_size + 1;
     for (DBuf* d : {&lc->l_q, &lc->l_qadd, &lc->l_bm_new, &lc->l_wc_new, &lc->l_wp_new, &lc->l_bm_m, &lc->l_wp_m, &lc->l_wp_q})
         PMS_CUDA(lc, d->ensure(4 * (W + 1)));
-    for (DBuf* d : {&lc->l_vlist_new, &lc->l_vlist_m, &lc->l_field_m, &lc->l_qlist})
+    for (DBuf* d : {&lc->l_vlist_new, &lc->l_vlist_m, &lc->l_qlist})
         PMS_CUDA(lc, d->ensure(4 * S));
     // the buffers that trade places with these in the rounds must be as large
     PMS_CUDA(lc, lc->bm.ensure(4 * (W + 1)));

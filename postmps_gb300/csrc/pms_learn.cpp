@@ -164,15 +164,11 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
         if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
         nv_bound = std::min<uint64_t>(nv_bound + nnew_bound, (uint64_t)c->grid.sc_size);
         PMS_CUDA(c, c->l_vlist_m.ensure(4 * (nv_bound + 1)));
-        PMS_CUDA(c, c->l_field_m.ensure(4 * (nv_bound + 1)));
         if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
-            return st;
-        if ((st = launch_field_gather(c, c->l_vlist_m.as<uint32_t>(), &cnt->nv, (uint32_t)nv_bound, c->l_field_m.as<float>())))
             return st;
         std::swap(c->bm, c->l_bm_m);
         std::swap(c->wprefix, c->l_wp_m);
         std::swap(c->vlist, c->l_vlist_m);
-        std::swap(c->field, c->l_field_m);
         // border check of the queued cubes, now evaluated; the next queue goes into l_q
         PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
         PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
@@ -189,6 +185,9 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     }
     c->nv = c->h_counters->nv;
     if ((st = ensure_band_buffers(c, c->nv))) return st;
+    // the band-order field of the final vertex set (the rounds work on the dense field)
+    if (c->l_iters && c->nv && (st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, c->nv, c->field.as<float>())))
+        return st;
     c->mc_classified = (added == 0);           // the last full check classified the final vertex set
     c->have_field = true;
     mark_stage(c, kStageField + 1);
