@@ -415,9 +415,20 @@ __global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a,
 // neighbour is a valid cube too; if not all of the neighbour's corners have a
 // field value yet, the neighbour cube is queued.  One thread per valid cube
 // of the classification ({vertex id, case} records of the compaction).
+// Queue cube nid once: its bit in qadd, the count, and (when qlist is given)
+// the list entry, kept while the list has room (the count tells the caller).
+__device__ __forceinline__ void queue_cube(uint32_t nid, uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
+                                           uint32_t* __restrict__ qlist, uint32_t qcap) {
+    const uint32_t bit = 1u << (nid & 31u);
+    const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
+    if (old & bit) return;
+    const uint32_t slot = atomicAdd(n_added, 1u);
+    if (qlist && slot < qcap) qlist[slot] = nid;
+}
+
 __global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
                                                 const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
-                                                uint32_t* __restrict__ n_added) {
+                                                uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist, uint32_t qcap) {
     const uint32_t n = cnt->nvalid;
     const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
     // face masks over the corner order {000,001,011,010,100,101,111,110} (x,y,z)
@@ -441,10 +452,7 @@ __global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restr
                 const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
                 all = all && ((vbm[c >> 5] >> (c & 31u)) & 1u);
             }
-            if (all) continue;
-            const uint32_t bit = 1u << (nid & 31u);
-            const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
-            if (!(old & bit)) atomicAdd(n_added, 1u);
+            if (!all) queue_cube(nid, qadd, n_added, qlist, qcap);
         }
     }
 }
@@ -456,7 +464,8 @@ __global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restr
 __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes,
                                                      uint32_t n_host, const uint32_t* __restrict__ n_dev,
                                                      const uint32_t* __restrict__ vbm, const float* __restrict__ fdense,
-                                                     uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added) {
+                                                     uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
+                                                     uint32_t* __restrict__ qlist, uint32_t qcap) {
     const uint32_t n = n_dev ? *n_dev : n_host;
     const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
     const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
@@ -488,10 +497,25 @@ __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const u
                 const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
                 have = have && ((vbm[c >> 5] >> (c & 31u)) & 1u);
             }
-            if (have) continue;
-            const uint32_t bit = 1u << (nid & 31u);
-            const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
-            if (!(old & bit)) atomicAdd(n_added, 1u);
+            if (!have) queue_cube(nid, qadd, n_added, qlist, qcap);
+        }
+    }
+}
+
+// The corners of queued cubes that have no field value yet: set in the vertex
+// bitmap and appended to vnew (one entry per new vertex, in no fixed order).
+__global__ void __launch_bounds__(256) k_queue_corners(KGrid g, const uint32_t* __restrict__ cubes, uint32_t n,
+                                                       uint32_t* __restrict__ vbm, uint32_t* __restrict__ vnew,
+                                                       uint32_t* __restrict__ n_new) {
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t id = cubes[t];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t c = id + (uint32_t)(k & 1) + (uint32_t)((k >> 1) & 1) * rx + (uint32_t)(k >> 2) * rxy;
+            const uint32_t bit = 1u << (c & 31u);
+            if (atomicOr(&vbm[c >> 5], bit) & bit) continue;
+            vnew[atomicAdd(n_new, 1u)] = c;      // at most 8 n entries
         }
     }
 }
@@ -823,21 +847,29 @@ pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, ui
 
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 
-pms_status launch_border(pms_ctx* ctx, uint32_t* qadd) {
+pms_status launch_border(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist, uint32_t qcap) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     // ctx->nv bounds the valid cubes; the kernel reads their count
     k_border<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), ctx->bm.as<uint32_t>(), qadd,
-                                                              &cnt->l_added);
+                                                              &cnt->l_added, qlist, qcap);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
-pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd, const uint32_t* n_dev) {
+pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd, const uint32_t* n_dev,
+                              uint32_t* qlist, uint32_t qcap) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, n_dev, ctx->bm.as<uint32_t>(),
-                                                              ctx->fdense.as<float>(), qadd, &cnt->l_added);
+                                                              ctx->fdense.as<float>(), qadd, &cnt->l_added, qlist, qcap);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* vnew, uint32_t* n_new) {
+    const KGrid g = kgrid_of(ctx->grid);
+    k_queue_corners<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, cubes, n, ctx->bm.as<uint32_t>(), vnew, n_new);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

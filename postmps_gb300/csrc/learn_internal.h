@@ -40,11 +40,15 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
 pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
                                uint32_t* wcount);
 pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount);
-pms_status launch_border(pms_ctx* ctx, uint32_t* qadd);
+// border checks queue cubes in qadd (a bitmap) and, when qlist is given, in a
+// list of at most qcap entries; the count (l_added) may exceed qcap
+pms_status launch_border(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist = nullptr, uint32_t qcap = 0);
+// corners of n queued cubes not yet in the vertex bitmap: set there and appended to vnew
+pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* vnew, uint32_t* n_new);
 pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
 // n: the list length, or a bound when n_dev holds it on the device
 pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd,
-                              const uint32_t* n_dev = nullptr);
+                              const uint32_t* n_dev = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount);
 pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x);
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,

@@ -147,7 +147,7 @@ struct pms_ctx {
     // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
     pms::DBuf l_dens, l_clist;   // bf16 coarse density pairs (padded grid), candidate cube records
     pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
-              l_field_new, l_vlist_m, l_cand, l_logit, l_label, l_qlist, l_wp_q;
+              l_field_new, l_vlist_m, l_qnext, l_cand, l_logit, l_label, l_qlist, l_wp_q;
     bool have_model = false, band_learned = false, mc_classified = false;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;

@@ -99,11 +99,6 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     pms_status st;
     PMS_CUDA(c, c->l_q.ensure(4 * (W + 1)));
     PMS_CUDA(c, c->l_qadd.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_bm_new.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_wc_new.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_wp_new.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_bm_m.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_wp_m.ensure(4 * (W + 1)));
     if ((st = zero_learn_counters(c))) return st;
     // predicted cubes -> their corners -> vertex list
     if ((st = launch_coarse_counts(c))) return st;
@@ -117,71 +112,75 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     c->have_band = true;
     mark_stage(c, kStageBand + 1);
     // exact field at those vertices, then the border check until no cube is missing:
-    // a full check over every valid cube, then rounds that evaluate the queued cubes'
-    // new corners and check only those cubes; one synchronisation per round
+    // a full check over every valid cube queues the cubes across crossed faces whose
+    // corners lack a value; each round evaluates the queued cubes' new corners (set in
+    // the vertex bitmap and listed as they are found) and checks only those cubes, one
+    // synchronisation per round; when a round queues nothing, the sorted vertex list
+    // is rebuilt from the bitmap and one more full check catches cubes whose corners
+    // other cubes' rounds completed
     if (c->nv && (st = launch_field(c))) return st;
     uint64_t nv_bound = c->nv;                 // host bound on the vertex count while rounds run
     uint32_t added = 0;
+    // queue lists: grow-only; a check whose queue overflowed its list runs again
+    auto qcap_of = [](const DBuf& d) { return (uint32_t)std::min<size_t>(d.cap / 4, 0xffffffffu); };
+    PMS_CUDA(c, c->l_qlist.ensure(4 * std::max<size_t>(1u << 16, nv_bound / 16)));
+    PMS_CUDA(c, c->l_qnext.ensure(c->l_qlist.cap));
+    auto run_check = [&](auto&& launch) -> pms_status {
+        pms_status s2;
+        for (int pass = 0; pass < 2; ++pass) {
+            PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
+            PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
+            if ((s2 = launch())) return s2;
+            if ((s2 = sync_counters(c))) return s2;
+            added = c->h_counters->l_added;
+            if (added <= qcap_of(c->l_qnext)) return PMS_OK;
+            PMS_CUDA(c, c->l_qnext.ensure(4 * (size_t)added));
+        }
+        return pms_fail(c, PMS_ERR_CAPACITY, "border queue outgrew its list");
+    };
     auto full_check = [&]() -> pms_status {
         pms_status s2;
         c->nv = (uint32_t)nv_bound;
         if ((s2 = launch_mc_classify(c))) return s2;
-        PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
-        PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-        if ((s2 = launch_border(c, c->l_qadd.as<uint32_t>()))) return s2;
-        if ((s2 = sync_counters(c))) return s2;
-        added = c->h_counters->l_added;
+        if ((s2 = run_check([&] { return launch_border(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
+                                                       qcap_of(c->l_qnext)); })))
+            return s2;
         c->nv = c->h_counters->nv;
         nv_bound = c->nv;
+        std::swap(c->l_qlist, c->l_qnext);
         return PMS_OK;
     };
     if (c->nv && (st = full_check())) return st;
     for (uint32_t round = 0; added && round < kMaxBorderRounds; ++round) {
         c->l_nadded += added;
         c->l_iters++;
-        // the queued cubes as a list
-        if ((st = launch_popc(c, c->l_qadd.as<uint32_t>(), c->l_wc_new.as<uint32_t>()))) return st;
-        PMS_CUDA(c, c->l_wp_q.ensure(4 * (W + 1)));
-        if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), W, nullptr))) return st;
-        PMS_CUDA(c, c->l_qlist.ensure(4 * (size_t)added));
-        if ((st = launch_bits_list(c, c->l_qadd.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), c->l_qlist.as<uint32_t>())))
-            return st;
-        // their corners without a value yet, and the field there
-        if ((st = launch_cube_corners(c, c->l_qadd.as<uint32_t>(), c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(),
-                                      c->l_wc_new.as<uint32_t>())))
-            return st;
-        if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
-        const uint64_t nnew_bound = std::min<uint64_t>(8ull * added, (uint64_t)c->grid.sc_size);
+        const uint32_t nq = added;
+        // the queued cubes' corners without a value, and the field there
+        const uint64_t nnew_bound = std::min<uint64_t>(8ull * nq, (uint64_t)c->grid.sc_size);
         PMS_CUDA(c, c->l_vlist_new.ensure(4 * (nnew_bound + 1)));
-        if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
+        PMS_CUDA(c, cudaMemsetAsync(&cnt->l_nnew, 0, sizeof(uint32_t), c->stream));
+        if ((st = launch_queue_corners(c, c->l_qlist.as<uint32_t>(), nq, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew)))
             return st;
         if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, (uint32_t)nnew_bound, nullptr)))
             return st;
-        // merged vertex set: bitmap, ranks, list, field
-        if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
-                                 c->wcount.as<uint32_t>())))
-            return st;
-        if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
         nv_bound = std::min<uint64_t>(nv_bound + nnew_bound, (uint64_t)c->grid.sc_size);
-        PMS_CUDA(c, c->l_vlist_m.ensure(4 * (nv_bound + 1)));
-        if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
+        // border check of the queued cubes, now evaluated
+        if ((st = run_check([&] { return launch_border_list(c, c->l_qlist.as<uint32_t>(), nq, c->l_qadd.as<uint32_t>(),
+                                                            nullptr, c->l_qnext.as<uint32_t>(), qcap_of(c->l_qnext)); })))
             return st;
-        std::swap(c->bm, c->l_bm_m);
-        std::swap(c->wprefix, c->l_wp_m);
-        std::swap(c->vlist, c->l_vlist_m);
-        // border check of the queued cubes, now evaluated; the next queue goes into l_q
-        PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
-        PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-        if ((st = launch_border_list(c, c->l_qlist.as<uint32_t>(), added, c->l_q.as<uint32_t>()))) return st;
-        std::swap(c->l_q, c->l_qadd);
-        if ((st = sync_counters(c))) return st;
-        added = c->h_counters->l_added;
+        std::swap(c->l_qlist, c->l_qnext);
         if (!added) {
-            // cubes whose corners were completed by other cubes' rounds: one full check
-            if ((st = ensure_band_buffers(c, (uint32_t)c->h_counters->nv))) return st;
-            nv_bound = c->h_counters->nv;
+            // the sorted vertex list of the grown set, then one full check
+            if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
+            if ((st = finish_vertex_set(c))) return st;
+            nv_bound = c->nv;
             if ((st = full_check())) return st;
         }
+    }
+    if (added) {
+        // round limit reached: the vertex list still covers every value computed
+        if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
+        if ((st = finish_vertex_set(c))) return st;
     }
     c->nv = c->h_counters->nv;
     if ((st = ensure_band_buffers(c, c->nv))) return st;
