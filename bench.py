@@ -274,16 +274,12 @@ def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse
         ctx.run_frame()
 
     def step_e2e():
-        # the user's calls: upload from pinned host memory, reconstruct, read the
-        # triangle soup (and the live diffuse particles) back into pinned memory
+        # the user's calls: upload from pinned host memory, reconstruct with the
+        # triangle soup streamed into pinned host memory while the diffuse stage
+        # runs, wait for it, read the live diffuse particles back
         ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
         ctx.run_frame()
-        nv = C.c_uint64()
-        pms.lib().pms_download_mesh(ctx.handle, None, None, 0, C.byref(nv))
-        buf = host.get("mesh")
-        if buf is None or buf.numel() < 3 * nv.value:
-            buf = host["mesh"] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
-        ctx._call("pms_download_mesh", buf.data_ptr(), None, buf.numel() // 3, C.byref(nv))
+        host["n_mesh"] = ctx.wait_mesh()
         if diffuse:
             host["diffuse"] = ctx.diffuse_particles(-1)
 
@@ -304,9 +300,13 @@ def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse
     ms = timer(step_device, args.steps, collect)
     launches = (ctx.launches - l0) // max(1, args.steps)
     clk = clocks.stop() if clocks else None
+    # the host mesh buffer (pinned), sized from the frame's mesh
+    host["mesh"] = torch.empty(max(3, int(3 * counts["n_mesh_vertices"] * 1.25)), dtype=torch.float32).pin_memory()
+    ctx.stream_mesh_to_host(host["mesh"].data_ptr(), None, host["mesh"].numel() // 3)
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
     ms_e2e = timer(step_e2e, args.steps)
+    ctx.stream_mesh_to_host(0, None, 0)
     return {"ms": ms, "ms_e2e": ms_e2e, "counts": counts, "sp_size": grid.sp_size, "sc_size": grid.sc_size,
             "launches": launches, "clocks": clk, "stage_ms": {k: v / args.steps for k, v in stage_sum.items()},
             "h2d": 28 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(counts["n_diffuse"])}

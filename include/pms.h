@@ -198,6 +198,17 @@ pms_status pms_get_grid(pms_ctx* ctx, pms_grid* out);
  * (FileData.cpp:1297-1300).  *n_vertices receives the count even on PMS_ERR_CAPACITY. */
 pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices,
                              uint64_t* n_vertices);
+/* Registers host buffers (page-locked, e.g. cudaHostAlloc or cudaHostRegister,
+ * for the copy to overlap) that every following pms_marching_cubes fills with
+ * the frame's triangle soup on a copy stream of its own, while the stages after
+ * it (diffuse generation) run; nrm_xyz may be NULL, pos_xyz NULL unregisters.
+ * pms_wait_mesh blocks until the copy has landed and returns the vertex count
+ * (PMS_ERR_CAPACITY, with the count, when cap_vertices was too small; nothing
+ * is copied then).  The buffers must stay valid until that wait.  No
+ * counterpart in the reference, which copies the soup back with a blocking
+ * cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
+pms_status pms_stream_mesh_to_host(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices);
+pms_status pms_wait_mesh(pms_ctx* ctx, uint64_t* n_vertices);
 /* The scalar values of the mesh vertices (any array may be NULL): velocity xyz,
  * its length and the density (the reference's ScalarValue). */
 pms_status pms_download_scalar_values(pms_ctx* ctx, float* vel_xyz, float* vel_len, float* rhop, uint64_t cap,

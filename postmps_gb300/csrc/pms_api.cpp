@@ -98,6 +98,9 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
+    if (c->mesh_ready) cudaEventDestroy(c->mesh_ready);
+    if (c->mesh_copied) cudaEventDestroy(c->mesh_copied);
     pms_batch_release(c);
     release_all(c);
     for (int i = 0; i <= kNumStages; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -368,9 +371,25 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         c->nvalid = c->h_counters->nvalid;
         c->nmesh = c->h_counters->nmesh;
         const size_t M = c->nmesh ? c->nmesh : 1;
+        // the previous frame's mesh may still be on its way to the host
+        if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
         PMS_CUDA(c, c->vert.ensure(12 * M));
         PMS_CUDA(c, c->vnorm.ensure(12 * M));
         if ((st = launch_mc_emit(c))) return st;
+    }
+    if (c->out_pos) {
+        // stream the mesh to the registered host buffers while the next stages run
+        c->out_n = c->nmesh;
+        c->out_overflow = c->nmesh > c->out_cap;
+        if (c->nmesh && !c->out_overflow) {
+            PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
+            PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
+            PMS_CUDA(c, cudaMemcpyAsync(c->out_pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
+            if (c->out_nrm)
+                PMS_CUDA(c, cudaMemcpyAsync(c->out_nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
+        }
+        PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
+        c->out_pending = true;
     }
     c->have_mc = true;
     mark(c, kStageMc + 1);
@@ -485,6 +504,36 @@ extern "C" pms_status pms_download_mesh(pms_ctx* c, float* pos, float* nrm, uint
     PMS_CUDA(c, cudaMemcpyAsync(pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     if (nrm) PMS_CUDA(c, cudaMemcpyAsync(nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_stream_mesh_to_host(pms_ctx* c, float* pos, float* nrm, uint64_t cap) {
+    if (!c || (!pos && nrm)) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
+    c->out_pending = false;
+    if (pos && !c->copy_stream) {
+        PMS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        PMS_CUDA(c, cudaEventCreateWithFlags(&c->mesh_ready, cudaEventDisableTiming));
+        PMS_CUDA(c, cudaEventCreateWithFlags(&c->mesh_copied, cudaEventDisableTiming));
+    }
+    c->out_pos = pos;
+    c->out_nrm = pos ? nrm : nullptr;
+    c->out_cap = pos ? cap : 0;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_wait_mesh(pms_ctx* c, uint64_t* n_vertices) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->out_pos) return pms_fail(c, PMS_ERR_STATE, "pms_wait_mesh without pms_stream_mesh_to_host");
+    if (!c->out_pending) return pms_fail(c, PMS_ERR_STATE, "no mesh streamed since the last wait");
+    cudaSetDevice(c->device);
+    PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
+    c->out_pending = false;
+    if (n_vertices) *n_vertices = c->out_n;
+    if (c->out_overflow)
+        return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices, the host buffers %llu",
+                        (unsigned long long)c->out_n, (unsigned long long)c->out_cap);
     return PMS_OK;
 }
 

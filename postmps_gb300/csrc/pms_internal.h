@@ -113,6 +113,13 @@ struct pms_ctx {
     pms_grid grid;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // mesh streamed to registered host buffers on a copy stream while later stages run
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t mesh_ready = nullptr, mesh_copied = nullptr;
+    float* out_pos = nullptr;
+    float* out_nrm = nullptr;
+    uint64_t out_cap = 0, out_n = 0;
+    bool out_pending = false, out_overflow = false;
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;

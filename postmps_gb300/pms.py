@@ -486,6 +486,19 @@ class Context:
             self._call("pms_download_mesh", _ptr(pos), _ptr(nrm), m, C.byref(n))
         return pos, nrm
 
+    def stream_mesh_to_host(self, pos_ptr: int, nrm_ptr: int | None, cap_vertices: int) -> None:
+        """Register page-locked host buffers (raw addresses) that each frame's
+        marching cubes fill on a copy stream while the later stages run;
+        pos_ptr 0 unregisters."""
+        self._call("pms_stream_mesh_to_host", C.c_void_p(pos_ptr or None), C.c_void_p(nrm_ptr or None),
+                   C.c_uint64(cap_vertices))
+
+    def wait_mesh(self) -> int:
+        """Wait for the streamed mesh of the last frame; returns its vertex count."""
+        n = C.c_uint64()
+        self._call("pms_wait_mesh", C.byref(n))
+        return n.value
+
     def diffuse_particles(self, type_: int = -1) -> dict:
         n = C.c_uint32()
         st = lib().pms_download_diffuse(self._h, type_, None, None, None, None, None, None, None, 0, C.byref(n))

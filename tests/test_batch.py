@@ -2,7 +2,8 @@
 same counts and the same triangle soup, bit for bit, as the frame run alone;
 the graph is captured once and relaunched while the frames' grids stay the
 same and captured again when they change; the learned band in a batch equals
-the learned band frame by frame."""
+the learned band frame by frame.  Also the pipelined output: a mesh streamed
+to pinned host memory during the later stages equals the downloaded one."""
 from __future__ import annotations
 
 import numpy as np
@@ -118,3 +119,34 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
             assert np.array_equal(mesh, ref_mesh)
         with pytest.raises(pms.PmsError):
             ctx.set_tune({"field_threads": 96, "field_waves": 1, "density_threads": 64, "moments_threads": 64})
+
+
+@pytest.mark.gpu
+def test_streamed_mesh_equals_download(pms_lib):
+    """pms_stream_mesh_to_host: the soup copied to pinned host memory on the copy
+    stream, frame after frame, equals pms_download_mesh's; a buffer that is too
+    small reports the count with PMS_ERR_CAPACITY."""
+    import torch
+    pms = pms_lib
+    frames = _frames(3)
+    with _ctx(pms, 0.02) as ctx:
+        buf = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
+        nrm = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
+        ctx.stream_mesh_to_host(buf.data_ptr(), nrm.data_ptr(), buf.numel() // 3)
+        for fr in frames:
+            ctx.upload(*fr)
+            ctx.run_frame()
+            n = ctx.wait_mesh()
+            pos_ref, nrm_ref = ctx.mesh(normals=True)
+            assert n == len(pos_ref) > 0
+            assert np.array_equal(buf.numpy()[: 3 * n].reshape(-1, 3), pos_ref)
+            assert np.array_equal(nrm.numpy()[: 3 * n].reshape(-1, 3), nrm_ref)
+        small = torch.empty(30, dtype=torch.float32).pin_memory()
+        ctx.stream_mesh_to_host(small.data_ptr(), None, 10)
+        ctx.upload(*frames[0])
+        ctx.run_frame()
+        with pytest.raises(pms.PmsError):
+            ctx.wait_mesh()
+        ctx.stream_mesh_to_host(0, None, 0)
+        with pytest.raises(pms.PmsError):
+            ctx.wait_mesh()
