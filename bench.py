@@ -309,7 +309,7 @@ def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse
     ctx.stream_mesh_to_host(0, None, 0)
     return {"ms": ms, "ms_e2e": ms_e2e, "counts": counts, "sp_size": grid.sp_size, "sc_size": grid.sc_size,
             "launches": launches, "clocks": clk, "stage_ms": {k: v / args.steps for k, v in stage_sum.items()},
-            "h2d": 28 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(counts["n_diffuse"])}
+            "h2d": 24 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(counts["n_diffuse"])}
 
 
 def batch_arm(pms, ctx, frames, learned: bool, args, timer, torch, clocks=None) -> dict:

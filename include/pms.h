@@ -164,9 +164,11 @@ pms_status pms_set_stream(pms_ctx* ctx, void* cuda_stream);
  * replaced by this grow-only reservation. */
 pms_status pms_reserve(pms_ctx* ctx, uint32_t max_particles, uint64_t max_scalar_vertices);
 
-/* Uploads one frame from host arrays (vel and rhop may be NULL -> zeros).
- * Replaces FileData::loadFluidFile + GPUmemory::memAlcandCpy_fluid
- * (FileData.cpp:214-305, GPUmemory.cpp:47-72). */
+/* Uploads one frame from host arrays (vel may be NULL -> zeros).  rhop may be
+ * NULL and is not read: every stage uses the density recomputed from the
+ * positions, as the reference overwrites Rhop before its first use
+ * (Anisotropic_kernel.cuh:212).  Replaces FileData::loadFluidFile +
+ * GPUmemory::memAlcandCpy_fluid (FileData.cpp:214-305, GPUmemory.cpp:47-72). */
 pms_status pms_upload_particles(pms_ctx* ctx, const float* pos_xyz, const float* vel_xyz,
                                 const float* rhop, uint32_t n);
 /* Same, from device-resident arrays (copied device-to-device on the context stream). */
@@ -204,7 +206,10 @@ pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint6
  * it (diffuse generation) run; nrm_xyz may be NULL, pos_xyz NULL unregisters.
  * pms_wait_mesh blocks until the copy has landed and returns the vertex count
  * (PMS_ERR_CAPACITY, with the count, when cap_vertices was too small; nothing
- * is copied then).  The buffers must stay valid until that wait.  No
+ * is copied then).  The buffers must stay valid until that wait, and the next
+ * frame's marching cubes writes them again.  When no stage follows the marching
+ * cubes (diffuse generation off) and the GPU can address the buffers (page-
+ * locked memory), the triangle emission writes them itself.  No
  * counterpart in the reference, which copies the soup back with a blocking
  * cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
 pms_status pms_stream_mesh_to_host(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices);

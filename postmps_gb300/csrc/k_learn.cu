@@ -415,45 +415,16 @@ __global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a,
 // neighbour is a valid cube too; if not all of the neighbour's corners have a
 // field value yet, the neighbour cube is queued.  One thread per valid cube
 // of the classification ({vertex id, case} records of the compaction).
-// Queue cube nid once: its bit in qadd, the count, and (when qlist is given)
-// the list entry, kept while the list has room (the count tells the caller).
-__device__ __forceinline__ void queue_cube(uint32_t nid, uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
-                                           uint32_t* __restrict__ qlist, uint32_t qcap) {
-    const uint32_t bit = 1u << (nid & 31u);
-    const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
-    if (old & bit) return;
-    const uint32_t slot = atomicAdd(n_added, 1u);
-    if (qlist && slot < qcap) qlist[slot] = nid;
-}
-
 __global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
                                                 const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
                                                 uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist, uint32_t qcap) {
     const uint32_t n = cnt->nvalid;
-    const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
-    // face masks over the corner order {000,001,011,010,100,101,111,110} (x,y,z)
-    const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
-    const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const uint4 cr = __ldg(&cube[t]);
         const uint32_t cs = cr.y, id = cr.x;
         const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-            const uint32_t m = cs & mask[f];
-            if (m == 0u || m == mask[f]) continue;
-            const int X = x + dxs[f], Y = y + dys[f], Z = z + dzs[f];
-            if (X < 0 || Y < 0 || Z < 0 || X > (int)rx - 2 || Y > (int)ry - 2 || Z > (int)rz - 2) continue;
-            const uint32_t nid = (uint32_t)Z * rxy + (uint32_t)Y * rx + (uint32_t)X;
-            // corners (x,y,z) + {0,1}^3
-            bool all = true;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
-                all = all && ((vbm[c >> 5] >> (c & 31u)) & 1u);
-            }
-            if (!all) queue_cube(nid, qadd, n_added, qlist, qcap);
-        }
+        border_faces(g, x, y, z, cs, vbm, qadd, n_added, qlist, qcap);
     }
 }
 
@@ -467,9 +438,7 @@ __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const u
                                                      uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
                                                      uint32_t* __restrict__ qlist, uint32_t qcap) {
     const uint32_t n = n_dev ? *n_dev : n_host;
-    const uint32_t rx = g.scres[0], ry = g.scres[1], rz = g.scres[2], rxy = rx * ry;
-    const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
-    const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
+    const uint32_t rx = g.scres[0], rxy = rx * g.scres[1];
     // corner order {000,001,011,010,100,101,111,110} as (x, y, z) offsets
     const uint32_t cx[8] = {0, 0, 0, 0, 1, 1, 1, 1}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 1, 1, 0, 0, 1, 1, 0};
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -484,21 +453,7 @@ __global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const u
         }
         if (!all || cs == 0u || cs == 255u) continue;
         const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-#pragma unroll
-        for (int f = 0; f < 6; ++f) {
-            const uint32_t m = cs & mask[f];
-            if (m == 0u || m == mask[f]) continue;
-            const int X = x + dxs[f], Y = y + dys[f], Z = z + dzs[f];
-            if (X < 0 || Y < 0 || Z < 0 || X > (int)rx - 2 || Y > (int)ry - 2 || Z > (int)rz - 2) continue;
-            const uint32_t nid = (uint32_t)Z * rxy + (uint32_t)Y * rx + (uint32_t)X;
-            bool have = true;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const uint32_t c = nid + (uint32_t)(k & 1) + ((uint32_t)((k >> 1) & 1) * rx) + ((uint32_t)(k >> 2) * rxy);
-                have = have && ((vbm[c >> 5] >> (c & 31u)) & 1u);
-            }
-            if (!have) queue_cube(nid, qadd, n_added, qlist, qcap);
-        }
+        border_faces(g, x, y, z, cs, vbm, qadd, n_added, qlist, qcap);
     }
 }
 

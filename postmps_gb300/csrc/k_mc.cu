@@ -73,11 +73,15 @@ pms_status upload_mc_tables(pms_ctx* ctx) {
     return PMS_OK;
 }
 
-// detectValidSurfaceCubes (6-argument version)
+// detectValidSurfaceCubes (6-argument version); with qadd set, also the learned
+// band's border check of every valid cube (border_faces)
+template <bool BORDER>
 __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, const Counters* __restrict__ cnt,
                                                           const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ bm,
                                                           const float* __restrict__ fdense, uint32_t* __restrict__ mc_case,
-                                                          unsigned long long* __restrict__ mc_key) {
+                                                          unsigned long long* __restrict__ mc_key, uint32_t* __restrict__ qadd,
+                                                          uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist,
+                                                          uint32_t qcap) {
     const uint32_t nv = cnt->nv;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint64_t nbits = g.sc_size;
@@ -98,6 +102,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, co
         else cs = 0;
         mc_case[t] = cs;
         mc_key[t] = nvert ? ((1ull << 32) | nvert) : 0ull;
+        if (BORDER && nvert) border_faces(g, (int)x, (int)y, (int)z, cs, bm, qadd, n_added, qlist, qcap);
     }
 }
 
@@ -146,7 +151,8 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                                                       const uint4* __restrict__ cube, const float* __restrict__ fdense,
                                                       float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
-                                                      unsigned long long cap) {
+                                                      unsigned long long cap, float* __restrict__ hvert,
+                                                      float* __restrict__ hnorm) {
     __shared__ float stage[kEmitWarps][kEmitStage];
     const uint32_t nvalid = cnt->nvalid;
     // batched frames write behind the earlier frames' vertices, within cap
@@ -219,24 +225,37 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
         // whole lines: positions, then normals
         for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
             const uint32_t v = i / 3u, c = i - 3u * v;
-            vert[3 * (size_t)w0 + i] = st[6 * v + c];
+            const float x = st[6 * v + c];
+            vert[3 * (size_t)w0 + i] = x;
+            if (hvert) hvert[3 * (size_t)w0 + i] = x;
         }
         if (vnorm)
             for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
                 const uint32_t v = i / 3u, c = i - 3u * v;
-                vnorm[3 * (size_t)w0 + i] = st[6 * v + 3 + c];
+                const float x = st[6 * v + 3 + c];
+                vnorm[3 * (size_t)w0 + i] = x;
+                if (hnorm) hnorm[3 * (size_t)w0 + i] = x;
             }
         __syncwarp();
     }
 }
 
-pms_status launch_mc_classify(pms_ctx* ctx) {
+pms_status launch_mc_cases(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist, uint32_t qcap) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
-    k_mc_classify<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(),
-        ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
+    auto go = [&](auto kern) {
+        kern<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
+            g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(),
+            ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>(), qadd, &cnt->l_added, qlist, qcap);
+    };
+    if (qadd) go(k_mc_classify<true>);
+    else go(k_mc_classify<false>);
     PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_mc_compact(pms_ctx* ctx) {
+    Counters* cnt = ctx->counters.as<Counters>();
     // ctx->nv may be a bound (batched frames): the scan stops at the device count
     pms_status st = scan_u64(ctx, ctx->mc_key.as<unsigned long long>(), ctx->mc_off.as<unsigned long long>(), ctx->nv,
                              ctx->tmp.as<unsigned long long>(), &cnt->nv);
@@ -248,6 +267,11 @@ pms_status launch_mc_classify(pms_ctx* ctx) {
         ctx->mc_case.as<uint32_t>(), ctx->valid.as<uint32_t>(), ctx->cube.as<uint4>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
+}
+
+pms_status launch_mc_classify(pms_ctx* ctx) {
+    pms_status st = launch_mc_cases(ctx);
+    return st ? st : launch_mc_compact(ctx);
 }
 
 // ---------------------------------------------------------------------------
@@ -319,17 +343,18 @@ pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long lo
 }
 
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap) {
+                             unsigned long long cap, float* hvert, float* hnorm) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap);
+        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, hvert,
+        hnorm);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
-pms_status launch_mc_emit(pms_ctx* ctx) {
-    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull);
+pms_status launch_mc_emit(pms_ctx* ctx, float* hvert, float* hnorm) {
+    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, hvert, hnorm);
 }
 
 }  // namespace pms

@@ -258,13 +258,15 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
         PMS_CUDA(c, cudaMemcpyAsync(c->in_pos.p, pos, 12 * (size_t)n, kind, c->stream));
         if (vel) PMS_CUDA(c, cudaMemcpyAsync(c->in_vel.p, vel, 12 * (size_t)n, kind, c->stream));
         else PMS_CUDA(c, cudaMemsetAsync(c->in_vel.p, 0, 12 * (size_t)n, c->stream));
-        if (rho) PMS_CUDA(c, cudaMemcpyAsync(c->in_rho.p, rho, 4 * (size_t)n, kind, c->stream));
-        else PMS_CUDA(c, cudaMemsetAsync(c->in_rho.p, 0, 4 * (size_t)n, c->stream));
+        // the input density is not read: every stage uses the density recomputed from
+        // the positions (the reference overwrites Rhop before its first use,
+        // Anisotropic_kernel.cuh:212), so it is not copied
+        (void)rho;
     }
     c->n = n;
     c->have_particles = true;
     c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = false;
-    c->band_learned = c->mc_classified = false;
+    c->band_learned = c->mc_classified = c->mc_compacted = false;
     c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     c->ns = c->nv = c->nvalid = 0;
     c->nmesh = 0;
@@ -331,7 +333,7 @@ extern "C" pms_status pms_band(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
     cudaSetDevice(c->device);
-    c->band_learned = c->mc_classified = false;
+    c->band_learned = c->mc_classified = c->mc_compacted = false;
     c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
     pms_status st;
@@ -363,11 +365,15 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     cudaSetDevice(c->device);
     c->nvalid = 0;
     c->nmesh = 0;
+    c->out_direct = false;
     if (c->nv) {
         pms_status st;
-        // the learned band's last border check already classified the final vertex set
-        if (!c->mc_classified && (st = launch_mc_classify(c))) return st;
-        if (!c->mc_classified && (st = sync_counters(c))) return st;
+        // the learned band's last border check already computed the final vertex set's cases
+        if (!c->mc_classified && (st = launch_mc_cases(c))) return st;
+        if (!(c->mc_classified && c->mc_compacted)) {
+            if ((st = launch_mc_compact(c))) return st;
+            if ((st = sync_counters(c))) return st;
+        }
         c->nvalid = c->h_counters->nvalid;
         c->nmesh = c->h_counters->nmesh;
         const size_t M = c->nmesh ? c->nmesh : 1;
@@ -375,20 +381,26 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
         PMS_CUDA(c, c->vert.ensure(12 * M));
         PMS_CUDA(c, c->vnorm.ensure(12 * M));
-        if ((st = launch_mc_emit(c))) return st;
+        // when no stage follows, the emission writes the registered host buffers itself
+        // (over the host link, as the triangles are made); otherwise a copy stream moves
+        // the mesh while the next stages run
+        const bool direct = c->out_pos_dev && !c->cfg.is_diffuse && c->nmesh <= c->out_cap;
+        if ((st = launch_mc_emit(c, direct ? c->out_pos_dev : nullptr, direct ? c->out_nrm_dev : nullptr))) return st;
+        c->out_direct = direct;
     }
     if (c->out_pos) {
-        // stream the mesh to the registered host buffers while the next stages run
         c->out_n = c->nmesh;
         c->out_overflow = c->nmesh > c->out_cap;
-        if (c->nmesh && !c->out_overflow) {
+        if (c->nmesh && !c->out_overflow && c->out_direct) {
+            PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->stream));
+        } else if (c->nmesh && !c->out_overflow) {
             PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
             PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
             PMS_CUDA(c, cudaMemcpyAsync(c->out_pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
             if (c->out_nrm)
                 PMS_CUDA(c, cudaMemcpyAsync(c->out_nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
         }
-        PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
+        if (!c->out_direct || !c->nmesh || c->out_overflow) PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
         c->out_pending = true;
     }
     c->have_mc = true;
@@ -520,6 +532,18 @@ extern "C" pms_status pms_stream_mesh_to_host(pms_ctx* c, float* pos, float* nrm
     c->out_pos = pos;
     c->out_nrm = pos ? nrm : nullptr;
     c->out_cap = pos ? cap : 0;
+    // page-locked buffers the GPU can address directly (their device addresses)
+    c->out_pos_dev = c->out_nrm_dev = nullptr;
+    auto device_view = [&](float* h) -> float* {
+        cudaPointerAttributes a;
+        if (!h || cudaPointerGetAttributes(&a, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        return a.type == cudaMemoryTypeHost && a.devicePointer ? static_cast<float*>(a.devicePointer) : nullptr;
+    };
+    if (pos) {
+        c->out_pos_dev = device_view(pos);
+        c->out_nrm_dev = nrm ? device_view(nrm) : nullptr;
+        if (!c->out_pos_dev || (nrm && !c->out_nrm_dev)) c->out_pos_dev = c->out_nrm_dev = nullptr;
+    }
     return PMS_OK;
 }
 

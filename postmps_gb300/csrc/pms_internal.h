@@ -120,6 +120,9 @@ struct pms_ctx {
     float* out_nrm = nullptr;
     uint64_t out_cap = 0, out_n = 0;
     bool out_pending = false, out_overflow = false;
+    float* out_pos_dev = nullptr;    // device addresses of the host buffers when the GPU can write them
+    float* out_nrm_dev = nullptr;
+    bool out_direct = false;         // this frame's emission wrote them
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;
@@ -155,7 +158,7 @@ struct pms_ctx {
     pms::DBuf l_dens, l_clist;   // bf16 coarse density pairs (padded grid), candidate cube records
     pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
               l_field_new, l_vlist_m, l_qnext, l_cand, l_logit, l_label, l_qlist, l_wp_q;
-    bool have_model = false, band_learned = false, mc_classified = false;
+    bool have_model = false, band_learned = false, mc_classified = false, mc_compacted = false;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;
     // batched frames (pms_batch.cpp)
@@ -227,12 +230,17 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
 pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
+// marching-cube cases of the band vertices (with qadd set, also the learned band's
+// border check of every valid cube), then the scan and compaction; classify = both
+pms_status launch_mc_cases(pms_ctx* ctx, uint32_t* qadd = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);
+pms_status launch_mc_compact(pms_ctx* ctx);
 pms_status launch_mc_classify(pms_ctx* ctx);
-pms_status launch_mc_emit(pms_ctx* ctx);
+// hvert / hnorm: device addresses of host buffers that receive a second copy (may be null)
+pms_status launch_mc_emit(pms_ctx* ctx, float* hvert = nullptr, float* hnorm = nullptr);
 pms_status launch_scalar_values(pms_ctx* ctx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap);
+                             unsigned long long cap, float* hvert = nullptr, float* hnorm = nullptr);
 pms_status launch_diffuse(pms_ctx* ctx);
 pms_status upload_mc_tables(pms_ctx* ctx);
 

@@ -92,7 +92,7 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     cudaSetDevice(c->device);
     c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
     c->band_learned = true;
-    c->mc_classified = false;
+    c->mc_classified = c->mc_compacted = false;
     if (c->n == 0) { c->nv = 0; c->have_band = c->have_field = true; return PMS_OK; }
     Counters* cnt = c->counters.as<Counters>();
     const uint64_t W = words_of(c);
@@ -141,10 +141,17 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     auto full_check = [&]() -> pms_status {
         pms_status s2;
         c->nv = (uint32_t)nv_bound;
-        if ((s2 = launch_mc_classify(c))) return s2;
-        if ((s2 = run_check([&] { return launch_border(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
-                                                       qcap_of(c->l_qnext)); })))
+        // the cases of every cube with the border check of the valid ones; after border
+        // rounds the check is usually the last, so the scan and compaction the marching
+        // cubes need run before its synchronisation (the first check usually queues cubes)
+        const bool compact = c->l_iters > 0;
+        if ((s2 = run_check([&] {
+                 pms_status s3 = launch_mc_cases(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
+                                                 qcap_of(c->l_qnext));
+                 return (s3 || !compact) ? s3 : launch_mc_compact(c);
+             })))
             return s2;
+        c->mc_compacted = compact;
         c->nv = c->h_counters->nv;
         nv_bound = c->nv;
         std::swap(c->l_qlist, c->l_qnext);
@@ -187,7 +194,8 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     // the band-order field of the final vertex set (the rounds work on the dense field)
     if (c->l_iters && c->nv && (st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, c->nv, c->field.as<float>())))
         return st;
-    c->mc_classified = (added == 0);           // the last full check classified the final vertex set
+    c->mc_classified = (added == 0);           // the last full check computed the final vertex set's cases
+    c->mc_compacted = c->mc_classified && c->mc_compacted;
     c->have_field = true;
     mark_stage(c, kStageField + 1);
     return PMS_OK;

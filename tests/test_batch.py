@@ -17,13 +17,14 @@ def _frames(k, spacing=0.02):
             for f in range(k)]
 
 
-def _ctx(pms, spacing):
+def _ctx(pms, spacing, diffuse=False):
     from postmps_gb300 import synth
     import os
     import tempfile
     fd, path = tempfile.mkstemp(suffix=".txt")
     with os.fdopen(fd, "w") as f:
-        f.write(synth.config_text(**{"sim.particlespacing": spacing}))
+        f.write(synth.config_text(**{"sim.particlespacing": spacing,
+                                     "config.isdiffusegeneration": "true" if diffuse else "false"}))
     cfg = pms.load_config(path)
     os.unlink(path)
     return pms.Context(cfg, 0)
@@ -122,14 +123,17 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
 
 
 @pytest.mark.gpu
-def test_streamed_mesh_equals_download(pms_lib):
-    """pms_stream_mesh_to_host: the soup copied to pinned host memory on the copy
-    stream, frame after frame, equals pms_download_mesh's; a buffer that is too
-    small reports the count with PMS_ERR_CAPACITY."""
+@pytest.mark.parametrize("diffuse", [False, True])
+def test_streamed_mesh_equals_download(pms_lib, diffuse):
+    """pms_stream_mesh_to_host: the soup that reaches pinned host memory --
+    written by the emission itself (no stage after the marching cubes) or copied
+    on the copy stream while the diffuse stage runs -- equals pms_download_mesh's,
+    frame after frame; a buffer that is too small reports the count with
+    PMS_ERR_CAPACITY."""
     import torch
     pms = pms_lib
     frames = _frames(3)
-    with _ctx(pms, 0.02) as ctx:
+    with _ctx(pms, 0.02, diffuse) as ctx:
         buf = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
         nrm = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
         ctx.stream_mesh_to_host(buf.data_ptr(), nrm.data_ptr(), buf.numel() // 3)
