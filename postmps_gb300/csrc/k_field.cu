@@ -139,11 +139,21 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                 }
                 for (int x0 = X0; x0 < X1; x0 += 32) {
                     const int nx = min(X1 - x0, 32);
+                    // cells of the chunk inside some live vertex's range (a vertex past the
+                    // threshold needs only its window's first cell, which can sit well left
+                    // of the others' ranges)
+                    uint32_t need = 0u;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        const int a = max(xs[k] - x0, 0), b = min(xe[k] - x0, nx);
+                        if (live[k] && a < b) need |= (b - a == 32 ? ~0u : ((1u << (b - a)) - 1u)) << a;
+                    }
                     // cells whose record each vertex reaches (independent loads)
                     uint32_t reach[K];
 #pragma unroll
                     for (int k = 0; k < K; ++k) reach[k] = 0u;
-                    for (int i = 0; i < nx; ++i) {
+                    for (uint32_t todo = need; todo; todo &= todo - 1u) {
+                        const int i = __ffs(todo) - 1;
                         const int x = x0 + i;
                         const uint32_t c = row + (uint32_t)x;
                         const float4 b0 = __ldg(&rec[2 * (size_t)c]), b1 = __ldg(&rec[2 * (size_t)c + 1]);
