@@ -96,7 +96,7 @@ struct ScanTemp {
 // Launch shapes chosen by the autotuner (pms_autotune): threads per block of
 // the neighbour walks and the field's resident-block cap (blocks per SM).
 struct Tune {
-    int field_threads = 128, field_waves = 8, density_threads = 128, moments_threads = 128, field_vpt = 4;
+    int field_threads = 128, field_waves = 8, density_threads = 128, moments_threads = 128, field_vpt = 2;
 };
 
 // Stage timing events.

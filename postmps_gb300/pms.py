@@ -412,7 +412,7 @@ class Context:
 
     def set_tune(self, d: dict) -> None:
         t = Tune(**{k: d[k] for k in ("field_threads", "field_waves", "density_threads", "moments_threads")},
-                 field_vpt=d.get("field_vpt", 4))
+                 field_vpt=d.get("field_vpt", 2))
         self._call("pms_set_tune", C.byref(t))
 
     def get_tune(self) -> dict:
