@@ -56,6 +56,11 @@ struct DiffuseParams {
     float min_wc, max_wc, min_ta, max_ta, min_ke, max_ke;
     int ta_mult, wc_mult, life_time;
     float lo_bound[3], hi_bound[3];    // grid min + 4.5 spacing, grid max - 4.5 spacing
+    // exact bounds on a squared distance x for the loops' distance tests (the square
+    // root and the division correctly rounded, as the kernels compute them):
+    float d2_eps;    // sqrt(x) > EPSILON_     <=>  x > d2_eps
+    float d2_hd;     // sqrt(x) <= hd          <=>  x <= d2_hd
+    float d2_q1;     // sqrt(x) / hd < 1       <=>  x <= d2_q1
     uint64_t seed;
     uint32_t frame;
 };
@@ -118,9 +123,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParam
             const float4 q = __ldg(&spos[j]);
             const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
             const float mp2 = sx * sx + sy * sy + sz * sz;
-            const float mp = sqrtf(mp2);
-            const float qq = mp / dp.hd;
-            if (qq > 0.f && qq < 1.f) {
+            // q = |s| / hd in (0, 1), decided on |s|^2 before the square root
+            if (mp2 > 0.f && mp2 <= dp.d2_q1) {
+                const float mp = sqrtf(mp2);
                 const float d = dp.hd_sq - mp2;
                 const float derivative = d * d * 6.f;
                 const float c = dp.coefficient / mp * derivative;
@@ -153,8 +158,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
             const float4 q = __ldg(&spos[j]);
             const float4 w = __ldg(&svel[j]);
             const float sx = p.x - q.x, sy = p.y - q.y, sz = p.z - q.z;
-            const float mp = sqrtf(sx * sx + sy * sy + sz * sz);
-            if (mp > kEpsDown && mp <= dp.hd) {
+            const float mp2 = sx * sx + sy * sy + sz * sz;
+            // EPSILON_ < |s| <= hd, decided on |s|^2 before the square root
+            if (mp2 > dp.d2_eps && mp2 <= dp.d2_hd) {
+                const float mp = sqrtf(mp2);
                 const float ux = v.x - w.x, uy = v.y - w.y, uz = v.z - w.z;
                 float mv = ux * ux + uy * uy + uz * uz;
                 if (mv > kEpsDown) {
@@ -202,6 +209,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
             const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
             const float l2 = dx * dx + dy * dy + dz * dz;
             if (l2 == 0.f) return;                      // normalize(0) is NaN: contributes 0
+            if (l2 > dp.d2_hd) return;                  // |x_ij| > hd: the weight below is 0
             const float il = 1.f / sqrtf(l2);
             const float c = (dx * il) * ni.x + (dy * il) * ni.y + (dz * il) * ni.z;
             if (c < -kEpsDown) {
@@ -427,6 +435,16 @@ __global__ void __launch_bounds__(256) k_df_append(const DiffuseParticle* __rest
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// The largest float x >= 0 for which ok(x) holds, ok true up to some bound and
+// false beyond it (monotone), searched from a nearby start.
+template <class Ok>
+static float largest_float_where(float start, Ok ok) {
+    float x = start;
+    while (x > 0.f && !ok(x)) x = std::nextafter(x, 0.f);
+    while (ok(std::nextafter(x, INFINITY))) x = std::nextafter(x, INFINITY);
+    return x;
+}
+
 static DiffuseParams diffuse_params(const pms_ctx* ctx) {
     const pms_params& P = ctx->prm;
     DiffuseParams d;
@@ -438,6 +456,9 @@ static DiffuseParams diffuse_params(const pms_ctx* ctx) {
     // dGridParams.maxPos - particleSpacing * 4.5 (a double product passed as float)
     const float m = (float)((double)P.particle_spacing * 4.5);
     for (int k = 0; k < 3; ++k) { d.lo_bound[k] = ctx->grid.min_pos[k] + m; d.hi_bound[k] = ctx->grid.max_pos[k] - m; }
+    d.d2_eps = largest_float_where(kEpsDown * kEpsDown, [](float x) { return std::sqrt(x) <= kEpsDown; });
+    d.d2_hd = largest_float_where(d.hd * d.hd, [&](float x) { return std::sqrt(x) <= d.hd; });
+    d.d2_q1 = largest_float_where(d.hd * d.hd, [&](float x) { return std::sqrt(x) / d.hd < 1.f; });
     d.seed = ctx->cfg.rng_seed;
     d.frame = ctx->frame_index;
     return d;
