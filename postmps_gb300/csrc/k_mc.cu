@@ -152,16 +152,29 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                                                       float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
                                                       unsigned long long cap, float* __restrict__ hvert,
-                                                      float* __restrict__ hnorm) {
+                                                      float* __restrict__ hnorm, uint32_t v_lo, uint32_t v_hi) {
     __shared__ float stage[kEmitWarps][kEmitStage];
-    const uint32_t nvalid = cnt->nvalid;
+    // the cubes whose first mesh vertex lies in [v_lo, v_hi): cube records are in
+    // ascending first-vertex order, so both ends are lower bounds
+    const uint32_t nvalid_all = cnt->nvalid;
+    auto lower = [&](uint32_t v) {
+        uint32_t a = 0, b = nvalid_all;
+        while (a < b) {
+            const uint32_t mid = (a + b) >> 1;
+            if (__ldg(&cube[mid]).z < v) a = mid + 1;
+            else b = mid;
+        }
+        return a;
+    };
+    const uint32_t ka = v_lo ? lower(v_lo) : 0u;
+    const uint32_t nvalid = v_hi == 0xffffffffu ? nvalid_all : lower(v_hi);
     // batched frames write behind the earlier frames' vertices, within cap
     const unsigned long long fb = frame_base ? *frame_base : 0ull;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const float sgn = (iso < 0.f) ? -1.f : 1.f;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* st = stage[warp];
-    for (uint32_t k0 = (blockIdx.x * kEmitWarps + warp) * 32u; k0 < nvalid; k0 += gridDim.x * kEmitWarps * 32u) {
+    for (uint32_t k0 = ka + (blockIdx.x * kEmitWarps + warp) * 32u; k0 < nvalid; k0 += gridDim.x * kEmitWarps * 32u) {
         const uint32_t k = k0 + (uint32_t)lane;
         const bool active = k < nvalid;
         const uint4 cr = active ? __ldg(&cube[k]) : make_uint4(0u, 0u, 0u, 0u);
@@ -343,18 +356,18 @@ pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long lo
 }
 
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, float* hvert, float* hnorm) {
+                             unsigned long long cap, float* hvert, float* hnorm, uint32_t v_lo, uint32_t v_hi) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
         g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, hvert,
-        hnorm);
+        hnorm, v_lo, v_hi);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
-pms_status launch_mc_emit(pms_ctx* ctx, float* hvert, float* hnorm) {
-    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, hvert, hnorm);
+pms_status launch_mc_emit(pms_ctx* ctx, float* hvert, float* hnorm, uint32_t v_lo, uint32_t v_hi) {
+    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, hvert, hnorm, v_lo, v_hi);
 }
 
 }  // namespace pms

@@ -385,21 +385,31 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         // (over the host link, as the triangles are made); otherwise a copy stream moves
         // the mesh while the next stages run
         const bool direct = c->out_pos_dev && !c->cfg.is_diffuse && c->nmesh <= c->out_cap;
-        if ((st = launch_mc_emit(c, direct ? c->out_pos_dev : nullptr, direct ? c->out_nrm_dev : nullptr))) return st;
+        const bool copy = c->out_pos && !direct && c->nmesh <= c->out_cap;
+        // copied meshes go in pieces: the emission runs in vertex ranges and each piece
+        // travels while the next is made (and while the stages after run)
+        const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? 4u : 1u) : 0u;
+        if (!pieces) {
+            if ((st = launch_mc_emit(c, direct ? c->out_pos_dev : nullptr, direct ? c->out_nrm_dev : nullptr))) return st;
+        }
+        for (uint32_t q = 0; q < pieces; ++q) {
+            const uint32_t v_lo = (uint32_t)((uint64_t)c->nmesh * q / pieces);
+            const uint32_t v_end = (uint32_t)((uint64_t)c->nmesh * (q + 1) / pieces);
+            if ((st = launch_mc_emit(c, nullptr, nullptr, v_lo, q + 1 == pieces ? 0xffffffffu : v_end))) return st;
+            PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
+            PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
+            PMS_CUDA(c, cudaMemcpyAsync(c->out_pos + 3 * (size_t)v_lo, c->vert.as<float>() + 3 * (size_t)v_lo,
+                                        12 * (size_t)(v_end - v_lo), cudaMemcpyDeviceToHost, c->copy_stream));
+            if (c->out_nrm)
+                PMS_CUDA(c, cudaMemcpyAsync(c->out_nrm + 3 * (size_t)v_lo, c->vnorm.as<float>() + 3 * (size_t)v_lo,
+                                            12 * (size_t)(v_end - v_lo), cudaMemcpyDeviceToHost, c->copy_stream));
+        }
         c->out_direct = direct;
     }
     if (c->out_pos) {
         c->out_n = c->nmesh;
         c->out_overflow = c->nmesh > c->out_cap;
-        if (c->nmesh && !c->out_overflow && c->out_direct) {
-            PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->stream));
-        } else if (c->nmesh && !c->out_overflow) {
-            PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
-            PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
-            PMS_CUDA(c, cudaMemcpyAsync(c->out_pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
-            if (c->out_nrm)
-                PMS_CUDA(c, cudaMemcpyAsync(c->out_nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->copy_stream));
-        }
+        if (c->nmesh && !c->out_overflow && c->out_direct) PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->stream));
         if (!c->out_direct || !c->nmesh || c->out_overflow) PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
         c->out_pending = true;
     }

@@ -236,11 +236,14 @@ pms_status launch_mc_cases(pms_ctx* ctx, uint32_t* qadd = nullptr, uint32_t* qli
 pms_status launch_mc_compact(pms_ctx* ctx);
 pms_status launch_mc_classify(pms_ctx* ctx);
 // hvert / hnorm: device addresses of host buffers that receive a second copy (may be null)
-pms_status launch_mc_emit(pms_ctx* ctx, float* hvert = nullptr, float* hnorm = nullptr);
+// [v_lo, v_hi): emit only the cubes whose first mesh vertex lies there (all by default)
+pms_status launch_mc_emit(pms_ctx* ctx, float* hvert = nullptr, float* hnorm = nullptr, uint32_t v_lo = 0,
+                          uint32_t v_hi = 0xffffffffu);
 pms_status launch_scalar_values(pms_ctx* ctx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, float* hvert = nullptr, float* hnorm = nullptr);
+                             unsigned long long cap, float* hvert = nullptr, float* hnorm = nullptr, uint32_t v_lo = 0,
+                             uint32_t v_hi = 0xffffffffu);
 pms_status launch_diffuse(pms_ctx* ctx);
 pms_status upload_mc_tables(pms_ctx* ctx);
 
