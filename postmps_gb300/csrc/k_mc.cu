@@ -73,15 +73,11 @@ pms_status upload_mc_tables(pms_ctx* ctx) {
     return PMS_OK;
 }
 
-// detectValidSurfaceCubes (6-argument version); with qadd set, also the learned
-// band's border check of every valid cube (border_faces)
-template <bool BORDER>
+// detectValidSurfaceCubes (6-argument version)
 __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, const Counters* __restrict__ cnt,
                                                           const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ bm,
                                                           const float* __restrict__ fdense, uint32_t* __restrict__ mc_case,
-                                                          unsigned long long* __restrict__ mc_key, uint32_t* __restrict__ qadd,
-                                                          uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist,
-                                                          uint32_t qcap) {
+                                                          unsigned long long* __restrict__ mc_key) {
     const uint32_t nv = cnt->nv;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint64_t nbits = g.sc_size;
@@ -102,7 +98,6 @@ __global__ void __launch_bounds__(kThreads) k_mc_classify(KGrid g, float iso, co
         else cs = 0;
         mc_case[t] = cs;
         mc_key[t] = nvert ? ((1ull << 32) | nvert) : 0ull;
-        if (BORDER && nvert) border_faces(g, (int)x, (int)y, (int)z, cs, bm, qadd, n_added, qlist, qcap);
     }
 }
 
@@ -253,16 +248,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
     }
 }
 
-pms_status launch_mc_cases(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist, uint32_t qcap) {
+pms_status launch_mc_cases(pms_ctx* ctx) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
-    auto go = [&](auto kern) {
-        kern<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
-            g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(),
-            ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>(), qadd, &cnt->l_added, qlist, qcap);
-    };
-    if (qadd) go(k_mc_classify<true>);
-    else go(k_mc_classify<false>);
+    k_mc_classify<<<grid_for(ctx->nv, kThreads), kThreads, 0, ctx->stream>>>(
+        g, ctx->prm.iso_value, cnt, ctx->vlist.as<uint32_t>(), ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(),
+        ctx->mc_case.as<uint32_t>(), ctx->mc_key.as<unsigned long long>());
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -230,9 +230,8 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
 pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
-// marching-cube cases of the band vertices (with qadd set, also the learned band's
-// border check of every valid cube), then the scan and compaction; classify = both
-pms_status launch_mc_cases(pms_ctx* ctx, uint32_t* qadd = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);
+// marching-cube cases of the band vertices, then the scan and compaction; classify = both
+pms_status launch_mc_cases(pms_ctx* ctx);
 pms_status launch_mc_compact(pms_ctx* ctx);
 pms_status launch_mc_classify(pms_ctx* ctx);
 // hvert / hnorm: device addresses of host buffers that receive a second copy (may be null)

@@ -141,17 +141,13 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
     auto full_check = [&]() -> pms_status {
         pms_status s2;
         c->nv = (uint32_t)nv_bound;
-        // the cases of every cube with the border check of the valid ones; after border
-        // rounds the check is usually the last, so the scan and compaction the marching
-        // cubes need run before its synchronisation (the first check usually queues cubes)
-        const bool compact = c->l_iters > 0;
-        if ((s2 = run_check([&] {
-                 pms_status s3 = launch_mc_cases(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
-                                                 qcap_of(c->l_qnext));
-                 return (s3 || !compact) ? s3 : launch_mc_compact(c);
-             })))
+        // classification (cases, scan, compaction: the valid-cube records), then the
+        // border check over those records
+        if ((s2 = launch_mc_classify(c))) return s2;
+        if ((s2 = run_check([&] { return launch_border(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
+                                                       qcap_of(c->l_qnext)); })))
             return s2;
-        c->mc_compacted = compact;
+        c->mc_compacted = true;
         c->nv = c->h_counters->nv;
         nv_bound = c->nv;
         std::swap(c->l_qlist, c->l_qnext);
