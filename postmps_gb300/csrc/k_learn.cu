@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kCandThreads) k_learn_cand(KGrid g, LearnDims 
 // the network over the candidate list: a persistent kernel, 16 candidates per
 // warp per step
 // ---------------------------------------------------------------------------
-static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 3;
+static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 5;
 
 struct PredictOut {
     uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
@@ -298,9 +298,18 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
     const int lane = threadIdx.x & 31;
     const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
     const uint32_t ngroups = (n + 15) / 16;
+    // W1 as B fragments in shared memory, laid out per lane (each lane reads its own
+    // 8 bytes: no bank conflicts); registers stay free for five blocks per SM
+    __shared__ uint2 s_w1[4][8][32];
+    for (int e = threadIdx.x; e < 4 * 8 * 32; e += blockDim.x) {
+        const int kk = e >> 8, nt = (e >> 5) & 7, ln = e & 31;
+        const int i0 = kk * 16 + (ln & 3) * 2, j = nt * 8 + (ln >> 2);
+        const uint16_t* w1 = model->w1;
+        s_w1[kk][nt][ln] = make_uint2(pack_raw(w1[(i0 + 0) * kHid + j], w1[(i0 + 1) * kHid + j]),
+                                      pack_raw(w1[(i0 + 8) * kHid + j], w1[(i0 + 9) * kHid + j]));
+    }
+    __syncthreads();
     if (gw >= ngroups) return;
-    uint32_t b[4][8][2];
-    load_w1_frags(model, b, lane);
     const int kq = (lane & 3) * 2;
     float b1v[8][2], w2v[8][2];
 #pragma unroll
@@ -335,7 +344,10 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
             a[2] = patch_pair(dens2, r0, kk, 1);
             a[3] = patch_pair(dens2, r1, kk, 1);
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) mma_bf16(acc[nt], a, b[kk][nt][0], b[kk][nt][1]);
+            for (int nt = 0; nt < 8; ++nt) {
+                const uint2 bf = s_w1[kk][nt][lane];
+                mma_bf16(acc[nt], a, bf.x, bf.y);
+            }
         }
         float z0s = 0.f, z1s = 0.f;
 #pragma unroll
