@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kCandThreads) k_learn_cand(KGrid g, LearnDims 
 // the network over the candidate list: a persistent kernel, 16 candidates per
 // warp per step
 // ---------------------------------------------------------------------------
-static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 5;
+static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 8;
 
 struct PredictOut {
     uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
@@ -301,6 +301,12 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
     // W1 as B fragments in shared memory, laid out per lane (each lane reads its own
     // 8 bytes: no bank conflicts); registers stay free for five blocks per SM
     __shared__ uint2 s_w1[4][8][32];
+    __shared__ float4 s_bw[8][4];     // {b1[j], b1[j + 1], w2[j], w2[j + 1]}, j = 8 nt + 2 q
+    if (threadIdx.x < 32) {
+        const int nt = threadIdx.x >> 2, j = nt * 8 + (threadIdx.x & 3) * 2;
+        s_bw[nt][threadIdx.x & 3] = make_float4(model->b1[j], model->b1[j + 1], bf16_to_f(model->w2[j]),
+                                                bf16_to_f(model->w2[j + 1]));
+    }
     for (int e = threadIdx.x; e < 4 * 8 * 32; e += blockDim.x) {
         const int kk = e >> 8, nt = (e >> 5) & 7, ln = e & 31;
         const int i0 = kk * 16 + (ln & 3) * 2, j = nt * 8 + (ln >> 2);
@@ -311,15 +317,6 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
     __syncthreads();
     if (gw >= ngroups) return;
     const int kq = (lane & 3) * 2;
-    float b1v[8][2], w2v[8][2];
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int j = nt * 8 + kq + e;
-            b1v[nt][e] = model->b1[j];
-            w2v[nt][e] = bf16_to_f(model->w2[j]);
-        }
     const float b2 = model->b2, thr = model->threshold;
     // features (dz = kk, dy, dx) with c = dy * 4 + dx in {kq, kq + 1, kq + 8, kq + 9}
     const int dx0 = kq & 3, dy0 = kq >> 2;
@@ -351,12 +348,13 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
         }
         float z0s = 0.f, z1s = 0.f;
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                z0s += fmaxf(acc[nt][e] + b1v[nt][e], 0.f) * w2v[nt][e];
-                z1s += fmaxf(acc[nt][2 + e] + b1v[nt][e], 0.f) * w2v[nt][e];
-            }
+        for (int nt = 0; nt < 8; ++nt) {
+            const float4 bw = s_bw[nt][lane & 3];
+            z0s += fmaxf(acc[nt][0] + bw.x, 0.f) * bw.z;
+            z0s += fmaxf(acc[nt][1] + bw.y, 0.f) * bw.w;
+            z1s += fmaxf(acc[nt][2] + bw.x, 0.f) * bw.z;
+            z1s += fmaxf(acc[nt][3] + bw.y, 0.f) * bw.w;
+        }
         z0s += __shfl_xor_sync(0xffffffffu, z0s, 1);
         z0s += __shfl_xor_sync(0xffffffffu, z0s, 2);
         z1s += __shfl_xor_sync(0xffffffffu, z1s, 1);
