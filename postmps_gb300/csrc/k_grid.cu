@@ -192,6 +192,10 @@ pms_status launch_hash_sort(pms_ctx* ctx) {
     k_cell_sort_big<<<32, 1024, 0, ctx->stream>>>(ctx->cell_count.as<uint32_t>(), ctx->cell_start.as<uint32_t>(),
                                                    ctx->big_cells.as<uint32_t>(), cnt, ctx->order.as<uint32_t>());
     PMS_LAUNCHED(ctx);
+    if (ctx->vel_pending) {
+        PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->vel_ready, 0));   // the uploaded velocities
+        ctx->vel_pending = false;
+    }
     k_gather<<<gb, kThreads, 0, ctx->stream>>>(ctx->order.as<uint32_t>(), ctx->keys.as<uint32_t>(),
                                                ctx->in_pos.as<float>(), ctx->in_vel.as<float>(), n,
                                                ctx->skeys.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>());

@@ -99,6 +99,9 @@ extern "C" void pms_destroy(pms_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->copy_stream) { cudaStreamSynchronize(c->copy_stream); cudaStreamDestroy(c->copy_stream); }
+    if (c->up_stream) { cudaStreamSynchronize(c->up_stream); cudaStreamDestroy(c->up_stream); }
+    if (c->up_start) cudaEventDestroy(c->up_start);
+    if (c->vel_ready) cudaEventDestroy(c->vel_ready);
     if (c->mesh_ready) cudaEventDestroy(c->mesh_ready);
     if (c->mesh_copied) cudaEventDestroy(c->mesh_copied);
     pms_batch_release(c);
@@ -256,8 +259,23 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     if (st) return st;
     if (n) {
         PMS_CUDA(c, cudaMemcpyAsync(c->in_pos.p, pos, 12 * (size_t)n, kind, c->stream));
-        if (vel) PMS_CUDA(c, cudaMemcpyAsync(c->in_vel.p, vel, 12 * (size_t)n, kind, c->stream));
-        else PMS_CUDA(c, cudaMemsetAsync(c->in_vel.p, 0, 12 * (size_t)n, c->stream));
+        if (vel) {
+            // the velocities are first read by the sort's gather: they travel on their own
+            // stream while the bounding box, keys and counting sort run
+            if (!c->up_stream) {
+                PMS_CUDA(c, cudaStreamCreateWithFlags(&c->up_stream, cudaStreamNonBlocking));
+                PMS_CUDA(c, cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming));
+                PMS_CUDA(c, cudaEventCreateWithFlags(&c->vel_ready, cudaEventDisableTiming));
+            }
+            PMS_CUDA(c, cudaEventRecord(c->up_start, c->stream));
+            PMS_CUDA(c, cudaStreamWaitEvent(c->up_stream, c->up_start, 0));
+            PMS_CUDA(c, cudaMemcpyAsync(c->in_vel.p, vel, 12 * (size_t)n, kind, c->up_stream));
+            PMS_CUDA(c, cudaEventRecord(c->vel_ready, c->up_stream));
+            c->vel_pending = true;
+        } else {
+            PMS_CUDA(c, cudaMemsetAsync(c->in_vel.p, 0, 12 * (size_t)n, c->stream));
+            c->vel_pending = false;
+        }
         // the input density is not read: every stage uses the density recomputed from
         // the positions (the reference overwrites Rhop before its first use,
         // Anisotropic_kernel.cuh:212), so it is not copied

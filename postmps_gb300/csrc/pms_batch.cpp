@@ -319,6 +319,12 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     for (uint32_t f = 0; f < k; ++f)
         if (frames[f].n && !frames[f].pos_xyz) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: no positions", f);
     cudaSetDevice(c->device);
+    // a single frame's velocity upload may still be in flight: order it before the batch
+    // (whose captured sort must not wait on work outside the capture)
+    if (c->vel_pending) {
+        PMS_CUDA(c, cudaStreamWaitEvent(c->stream, c->vel_ready, 0));
+        c->vel_pending = false;
+    }
     BatchState* b = batch_of(c);
     if (k == 0) { b->n.clear(); b->hcnt.clear(); b->rerun.clear(); b->rerun_mesh.clear(); return PMS_OK; }
     // ---- pass 1: arena, uploads, bounding boxes

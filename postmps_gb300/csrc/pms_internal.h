@@ -113,6 +113,11 @@ struct pms_ctx {
     pms_grid grid;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // velocities uploaded on a stream of their own while the grid is built (the sort's
+    // gather waits for them)
+    cudaStream_t up_stream = nullptr;
+    cudaEvent_t up_start = nullptr, vel_ready = nullptr;
+    bool vel_pending = false;
     // mesh streamed to registered host buffers on a copy stream while later stages run
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t mesh_ready = nullptr, mesh_copied = nullptr;
