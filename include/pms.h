@@ -207,9 +207,8 @@ pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint6
  * pms_wait_mesh blocks until the copy has landed and returns the vertex count
  * (PMS_ERR_CAPACITY, with the count, when cap_vertices was too small; nothing
  * is copied then).  The buffers must stay valid until that wait, and the next
- * frame's marching cubes writes them again.  When no stage follows the marching
- * cubes (diffuse generation off) and the GPU can address the buffers (page-
- * locked memory), the triangle emission writes them itself.  No
+ * frame's marching cubes writes them again.  The emission runs in vertex ranges
+ * and each range is copied while the next is made.  No
  * counterpart in the reference, which copies the soup back with a blocking
  * cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
 pms_status pms_stream_mesh_to_host(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices);

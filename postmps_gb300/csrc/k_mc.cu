@@ -146,8 +146,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                                                       const uint4* __restrict__ cube, const float* __restrict__ fdense,
                                                       float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
-                                                      unsigned long long cap, float* __restrict__ hvert,
-                                                      float* __restrict__ hnorm, uint32_t v_lo, uint32_t v_hi) {
+                                                      unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
     __shared__ float stage[kEmitWarps][kEmitStage];
     // the cubes whose first mesh vertex lies in [v_lo, v_hi): cube records are in
     // ascending first-vertex order, so both ends are lower bounds
@@ -233,16 +232,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
         // whole lines: positions, then normals
         for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
             const uint32_t v = i / 3u, c = i - 3u * v;
-            const float x = st[6 * v + c];
-            vert[3 * (size_t)w0 + i] = x;
-            if (hvert) hvert[3 * (size_t)w0 + i] = x;
+            vert[3 * (size_t)w0 + i] = st[6 * v + c];
         }
         if (vnorm)
             for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
                 const uint32_t v = i / 3u, c = i - 3u * v;
-                const float x = st[6 * v + 3 + c];
-                vnorm[3 * (size_t)w0 + i] = x;
-                if (hnorm) hnorm[3 * (size_t)w0 + i] = x;
+                vnorm[3 * (size_t)w0 + i] = st[6 * v + 3 + c];
             }
         __syncwarp();
     }
@@ -347,18 +342,18 @@ pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long lo
 }
 
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, float* hvert, float* hnorm, uint32_t v_lo, uint32_t v_hi) {
+                             unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, hvert,
-        hnorm, v_lo, v_hi);
+        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, v_lo,
+        v_hi);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
-pms_status launch_mc_emit(pms_ctx* ctx, float* hvert, float* hnorm, uint32_t v_lo, uint32_t v_hi) {
-    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, hvert, hnorm, v_lo, v_hi);
+pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo, uint32_t v_hi) {
+    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, v_lo, v_hi);
 }
 
 }  // namespace pms

@@ -383,7 +383,6 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     cudaSetDevice(c->device);
     c->nvalid = 0;
     c->nmesh = 0;
-    c->out_direct = false;
     if (c->nv) {
         pms_status st;
         // the learned band's last border check already computed the final vertex set's cases
@@ -399,21 +398,15 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
         PMS_CUDA(c, c->vert.ensure(12 * M));
         PMS_CUDA(c, c->vnorm.ensure(12 * M));
-        // when no stage follows, the emission writes the registered host buffers itself
-        // (over the host link, as the triangles are made); otherwise a copy stream moves
-        // the mesh while the next stages run
-        const bool direct = c->out_pos_dev && !c->cfg.is_diffuse && c->nmesh <= c->out_cap;
-        const bool copy = c->out_pos && !direct && c->nmesh <= c->out_cap;
-        // copied meshes go in pieces: the emission runs in vertex ranges and each piece
-        // travels while the next is made (and while the stages after run)
+        // a streamed mesh goes in pieces: the emission runs in vertex ranges and each
+        // piece travels on the copy stream while the next is made and the stages after run
+        const bool copy = c->out_pos && c->nmesh <= c->out_cap;
         const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? 4u : 1u) : 0u;
-        if (!pieces) {
-            if ((st = launch_mc_emit(c, direct ? c->out_pos_dev : nullptr, direct ? c->out_nrm_dev : nullptr))) return st;
-        }
+        if (!pieces && (st = launch_mc_emit(c))) return st;
         for (uint32_t q = 0; q < pieces; ++q) {
             const uint32_t v_lo = (uint32_t)((uint64_t)c->nmesh * q / pieces);
             const uint32_t v_end = (uint32_t)((uint64_t)c->nmesh * (q + 1) / pieces);
-            if ((st = launch_mc_emit(c, nullptr, nullptr, v_lo, q + 1 == pieces ? 0xffffffffu : v_end))) return st;
+            if ((st = launch_mc_emit(c, v_lo, q + 1 == pieces ? 0xffffffffu : v_end))) return st;
             PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
             PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
             PMS_CUDA(c, cudaMemcpyAsync(c->out_pos + 3 * (size_t)v_lo, c->vert.as<float>() + 3 * (size_t)v_lo,
@@ -422,13 +415,11 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
                 PMS_CUDA(c, cudaMemcpyAsync(c->out_nrm + 3 * (size_t)v_lo, c->vnorm.as<float>() + 3 * (size_t)v_lo,
                                             12 * (size_t)(v_end - v_lo), cudaMemcpyDeviceToHost, c->copy_stream));
         }
-        c->out_direct = direct;
     }
     if (c->out_pos) {
         c->out_n = c->nmesh;
         c->out_overflow = c->nmesh > c->out_cap;
-        if (c->nmesh && !c->out_overflow && c->out_direct) PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->stream));
-        if (!c->out_direct || !c->nmesh || c->out_overflow) PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
+        PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
         c->out_pending = true;
     }
     c->have_mc = true;
@@ -560,18 +551,6 @@ extern "C" pms_status pms_stream_mesh_to_host(pms_ctx* c, float* pos, float* nrm
     c->out_pos = pos;
     c->out_nrm = pos ? nrm : nullptr;
     c->out_cap = pos ? cap : 0;
-    // page-locked buffers the GPU can address directly (their device addresses)
-    c->out_pos_dev = c->out_nrm_dev = nullptr;
-    auto device_view = [&](float* h) -> float* {
-        cudaPointerAttributes a;
-        if (!h || cudaPointerGetAttributes(&a, h) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-        return a.type == cudaMemoryTypeHost && a.devicePointer ? static_cast<float*>(a.devicePointer) : nullptr;
-    };
-    if (pos) {
-        c->out_pos_dev = device_view(pos);
-        c->out_nrm_dev = nrm ? device_view(nrm) : nullptr;
-        if (!c->out_pos_dev || (nrm && !c->out_nrm_dev)) c->out_pos_dev = c->out_nrm_dev = nullptr;
-    }
     return PMS_OK;
 }
 

@@ -125,9 +125,6 @@ struct pms_ctx {
     float* out_nrm = nullptr;
     uint64_t out_cap = 0, out_n = 0;
     bool out_pending = false, out_overflow = false;
-    float* out_pos_dev = nullptr;    // device addresses of the host buffers when the GPU can write them
-    float* out_nrm_dev = nullptr;
-    bool out_direct = false;         // this frame's emission wrote them
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;
@@ -239,14 +236,13 @@ pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wp
 pms_status launch_mc_cases(pms_ctx* ctx);
 pms_status launch_mc_compact(pms_ctx* ctx);
 pms_status launch_mc_classify(pms_ctx* ctx);
-// hvert / hnorm: device addresses of host buffers that receive a second copy (may be null)
 // [v_lo, v_hi): emit only the cubes whose first mesh vertex lies there (all by default)
-pms_status launch_mc_emit(pms_ctx* ctx, float* hvert = nullptr, float* hnorm = nullptr, uint32_t v_lo = 0,
+pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo = 0,
                           uint32_t v_hi = 0xffffffffu);
 pms_status launch_scalar_values(pms_ctx* ctx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, float* hvert = nullptr, float* hnorm = nullptr, uint32_t v_lo = 0,
+                             unsigned long long cap, uint32_t v_lo = 0,
                              uint32_t v_hi = 0xffffffffu);
 pms_status launch_diffuse(pms_ctx* ctx);
 pms_status upload_mc_tables(pms_ctx* ctx);

@@ -125,11 +125,11 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
 @pytest.mark.gpu
 @pytest.mark.parametrize("diffuse", [False, True])
 def test_streamed_mesh_equals_download(pms_lib, diffuse):
-    """pms_stream_mesh_to_host: the soup that reaches pinned host memory --
-    written by the emission itself (no stage after the marching cubes) or copied
-    on the copy stream while the diffuse stage runs -- equals pms_download_mesh's,
-    frame after frame; a buffer that is too small reports the count with
-    PMS_ERR_CAPACITY."""
+    """pms_stream_mesh_to_host: the soup that reaches pinned host memory -- copied
+    in vertex ranges on the copy stream while the emission continues and, with
+    diffuse generation on, while the diffuse stage runs -- equals
+    pms_download_mesh's, frame after frame; a buffer that is too small reports
+    the count with PMS_ERR_CAPACITY."""
     import torch
     pms = pms_lib
     frames = _frames(3)
