@@ -52,15 +52,16 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_density(KGrid g, AnisoParams 
         uint3 lo, hi;
         box_clamp(g, c, (uint32_t)g.spexpand, lo, hi);
         hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
+        // sum of max(1 - d^2/h^2, 0)^3, times sigma / h^3 once at the end
         float w = 0.f;
         row_walk(g, p, lo, hi, ap.h_sq, pad, cell_start, [&](uint32_t j) {
             const float4 q = __ldg(&spos[j]);
             const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
             const float d2 = dx * dx + dy * dy + dz * dz;
-            const float s = 1.f - d2 * ap.inv_h2;
-            w += (d2 < ap.h_sq) ? ap.kdens * s * s * s : 0.f;   // + 0 leaves the sum unchanged
+            const float s = fmaxf(fmaf(-d2, ap.inv_h2, 1.f), 0.f);   // 0 beyond h: adds nothing
+            w = fmaf(s * s, s, w);
         });
-        rho[i] = w;
+        rho[i] = ap.kdens * w;
     }
 }
 
