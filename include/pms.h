@@ -298,7 +298,13 @@ typedef struct pms_band_model {
 
 pms_status pms_set_band_model(pms_ctx* ctx, const pms_band_model* model);
 /* Which band pms_run_frame uses: PMS_BAND_LEARNED needs a model.  A context
- * created from a config naming [GB300] BandModel starts in PMS_BAND_LEARNED. */
+ * created from a config naming [GB300] BandModel starts in PMS_BAND_LEARNED.
+ * The learned band gives the plain band's triangle positions (what the PLY
+ * file holds, FileData.cpp:1322-1327) but evaluates the field at fewer vertices:
+ * a vertex normal whose central difference reaches a vertex outside that set
+ * reads 0 there, as the reference does outside its band, so the normals from
+ * pms_download_mesh differ from the plain band's at a few per cent of the
+ * vertices (3 % by more than 10 degrees on the crown splash frame). */
 #define PMS_BAND_PLAIN 0
 #define PMS_BAND_LEARNED 1
 pms_status pms_set_band_mode(pms_ctx* ctx, int mode);
