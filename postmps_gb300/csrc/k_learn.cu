@@ -129,10 +129,11 @@ __host__ __device__ inline PadDims pad_dims(const LearnDims& ld) {
     return d;
 }
 
+// (the padded grid holds fewer than 2^29 vertices: 32-bit index arithmetic)
 __device__ __forceinline__ uint32_t padded_feature(const uint32_t* __restrict__ counts, const LearnDims& ld,
-                                                   const PadDims& pd, size_t p) {
-    if (p >= pd.np) return 0u;
-    const uint32_t px = (uint32_t)(p % pd.p0), py = (uint32_t)((p / pd.p0) % pd.p1), pz = (uint32_t)(p / ((size_t)pd.p0 * pd.p1));
+                                                   const PadDims& pd, uint32_t p) {
+    if (p >= (uint32_t)pd.np) return 0u;
+    const uint32_t row = p / pd.p0, px = p - row * pd.p0, pz = row / pd.p1, py = row - pz * pd.p1;
     if (px == 0 || py == 0 || pz == 0) return 0u;
     const size_t c = ((size_t)(pz - 1) * ld.cres[1] + (py - 1)) * ld.cres[0] + (px - 1);
     return __bfloat16_as_ushort(__float2bfloat16_rn(density_of(counts[c], ld.inv_expected)));
@@ -141,8 +142,9 @@ __device__ __forceinline__ uint32_t padded_feature(const uint32_t* __restrict__ 
 __global__ void __launch_bounds__(256) k_coarse_dens(const uint32_t* __restrict__ counts, LearnDims ld,
                                                      uint32_t* __restrict__ dens2) {
     const PadDims pd = pad_dims(ld);
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < pd.np; p += (size_t)gridDim.x * blockDim.x)
-        dens2[p] = padded_feature(counts, ld, pd, p) | (padded_feature(counts, ld, pd, p + 1) << 16);
+    const uint32_t np = (uint32_t)pd.np;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x)
+        dens2[p] = padded_feature(counts, ld, pd, p) | (padded_feature(counts, ld, pd, p + 1u) << 16);
 }
 
 // ---------------------------------------------------------------------------
