@@ -133,6 +133,7 @@ typedef struct pms_counts {
     uint32_t n_band_predicted;         /* cubes it predicted crossed */
     uint32_t n_band_fallback;          /* cubes the border check added */
     uint32_t n_band_iterations;        /* border-check rounds that added cubes */
+    uint32_t n_band_removed;           /* corners of valid cubes outside the plain band, removed */
 } pms_counts;
 
 typedef struct pms_ctx pms_ctx;

@@ -128,6 +128,191 @@ __global__ void __launch_bounds__(256) k_band_list(const uint32_t* __restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Plain-band membership of single vertices, for the learned band: a vertex
+// belongs to the band of k_band_mark + k_band_dilate when a surface particle
+// marks it or the vertex one step lower in linear order along x, y or z (the
+// dilation B0 | B0 << 1 | B0 << rx | B0 << rx*ry, row wrap included).  The
+// test looks from the vertex at the surface cells within h instead of marking
+// from every surface particle, and repeats k_band_mark's per-particle test
+// with the same roundings, so it answers exactly what the bitmap would hold.
+// ---------------------------------------------------------------------------
+
+// k_band_mark's test of one (particle, vertex) pair: the AABB p +- h, the
+// direction flag || n . (v - p) > 0, and the index box c +- ext clamped to the grid
+__device__ __forceinline__ bool marks(const KGrid& g, float h, int ext, float4 p, float4 n, int ix, int iy, int iz,
+                                      float vx, float vy, float vz) {
+    if (vx < __fsub_rn(p.x, h) || vy < __fsub_rn(p.y, h) || vz < __fsub_rn(p.z, h) || vx > __fadd_rn(p.x, h) ||
+        vy > __fadd_rn(p.y, h) || vz > __fadd_rn(p.z, h))
+        return false;
+    if (n.w == 0.f) {
+        const float dx = __fsub_rn(vx, p.x), dy = __fsub_rn(vy, p.y), dz = __fsub_rn(vz, p.z);
+        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n.x, dx), __fmul_rn(n.y, dy)), __fmul_rn(n.z, dz));
+        if (!(dot > 0.f)) return false;
+    }
+    const int cx = __float2int_rz(__fdiv_rn(__fsub_rn(p.x, g.scmin_pos[0]), g.sc_cs));
+    const int cy = __float2int_rz(__fdiv_rn(__fsub_rn(p.y, g.scmin_pos[1]), g.sc_cs));
+    const int cz = __float2int_rz(__fdiv_rn(__fsub_rn(p.z, g.scmin_pos[2]), g.sc_cs));
+    const int rx = (int)g.scres[0] - 1, ry = (int)g.scres[1] - 1, rz = (int)g.scres[2] - 1;
+    return ix >= min(max(cx - ext, 0), rx) && ix <= min(max(cx + ext, 0), rx) && iy >= min(max(cy - ext, 0), ry) &&
+           iy <= min(max(cy + ext, 0), ry) && iz >= min(max(cz - ext, 0), rz) && iz <= min(max(cz + ext, 0), rz);
+}
+
+// Does a particle of the surface cells [xa, xb) x [ya, yb) x [za, zb) mark one
+// of the NT (1 or 3) target vertices?  Targets t with bit t of `use` clear are skipped.
+template <int NT>
+__device__ bool scan_cells(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
+                           const float4* __restrict__ spos, const float4* __restrict__ nrm4, int xa, int xb, int ya,
+                           int yb, int za, int zb, const int (&ix)[NT], const int (&iy)[NT], const int (&iz)[NT],
+                           const float (&vx)[NT], const float (&vy)[NT], const float (&vz)[NT], uint32_t use) {
+    for (int cz = za; cz < zb; ++cz)
+        for (int cy = ya; cy < yb; ++cy) {
+            const uint32_t row = ((uint32_t)cz * g.spres[1] + (uint32_t)cy) * g.spres[0];
+            for (int cx = xa; cx < xb; ++cx) {
+                const uint2 ci = __ldg(&cell_info[row + (uint32_t)cx]);
+                if (!(ci.y & 0x80000000u)) continue;         // empty or not a surface cell
+                const uint32_t j1 = ci.x + (ci.y & 0x7fffffffu);
+                for (uint32_t j = ci.x; j < j1; ++j) {
+                    const float4 p = __ldg(&spos[j]), n = __ldg(&nrm4[j]);
+#pragma unroll
+                    for (int t = 0; t < NT; ++t)
+                        if (((use >> t) & 1u) && marks(g, h, ext, p, n, ix[t], iy[t], iz[t], vx[t], vy[t], vz[t]))
+                            return true;
+                }
+            }
+        }
+    return false;
+}
+
+// the surface cells within h of the box [lo, hi]: every particle that can mark a vertex of the box
+template <int NT>
+__device__ __forceinline__ bool scan_marks(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
+                                           const float4* __restrict__ spos, const float4* __restrict__ nrm4, float lox,
+                                           float loy, float loz, float hix, float hiy, float hiz, const int (&ix)[NT],
+                                           const int (&iy)[NT], const int (&iz)[NT], const float (&vx)[NT],
+                                           const float (&vy)[NT], const float (&vz)[NT], uint32_t use) {
+    const float inv = 1.f / g.sp_cs, r = h * inv + kRangeMargin;
+    return scan_cells<NT>(g, h, ext, cell_info, spos, nrm4, max((int)floorf((lox - g.min_pos[0]) * inv - r), 0),
+                          min((int)floorf((hix - g.min_pos[0]) * inv + r) + 1, (int)g.spres[0]),
+                          max((int)floorf((loy - g.min_pos[1]) * inv - r), 0),
+                          min((int)floorf((hiy - g.min_pos[1]) * inv + r) + 1, (int)g.spres[1]),
+                          max((int)floorf((loz - g.min_pos[2]) * inv - r), 0),
+                          min((int)floorf((hiz - g.min_pos[2]) * inv + r) + 1, (int)g.spres[2]), ix, iy, iz, vx, vy, vz, use);
+}
+
+// B0 at vertex (x, y, z)
+__device__ __forceinline__ bool in_b0(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
+                                      const float4* __restrict__ spos, const float4* __restrict__ nrm4, int x, int y, int z) {
+    const int ix[1] = {x}, iy[1] = {y}, iz[1] = {z};
+    const float vx[1] = {sc_coord_i(g, x, 0)}, vy[1] = {sc_coord_i(g, y, 1)}, vz[1] = {sc_coord_i(g, z, 2)};
+    return scan_marks<1>(g, h, ext, cell_info, spos, nrm4, vx[0], vy[0], vz[0], vx[0], vy[0], vz[0], ix, iy, iz, vx, vy, vz, 1u);
+}
+
+// One side of the test: B0 at v from the 2 x 2 x 2 particle cells nearest to
+// it (most band vertices are marked by a particle there).  A vertex it cannot
+// confirm goes to `rest` for the full test.
+__global__ void __launch_bounds__(128) k_plain_quick(KGrid g, float h, const uint32_t* __restrict__ n_dev,
+                                                     const uint32_t* __restrict__ list, const uint2* __restrict__ cell_info,
+                                                     const float4* __restrict__ spos, const float4* __restrict__ nrm4,
+                                                     uint32_t* __restrict__ rest, uint32_t* __restrict__ n_rest) {
+    const uint32_t n = *n_dev;
+    const int ext = (int)(uint32_t)ceilf(__fdiv_rn(h, g.sc_cs));   // as k_band_mark
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    const float inv = 1.f / g.sp_cs;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {
+        const uint32_t t = t0 + threadIdx.x;
+        bool open = false;
+        uint32_t v = 0;
+        if (t < n) {
+            v = list[t];
+            const int z = (int)(v / rxy), y = (int)((v - (uint32_t)z * rxy) / rx), x = (int)(v - (uint32_t)z * rxy - (uint32_t)y * rx);
+            const int ix[1] = {x}, iy[1] = {y}, iz[1] = {z};
+            const float vx[1] = {sc_coord_i(g, x, 0)}, vy[1] = {sc_coord_i(g, y, 1)}, vz[1] = {sc_coord_i(g, z, 2)};
+            int a[3], b[3];
+            const float u[3] = {(vx[0] - g.min_pos[0]) * inv, (vy[0] - g.min_pos[1]) * inv, (vz[0] - g.min_pos[2]) * inv};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int c = (int)floorf(u[k]);
+                const int lo = u[k] - (float)c < 0.5f ? c - 1 : c;
+                a[k] = max(lo, 0);
+                b[k] = min(lo + 2, (int)g.spres[k]);
+            }
+            open = !scan_cells<1>(g, h, ext, cell_info, spos, nrm4, a[0], b[0], a[1], b[1], a[2], b[2], ix, iy, iz, vx, vy,
+                                  vz, 1u);
+        }
+        // warp-aggregated append of the open vertices
+        const uint32_t m = __ballot_sync(0xffffffffu, open);
+        uint32_t base = 0;
+        if (lane == 0 && m) base = atomicAdd(n_rest, (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (open) rest[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = v;
+    }
+}
+
+// membership of vertex v = (x, y, z) in the dilated band
+__device__ bool in_plain_band(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
+                              const float4* __restrict__ spos, const float4* __restrict__ nrm4, uint32_t v) {
+    const uint32_t rx = g.scres[0], ry = g.scres[1], rxy = rx * ry;
+    const int z = (int)(v / rxy), y = (int)((v - (uint32_t)z * rxy) / rx), x = (int)(v - (uint32_t)z * rxy - (uint32_t)y * rx);
+    if (in_b0(g, h, ext, cell_info, spos, nrm4, x, y, z)) return true;
+    // the lower neighbours v - 1, v - rx, v - rx*ry where they do not wrap, in one scan
+    const uint32_t use = (x > 0 ? 1u : 0u) | (y > 0 ? 2u : 0u) | (z > 0 ? 4u : 0u);
+    if (use) {
+        const int ix[3] = {x - 1, x, x}, iy[3] = {y, y - 1, y}, iz[3] = {z, z, z - 1};
+        const float px = sc_coord_i(g, x, 0), py = sc_coord_i(g, y, 1), pz = sc_coord_i(g, z, 2);
+        const float qx = sc_coord_i(g, x - 1, 0), qy = sc_coord_i(g, y - 1, 1), qz = sc_coord_i(g, z - 1, 2);
+        const float vx[3] = {qx, px, px}, vy[3] = {py, qy, py}, vz[3] = {pz, pz, qz};
+        if (scan_marks<3>(g, h, ext, cell_info, spos, nrm4, (use & 1u) ? qx : px, (use & 2u) ? qy : py,
+                          (use & 4u) ? qz : pz, px, py, pz, ix, iy, iz, vx, vy, vz, use))
+            return true;
+    }
+    // at x == 0 (y == 0) the linear shift wraps to the row (slab) below; z == 0 has nothing below
+    if (x == 0 && v >= 1) {
+        const uint32_t u = v - 1, uz = u / rxy, uy = (u - uz * rxy) / rx;
+        if (in_b0(g, h, ext, cell_info, spos, nrm4, (int)(u - uz * rxy - uy * rx), (int)uy, (int)uz)) return true;
+    }
+    if (y == 0 && v >= rx) {
+        const uint32_t u = v - rx, uz = u / rxy, uy = (u - uz * rxy) / rx;
+        if (in_b0(g, h, ext, cell_info, spos, nrm4, (int)(u - uz * rxy - uy * rx), (int)uy, (int)uz)) return true;
+    }
+    (void)ry;
+    return false;
+}
+
+// The listed vertices outside the plain band leave the vertex set: the bit in
+// vbm is cleared, the dense field value set to 0 (what a vertex off the band
+// reads) and n_removed counts them.
+__global__ void __launch_bounds__(128) k_plain_member(KGrid g, float h, const uint32_t* __restrict__ n_dev,
+                                                      const uint32_t* __restrict__ list, const uint2* __restrict__ cell_info,
+                                                      const float4* __restrict__ spos, const float4* __restrict__ nrm4,
+                                                      uint32_t* __restrict__ vbm, float* __restrict__ fdense,
+                                                      uint32_t* __restrict__ n_removed) {
+    const uint32_t n = *n_dev;
+    const int ext = (int)(uint32_t)ceilf(__fdiv_rn(h, g.sc_cs));   // as k_band_mark
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t v = list[t];
+        if (in_plain_band(g, h, ext, cell_info, spos, nrm4, v)) continue;
+        atomicAnd(&vbm[v >> 5], ~(1u << (v & 31u)));
+        fdense[v] = 0.f;
+        atomicAdd(n_removed, 1u);
+    }
+}
+
+pms_status launch_plain_member(pms_ctx* ctx, const uint32_t* list, const uint32_t* n_dev, uint32_t n_host, uint32_t* rest,
+                               uint32_t* n_rest, uint32_t* n_removed) {
+    const KGrid g = kgrid_of(ctx->grid);
+    PMS_CUDA(ctx, cudaMemsetAsync(n_rest, 0, sizeof(uint32_t), ctx->stream));
+    k_plain_quick<<<grid_for(n_host, 128), 128, 0, ctx->stream>>>(g, ctx->prm.h, n_dev, list, ctx->cell_info.as<uint2>(),
+                                                                  ctx->spos.as<float4>(), ctx->nrm4.as<float4>(), rest, n_rest);
+    PMS_LAUNCHED(ctx);
+    k_plain_member<<<grid_for(n_host, 128), 128, 0, ctx->stream>>>(
+        g, ctx->prm.h, n_rest, rest, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->nrm4.as<float4>(),
+        ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(), n_removed);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 pms_status launch_band(pms_ctx* ctx) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();

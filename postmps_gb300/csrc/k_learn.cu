@@ -412,6 +412,37 @@ __global__ void __launch_bounds__(256) k_cube_corners(const uint32_t* __restrict
     }
 }
 
+// corners(cubes) appended to a list in no particular order (one atomic per warp)
+__global__ void __launch_bounds__(256) k_corner_list(const uint32_t* __restrict__ cubes, uint64_t nwords, uint64_t nbits,
+                                                     uint64_t sy, uint64_t sz, uint32_t* __restrict__ list,
+                                                     uint32_t* __restrict__ n_list) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x; w0 < nwords; w0 += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t w = w0 + threadIdx.x;
+        uint32_t v = 0;
+        if (w < nwords) {
+            v = cubes[w] | shifted(cubes, w, 1) | shifted(cubes, w, sy) | shifted(cubes, w, sy + 1) | shifted(cubes, w, sz) |
+                shifted(cubes, w, sz + 1) | shifted(cubes, w, sz + sy) | shifted(cubes, w, sz + sy + 1);
+            if (w == nwords - 1 && (nbits & 31u)) v &= (1u << (nbits & 31u)) - 1u;
+        }
+        const uint32_t c = __popc(v);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        uint32_t base = 0;
+        if (lane == 31u && incl) base = atomicAdd(n_list, incl);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        uint32_t o = base + incl - c;
+        while (v) {
+            list[o++] = (uint32_t)(w * 32u) + (uint32_t)(__ffs(v) - 1);
+            v &= v - 1u;
+        }
+    }
+}
+
 // a | b with popcount per word
 __global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
                                                  uint32_t* __restrict__ out, uint32_t* __restrict__ wcount, uint64_t nwords) {
@@ -801,6 +832,16 @@ pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32
     const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
     const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
     k_cube_corners<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, exclude, out, wcount, nwords, nbits, sy, sz);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_corner_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t* list, uint32_t* n_list) {
+    const KGrid g = kgrid_of(ctx->grid);
+    const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
+    const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
+    PMS_CUDA(ctx, cudaMemsetAsync(n_list, 0, sizeof(uint32_t), ctx->stream));
+    k_corner_list<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, nwords, nbits, sy, sz, list, n_list);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

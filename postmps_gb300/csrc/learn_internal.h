@@ -39,6 +39,8 @@ pms_status launch_coarse_counts(pms_ctx* ctx);
 pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* cand, float* logit, uint32_t cand_cap);
 pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
                                uint32_t* wcount);
+// the corners of the cubes of a bitmap, listed in no particular order; *n_list their count
+pms_status launch_corner_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t* list, uint32_t* n_list);
 pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount);
 // border checks queue cubes in qadd (a bitmap) and, when qlist is given, in a
 // list of at most qcap entries; the count (l_added) may exceed qcap
@@ -50,6 +52,9 @@ pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
 pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd,
                               const uint32_t* n_dev = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount);
+// corners of the classified valid cubes outside the plain band leave the vertex
+// set (bitmap and dense field); Counters::l_removed counts them
+pms_status plain_band_filter(pms_ctx* ctx);
 pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x);
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,
                          float* loss_sum);

@@ -285,7 +285,7 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     c->have_particles = true;
     c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = false;
     c->band_learned = c->mc_classified = c->mc_compacted = false;
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
+    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
     c->ns = c->nv = c->nvalid = 0;
     c->nmesh = 0;
     for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
@@ -352,7 +352,7 @@ extern "C" pms_status pms_band(pms_ctx* c) {
     if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
     cudaSetDevice(c->device);
     c->band_learned = c->mc_classified = c->mc_compacted = false;
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
+    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
     if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
     pms_status st;
     if ((st = launch_band(c))) return st;
@@ -514,6 +514,7 @@ extern "C" pms_status pms_get_counts(pms_ctx* c, pms_counts* out) {
         out->n_band_predicted = c->l_npred;
         out->n_band_fallback = c->l_nadded;
         out->n_band_iterations = c->l_iters;
+        out->n_band_removed = c->l_nremoved;
     }
     return check_device_errors(c);
 }

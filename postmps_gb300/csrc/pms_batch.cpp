@@ -19,8 +19,9 @@
 //
 // With the learned band, the graph holds the prediction, the field at the
 // predicted corners and one border check per frame; a frame whose border
-// check finds missing cubes is re-run alone on the exact learned path
-// afterwards, so the batched result equals the single-frame result.
+// check finds missing cubes, or whose valid cubes have corners outside the
+// plain band, is re-run alone on the exact learned path afterwards, so the
+// batched result equals the single-frame result.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -181,6 +182,8 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool lear
         // the band-order field of the final vertex set (the rounds work on the dense field)
         if ((st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, g.sc_size, c->field.as<float>()))) return st;
         if ((st = full_check(c, W))) return st;              // what is still missing: the frame runs again alone
+        // corners of valid cubes outside the plain band: the frame runs again alone too
+        if ((st = plain_band_filter(c))) return st;
     } else {
         if ((st = launch_band(c))) return st;
         if ((st = launch_band_list(c))) return st;
@@ -445,7 +448,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     b->rerun_mesh.assign(k, {});
     if (learned) {
         for (uint32_t f = 0; f < k; ++f) {
-            if (b->hcnt[f].l_added == 0) continue;
+            if (b->hcnt[f].l_added == 0 && b->hcnt[f].l_removed == 0) continue;
             b->rerun[f] = 1;
             b->reruns++;
             if ((st = pms_upload_particles_device(c, b->pos.as<float>() + 3 * off[f], b->vel.as<float>() + 3 * off[f],
@@ -459,6 +462,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
             PMS_CUDA(c, cudaStreamSynchronize(c->stream));
             pms::Counters h = *c->h_counters;
             h.l_added = 0;
+            h.l_removed = 0;
             b->hcnt[f] = h;
             b->hcnt[f].nmesh = nv;
         }

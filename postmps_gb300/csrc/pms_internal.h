@@ -67,6 +67,8 @@ struct Counters {
     uint32_t l_nnew;        // vertices those cubes add
     uint32_t l_nq;          // cubes queued for a border-check round (batched frames)
     uint32_t n_items;       // work items of the last field launch
+    uint32_t l_removed;     // learned-band vertices outside the plain band
+    uint32_t l_open;        // vertices the quick plain-band test left open
 };
 
 enum : uint32_t {
@@ -166,7 +168,7 @@ struct pms_ctx {
     // batched frames (pms_batch.cpp)
     void* batch = nullptr;
     uint64_t batch_launches = 0;         // kernels in the batch graph
-    uint32_t l_ncand = 0, l_npred = 0, l_nadded = 0, l_iters = 0;
+    uint32_t l_ncand = 0, l_npred = 0, l_nadded = 0, l_iters = 0, l_nremoved = 0;
     uint32_t diffuse_old = 0;    // live diffuse particles carried to the next frame
     uint32_t frame_index = 0;
 
@@ -232,6 +234,11 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
 pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
+// the vertices list[0 .. *n_dev) outside the plain band leave ctx->bm / ctx->fdense
+// (n_host: a bound for the grid; rest: room for n_host vertices the quick pass
+// leaves open, counted in n_rest; n_removed: their count)
+pms_status launch_plain_member(pms_ctx* ctx, const uint32_t* list, const uint32_t* n_dev, uint32_t n_host, uint32_t* rest,
+                               uint32_t* n_rest, uint32_t* n_removed);
 // marching-cube cases of the band vertices, then the scan and compaction; classify = both
 pms_status launch_mc_cases(pms_ctx* ctx);
 pms_status launch_mc_compact(pms_ctx* ctx);

@@ -85,12 +85,30 @@ static pms_status finish_vertex_set(pms_ctx* c) {
     return launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>());
 }
 
+// The corners of the classified valid cubes (cube bitmap from the cases, then
+// the list of its corners), each tested against the plain band's rule; those
+// outside leave the vertex set and l_removed counts them.  Corners of valid
+// cubes are band vertices, so c->nv bounds the list.
+pms_status pms::plain_band_filter(pms_ctx* c) {
+    Counters* cnt = c->counters.as<Counters>();
+    const uint64_t W = words_of(c);
+    pms_status st;
+    PMS_CUDA(c, c->l_vlist_new.ensure(4 * ((size_t)c->nv + 1)));
+    PMS_CUDA(c, c->l_vlist_m.ensure(4 * ((size_t)c->nv + 1)));
+    PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
+    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_removed, 0, sizeof(uint32_t), c->stream));
+    if ((st = launch_label_bits(c, c->l_q.as<uint32_t>()))) return st;
+    if ((st = launch_corner_list(c, c->l_q.as<uint32_t>(), c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew))) return st;
+    return launch_plain_member(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, c->nv, c->l_vlist_m.as<uint32_t>(),
+                               &cnt->l_open, &cnt->l_removed);
+}
+
 extern "C" pms_status pms_band_learned(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band_learned before pms_anisotropy");
     if (!c->have_model) return pms_fail(c, PMS_ERR_STATE, "pms_band_learned without a model (pms_set_band_model)");
     cudaSetDevice(c->device);
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = 0;
+    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
     c->band_learned = true;
     c->mc_classified = c->mc_compacted = false;
     if (c->n == 0) { c->nv = 0; c->have_band = c->have_field = true; return PMS_OK; }
@@ -184,14 +202,30 @@ extern "C" pms_status pms_band_learned(pms_ctx* c) {
         // round limit reached: the vertex list still covers every value computed
         if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
         if ((st = finish_vertex_set(c))) return st;
+        if (c->nv && (st = launch_mc_classify(c))) return st;
+    }
+    // the plain band's membership test of the valid cubes' corners: a corner the
+    // plain band lacks leaves the set, so that every cube classified valid is one
+    // the plain band holds; the set then gets its sorted list again
+    uint32_t removed = 0;
+    if (c->nv) {
+        if ((st = plain_band_filter(c))) return st;
+        if ((st = sync_counters(c))) return st;
+        removed = c->l_nremoved = c->h_counters->l_removed;
+        if (removed) {
+            if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
+            if ((st = finish_vertex_set(c))) return st;
+        }
     }
     c->nv = c->h_counters->nv;
     if ((st = ensure_band_buffers(c, c->nv))) return st;
     // the band-order field of the final vertex set (the rounds work on the dense field)
-    if (c->l_iters && c->nv && (st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, c->nv, c->field.as<float>())))
+    if ((c->l_iters || removed) && c->nv && (st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, c->nv, c->field.as<float>())))
         return st;
-    c->mc_classified = (added == 0);           // the last full check computed the final vertex set's cases
-    c->mc_compacted = c->mc_classified && c->mc_compacted;
+    // the last full check (or classification) computed the final vertex set's cases
+    // unless corners were removed since
+    c->mc_classified = removed == 0;
+    c->mc_compacted = c->mc_classified;
     c->have_field = true;
     mark_stage(c, kStageField + 1);
     return PMS_OK;

@@ -190,7 +190,7 @@ def compare(ctx: "pms.Context", model: "pms.BandModel", h: float, pos, vel=None,
            "learned": {"band_vertices": cl.n_band_vertices, "valid_cubes": cl.n_valid_cubes,
                        "triangles": cl.n_mesh_vertices // 3, "candidates": cl.n_band_candidates,
                        "predicted": cl.n_band_predicted, "fallback_cubes": cl.n_band_fallback,
-                       "fallback_rounds": cl.n_band_iterations, "ms": tl},
+                       "fallback_rounds": cl.n_band_iterations, "removed": cl.n_band_removed, "ms": tl},
            "triangle_delta": int(cl.n_mesh_vertices // 3) - int(cp.n_mesh_vertices // 3)}
     res.update(hd)
     res["hausdorff_h"] = hd["hausdorff"] / h

@@ -95,7 +95,7 @@ class Counts(C.Structure):
         ("n_generated_diffuse", C.c_uint32), ("n_spawning", C.c_uint32), ("n_diffuse", C.c_uint32),
         ("n_spray", C.c_uint32), ("n_foam", C.c_uint32), ("n_bubble", C.c_uint32), ("n_fp64_svd", C.c_uint32),
         ("n_band_candidates", C.c_uint32), ("n_band_predicted", C.c_uint32), ("n_band_fallback", C.c_uint32),
-        ("n_band_iterations", C.c_uint32),
+        ("n_band_iterations", C.c_uint32), ("n_band_removed", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:

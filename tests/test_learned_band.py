@@ -228,7 +228,28 @@ def test_border_check_recovers_the_plain_mesh(pms_lib):
         assert r["learned"]["fallback_cubes"] > 0 and r["learned"]["fallback_rounds"] > 0
         assert missed > 0.3 * r["plain"]["valid_cubes"]
         assert r["cubes_only_plain"] <= 0.05 * missed, (r, missed)
+        assert r["cubes_only_learned"] == 0, r
         t.close()
+
+
+@pytest.mark.gpu
+def test_held_out_frame_has_no_cube_outside_the_plain_band(pms_lib):
+    """On a held-out frame the network predicts cubes whose corners the plain
+    band does not hold (its truncation leaves a hole there); the plain-band
+    membership test of the valid cubes' corners removes those corners, so
+    the learned surface has no cube the plain one lacks."""
+    pms = pms_lib
+    from postmps_gb300 import learned
+    if not os.path.exists(learned.DEFAULT_MODEL):
+        pytest.skip("no trained model committed")
+    model = learned.load_model()
+    ctx, cfg, pos, vel, rho = _crown_ctx(pms, 1.0, seed=201)
+    h = float(pms.derive_params(cfg).h)
+    with ctx:
+        r = learned.compare(ctx, model, h, pos, vel, rho)
+    assert r["learned"]["removed"] > 0, r
+    assert r["cubes_only_learned"] == 0, r
+    assert r["hausdorff"] <= 0.05 * h, r
 
 
 @pytest.mark.gpu
@@ -246,6 +267,7 @@ def test_committed_model_gain_on_held_out_frame(pms_lib):
     assert r["learned"]["band_vertices"] < 0.8 * r["plain"]["band_vertices"], r
     assert r["hausdorff"] <= 0.05 * h, r
     assert abs(r["triangle_delta"]) <= 0.002 * r["plain"]["triangles"] + 16, r
+    assert r["cubes_only_learned"] == 0, r
 
 
 def test_model_file_round_trip_and_config_key(pms_lib, tmp_path, tmp_config):
