@@ -208,9 +208,10 @@ __device__ __forceinline__ bool in_b0(const KGrid& g, float h, int ext, const ui
     return scan_marks<1>(g, h, ext, cell_info, spos, nrm4, vx[0], vy[0], vz[0], vx[0], vy[0], vz[0], ix, iy, iz, vx, vy, vz, 1u);
 }
 
-// One side of the test: B0 at v from the 2 x 2 x 2 particle cells nearest to
-// it (most band vertices are marked by a particle there).  A vertex it cannot
-// confirm goes to `rest` for the full test.
+// The quick side of the test: B0 at v, then at its three lower neighbours (no
+// row wrap), from the 2 x 2 x 2 particle cells nearest to v -- most band
+// vertices are marked by a particle there.  A vertex it cannot confirm goes to
+// `rest` for the full test.
 __global__ void __launch_bounds__(128) k_plain_quick(KGrid g, float h, const uint32_t* __restrict__ n_dev,
                                                      const uint32_t* __restrict__ list, const uint2* __restrict__ cell_info,
                                                      const float4* __restrict__ spos, const float4* __restrict__ nrm4,
@@ -240,6 +241,14 @@ __global__ void __launch_bounds__(128) k_plain_quick(KGrid g, float h, const uin
             }
             open = !scan_cells<1>(g, h, ext, cell_info, spos, nrm4, a[0], b[0], a[1], b[1], a[2], b[2], ix, iy, iz, vx, vy,
                                   vz, 1u);
+            const uint32_t use = (x > 0 ? 1u : 0u) | (y > 0 ? 2u : 0u) | (z > 0 ? 4u : 0u);
+            if (open && use) {
+                const int jx[3] = {x - 1, x, x}, jy[3] = {y, y - 1, y}, jz[3] = {z, z, z - 1};
+                const float qx = sc_coord_i(g, x - 1, 0), qy = sc_coord_i(g, y - 1, 1), qz = sc_coord_i(g, z - 1, 2);
+                const float wx[3] = {qx, vx[0], vx[0]}, wy[3] = {vy[0], qy, vy[0]}, wz[3] = {vz[0], vz[0], qz};
+                open = !scan_cells<3>(g, h, ext, cell_info, spos, nrm4, a[0], b[0], a[1], b[1], a[2], b[2], jx, jy, jz, wx, wy,
+                                      wz, use);
+            }
         }
         // warp-aggregated append of the open vertices
         const uint32_t m = __ballot_sync(0xffffffffu, open);

@@ -532,6 +532,25 @@ __global__ void __launch_bounds__(256) k_label_bits(const uint32_t* __restrict__
         if (mc_key[t]) atomicOr(&lbm[vlist[t] >> 5], 1u << (vlist[t] & 31u));
 }
 
+// cube bitmap of the compacted valid-cube records (one atomic per warp and word)
+__global__ void __launch_bounds__(256) k_valid_bits(const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
+                                                    uint32_t* __restrict__ bits) {
+    const uint32_t n = cnt->nvalid;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {
+        const uint32_t t = t0 + threadIdx.x;
+        uint32_t w = 0xffffffffu, b = 0u;
+        if (t < n) {
+            const uint32_t id = cube[t].x;
+            w = id >> 5;
+            b = 1u << (id & 31u);
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, w);
+        const uint32_t orv = __reduce_or_sync(peers, b);
+        if (t < n && (uint32_t)(__ffs(peers) - 1) == lane) atomicOr(&bits[w], orv);
+    }
+}
+
 // features of explicit cubes (bf16 bits, 64 per cube), for checks against the oracle
 __global__ void __launch_bounds__(256) k_features(KGrid g, LearnDims ld, const uint32_t* __restrict__ counts,
                                                   const uint32_t* __restrict__ cubes, uint32_t n, uint16_t* __restrict__ x) {
@@ -885,6 +904,14 @@ pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n,
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount) {
     const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
     k_popc<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(b, wcount, nwords);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+pms_status launch_valid_bits(pms_ctx* ctx, uint32_t* bits) {
+    Counters* cnt = ctx->counters.as<Counters>();
+    // ctx->nv bounds the valid cubes; the kernel reads their count
+    k_valid_bits<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(cnt, ctx->cube.as<uint4>(), bits);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

@@ -48,6 +48,8 @@ pms_status launch_border(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist = nullptr
 // corners of n queued cubes not yet in the vertex bitmap: set there and appended to vnew
 pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* vnew, uint32_t* n_new);
 pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
+// cube bitmap of the compacted valid-cube records (bits: zeroed)
+pms_status launch_valid_bits(pms_ctx* ctx, uint32_t* bits);
 // n: the list length, or a bound when n_dev holds it on the device
 pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd,
                               const uint32_t* n_dev = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);

@@ -85,8 +85,8 @@ static pms_status finish_vertex_set(pms_ctx* c) {
     return launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>());
 }
 
-// The corners of the classified valid cubes (cube bitmap from the cases, then
-// the list of its corners), each tested against the plain band's rule; those
+// The corners of the compacted valid cubes (cube bitmap from their records,
+// then the list of its corners), each tested against the plain band's rule; those
 // outside leave the vertex set and l_removed counts them.  Corners of valid
 // cubes are band vertices, so c->nv bounds the list.
 pms_status pms::plain_band_filter(pms_ctx* c) {
@@ -97,7 +97,7 @@ pms_status pms::plain_band_filter(pms_ctx* c) {
     PMS_CUDA(c, c->l_vlist_m.ensure(4 * ((size_t)c->nv + 1)));
     PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
     PMS_CUDA(c, cudaMemsetAsync(&cnt->l_removed, 0, sizeof(uint32_t), c->stream));
-    if ((st = launch_label_bits(c, c->l_q.as<uint32_t>()))) return st;
+    if ((st = launch_valid_bits(c, c->l_q.as<uint32_t>()))) return st;
     if ((st = launch_corner_list(c, c->l_q.as<uint32_t>(), c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew))) return st;
     return launch_plain_member(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, c->nv, c->l_vlist_m.as<uint32_t>(),
                                &cnt->l_open, &cnt->l_removed);
