@@ -228,10 +228,8 @@ __global__ void __launch_bounds__(kCandThreads) k_learn_cand(KGrid g, LearnDims 
 }
 
 // ---------------------------------------------------------------------------
-// the network over the candidate list: a persistent kernel, 16 candidates per
-// warp per step
+// the network over the candidate list
 // ---------------------------------------------------------------------------
-static constexpr int kMlpThreads = 128, kMlpBlocksPerSm = 8;
 
 struct PredictOut {
     uint32_t* q;              // cube bitmap (bit = origin vertex id); may be null
@@ -284,11 +282,92 @@ __device__ __forceinline__ uint32_t patch_pair(const uint32_t* __restrict__ dens
     return r.swap ? __byte_perm(v, 0u, 0x1032) : v;
 }
 
-__global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(LearnDims ld, const uint32_t* __restrict__ dens2,
-                                                           const uint2* __restrict__ clist,
-                                                           const uint32_t* __restrict__ n_dev,
-                                                           const DevModel* __restrict__ model, int use_model,
-                                                           PredictOut out) {
+// ---------------------------------------------------------------------------
+// The first layer on the fifth-generation tensor cores.  A block takes tiles
+// of 128 candidates.  Every thread gathers the 64 features of one candidate
+// into shared memory in the UMMA canonical K-major layout without swizzle
+// (8-row x 16-byte core matrices; the next one along K 128 B further, the next
+// 8-row group 1 KiB further), one thread issues four tcgen05.mma (M 128, N 64,
+// K 16; bf16 operands, fp32 accumulator in tensor memory) against W1 staged
+// once per block in the same layout, their completion arrives on an mbarrier,
+// and each warp reads its 32 rows of the accumulator back (tcgen05.ld
+// 32x32b) for b1, ReLU, w2 and b2.  The dynamic shared memory a block asks for
+// keeps at most five blocks on an SM, so their 5 x 64 tensor-memory columns fit
+// the SM's 512 and no allocation waits on another block.  Two A buffers let the
+// gathers of one tile overlap the MMA and the epilogue of the one before.
+// ---------------------------------------------------------------------------
+static constexpr int kTcThreads = 128, kTcRows = 128;
+static constexpr uint32_t kTcCols = 64;                         // tensor-memory columns: N fp32 accumulators
+static constexpr uint32_t kTcBytesA = kTcRows * kIn * 2, kTcBytesB = kHid * kIn * 2;   // one A buffer; two are used
+// 5 x (44 + 1) KiB fit an SM's 228 KiB, 6 x do not: five blocks per SM at most
+static constexpr uint32_t kTcSmem = 44u * 1024u;
+static constexpr uint32_t kTcSpin = 1u << 22;                   // bound on the polls of one mbarrier phase
+static constexpr int kTcBlocksPerSm = 5;
+static_assert(2 * kTcBytesA + kTcBytesB + 2 * kHid * 4 + 64 + 1024 <= kTcSmem, "shared memory plan");
+static_assert(kIn == 64 && kHid == 64, "the tile plan assumes 64 features and 64 hidden units");
+
+// byte offset of element (row r, k) of a K-major operand with 64 K elements (bf16)
+__device__ __forceinline__ uint32_t umma_off(uint32_t r, uint32_t k) {
+    return ((((r >> 3) << 3) + (k >> 3)) << 7) + ((r & 7u) << 4) + ((k & 7u) << 1);
+}
+
+// shared-memory matrix descriptor: start, leading byte offset 128 (next core
+// matrix along K), stride byte offset 1024 (next 8-row group), the fixed
+// version bits 46-48 = 0b001, no swizzle
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: fp32 accumulator (bits 4-5 = 1), A and B
+// bf16 (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 16 consecutive accumulator columns of this thread's lane, waited for
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+        "[%16];\n\ttcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnDims ld, const uint32_t* __restrict__ dens2,
+                                                          const uint2* __restrict__ clist, const uint32_t* __restrict__ n_dev,
+                                                          const DevModel* __restrict__ model, int use_model, PredictOut out,
+                                                          uint32_t* __restrict__ err) {
     const uint32_t n = *n_dev;
     if (!use_model) {
         // collect only
@@ -297,91 +376,167 @@ __global__ void __launch_bounds__(kMlpThreads, kMlpBlocksPerSm) k_learn_mlp(Lear
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(out.n_pred, n);
         return;
     }
-    const int lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t ngroups = (n + 15) / 16;
-    // W1 as B fragments in shared memory, laid out per lane (each lane reads its own
-    // 8 bytes: no bank conflicts); registers stay free for five blocks per SM
-    __shared__ uint2 s_w1[4][8][32];
-    __shared__ float4 s_bw[8][4];     // {b1[j], b1[j + 1], w2[j], w2[j + 1]}, j = 8 nt + 2 q
-    if (threadIdx.x < 32) {
-        const int nt = threadIdx.x >> 2, j = nt * 8 + (threadIdx.x & 3) * 2;
-        s_bw[nt][threadIdx.x & 3] = make_float4(model->b1[j], model->b1[j + 1], bf16_to_f(model->w2[j]),
-                                                bf16_to_f(model->w2[j + 1]));
+    extern __shared__ uint8_t tc_smem[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem) + 1023u) & ~(uintptr_t)1023u);
+    uint8_t* sA = sm;
+    uint8_t* sB = sm + 2 * kTcBytesA;
+    float* s_b1 = reinterpret_cast<float*>(sB + kTcBytesB);
+    float* s_w2 = s_b1 + kHid;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_w2 + kHid);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t a_saddr = (uint32_t)__cvta_generic_to_shared(sA), b_saddr = (uint32_t)__cvta_generic_to_shared(sB);
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
+    // W1 as the B operand (row j = hidden unit, K = input feature i)
+    for (uint32_t e = tid; e < (uint32_t)(kHid * kIn / 2); e += kTcThreads) {
+        const uint32_t j = e / (kIn / 2), i = (e % (kIn / 2)) * 2;
+        *reinterpret_cast<uint32_t*>(sB + umma_off(j, i)) =
+            pack_raw(model->w1[i * kHid + j], model->w1[(i + 1) * kHid + j]);
     }
-    for (int e = threadIdx.x; e < 4 * 8 * 32; e += blockDim.x) {
-        const int kk = e >> 8, nt = (e >> 5) & 7, ln = e & 31;
-        const int i0 = kk * 16 + (ln & 3) * 2, j = nt * 8 + (ln >> 2);
-        const uint16_t* w1 = model->w1;
-        s_w1[kk][nt][ln] = make_uint2(pack_raw(w1[(i0 + 0) * kHid + j], w1[(i0 + 1) * kHid + j]),
-                                      pack_raw(w1[(i0 + 8) * kHid + j], w1[(i0 + 9) * kHid + j]));
+    // {b1[j], b1[j + 1], w2[j], w2[j + 1]} for even j, one 16-byte load per two columns
+    if (tid < (uint32_t)kHid / 2) {
+        const uint32_t j = 2 * tid;
+        reinterpret_cast<float4*>(s_b1)[tid] =
+            make_float4(model->b1[j], model->b1[j + 1], bf16_to_f(model->w2[j]), bf16_to_f(model->w2[j + 1]));
     }
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(s_tmem)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_before_sync();
     __syncthreads();
-    if (gw >= ngroups) return;
-    const int kq = (lane & 3) * 2;
+    tc_after_sync();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t t_row = tmem + ((warp * 32u) << 16);      // this warp's 32 lanes
     const float b2 = model->b2, thr = model->threshold;
-    // features (dz = kk, dy, dx) with c = dy * 4 + dx in {kq, kq + 1, kq + 8, kq + 9}
-    const int dx0 = kq & 3, dy0 = kq >> 2;
     const PadDims pd = pad_dims(ld);
     const uint32_t p01 = pd.p0 * pd.p1;
-    uint32_t npred = 0;
-    for (uint32_t grp = gw; grp < ngroups; grp += nw) {
-        const uint32_t e0 = grp * 16 + (lane >> 2), e1 = e0 + 8;
-        const uint2 c0 = __ldg(&clist[min(e0, n - 1)]), c1 = __ldg(&clist[min(e1, n - 1)]);
-        const uint32_t id0 = c0.x, id1 = c1.x;
-        PatchRow r0, r1;
-        patch_row(c0.y, dx0, dy0, pd.p0, p01, r0);
-        patch_row(c1.y, dx0, dy0, pd.p0, p01, r1);
-        float acc[8][4];
+    const uint32_t ntiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0, npred = 0;
+    bool ok = true;
+    // Software pipeline: while the tensor cores work on tile t (A buffer t & 1),
+    // the threads load tile t + 1's features into registers and finish tile t's
+    // epilogue; then they store those features into the other buffer and one
+    // thread issues tile t + 1's MMA.  Candidate records come one tile earlier.
+    const uint32_t e_step = gridDim.x * (uint32_t)kTcRows;
+    uint32_t g[32];
+    auto gather = [&](uint2 c) {
+        PatchRow r[4];
+        patch_row(c.y, 0, 0, pd.p0, p01, r[0]);
+        patch_row(c.y, 2, 0, pd.p0, p01, r[1]);
+        patch_row(c.y, 0, 1, pd.p0, p01, r[2]);
+        patch_row(c.y, 2, 1, pd.p0, p01, r[3]);
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+        for (int kk = 0; kk < 4; ++kk)
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            uint32_t a[4];
-            a[0] = patch_pair(dens2, r0, kk, 0);
-            a[1] = patch_pair(dens2, r1, kk, 0);
-            a[2] = patch_pair(dens2, r0, kk, 1);
-            a[3] = patch_pair(dens2, r1, kk, 1);
+            for (int yi = 0; yi < 2; ++yi)
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const uint2 bf = s_w1[kk][nt][lane];
-                mma_bf16(acc[nt], a, bf.x, bf.y);
-            }
+                for (int q = 0; q < 4; ++q) g[(kk * 2 + yi) * 4 + q] = patch_pair(dens2, r[q], kk, yi);
+    };
+    // this thread's row: features f = 16 dz + 4 dy + dx; chunk (dz, dy >> 1)
+    // holds dy & 1 = 0, 1 and dx = 0..3 as four bf16 pairs
+    auto store = [&](uint32_t buf, bool live) {
+        uint8_t* a = sA + buf * kTcBytesA;
+#pragma unroll
+        for (int ch = 0; ch < 8; ++ch)
+            *reinterpret_cast<uint4*>(a + umma_off(tid, (uint32_t)ch * 8u)) =
+                live ? make_uint4(g[ch * 4], g[ch * 4 + 1], g[ch * 4 + 2], g[ch * 4 + 3]) : make_uint4(0u, 0u, 0u, 0u);
+    };
+    auto issue = [&](uint32_t buf) {
+        if (tid == 0) {
+            tc_after_sync();
+            const uint32_t a0 = a_saddr + buf * kTcBytesA;
+#pragma unroll
+            for (uint32_t kk = 0; kk < 4; ++kk)
+                tc_mma(tmem, umma_desc(a0 + kk * 256u), umma_desc(b_saddr + kk * 256u), kk);
+            tc_commit(bar);
         }
-        float z0s = 0.f, z1s = 0.f;
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const float4 bw = s_bw[nt][lane & 3];
-            z0s += fmaxf(acc[nt][0] + bw.x, 0.f) * bw.z;
-            z0s += fmaxf(acc[nt][1] + bw.y, 0.f) * bw.w;
-            z1s += fmaxf(acc[nt][2] + bw.x, 0.f) * bw.z;
-            z1s += fmaxf(acc[nt][3] + bw.y, 0.f) * bw.w;
+    };
+    uint32_t tile = blockIdx.x, buf = 0;
+    uint32_t e = tile * kTcRows + tid;
+    bool live = tile < ntiles && e < n;
+    uint32_t id = 0;
+    uint2 c_pref = make_uint2(0u, 0u);
+    if (tile < ntiles) {
+        if (live) {
+            const uint2 c = __ldg(&clist[e]);
+            id = c.x;
+            gather(c);
         }
-        z0s += __shfl_xor_sync(0xffffffffu, z0s, 1);
-        z0s += __shfl_xor_sync(0xffffffffu, z0s, 2);
-        z1s += __shfl_xor_sync(0xffffffffu, z1s, 1);
-        z1s += __shfl_xor_sync(0xffffffffu, z1s, 2);
-        if ((lane & 3) == 0) {
-#pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-                const uint32_t e = rr ? e1 : e0;
-                if (e >= n) continue;
-                const float z = (rr ? z1s : z0s) + b2;
-                const uint32_t id = rr ? id1 : id0;
-                if (out.logit) {
-                    if (e < out.cand_cap) { out.cand[e] = id; out.logit[e] = z; }
-                    ++npred;
-                } else if (z > thr) {
-                    atomicOr(&out.q[id >> 5], 1u << (id & 31u));
-                    ++npred;
-                }
-            }
-        }
+        if (e + e_step < n) c_pref = __ldg(&clist[e + e_step]);
+        store(0, live);
+        fence_async_smem();                  // generic-proxy stores, read by the tensor cores
+        tc_before_sync();
+        __syncthreads();
+        issue(0);
     }
+    for (; tile < ntiles; tile += gridDim.x) {
+        const uint32_t tnext = tile + gridDim.x;
+        const uint32_t e_n = e + e_step;
+        const bool live_n = tnext < ntiles && e_n < n;
+        const uint2 c_n = c_pref;
+        uint32_t id_n = 0;
+        if (live_n) {
+            id_n = c_n.x;
+            gather(c_n);                     // in flight during the wait and the epilogue
+            if (e_n + e_step < n) c_pref = __ldg(&clist[e_n + e_step]);
+        }
+        uint32_t spins = 0;
+        bool done = false;
+        while (!(done = mbar_try(bar, phase)) && ++spins < kTcSpin) {
+        }
+        phase ^= 1u;
+        ok = __syncthreads_and(done) != 0;
+        if (!ok) break;
+        tc_after_sync();
+        float z = b2;
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            float v[16];
+            tc_ld16(t_row + q * 16u, v);
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+                const float4 bw = reinterpret_cast<const float4*>(s_b1)[(q * 16 + i) / 2];
+                z += fmaxf(v[i] + bw.x, 0.f) * bw.z;
+                z += fmaxf(v[i + 1] + bw.y, 0.f) * bw.w;
+            }
+        }
+        if (live) {
+            if (out.logit) {
+                if (e < out.cand_cap) { out.cand[e] = id; out.logit[e] = z; }
+                ++npred;
+            } else if (z > thr) {
+                atomicOr(&out.q[id >> 5], 1u << (id & 31u));
+                ++npred;
+            }
+        }
+        if (tnext < ntiles) {
+            // the other buffer was read by the MMA two tiles back, finished before this wait
+            store(buf ^ 1u, live_n);
+            fence_async_smem();
+        }
+        tc_before_sync();                    // this tile's accumulator reads finish before the next MMA
+        __syncthreads();
+        if (tnext < ntiles) issue(buf ^ 1u);
+        buf ^= 1u;
+        e = e_n;
+        live = live_n;
+        id = id_n;
+    }
+    if (!ok && tid == 0) atomicOr(err, kErrTimeout);
     // one count per warp
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) npred += __shfl_xor_sync(0xffffffffu, npred, o);
-    if (lane == 0 && npred) atomicAdd(out.n_pred, npred);
+    if ((tid & 31u) == 0 && npred) atomicAdd(out.n_pred, npred);
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -838,9 +993,12 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
     PredictOut out;
     out.q = q; out.cand = cand; out.logit = logit; out.cand_cap = cand_cap;
     out.n_pred = &cnt->l_pred;
-    k_learn_mlp<<<152u * kMlpBlocksPerSm, kMlpThreads, 0, ctx->stream>>>(
+    PMS_CUDA(ctx, cudaFuncSetAttribute(k_learn_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+    PMS_CUDA(ctx, cudaFuncSetAttribute(k_learn_mlp, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                       (int)cudaSharedmemCarveoutMaxShared));
+    k_learn_mlp<<<152u * kTcBlocksPerSm, kTcThreads, kTcSmem, ctx->stream>>>(
         ld, ctx->l_dens.as<uint32_t>(), ctx->l_clist.as<uint2>(), &cnt->l_cand,
-        ctx->l_model.as<DevModel>(), use_model, out);
+        ctx->l_model.as<DevModel>(), use_model, out, &cnt->err);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

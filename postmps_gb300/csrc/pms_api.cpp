@@ -229,6 +229,7 @@ static pms_status check_device_errors(pms_ctx* c) {
         return pms_fail(c, PMS_ERR_UNSUPPORTED, "a spatial cell holds more than 4096 particles (particles nearly coincide)");
     if (e & kErrKeyRange) return pms_fail(c, PMS_ERR_CUDA, "internal: a cell key fell outside the grid");
     if (e & kErrCapacity) return pms_fail(c, PMS_ERR_CAPACITY, "internal: device capacity exceeded");
+    if (e & kErrTimeout) return pms_fail(c, PMS_ERR_CUDA, "internal: a wait on the tensor cores timed out");
     return PMS_OK;
 }
 

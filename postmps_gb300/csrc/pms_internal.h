@@ -76,6 +76,7 @@ enum : uint32_t {
     kErrKeyRange = 2u,      // a cell key outside the grid
     kErrBigCell = 4u,       // a cell above the largest supported occupancy
     kErrCapacity = 8u,      // a device-side capacity was exceeded
+    kErrTimeout = 16u,      // a bounded wait on the tensor cores gave up
 };
 
 // Marching-cubes tables (see mc_tables.cu): 256 cases, corner order
