@@ -285,25 +285,27 @@ __device__ __forceinline__ uint32_t patch_pair(const uint32_t* __restrict__ dens
 // ---------------------------------------------------------------------------
 // The first layer on the fifth-generation tensor cores.  A block takes tiles
 // of 128 candidates.  Every thread gathers the 64 features of one candidate
-// into shared memory in the UMMA canonical K-major layout without swizzle
-// (8-row x 16-byte core matrices; the next one along K 128 B further, the next
-// 8-row group 1 KiB further), one thread issues four tcgen05.mma (M 128, N 64,
-// K 16; bf16 operands, fp32 accumulator in tensor memory) against W1 staged
-// once per block in the same layout, their completion arrives on an mbarrier,
-// and each warp reads its 32 rows of the accumulator back (tcgen05.ld
-// 32x32b) for b1, ReLU, w2 and b2.  The dynamic shared memory a block asks for
-// keeps at most five blocks on an SM, so their 5 x 64 tensor-memory columns fit
-// the SM's 512 and no allocation waits on another block.  Two A buffers let the
-// gathers of one tile overlap the MMA and the epilogue of the one before.
+// into registers and writes them to its lane of tensor memory (tcgen05.st
+// 32x32b: row = lane, two bf16 of K per 32-bit column); one thread issues four
+// tcgen05.mma (M 128, N 64, K 16; A from tensor memory, B = W1 from shared
+// memory in the UMMA canonical K-major layout without swizzle, staged once per
+// block; fp32 accumulator in tensor memory), their completion arrives on an
+// mbarrier, and each warp reads its 32 rows of the accumulator back
+// (tcgen05.ld 32x32b) for b1, ReLU, w2 and b2.  Two A buffers let the gathers
+// of one tile overlap the MMA and the epilogue of the one before.  The dynamic
+// shared memory a block asks for keeps at most four blocks on an SM, so their
+// 4 x 128 tensor-memory columns fit the SM's 512 and no allocation waits.
 // ---------------------------------------------------------------------------
 static constexpr int kTcThreads = 128, kTcRows = 128;
-static constexpr uint32_t kTcCols = 64;                         // tensor-memory columns: N fp32 accumulators
-static constexpr uint32_t kTcBytesA = kTcRows * kIn * 2, kTcBytesB = kHid * kIn * 2;   // one A buffer; two are used
-// 5 x (44 + 1) KiB fit an SM's 228 KiB, 6 x do not: five blocks per SM at most
-static constexpr uint32_t kTcSmem = 44u * 1024u;
+// tensor-memory columns: the N fp32 accumulators (0..63), then two A buffers of
+// 64 bf16 per row, two to a 32-bit column (64..95, 96..127)
+static constexpr uint32_t kTcCols = 128, kTcColA = 64;
+static constexpr uint32_t kTcBytesB = kHid * kIn * 2;
+// 4 x (50 + 1) KiB fit an SM's 228 KiB, 5 x do not: four blocks per SM at most
+static constexpr uint32_t kTcSmem = 50u * 1024u;
 static constexpr uint32_t kTcSpin = 1u << 22;                   // bound on the polls of one mbarrier phase
-static constexpr int kTcBlocksPerSm = 5;
-static_assert(2 * kTcBytesA + kTcBytesB + 2 * kHid * 4 + 64 + 1024 <= kTcSmem, "shared memory plan");
+static constexpr int kTcBlocksPerSm = 4;
+static_assert(kTcBytesB + 2 * kHid * 4 + 64 + 1024 <= kTcSmem, "shared memory plan");
 static_assert(kIn == 64 && kHid == 64, "the tile plan assumes 64 features and 64 hidden units");
 
 // byte offset of element (row r, k) of a K-major operand with 64 K elements (bf16)
@@ -324,11 +326,24 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
 constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) |
                               ((uint32_t)(kTcRows >> 4) << 24);
 
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+// A from tensor memory (lane = row, 16 bf16 of K in 8 columns), B from shared memory
+__device__ __forceinline__ void tc_mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+}
+// 32 consecutive 32-bit columns of this thread's lane, waited for
+__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+        "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]),
+        "r"(r[19]), "r"(r[20]), "r"(r[21]), "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]),
+        "r"(r[28]), "r"(r[29]), "r"(r[30]), "r"(r[31])
+        : "memory");
 }
 __device__ __forceinline__ void tc_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -378,14 +393,13 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
     }
     extern __shared__ uint8_t tc_smem[];
     uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tc_smem) + 1023u) & ~(uintptr_t)1023u);
-    uint8_t* sA = sm;
-    uint8_t* sB = sm + 2 * kTcBytesA;
+    uint8_t* sB = sm;
     float* s_b1 = reinterpret_cast<float*>(sB + kTcBytesB);
     float* s_w2 = s_b1 + kHid;
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_w2 + kHid);
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t a_saddr = (uint32_t)__cvta_generic_to_shared(sA), b_saddr = (uint32_t)__cvta_generic_to_shared(sB);
+    const uint32_t b_saddr = (uint32_t)__cvta_generic_to_shared(sB);
     const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
     // W1 as the B operand (row j = hidden unit, K = input feature i)
     for (uint32_t e = tid; e < (uint32_t)(kHid * kIn / 2); e += kTcThreads) {
@@ -438,22 +452,20 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
 #pragma unroll
                 for (int q = 0; q < 4; ++q) g[(kk * 2 + yi) * 4 + q] = patch_pair(dens2, r[q], kk, yi);
     };
-    // this thread's row: features f = 16 dz + 4 dy + dx; chunk (dz, dy >> 1)
-    // holds dy & 1 = 0, 1 and dx = 0..3 as four bf16 pairs
+    // this thread's row, features f = 16 dz + 4 dy + dx in K order: g[i] holds
+    // f = 2i, 2i + 1, the 32-bit column i of the row's lane in an A buffer
     auto store = [&](uint32_t buf, bool live) {
-        uint8_t* a = sA + buf * kTcBytesA;
+        if (!live)
 #pragma unroll
-        for (int ch = 0; ch < 8; ++ch)
-            *reinterpret_cast<uint4*>(a + umma_off(tid, (uint32_t)ch * 8u)) =
-                live ? make_uint4(g[ch * 4], g[ch * 4 + 1], g[ch * 4 + 2], g[ch * 4 + 3]) : make_uint4(0u, 0u, 0u, 0u);
+            for (int i = 0; i < 32; ++i) g[i] = 0u;
+        tc_st32(t_row + kTcColA + 32u * buf, g);
     };
     auto issue = [&](uint32_t buf) {
         if (tid == 0) {
             tc_after_sync();
-            const uint32_t a0 = a_saddr + buf * kTcBytesA;
 #pragma unroll
             for (uint32_t kk = 0; kk < 4; ++kk)
-                tc_mma(tmem, umma_desc(a0 + kk * 256u), umma_desc(b_saddr + kk * 256u), kk);
+                tc_mma_ts(tmem, tmem + kTcColA + 32u * buf + 8u * kk, umma_desc(b_saddr + kk * 256u), kk);
             tc_commit(bar);
         }
     };
@@ -470,7 +482,6 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
         }
         if (e + e_step < n) c_pref = __ldg(&clist[e + e_step]);
         store(0, live);
-        fence_async_smem();                  // generic-proxy stores, read by the tensor cores
         tc_before_sync();
         __syncthreads();
         issue(0);
@@ -518,7 +529,6 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
         if (tnext < ntiles) {
             // the other buffer was read by the MMA two tiles back, finished before this wait
             store(buf ^ 1u, live_n);
-            fence_async_smem();
         }
         tc_before_sync();                    // this tile's accumulator reads finish before the next MMA
         __syncthreads();
