@@ -142,12 +142,16 @@ __device__ __forceinline__ float3 normalized(float3 v) {
 static constexpr int kEmitWarps = kThreads / 32;
 static constexpr int kEmitStage = 32 * 15 * 6;     // floats: 32 cubes x 15 mesh vertices x {p, n}
 
+// kNormals: also the vertex normals (into vnorm); without them only positions
+// are made, from the same arithmetic, so the positions are the same either way.
+template <bool kNormals>
 __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counters* __restrict__ cnt,
                                                       const uint4* __restrict__ cube, const float* __restrict__ fdense,
                                                       float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
                                                       unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
-    __shared__ float stage[kEmitWarps][kEmitStage];
+    constexpr int kS = kNormals ? 6 : 3;       // staged floats per mesh vertex
+    __shared__ float stage[kEmitWarps][kEmitStage / 6 * kS];
     // the cubes whose first mesh vertex lies in [v_lo, v_hi): cube records are in
     // ascending first-vertex order, so both ends are lower bounds
     const uint32_t nvalid_all = cnt->nvalid;
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
             // is the cube's other corner on that axis, the other lies outside the cube
             float3 cn[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
+            for (int c = 0; c < 8 && kNormals; ++c) {
                 const int ox = corner_off(c, 0), oy = corner_off(c, 1), oz = corner_off(c, 2);
                 const int X = x + ox, Y = y + oy, Z = z + oz;
                 const float fx = grid_value(g, fdense, ox ? X + 1 : X - 1, Y, Z);
@@ -217,28 +221,39 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                 const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
                 const float ax = px[corner_off(a, 0)], ay = py[corner_off(a, 1)], az = pz[corner_off(a, 2)];
                 const float bx = px[corner_off(b, 0)], by = py[corner_off(b, 1)], bz = pz[corner_off(b, 2)];
-                const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x), cn[a].y + tt * (cn[b].y - cn[a].y),
-                                                         cn[a].z + tt * (cn[b].z - cn[a].z)));
-                const float q[6] = {ax + tt * (bx - ax), ay + tt * (by - ay), az + tt * (bz - az),
-                                    sgn * nn.x, sgn * nn.y, sgn * nn.z};
+                float q[kS];
+                q[0] = ax + tt * (bx - ax);
+                q[1] = ay + tt * (by - ay);
+                q[2] = az + tt * (bz - az);
+                if constexpr (kNormals) {
+                    const float3 nn = normalized(make_float3(cn[a].x + tt * (cn[b].x - cn[a].x),
+                                                             cn[a].y + tt * (cn[b].y - cn[a].y),
+                                                             cn[a].z + tt * (cn[b].z - cn[a].z)));
+                    q[3] = sgn * nn.x;
+                    q[4] = sgn * nn.y;
+                    q[5] = sgn * nn.z;
+                }
                 for (uint32_t m = __ldg(&slots[e]); m; m &= m - 1u) {
-                    float* dst = st + 6 * (o + (uint32_t)(__ffs(m) - 1));
+                    float* dst = st + kS * (o + (uint32_t)(__ffs(m) - 1));
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) dst[c] = q[c];
+                    for (int c = 0; c < kS; ++c) dst[c] = q[c];
                 }
             }
         }
         __syncwarp();
         // whole lines: positions, then normals
-        for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
-            const uint32_t v = i / 3u, c = i - 3u * v;
-            vert[3 * (size_t)w0 + i] = st[6 * v + c];
-        }
-        if (vnorm)
+        if constexpr (kNormals) {
+            for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
+                const uint32_t v = i / 3u, c = i - 3u * v;
+                vert[3 * (size_t)w0 + i] = st[6 * v + c];
+            }
             for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) {
                 const uint32_t v = i / 3u, c = i - 3u * v;
                 vnorm[3 * (size_t)w0 + i] = st[6 * v + 3 + c];
             }
+        } else {
+            for (uint32_t i = (uint32_t)lane; i < 3u * room; i += 32u) vert[3 * (size_t)w0 + i] = st[i];
+        }
         __syncwarp();
     }
 }
@@ -345,15 +360,21 @@ pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsi
                              unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
-    k_mc_emit<<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-        g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, v_lo,
-        v_hi);
+    if (vnorm)
+        k_mc_emit<true><<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
+            g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, v_lo,
+            v_hi);
+    else
+        k_mc_emit<false><<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
+            g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, nullptr, frame_base, cap,
+            v_lo, v_hi);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
 pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo, uint32_t v_hi) {
-    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->vnorm.as<float>(), nullptr, ~0ull, v_lo, v_hi);
+    return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->mesh_normals ? ctx->vnorm.as<float>() : nullptr, nullptr,
+                             ~0ull, v_lo, v_hi);
 }
 
 }  // namespace pms

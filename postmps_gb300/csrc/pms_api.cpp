@@ -398,7 +398,8 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         // the previous frame's mesh may still be on its way to the host
         if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
         PMS_CUDA(c, c->vert.ensure(12 * M));
-        PMS_CUDA(c, c->vnorm.ensure(12 * M));
+        c->mesh_normals = c->out_pos && c->out_nrm;
+        if (c->mesh_normals) PMS_CUDA(c, c->vnorm.ensure(12 * M));
         // a streamed mesh goes in pieces: the emission runs in vertex ranges and each
         // piece travels on the copy stream while the next is made and the stages after run
         const bool copy = c->out_pos && c->nmesh <= c->out_cap;
@@ -534,6 +535,14 @@ extern "C" pms_status pms_download_mesh(pms_ctx* c, float* pos, float* nrm, uint
     if (n_out) *n_out = c->nmesh;
     if (c->nmesh == 0) return PMS_OK;
     if (cap < c->nmesh || !pos) return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices", (unsigned long long)c->nmesh);
+    if (nrm && !c->mesh_normals) {
+        // the normals on demand: the emission once more, with them (same positions)
+        if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
+        PMS_CUDA(c, c->vnorm.ensure(12 * c->nmesh));
+        c->mesh_normals = true;
+        pms_status st = launch_mc_emit(c);
+        if (st) return st;
+    }
     PMS_CUDA(c, cudaMemcpyAsync(pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     if (nrm) PMS_CUDA(c, cudaMemcpyAsync(nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -156,6 +156,9 @@ struct pms_ctx {
     // field work items (runs of x-neighbouring band vertices)
     pms::DBuf fitems, fitem_cnt, fitem_off;
     bool have_values = false;
+    // vertex normals of the current mesh: made by the emission only when a streamed
+    // mesh asks for them, else on the first download that does
+    bool mesh_normals = false;
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
