@@ -198,7 +198,9 @@ pms_status pms_get_counts(pms_ctx* ctx, pms_counts* out);
 pms_status pms_get_grid(pms_ctx* ctx, pms_grid* out);
 /* Triangle soup, 3 vertices per triangle (positions and normals xyz float32);
  * nrm_xyz may be NULL.  Replaces the D2H copies of FileData::saveSurfacePLYfile
- * (FileData.cpp:1297-1300).  *n_vertices receives the count even on PMS_ERR_CAPACITY. */
+ * (FileData.cpp:1297-1300).  *n_vertices receives the count even on PMS_ERR_CAPACITY.
+ * The marching cubes make the normals only when a streamed mesh asked for them;
+ * otherwise the first call that passes nrm_xyz makes them (one more emission pass). */
 pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices,
                              uint64_t* n_vertices);
 /* Registers host buffers (page-locked, e.g. cudaHostAlloc or cudaHostRegister,
