@@ -123,6 +123,36 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
 
 
 @pytest.mark.gpu
+def test_normals_on_demand_equal_streamed_normals(pms_lib):
+    """Without a streamed normal buffer the marching cubes write positions only;
+    the first download that asks for normals runs the emission again with them.
+    Positions before and after, and the normals, equal those of a frame whose
+    streamed mesh carried normals."""
+    import torch
+    pms = pms_lib
+    frames = _frames(2)
+    with _ctx(pms, 0.02) as ctx:
+        buf = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
+        nrm = torch.empty(3 * 2_000_000, dtype=torch.float32).pin_memory()
+        ref = []
+        ctx.stream_mesh_to_host(buf.data_ptr(), nrm.data_ptr(), buf.numel() // 3)
+        for fr in frames:
+            ctx.upload(*fr)
+            ctx.run_frame()
+            n = ctx.wait_mesh()
+            ref.append((buf.numpy()[: 3 * n].reshape(-1, 3).copy(), nrm.numpy()[: 3 * n].reshape(-1, 3).copy()))
+        ctx.stream_mesh_to_host(0, None, 0)
+        for fr, (pos_s, nrm_s) in zip(frames, ref):
+            ctx.upload(*fr)
+            ctx.run_frame()
+            pos_only, _ = ctx.mesh(normals=False)
+            pos, nrm_d = ctx.mesh(normals=True)
+            assert np.array_equal(pos_only, pos_s)
+            assert np.array_equal(pos, pos_s)
+            assert np.array_equal(nrm_d, nrm_s)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("diffuse", [False, True])
 def test_streamed_mesh_equals_download(pms_lib, diffuse):
     """pms_stream_mesh_to_host: the soup that reaches pinned host memory -- copied
