@@ -501,9 +501,18 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
         bool done = false;
         while (!(done = mbar_try(bar, phase)) && ++spins < kTcSpin) {
         }
-        phase ^= 1u;
         ok = __syncthreads_and(done) != 0;
-        if (!ok) break;
+        if (!ok) {
+            // give the MMA in flight a second bounded wait before its tensor memory is freed
+            if (tid == 0) {
+                uint32_t again = 0;
+                while (!mbar_try(bar, phase) && ++again < kTcSpin) {
+                }
+            }
+            __syncthreads();
+            break;
+        }
+        phase ^= 1u;
         tc_after_sync();
         float z = b2;
 #pragma unroll
