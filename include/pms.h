@@ -253,6 +253,13 @@ typedef enum pms_array {
     PMS_ARRAY_FREE_NORMAL = 21        /* float[3 n] particle normals after the diffuse colour-gradient pass */
 } pms_array;
 pms_status pms_debug_download(pms_ctx* ctx, int array_id, void* dst, uint64_t cap_bytes, uint64_t* needed);
+/* Tests of the failure path: the first bounded wait of the band network on the
+ * tensor cores gives up after `polls` polls (0: at once; negative: the default
+ * bound).  A wait that gives up sets an error the next pms_get_counts reports
+ * ("a wait on the tensor cores timed out"); a second bounded wait lets the
+ * work in flight finish before the kernel frees its tensor memory, so the
+ * context stays usable.  No reference counterpart. */
+pms_status pms_debug_set_wait_limit(pms_ctx* ctx, int64_t polls);
 
 /* Device time of each stage of the last frame, in milliseconds (CUDA events on
  * the context stream): [grid, anisotropy, band, field, marching cubes, diffuse]. */

@@ -382,7 +382,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
 __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnDims ld, const uint32_t* __restrict__ dens2,
                                                           const uint2* __restrict__ clist, const uint32_t* __restrict__ n_dev,
                                                           const DevModel* __restrict__ model, int use_model, PredictOut out,
-                                                          uint32_t* __restrict__ err) {
+                                                          uint32_t* __restrict__ err, uint32_t wait_polls) {
     const uint32_t n = *n_dev;
     if (!use_model) {
         // collect only
@@ -497,9 +497,8 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
             gather(c_n);                     // in flight during the wait and the epilogue
             if (e_n + e_step < n) c_pref = __ldg(&clist[e_n + e_step]);
         }
-        uint32_t spins = 0;
         bool done = false;
-        while (!(done = mbar_try(bar, phase)) && ++spins < kTcSpin) {
+        for (uint32_t spins = 0; spins < wait_polls && !(done = mbar_try(bar, phase)); ++spins) {
         }
         ok = __syncthreads_and(done) != 0;
         if (!ok) {
@@ -1017,7 +1016,7 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
                                        (int)cudaSharedmemCarveoutMaxShared));
     k_learn_mlp<<<152u * kTcBlocksPerSm, kTcThreads, kTcSmem, ctx->stream>>>(
         ld, ctx->l_dens.as<uint32_t>(), ctx->l_clist.as<uint2>(), &cnt->l_cand,
-        ctx->l_model.as<DevModel>(), use_model, out, &cnt->err);
+        ctx->l_model.as<DevModel>(), use_model, out, &cnt->err, ctx->tc_wait_polls ? ctx->tc_wait_polls - 1u : kTcSpin);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

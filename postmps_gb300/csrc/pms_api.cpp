@@ -603,6 +603,12 @@ static pms_status d2h(pms_ctx* c, std::vector<T>& v, const void* src, size_t cou
     return PMS_OK;
 }
 
+extern "C" pms_status pms_debug_set_wait_limit(pms_ctx* c, int64_t polls) {
+    if (!c || polls > 0xfffffffell) return PMS_ERR_INVALID_ARGUMENT;
+    c->tc_wait_polls = polls < 0 ? 0u : (uint32_t)polls + 1u;
+    return PMS_OK;
+}
+
 extern "C" pms_status pms_debug_download(pms_ctx* c, int id, void* dst, uint64_t cap, uint64_t* needed) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(c->device);

@@ -167,6 +167,8 @@ struct pms_ctx {
     pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
               l_field_new, l_vlist_m, l_qnext, l_cand, l_logit, l_label, l_qlist, l_wp_q;
     bool have_model = false, band_learned = false, mc_classified = false, mc_compacted = false;
+    // polls + 1 of the first bounded wait on the tensor cores (0: the default bound)
+    uint32_t tc_wait_polls = 0;
     int band_mode = PMS_BAND_PLAIN;
     pms::Tune tune;
     // batched frames (pms_batch.cpp)

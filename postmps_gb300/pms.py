@@ -181,6 +181,7 @@ def lib() -> C.CDLL:
         L.pms_download_mesh.argtypes = [vp, vp, vp, C.c_uint64, C.POINTER(C.c_uint64)]
         L.pms_download_diffuse.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32)]
         L.pms_debug_download.argtypes = [vp, C.c_int, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.pms_debug_set_wait_limit.argtypes = [vp, C.c_int64]
         L.pms_stage_times.argtypes = [vp, _f32p, C.c_int]
         L.pms_kernel_launches.argtypes = [vp]
         L.pms_kernel_launches.restype = C.c_uint64
@@ -531,6 +532,11 @@ class Context:
         ms = np.zeros(6, np.float32)
         _check(lib().pms_stage_times(self._h, ms, 6), self._h)
         return dict(zip(("grid", "anisotropy", "band", "field", "marching_cubes", "diffuse"), ms.tolist()))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """First bounded wait on the tensor cores: give up after `polls` polls
+        (0: at once; negative: the default bound).  For tests of the timeout path."""
+        self._call("pms_debug_set_wait_limit", polls)
 
     @property
     def launches(self) -> int:

@@ -253,6 +253,35 @@ def test_held_out_frame_has_no_cube_outside_the_plain_band(pms_lib):
 
 
 @pytest.mark.gpu
+def test_tensor_core_wait_that_gives_up_reports_and_recovers(pms_lib):
+    """The band network's wait on the tensor cores is bounded: made to give up at
+    once, the frame reports the timeout (no fault, no hang), and with the bound
+    restored the same context reconstructs the frame as before."""
+    pms = pms_lib
+    from postmps_gb300 import learned
+    if not os.path.exists(learned.DEFAULT_MODEL):
+        pytest.skip("no trained model committed")
+    ctx, cfg, pos, vel, rho = _crown_ctx(pms, 0.03, seed=202)
+    with ctx:
+        ctx.set_band_model(learned.load_model())
+
+        def frame():
+            ctx.upload(pos, vel, rho)
+            ctx.build_grid()
+            ctx.surface_learned()
+            return ctx.counts()
+
+        ref = frame()
+        ctx.set_wait_limit(0)
+        with pytest.raises(pms.PmsError, match="tensor cores"):
+            frame()
+        ctx.set_wait_limit(-1)
+        again = frame()
+        assert again.n_valid_cubes == ref.n_valid_cubes > 0
+        assert again.n_mesh_vertices == ref.n_mesh_vertices
+
+
+@pytest.mark.gpu
 def test_committed_model_gain_on_held_out_frame(pms_lib):
     pms = pms_lib
     from postmps_gb300 import learned
