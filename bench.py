@@ -60,7 +60,7 @@ def workload(name: str):
     from postmps_gb300 import synth
     if name == "crown":
         frames = [synth.crown_splash()]
-        keys = {"sim.particlespacing": 0.005}
+        keys = dict(synth.CROWN_KEYS)
         desc = {"workload": "crown_splash_2M", "particles": int(len(frames[0][0])), "h": 0.01, "grid_cell": 0.0025,
                 "iso": 0.5, "clamp_ratio": 4}
         return frames, keys, desc, True

@@ -274,15 +274,6 @@ uint64_t pms_kernel_launches(const pms_ctx* ctx);
 int pms_mc_tables(uint32_t* edge_flags /*256*/, int32_t* tri /*256*16*/, uint32_t* num_vertices /*256*/,
                   uint32_t* edge_vertices /*24*/, int derived);
 
-/* Exclusive prefix sum of n uint32 device values into d_out (d_total, if not
- * NULL, receives the sum), on cuda_stream (NULL: the default stream).  It
- * allocates nothing -- for host programs that own all device memory or that
- * cannot afford cudaMalloc's implicit synchronisation inside a frame; its only
- * scratch is a 16 KiB file-scope device array held by every GPU that loads the
- * library.  n above 33,554,432 returns PMS_ERR_CAPACITY.  The first call on
- * each device looks up that array's device address (make it before any stream
- * capture).  Concurrent calls on the GPU share the scratch and race.
- * No counterpart in the reference (its scans allocate through thrust). */
 /* ---------------------------------------------------------------------------
  * Learned narrow band.  No counterpart in the reference: it replaces the band
  * marking of Anisotropic::processingOfVertices (Anisotropic.cu:43-50,
@@ -401,6 +392,16 @@ pms_status pms_autotune(pms_ctx* ctx, pms_tune* out);
 pms_status pms_set_tune(pms_ctx* ctx, const pms_tune* t);
 pms_status pms_get_tune(pms_ctx* ctx, pms_tune* out);
 
+
+/* Exclusive prefix sum of n uint32 device values into d_out (d_total, if not
+ * NULL, receives the sum), on cuda_stream (NULL: the default stream).  It
+ * allocates nothing -- for host programs that own all device memory or that
+ * cannot afford cudaMalloc's implicit synchronisation inside a frame; its only
+ * scratch is a 16 KiB file-scope device array held by every GPU that loads the
+ * library.  n above 33,554,432 returns PMS_ERR_CAPACITY.  The first call on
+ * each device looks up that array's device address (make it before any stream
+ * capture).  Concurrent calls on the GPU share the scratch and race.
+ * No counterpart in the reference (its scans allocate through thrust). */
 pms_status pms_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, uint32_t* d_total,
                                           void* cuda_stream);
 

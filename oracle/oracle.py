@@ -80,8 +80,8 @@ def build(quiet: bool = True) -> None:
     """Compile liboracle.so (and libref_emu.so when the reference tree exists)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE], stdout=out)
-    ref = os.environ.get("PMS_REFERENCE_DIR", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "src", "cuda")):
+    ref = os.environ.get("PMS_REFERENCE_DIR")       # the reference checkout, when there is one
+    if ref and os.path.isdir(os.path.join(ref, "src", "cuda")):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], stdout=out)
 
 

@@ -505,8 +505,11 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
             // give the MMA in flight a second bounded wait before its tensor memory is freed
             if (tid == 0) {
                 uint32_t again = 0;
-                while (!mbar_try(bar, phase) && ++again < kTcSpin) {
+                bool landed = false;
+                while (!(landed = mbar_try(bar, phase)) && ++again < kTcSpin) {
                 }
+                // the tensor memory is freed below either way: the host must not trust this context
+                if (!landed) atomicOr(err, kErrTcLost);
             }
             __syncthreads();
             break;

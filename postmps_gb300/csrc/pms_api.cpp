@@ -229,6 +229,8 @@ static pms_status check_device_errors(pms_ctx* c) {
         return pms_fail(c, PMS_ERR_UNSUPPORTED, "a spatial cell holds more than 4096 particles (particles nearly coincide)");
     if (e & kErrKeyRange) return pms_fail(c, PMS_ERR_CUDA, "internal: a cell key fell outside the grid");
     if (e & kErrCapacity) return pms_fail(c, PMS_ERR_CAPACITY, "internal: device capacity exceeded");
+    if (e & kErrTcLost)
+        return pms_fail(c, PMS_ERR_CUDA, "a tensor-core operation outlived two bounded waits; destroy this context");
     if (e & kErrTimeout) return pms_fail(c, PMS_ERR_CUDA, "internal: a wait on the tensor cores timed out");
     return PMS_OK;
 }
@@ -604,7 +606,8 @@ static pms_status d2h(pms_ctx* c, std::vector<T>& v, const void* src, size_t cou
 }
 
 extern "C" pms_status pms_debug_set_wait_limit(pms_ctx* c, int64_t polls) {
-    if (!c || polls > 0xfffffffell) return PMS_ERR_INVALID_ARGUMENT;
+    // the stored value is polls + 1 (0 selects the default bound), so polls stays below 2^32 - 1
+    if (!c || polls >= 0xffffffffll) return PMS_ERR_INVALID_ARGUMENT;
     c->tc_wait_polls = polls < 0 ? 0u : (uint32_t)polls + 1u;
     return PMS_OK;
 }

@@ -58,6 +58,7 @@ struct BatchState {
     uint32_t captures = 0, reruns = 0;
     uint64_t gen = 0;                 // buffer generation the graph was captured against
     uint32_t nlanes_captured = 0;
+    uint32_t wait_captured = 0;       // the debug wait limit baked into the captured launches
     ~BatchState() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -270,6 +271,7 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
     if ((st = ensure_band_buffers(lc, gmax.sc_size))) return st;
     PMS_CUDA(lc, lc->scan.partial.ensure(sizeof(unsigned long long) * 1024));
     lc->tune = c->tune;
+    lc->tc_wait_polls = c->tc_wait_polls;     // the debug wait limit holds on every lane
     if (!learned) return PMS_OK;
     const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
     const size_t S = (size_t)gmax.sc_size + 1;
@@ -305,6 +307,9 @@ static pms_status check_frame_errors(pms_ctx* c, const Counters& h, uint32_t f) 
     if (h.err & kErrNonFinite) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: positions contain NaN or Inf", f);
     if (h.err & kErrBigCell) return pms_fail(c, PMS_ERR_UNSUPPORTED, "frame %u: a spatial cell holds more than 4096 particles", f);
     if (h.err & kErrKeyRange) return pms_fail(c, PMS_ERR_CUDA, "frame %u: internal: a cell key fell outside the grid", f);
+    if (h.err & kErrTcLost)
+        return pms_fail(c, PMS_ERR_CUDA, "frame %u: a tensor-core operation outlived two bounded waits; destroy this context", f);
+    if (h.err & kErrTimeout) return pms_fail(c, PMS_ERR_CUDA, "frame %u: internal: a wait on the tensor cores timed out", f);
     return PMS_OK;
 }
 
@@ -402,7 +407,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     if (!b->fork) PMS_CUDA(c, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     for (uint32_t l = 0; l < nlanes; ++l)
         if ((st = ensure_lane(lane_ctx(c, b, l), c, nmax, gmax, grid, learned))) return st;
-    if (nlanes != b->nlanes_captured) grids_same = false;
+    if (nlanes != b->nlanes_captured || c->tc_wait_polls != b->wait_captured) grids_same = false;
     uint64_t want_cap = 0;
     for (uint32_t f = 0; f < k; ++f) {
         const uint64_t sx = grid[f].scres[0], sy = grid[f].scres[1], sz = grid[f].scres[2];
@@ -423,6 +428,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
             if ((st = capture(c, b, learned, nlanes))) return st;
             b->gen = g_dbuf_generation;
             b->nlanes_captured = nlanes;
+            b->wait_captured = c->tc_wait_polls;
             grids_same = true;
         }
         PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));

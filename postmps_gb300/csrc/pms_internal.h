@@ -77,6 +77,7 @@ enum : uint32_t {
     kErrBigCell = 4u,       // a cell above the largest supported occupancy
     kErrCapacity = 8u,      // a device-side capacity was exceeded
     kErrTimeout = 16u,      // a bounded wait on the tensor cores gave up
+    kErrTcLost = 32u,       // ... and the MMA in flight outlived a second bounded wait
 };
 
 // Marching-cubes tables (see mc_tables.cu): 256 cases, corner order

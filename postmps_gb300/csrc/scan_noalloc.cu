@@ -165,10 +165,10 @@ extern "C" pms_status pms_exclusive_scan_u32_noalloc(const uint32_t* d_in, uint3
     }
     const int ntiles = (int)((n + kTile - 1) / kTile);
     k_tile_sums<<<ntiles, kThreads, 0, s>>>(d_in, n, partials);
-    if (cudaPeekAtLastError() != cudaSuccess) return PMS_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return PMS_ERR_CUDA;
     k_tile_offsets<<<1, 1024, 0, s>>>(partials, ntiles, d_total);
-    if (cudaPeekAtLastError() != cudaSuccess) return PMS_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return PMS_ERR_CUDA;
     k_tile_scan<<<ntiles, kThreads, 0, s>>>(d_in, d_out, n, partials);
-    if (cudaPeekAtLastError() != cudaSuccess) return PMS_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return PMS_ERR_CUDA;
     return PMS_OK;
 }

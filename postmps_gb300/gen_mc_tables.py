@@ -1,7 +1,7 @@
 """Build step: extract the reference's marching-cubes tables.
 
-Reads MarchingCubesHelper.cpp from a reference checkout (default
-/root/reference, or $PMS_REFERENCE_DIR) and writes the git-ignored generated
+Reads MarchingCubesHelper.cpp from the reference checkout named by
+$PMS_REFERENCE_DIR (required for this step) and writes the git-ignored generated
 header postmps_gb300/_build/gen/mc_tables.inc that mc_tables.cu includes, so
 that triangle soups come out in the reference's exact order.  The tables are
 not committed; without a reference checkout the build uses the tables derived
@@ -75,7 +75,11 @@ def write_inc(t: dict, path: str = OUT) -> None:
 
 
 def main() -> int:
-    ref = os.environ.get("PMS_REFERENCE_DIR", "/root/reference")
+    ref = os.environ.get("PMS_REFERENCE_DIR")
+    if not ref:
+        have = "keeping existing " + OUT if os.path.exists(OUT) else "using the derived tables"
+        print(f"gen_mc_tables: PMS_REFERENCE_DIR is not set (the reference checkout), {have}")
+        return 0
     t = extract(ref)
     if t is None:
         if os.path.exists(OUT):

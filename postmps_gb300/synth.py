@@ -183,6 +183,20 @@ DEFAULT_KEYS = {
 }
 
 
+# The crown splash workloads (h = 0.01, scalar cell 0.0025).  Diffuse thresholds:
+# the reference's sample keys (kinetic energy 5-50, trapped air 5-20) are set for
+# its own scenes; with Mass = 1 the ring's kinetic energy 0.5 m |v|^2 is about 1.1
+# at 1.5 m/s and its trapped-air potential stays below 4, so both are clamped over
+# the ranges the ring covers, and the ring spawns spray, foam and bubbles.
+CROWN_KEYS = {
+    "sim.particlespacing": 0.005,
+    "diffuse.minkineticenergythreshold": 0.5,
+    "diffuse.maxkineticenergythreshold": 5.0,
+    "diffuse.mintrappedairthreshold": 0.5,
+    "diffuse.maxtrappedairthreshold": 4.0,
+}
+
+
 def config_text(**overrides) -> str:
     """config.txt text in the reference's INI layout (bin/config.txt)."""
     keys = dict(DEFAULT_KEYS)

@@ -4,10 +4,10 @@ The reference ships no tests or fixtures, so the fixtures are produced by
 running the reference's own kernels (NeighborSearch_kernel.cuh,
 Anisotropic_kernel.cuh, MarchingCube_kernel.cuh, SVD3.cuh, myCuda.cuh) and its
 Params.cpp, compiled unmodified for the CPU by ``make -C oracle ref`` (see
-oracle/ref_emu/).  Needs the reference tree (default /root/reference, or
-$PMS_REFERENCE_DIR); the committed .npz files are what the tests read.
+oracle/ref_emu/).  Needs the reference tree, named by $PMS_REFERENCE_DIR; the
+committed .npz files are what the tests read.
 
-    python tests/golden/make_golden.py
+    PMS_REFERENCE_DIR=path/to/PostMPS python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -125,9 +125,13 @@ def make_diffuse() -> str:
 
 
 def main() -> int:
+    if not os.environ.get("PMS_REFERENCE_DIR"):
+        print("set PMS_REFERENCE_DIR to the reference checkout: the fixtures come from its own kernels",
+              file=sys.stderr)
+        return 1
     O.build()
     if not O.ref_available():
-        print("reference tree not found: cannot generate fixtures", file=sys.stderr)
+        print("the reference's kernels did not build from PMS_REFERENCE_DIR: cannot generate fixtures", file=sys.stderr)
         return 1
     for name in CASES:
         p = make(name)

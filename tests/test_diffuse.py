@@ -86,22 +86,47 @@ def live_records(live: dict) -> np.ndarray:
 @pytest.mark.gpu
 def test_diffuse_gpu_two_frames(pms_lib, oracle, tmp_config):
     d = golden()
-    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(d["config"])))
     gpu = run_gpu_frames(pms_lib, tmp_config, d)
+    check_gpu_frames(oracle, d, gpu, reference=True)
+
+
+@pytest.mark.gpu
+def test_diffuse_gpu_crown_spawns(pms_lib, oracle, tmp_config):
+    """A small crown splash (83,200 particles, a 40k-particle ring) with the crown
+    workload's diffuse keys: the ring spawns spray, foam and bubbles, and two
+    frames of the GPU chain match the oracle (counts exact from the GPU's clamped
+    potentials, spawned and advected particles exact, velocities 1e-5)."""
+    from postmps_gb300 import synth
+    pos, vel, rho = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    dt = 0.004
+    d = {"config": synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"}), "seed": 7,
+         "f0_pos": pos, "f0_vel": vel, "f0_rho": rho,
+         "f1_pos": (pos + dt * vel).astype(np.float32), "f1_vel": vel, "f1_rho": rho}
+    gpu = run_gpu_frames(pms_lib, tmp_config, d)
+    assert gpu[0]["counts"]["n_generated_diffuse"] > 1000, gpu[0]["counts"]
+    assert min(gpu[1]["counts"][k] for k in ("n_spray", "n_foam", "n_bubble")) > 0, gpu[1]["counts"]
+    check_gpu_frames(oracle, d, gpu, reference=False)
+
+
+def check_gpu_frames(oracle, d, gpu, reference: bool):
+    p = oracle.derive_params(oracle.config_from_keys(oracle.parse_ini(d["config"])))
     prev_live = np.zeros((0, 8), np.float32)
     for fr, r in enumerate(gpu):
         pos, vel = d[f"f{fr}_pos"], d[f"f{fr}_vel"]
         g, perm, start, end, slist = sorted_frame(oracle, p, pos)
         np.testing.assert_array_equal(r["perm"], perm)
-        assert r["counts"]["n_free_surface"] == len(slist) == len(d[f"f{fr}_free_list"])
-        # potentials against the reference (float32 vs float32, different summation order)
-        assert float(np.abs(r["pot"] - d[f"f{fr}_pot"]).max()) < 1e-3
+        assert r["counts"]["n_free_surface"] == len(slist)
+        if reference:
+            assert len(slist) == len(d[f"f{fr}_free_list"])
+            # potentials against the reference (float32 vs float32, different summation order)
+            assert float(np.abs(r["pot"] - d[f"f{fr}_pot"]).max()) < 1e-3
         # counts: exact from the GPU's own clamped potentials
         spos, svel = pos[perm], vel[perm]
         res = oracle.diffuse_frame(p, g, spos, svel, start, end, slist, np.zeros_like(spos, np.float64),
                                    int(d["seed"]), fr, old=prev_live, nrm_for_crests=r["nrm"], pot_clamped=r["pot"])
         np.testing.assert_array_equal(r["num"], res["num"])
-        assert np.mean(r["num"] == d[f"f{fr}_num"]) > 0.99
+        if reference:
+            assert np.mean(r["num"] == d[f"f{fr}_num"]) > 0.99
         assert r["counts"]["n_generated_diffuse"] == int(np.clip(res["num"], 0, None).sum())
         # live particles: generated (from the GPU's counts) then advected old ones, type 3 dropped
         live = live_records(r["live"])

@@ -218,3 +218,23 @@ def test_scalar_values_match_oracle(pms_lib, oracle, tmp_config, tmp_path, case)
     pms.write_surface_vtk(path, verts, nrm, sv["vel"], sv["vel_len"], sv["rhop"])
     head = open(path, "rb").read(200)
     assert head.startswith(b"# vtk DataFile Version 3.0\nsurface\nBINARY\nDATASET POLYDATA\nPOINTS ")
+
+
+@pytest.mark.parametrize("case", ["drops_sheet", "block12_ratio4"])
+def test_fp64_eigen_branch_matches_oracle(pms_lib, oracle, tmp_config, case):
+    """Covariances whose condition number exceeds [GB300] Fp64SvdCondition are
+    re-solved in float64.  With the limit lowered to 2 nearly every surface
+    particle takes that branch; G, the band, field, cases and mesh still meet
+    the float32 branch's bounds against the float64 oracle, and the mesh equals
+    the float32 branch's mesh within 1e-4 cell."""
+    d = load_golden(case)
+    text = d["config"] + "\n[GB300]\nFp64SvdCondition = 2\n"
+    out = run_gpu(pms_lib, tmp_config(text), d["pos"], d["vel"], d["rho_in"])
+    c = out["counts"]
+    assert c["n_fp64_svd"] > 0.5 * c["n_surface_particles"] > 0, c
+    check_against_oracle(oracle, pms_lib, d["config"], d["pos"], out)
+    base = run_gpu(pms_lib, tmp_config(d["config"]), d["pos"], d["vel"], d["rho_in"])
+    assert base["counts"]["n_fp64_svd"] < c["n_fp64_svd"]
+    g = out["grid"]
+    if len(base["vpos"]) == len(out["vpos"]) and len(out["vpos"]):
+        assert float(np.abs(base["vpos"] - out["vpos"]).max()) < 1e-4 * g.sc_grid_size

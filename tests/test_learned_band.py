@@ -279,6 +279,20 @@ def test_tensor_core_wait_that_gives_up_reports_and_recovers(pms_lib):
         again = frame()
         assert again.n_valid_cubes == ref.n_valid_cubes > 0
         assert again.n_mesh_vertices == ref.n_mesh_vertices
+        # batched frames: every lane's captured launches carry the limit, and the
+        # frame reports the timeout too (no silent incomplete band)
+        frames = [(pos, vel, rho), (pos, vel, rho)]
+        ctx.run_batch(frames, learned=True)
+        ok = ctx.batch_frame(0)[0].n_mesh_vertices
+        assert ok == ref.n_mesh_vertices
+        ctx.set_wait_limit(0)
+        with pytest.raises(pms.PmsError, match="tensor cores"):
+            ctx.run_batch(frames, learned=True)
+        ctx.set_wait_limit(-1)
+        ctx.run_batch(frames, learned=True)
+        assert ctx.batch_frame(1)[0].n_mesh_vertices == ref.n_mesh_vertices
+        with pytest.raises(pms.PmsError):
+            ctx.set_wait_limit(0xffffffff)
 
 
 @pytest.mark.gpu
