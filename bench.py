@@ -11,11 +11,14 @@ Workloads (seeded synthetic data; --workload):
            graph launch); a step is the whole batch.
   dam      the 8M-particle dam break (400x100x200, spacing 0.005), diffuse off.
 
-Bands (--band): "learned" runs the learned narrow band with its exact
-border-check fallback, "plain" the reference's band; the default runs both on
-the same frames, reports the learned arm as the headline (when a trained model
-is present) and the plain arm beside it, and judges the learned mesh against
-the plain mesh (triangle-count delta, Hausdorff distance in units of h).
+Bands (--band): "learned" runs the learned narrow band (the network picks the
+band vertices evaluated exactly at once, the exact sign certification covers
+the rest), "certified" the certification alone, "plain" the reference's band;
+the default runs all three on the same frames, reports the learned arm as the
+headline (when a trained model is present, its meshes equal the plain ones and
+it is faster end to end) and the others beside it, and judges each mesh
+against the plain mesh (identical soups, triangle-count delta, Hausdorff
+distance in units of h).
 
 `value` is measured with the inputs already on the device (device-to-device
 upload inside the step); `e2e` goes through the C ABI from pinned host
@@ -102,13 +105,13 @@ def algorithmic_bytes(c: dict, sp_size: int, sc_size: int, diffuse: bool, learne
     P = max(1, -(-int(np.ceil(np.log2(max(Ssp, 2)))) // 8))
     grid = (16 * N + Ssp / 8) + 16 * N * P + (32 * N + (24 * N if diffuse else 0)) + (4 * N + 8 * Ssp)
     aniso = (Ssp / 8 + 8 * Ssp + 4 * Ns) + (16 * N + 68 * Ns) + 20 * N
+    band = 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
     if learned:
         coarse = Ssc / 8
-        # coarse counts (read positions, write counts), prediction (read counts, write
-        # cube bits), cube corners, vertex scan and list
-        band = (16 * N + 4 * coarse) + (4 * coarse + Ssc / 8) + 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
-    else:
-        band = 2 * Ssc / 8 + (Ssc / 8 + 4 * Vs)
+        # on top of the plain band: coarse counts (read positions, write counts), prediction
+        # (read counts, write cube bits), the split (read cube and band bits, write two
+        # bitmaps) and its two lists
+        band += (16 * N + 4 * coarse) + (4 * coarse + Ssc / 8) + 3 * Ssc / 8 + 4 * Vs
     field = 16 * N + 44 * Ns + 8 * Vs
     mc = (4 * Vs + Ssc / 8 + 9 * Vs) + (12 * 8 * Cv + 24 * M)
     dif = (64 * N + 44 * (c["n_generated_diffuse"] + c["n_diffuse"])) if diffuse else 0
@@ -261,12 +264,12 @@ class Timer:
         return max_over_ranks(ms, self.world, "cuda")
 
 
-def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse: bool, clocks=None) -> dict:
+def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bool, clocks=None) -> dict:
     pos, vel, rho = frame
     n = len(pos)
     d_pos, d_vel, d_rho = (torch.from_numpy(a).cuda() for a in (pos, vel, rho))
     h_pos, h_vel, h_rho = (torch.from_numpy(a).pin_memory() for a in (pos, vel, rho))
-    ctx.set_band_mode(learned)
+    ctx.set_band_mode(mode)
     host = {}
 
     def step_device():
@@ -276,12 +279,12 @@ def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse
     def step_e2e():
         # the user's calls: upload from pinned host memory, reconstruct with the
         # triangle soup streamed into pinned host memory while the diffuse stage
-        # runs, wait for it, read the live diffuse particles back
+        # runs and the live diffuse particles streamed after it, wait for both
         ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
         ctx.run_frame()
         host["n_mesh"] = ctx.wait_mesh()
         if diffuse:
-            host["diffuse"] = ctx.diffuse_particles(-1)
+            host["n_diffuse"] = ctx.wait_diffuse()
 
     stage_sum = {k: 0.0 for k in STAGES}
 
@@ -303,16 +306,24 @@ def single_frame_arm(pms, ctx, frame, learned: bool, args, timer, torch, diffuse
     # the host mesh buffer (pinned), sized from the frame's mesh
     host["mesh"] = torch.empty(max(3, int(3 * counts["n_mesh_vertices"] * 1.25)), dtype=torch.float32).pin_memory()
     ctx.stream_mesh_to_host(host["mesh"].data_ptr(), None, host["mesh"].numel() // 3)
+    if diffuse:
+        # 32-byte records; the live set grows while the same frame repeats (particles live
+        # LifefimeMultiplier frames), so the buffer has room for several times the current set
+        cap = 4 * int(counts["n_diffuse"]) + 4 * int(counts["n_generated_diffuse"]) + (1 << 20)
+        host["dbuf"] = torch.empty(32 * cap, dtype=torch.uint8).pin_memory()
+        ctx.stream_diffuse_to_host(host["dbuf"].data_ptr(), cap)
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
     ms_e2e = timer(step_e2e, args.steps)
     ctx.stream_mesh_to_host(0, None, 0)
+    if diffuse:
+        ctx.stream_diffuse_to_host(0, 0)
     return {"ms": ms, "ms_e2e": ms_e2e, "counts": counts, "sp_size": grid.sp_size, "sc_size": grid.sc_size,
             "launches": launches, "clocks": clk, "stage_ms": {k: v / args.steps for k, v in stage_sum.items()},
-            "h2d": 24 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(counts["n_diffuse"])}
+            "h2d": 24 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(host.get("n_diffuse", 0))}
 
 
-def batch_arm(pms, ctx, frames, learned: bool, args, timer, torch, clocks=None) -> dict:
+def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None) -> dict:
     dev = [tuple(torch.from_numpy(a).cuda() for a in fr) for fr in frames]
     pin = [tuple(torch.from_numpy(a).pin_memory() for a in fr) for fr in frames]
     dframes = [(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0])) for (p, v, r), fr in zip(dev, frames)]
@@ -320,10 +331,10 @@ def batch_arm(pms, ctx, frames, learned: bool, args, timer, torch, clocks=None) 
     host = {}
 
     def step_device():
-        ctx.run_batch(dframes, learned=learned)
+        ctx.run_batch(dframes, learned=mode)
 
     def step_e2e():
-        ctx.run_batch(hframes, learned=learned)
+        ctx.run_batch(hframes, learned=mode)
         for f in range(len(frames)):
             nv = C.c_uint64()
             pms.lib().pms_batch_mesh(ctx.handle, f, None, 0, C.byref(nv))
@@ -355,10 +366,10 @@ def batch_arm(pms, ctx, frames, learned: bool, args, timer, torch, clocks=None) 
             "counts": counts, "info": ctx.batch_info(), "h2d": sum(28 * len(fr[0]) for fr in frames), "d2h": 12 * mesh}
 
 
-def unbatched_ms(ctx, frames, learned: bool, args, timer, torch) -> float:
+def unbatched_ms(ctx, frames, mode: str, args, timer, torch) -> float:
     """The same frames through pms_run_frame one by one (device-resident inputs)."""
     dev = [tuple(torch.from_numpy(a).cuda() for a in fr) for fr in frames]
-    ctx.set_band_mode(learned)
+    ctx.set_band_mode(mode)
 
     def step():
         for (p, v, r), fr in zip(dev, frames):
@@ -402,7 +413,12 @@ def run_pms(args) -> None:
     if args.band in ("both", "learned") and os.path.exists(args.model):
         model = LN.load_model(args.model)
         ctx.set_band_model(model)
-    arms = (["learned", "plain"] if model is not None else ["plain"]) if args.band == "both" else [args.band]
+    # learned: the network plus the exact sign certification; certified: the
+    # certification alone (what the network adds); plain: the reference's band
+    if args.band == "both":
+        arms = (["learned"] if model is not None else []) + ["certified", "plain"]
+    else:
+        arms = [args.band]
     if "learned" in arms and model is None:
         raise SystemExit(f"--band learned needs a model ({args.model})")
     batched = args.workload == "slosh16"
@@ -413,38 +429,45 @@ def run_pms(args) -> None:
         big = max(frames, key=lambda fr: len(fr[0]))
         ctx.upload(*big)
         ctx.build_grid()
-        if arms[0] == "learned":
+        ctx.set_band_mode(arms[0])
+        if arms[0] != "plain":
             ctx.surface_learned()
         else:
             ctx.surface()
+        ctx.set_band_mode("plain")
         tune = ctx.autotune()
     res = {}
     for i, arm in enumerate(arms):
         if batched:
-            res[arm] = batch_arm(pms, ctx, frames, arm == "learned", args, timer, torch, ClockSampler(local))
+            res[arm] = batch_arm(pms, ctx, frames, arm, args, timer, torch, ClockSampler(local))
         else:
-            res[arm] = single_frame_arm(pms, ctx, frames[0], arm == "learned", args, timer, torch, diffuse,
-                                        ClockSampler(local))
-    # the judge: learned mesh against the plain mesh of the same frame (outside the timed region)
-    judge = None
-    if len(arms) == 2 and not args.no_judge:
-        # every frame of the workload (a batch gives each frame the single-frame result)
-        t0 = time.perf_counter()
-        ctx.set_band_mode(False)
-        js = [LN.compare(ctx, model, h, *fr) for fr in frames if len(fr[0])]
-        worst = max(js, key=lambda j: j["hausdorff"])
-        judge = {"hausdorff_h": worst["hausdorff_h"], "hausdorff": worst["hausdorff"],
-                 "frames": len(js), "triangle_delta": sum(j["triangle_delta"] for j in js),
-                 "cubes_only_plain": sum(j["cubes_only_plain"] for j in js),
-                 "cubes_only_learned": sum(j["cubes_only_learned"] for j in js),
-                 "fallback_cubes": sum(j["learned"]["fallback_cubes"] for j in js),
-                 "fallback_rounds": max(j["learned"]["fallback_rounds"] for j in js),
-                 "plain_vs_fp64": "vertex positions within 1e-4 cell of the float64 oracle (parity tests)",
-                 "seconds": time.perf_counter() - t0}
-    # headline: the learned band only when the judge passes it (<= 0.05 h) and it is faster
+            res[arm] = single_frame_arm(pms, ctx, frames[0], arm, args, timer, torch, diffuse, ClockSampler(local))
+    ctx.set_band_mode("plain")
+    # the judge: each non-plain band's mesh against the plain mesh of the same frame
+    # (outside the timed region; every frame of the workload -- a batch gives each
+    # frame the single-frame result)
+    judge = {}
+    if "plain" in arms and len(arms) > 1 and not args.no_judge:
+        for arm in arms:
+            if arm == "plain":
+                continue
+            t0 = time.perf_counter()
+            js = [LN.compare(ctx, model if arm == "learned" else None, h, *fr, mode=arm) for fr in frames if len(fr[0])]
+            worst = max(js, key=lambda j: j["hausdorff"])
+            judge[arm] = {"identical_frames": sum(j["identical"] for j in js), "frames": len(js),
+                          "hausdorff_h": worst["hausdorff_h"], "hausdorff": worst["hausdorff"],
+                          "triangle_delta": sum(j["triangle_delta"] for j in js),
+                          "cubes_only_plain": sum(j["cubes_only_plain"] for j in js),
+                          "cubes_only_learned": sum(j["cubes_only_learned"] for j in js),
+                          "work": {k: sum(j["learned"][k] for j in js)
+                                   for k in ("band_vertices", "exact_first", "certified", "rechecked", "full_walks",
+                                             "predicted")},
+                          "seconds": time.perf_counter() - t0}
+    # headline: the learned band when its meshes are the plain ones on every frame and it is faster
     head_arm = arms[0]
-    if len(arms) == 2:
-        ok = judge is not None and judge["hausdorff_h"] <= 0.05
+    if "learned" in arms and "plain" in arms:
+        j = judge.get("learned")
+        ok = j is not None and j["identical_frames"] == j["frames"]
         head_arm = "learned" if ok and res["learned"]["ms_e2e"] < res["plain"]["ms_e2e"] else "plain"
     head = res[head_arm]
     n_total = sum(len(fr[0]) for fr in frames)
@@ -482,18 +505,18 @@ def run_pms(args) -> None:
         else:
             line[arm].update({"stage_ms": r["stage_ms"], "counts": r["counts"]})
     if batched:
-        line["unbatched_ms_per_step"] = unbatched_ms(ctx, frames, head_arm == "learned", args, timer, torch)
+        line["unbatched_ms_per_step"] = unbatched_ms(ctx, frames, head_arm, args, timer, torch)
         # whole-path bytes of every frame over the whole batch time
         tot = 0.0
         for fr_c in head["counts"]:
             tot += sum(algorithmic_bytes(dict(fr_c, n_generated_diffuse=0, n_diffuse=0), fr_c["n_particles"],
-                                         fr_c["n_band_vertices"], False, head_arm == "learned").values())
+                                         fr_c["n_band_vertices"], False, head_arm != "plain").values())
         achieved = tot / (head["ms"] / 1e3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": "whole batch", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": None, "algorithmic_bytes": tot, "peak_source": peak_src}
     else:
         stage_ms = head["stage_ms"]
-        alg = algorithmic_bytes(head["counts"], head["sp_size"], head["sc_size"], diffuse, head_arm == "learned")
+        alg = algorithmic_bytes(head["counts"], head["sp_size"], head["sc_size"], diffuse, head_arm != "plain")
         dom = max(alg, key=lambda k: stage_ms.get(k, 0.0))
         achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else None
         traffic = None
@@ -507,7 +530,7 @@ def run_pms(args) -> None:
                             "algorithmic_bytes": alg[dom], "peak_source": peak_src}
         line["stage_ms"] = stage_ms
         line["counts"] = head["counts"]
-    if judge is not None:
+    if judge:
         line["judge"] = judge
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(frames[0][0], keys, args.cpu_fraction)
@@ -526,7 +549,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pms", choices=["pms", "reference"])
     ap.add_argument("--workload", default="crown", choices=["crown", "block", "slosh16", "dam"])
-    ap.add_argument("--band", default="both", choices=["both", "learned", "plain"])
+    ap.add_argument("--band", default="both", choices=["both", "learned", "certified", "plain"])
     ap.add_argument("--model", default=LN.DEFAULT_MODEL)
     ap.add_argument("--cpu-fraction", type=float, default=0.25)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -128,12 +128,12 @@ typedef struct pms_counts {
     uint32_t n_diffuse;                /* OldNumDiffuseParticles after delete/append */
     uint32_t n_spray, n_foam, n_bubble;
     uint32_t n_fp64_svd;               /* covariances re-solved in FP64 */
-    /* learned band (pms_band_learned); zero after the plain band */
+    /* learned / certified band (pms_band_learned); zero after the plain band */
     uint32_t n_band_candidates;        /* cubes the network evaluated */
     uint32_t n_band_predicted;         /* cubes it predicted crossed */
-    uint32_t n_band_fallback;          /* cubes the border check added */
-    uint32_t n_band_iterations;        /* border-check rounds that added cubes */
-    uint32_t n_band_removed;           /* corners of valid cubes outside the plain band, removed */
+    uint32_t n_band_exact;             /* band vertices evaluated exactly first (corners of predicted cubes) */
+    uint32_t n_band_certified;         /* band vertices certified above iso without an exact value */
+    uint32_t n_band_rechecked;         /* ... of those, corners of valid cubes, then evaluated exactly */
 } pms_counts;
 
 typedef struct pms_ctx pms_ctx;
@@ -227,6 +227,25 @@ pms_status pms_download_diffuse(pms_ctx* ctx, int type, float* pos_xyz, float* v
                                 int32_t* ttl, float* wave_crest, float* trapped_air, float* energy,
                                 uint32_t cap, uint32_t* n_out);
 
+/* One live diffuse particle as the library keeps it (32 bytes). */
+typedef struct pms_diffuse_particle {
+    float pos[3];
+    int32_t ttl;
+    float vel[3];
+    int32_t type;                      /* 0 spray, 1 foam, 2 bubble (the reference's classes) */
+} pms_diffuse_particle;
+/* Registers a host buffer (page-locked for the copy to overlap) that every
+ * following pms_diffuse fills with the frame's live diffuse particles, in the
+ * order of pms_download_diffuse, with one copy on the context's copy stream; out
+ * NULL unregisters.  pms_wait_diffuse blocks until it has landed and returns the
+ * count (PMS_ERR_CAPACITY, with the count, when cap was too small; nothing is
+ * copied then).  The next frame's diffuse stage waits on the device for the copy
+ * before it moves those particles.  No counterpart in the reference, which copies
+ * the particles back with blocking cudaMemcpy calls to write its diffuse files
+ * (DiffuseGeneration.cu:760-867). */
+pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_particle* out, uint64_t cap);
+pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n);
+
 /* Intermediate arrays, for parity tests.  Bytes needed are written to *needed;
  * nothing is copied when dst is NULL or cap_bytes is too small. */
 typedef enum pms_array {
@@ -275,16 +294,21 @@ int pms_mc_tables(uint32_t* edge_flags /*256*/, int32_t* tri /*256*16*/, uint32_
                   uint32_t* edge_vertices /*24*/, int derived);
 
 /* ---------------------------------------------------------------------------
- * Learned narrow band.  No counterpart in the reference: it replaces the band
- * marking of Anisotropic::processingOfVertices (Anisotropic.cu:43-50,
- * estimationOfSurfaceVertices, Anisotropic_kernel.cuh:522-636) as the source
- * of the vertices at which the field (Anisotropic_kernel.cuh:656-777) is
- * evaluated.  A 64 -> 64 -> 1 ReLU MLP with BF16 weights reads, for each fine
- * cube near the fluid boundary, a 4x4x4 patch of a coarse occupancy grid
- * (cells of 2x2x2 fine cubes) and predicts whether the surface crosses the
- * cube; the field is evaluated exactly at the corners of the predicted cubes;
- * a border check then adds every cube that shares a crossed face with a valid
- * cube but lacks field values, and repeats until none is missing.
+ * Learned narrow band.  No counterpart in the reference: it reshapes how the
+ * field (Anisotropic_kernel.cuh:656-777) is evaluated over the reference's own
+ * band (estimationOfSurfaceVertices, Anisotropic_kernel.cuh:522-636).  A
+ * 64 -> 64 -> 1 ReLU MLP with BF16 weights reads, for each fine cube near the
+ * fluid boundary, a 4x4x4 patch of a coarse occupancy grid (cells of 2x2x2
+ * fine cubes) and predicts whether the surface crosses the cube.  The field is
+ * evaluated exactly at the band corners of the predicted cubes.  Every other
+ * band vertex gets only a sign, which is exact: its walk stops as soon as a
+ * partial sum of its (non-negative) terms exceeds iso (a sum over its nearest
+ * cells first); a walk that never exceeds iso runs to the end and is the exact
+ * value.  With every sign known, the marching-cubes classification of the
+ * band is the plain band's; the certified corners of valid cubes are then
+ * evaluated exactly, so the triangle soup equals the plain band's, whatever
+ * the network predicted.  The network decides only which vertices are
+ * evaluated exactly at once.
  * ------------------------------------------------------------------------- */
 #define PMS_BAND_MLP_INPUTS 64
 #define PMS_BAND_MLP_HIDDEN 64
@@ -298,16 +322,19 @@ typedef struct pms_band_model {
 } pms_band_model;
 
 pms_status pms_set_band_model(pms_ctx* ctx, const pms_band_model* model);
-/* Which band pms_run_frame uses: PMS_BAND_LEARNED needs a model.  A context
- * created from a config naming [GB300] BandModel starts in PMS_BAND_LEARNED.
- * The learned band gives the plain band's triangle positions (what the PLY
- * file holds, FileData.cpp:1322-1327) but evaluates the field at fewer vertices:
- * a vertex normal whose central difference reaches a vertex outside that set
- * reads 0 there, as the reference does outside its band, so the normals from
- * pms_download_mesh differ from the plain band's at a few per cent of the
- * vertices (3 % by more than 10 degrees on the crown splash frame). */
+/* Which band pms_run_frame uses: PMS_BAND_LEARNED needs a model; PMS_BAND_CERTIFIED
+ * is the learned band's exact sign certification without the network (every band
+ * vertex certified first).  A context created from a config naming [GB300]
+ * BandModel starts in PMS_BAND_LEARNED.
+ * Both give the plain band's triangle soup exactly (positions: what the PLY file
+ * holds, FileData.cpp:1322-1327).  A vertex normal is a central difference of the
+ * field at the neighbours of a valid cube's corners; where such a neighbour is a
+ * certified vertex that is not itself a valid cube's corner, it reads the partial
+ * sum (above iso) instead of the exact value, so the normals from
+ * pms_download_mesh can differ slightly from the plain band's there. */
 #define PMS_BAND_PLAIN 0
 #define PMS_BAND_LEARNED 1
+#define PMS_BAND_CERTIFIED 2
 pms_status pms_set_band_mode(pms_ctx* ctx, int mode);
 /* Model files: "PMSBAND1", uint32 version 1, uint32 sizeof(pms_band_model),
  * the struct (little-endian), uint32 length and that many bytes of JSON
@@ -355,8 +382,8 @@ pms_status pms_trainer_get_model(pms_trainer* t, pms_band_model* out);
  * surface path of all of them in one CUDA graph launch (captured on first use
  * and relaunched while the frames' grids stay the same).  Diffuse particles
  * are not generated in a batch.  With PMS_BATCH_LEARNED the learned band is
- * used; a frame whose border check finds missing cubes is re-run alone on the
- * exact learned path, so results equal single-frame runs.
+ * used (PMS_BATCH_CERTIFIED: its sign certification without the network); every
+ * frame's result equals its single-frame run, and the plain band's.
  * ------------------------------------------------------------------------- */
 typedef struct pms_frame {
     const float* pos_xyz;
@@ -365,14 +392,14 @@ typedef struct pms_frame {
     uint32_t n;
 } pms_frame;
 #define PMS_BATCH_LEARNED 1
+#define PMS_BATCH_CERTIFIED 2
 pms_status pms_run_batch(pms_ctx* ctx, const pms_frame* frames, uint32_t k, int flags);
-/* Counts of frame f of the last batch and its device time inside the graph
- * (0 for a frame that was re-run alone). */
+/* Counts of frame f of the last batch and its device time inside the graph. */
 pms_status pms_batch_frame(pms_ctx* ctx, uint32_t f, pms_counts* counts, float* ms);
 /* Triangle soup of frame f (positions, 3 vertices per triangle). */
 pms_status pms_batch_mesh(pms_ctx* ctx, uint32_t f, float* pos_xyz, uint64_t cap, uint64_t* n_vertices);
-/* Kernels per graph launch, graph captures so far, frames re-run alone so far. */
-pms_status pms_batch_info(pms_ctx* ctx, uint32_t* graph_kernels, uint32_t* captures, uint32_t* reruns);
+/* Kernels per graph launch, graph captures so far. */
+pms_status pms_batch_info(pms_ctx* ctx, uint32_t* graph_kernels, uint32_t* captures);
 
 /* ---------------------------------------------------------------------------
  * Autotuner.  No counterpart in the reference (fixed launch shapes).  After a

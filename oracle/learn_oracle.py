@@ -5,8 +5,8 @@ module, and only as the checker.  The learned band has no counterpart in the
 reference (it is an addition of this project), so there is nothing of the
 reference to pin it to: it restates libpms's own definitions in float64 numpy,
 with the bf16 roundings of the GPU kernels mirrored, so that the GPU forward
-pass, gradients, Adam step, features, candidate set and border check can be
-checked against an independent implementation.
+pass, gradients, Adam step, features and candidate set can be checked
+against an independent implementation.
 
 Definitions (the same as postmps_gb300/csrc/k_learn.cu):
   * coarse density grid: vertex c on fine vertex 2c; particle p at coarse
@@ -187,30 +187,3 @@ def adam(params, grad, m, v, step: int, lr: float, beta1=0.9, beta2=0.999, eps=1
     mh = m / (1 - beta1 ** step)
     vh = v / (1 - beta2 ** step)
     return params - lr * mh / (np.sqrt(vh) + eps), m, v
-
-
-# ---------------------------------------------------------------------------
-# border check
-# ---------------------------------------------------------------------------
-FACE_MASKS = (0x0F, 0xF0, 0x33, 0xCC, 0x99, 0x66)
-FACE_DIRS = ((-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1))
-
-
-def border_queue(cubes_valid, cases, vertex_set: set, scres) -> set:
-    """Cubes across crossed faces of valid cubes that lack a corner in vertex_set."""
-    rx, ry, rz = (int(v) for v in scres)
-    out = set()
-    for cid, cs in zip(cubes_valid, cases):
-        x, y, z = cid % rx, (cid // rx) % ry, cid // (rx * ry)
-        for mask, (dx, dy, dz) in zip(FACE_MASKS, FACE_DIRS):
-            m = cs & mask
-            if m == 0 or m == mask:
-                continue
-            X, Y, Z = x + dx, y + dy, z + dz
-            if min(X, Y, Z) < 0 or X > rx - 2 or Y > ry - 2 or Z > rz - 2:
-                continue
-            nid = (Z * ry + Y) * rx + X
-            corners = [nid + (k & 1) + ((k >> 1) & 1) * rx + (k >> 2) * rx * ry for k in range(8)]
-            if not all(c in vertex_set for c in corners):
-                out.add(nid)
-    return out

@@ -8,86 +8,237 @@
 // vertex; thrust then scans all S_sc flags and compactationOfSurfaceVertices
 // (Anisotropic_kernel.cuh:639-653) gathers the ascending vertex list.
 //
-// GB300 design: marks are bits.  One warp handles one surface particle and
-// tests whole rows of its box at once; a ballot turns each row into a bit
-// mask that lands with at most two atomicOr per row.  The dilation is then a
-// pass over the bitmap: B = B0 | B0<<1 | B0<<rx | B0<<(rx*ry) in linear bit
-// order (the reference's index arithmetic, including its row wrap).  The
-// compaction is a popcount per 32-bit word, one scan over words and a
-// per-word bit extraction.  The bitmap (S_sc / 8 bytes) replaces three dense
-// S_sc-sized uint arrays.
+// GB300 design: marks are bits, made tile by tile.  Neighbouring surface
+// particles' boxes overlap heavily (each band vertex is marked by ~90 of them
+// on a 2M-particle crown), so marking straight into the global bitmap costs a
+// global atomic per particle and box row.  Instead the scalar grid is cut into
+// tiles of 32 x 8 x 8 vertices (one 32-bit shared word per tile row); the
+// tiles some surface particle's box reaches are listed first, then one block
+// per tile stages the surface particles of the rows of spatial cells around it
+// (contiguous stretches of the surface list) in shared memory, and each thread
+// collects one tile row's marks from its share of them in a register, with the
+// reference's own tests and roundings; each tile row then lands in the global
+// bitmap with at most two atomics.  The dilation is a pass over the bitmap:
+// B = B0 | B0<<1 | B0<<rx | B0<<(rx*ry) in linear bit order (the reference's
+// index arithmetic, including its row wrap).  The compaction is a popcount per
+// 32-bit word, one scan over words and a per-word bit extraction.  The bitmap
+// (S_sc / 8 bytes) replaces three dense S_sc-sized uint arrays.
 #include "pms_internal.h"
 #include "k_common.cuh"
 
 namespace pms {
 
-// one warp per surface particle; rows of the box packed into the 32 lanes
-__global__ void __launch_bounds__(256) k_band_mark(KGrid g, float h, const uint32_t* __restrict__ slist,
-                                                   const Counters* __restrict__ cnt, const float4* __restrict__ spos,
-                                                   const float4* __restrict__ nrm4, uint32_t* __restrict__ bm0) {
+// Tiles of the scalar grid: 32 vertices along x (one shared word per tile row) by 8 by 8.
+static constexpr int kTileX = 32, kTileY = 8, kTileZ = 8;
+static constexpr int kTileThreads = 256;
+
+struct TileDims {
+    uint32_t n[3];            // tiles per axis
+};
+
+// The clamped box [lo, hi] of scalar vertices a surface particle tests
+// (estimationOfSurfaceVertices: idx +- ceil(h / cell), clamped to the grid).
+__device__ __forceinline__ void particle_box(const KGrid& g, int ext, const float p[3], int lo[3], int hi[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int res = (int)g.scres[k];
+        const int c = __float2int_rz(__fdiv_rn(__fsub_rn(p[k], g.scmin_pos[k]), g.sc_cs));
+        lo[k] = min(max(c - ext, 0), res - 1);
+        hi[k] = min(max(c + ext, 0), res - 1);
+    }
+}
+
+// the tiles each surface particle's box reaches (read before the atomic: most are set already)
+__global__ void __launch_bounds__(256) k_band_tile_mark(KGrid g, int ext, TileDims td, const uint32_t* __restrict__ slist,
+                                                        const Counters* __restrict__ cnt, const float4* __restrict__ spos,
+                                                        uint32_t* __restrict__ tbits) {
     const uint32_t ns = cnt->ns;
-    const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int rx = (int)g.scres[0], ry = (int)g.scres[1], rz = (int)g.scres[2];
-    const uint64_t rxy = (uint64_t)g.scres[0] * g.scres[1];
-    const uint64_t nbits = g.sc_size;
-    // extent = ceil(maxdistance / scGridSize) (Anisotropic_kernel.cuh:551)
-    const int ext = (int)(uint32_t)ceilf(__fdiv_rn(h, g.sc_cs));
-    for (uint32_t s = warp; s < ns; s += nwarps) {
-        const uint32_t i = slist[s];
-        const float4 p4 = spos[i];
-        const float4 n4 = nrm4[i];
-        const bool flag = n4.w != 0.f;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const float4 p4 = __ldg(&spos[__ldg(&slist[s])]);
         const float p[3] = {p4.x, p4.y, p4.z};
-        int c[3], lo[3], hi[3];
-        float aa[3], bb[3];
-        const int res[3] = {rx, ry, rz};
+        int lo[3], hi[3];
+        particle_box(g, ext, p, lo, hi);
+        for (int tz = lo[2] / kTileZ; tz <= hi[2] / kTileZ; ++tz)
+            for (int ty = lo[1] / kTileY; ty <= hi[1] / kTileY; ++ty)
+                for (int tx = lo[0] / kTileX; tx <= hi[0] / kTileX; ++tx) {
+                    const uint32_t t = ((uint32_t)tz * td.n[1] + (uint32_t)ty) * td.n[0] + (uint32_t)tx;
+                    const uint32_t bit = 1u << (t & 31u);
+                    if (!(tbits[t >> 5] & bit)) atomicOr(&tbits[t >> 5], bit);
+                }
+    }
+}
+
+// Rows of spatial cells a tile block handles at once (their surface particles are
+// spread over the block's threads), and surface particles staged in shared memory
+// at once.
+static constexpr int kTileRows = 256;
+static constexpr int kTileChunk = 256;
+static constexpr int kTileGroups = kTileThreads / (kTileZ * kTileY);   // threads per tile row
+
+// One block per listed tile.  The rows of spatial cells whose particles can have a
+// box reaching the tile (a cell of margin on each side covers the rounding of
+// positions, keys and vertex coordinates) hold their surface particles as
+// contiguous stretches of the surface list (it is in cell order: surf_start is
+// the exclusive scan of the per-cell surface counts).  Those particles are staged
+// in shared memory a chunk at a time with what a tile row needs of them (the
+// part of their box inside the tile, their AABB p +- h, the x positions of the
+// tile inside it); then every thread owns one tile row and a quarter of the
+// chunk's particles and ORs into a register the vertices of its row that each of
+// them marks: inside the AABB and (flag || n . (v - p) > 0), evaluated as
+// estimationOfSurfaceVertices does (Anisotropic_kernel.cuh:551-606): vertex
+// coordinates i * cell + min, each difference, product and sum rounded on its own.
+__global__ void __launch_bounds__(kTileThreads) k_band_tiles(KGrid g, float h, int ext, TileDims td,
+                                                              const uint32_t* __restrict__ n_tiles_dev,
+                                                              const uint32_t* __restrict__ tiles,
+                                                              const uint32_t* __restrict__ surf_start,
+                                                              const uint32_t* __restrict__ surf_count,
+                                                              const uint32_t* __restrict__ slist,
+                                                              const float4* __restrict__ spos, const float4* __restrict__ nrm4,
+                                                              uint32_t* __restrict__ bm0) {
+    __shared__ uint32_t pre[kTileRows + 1];      // exclusive prefix of the rows' surface-particle counts
+    __shared__ uint32_t first[kTileRows];        // each row's first surface-list entry
+    __shared__ uint32_t wsum[kTileThreads / 32];
+    __shared__ float vxs[kTileX];                // the tile's vertex x coordinates
+    __shared__ float4 sp[kTileChunk];            // staged particle: p, and h (flag: n.w)
+    __shared__ float4 sn[kTileChunk];            // its normal, w: flag
+    __shared__ uint32_t sxin[kTileChunk];        // tile x positions inside its box and AABB (0: nothing to mark)
+    __shared__ uint32_t syz[kTileChunk];         // its box inside the tile: y0 | y1 << 8 | z0 << 16 | z1 << 24
+    __shared__ uint32_t red[kTileGroups][kTileZ * kTileY];
+    const uint32_t n_tiles = *n_tiles_dev;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t srx = g.spres[0], sry = g.spres[1];
+    const uint64_t rxy = (uint64_t)g.scres[0] * g.scres[1];
+    const int my_row = (int)(tid % (kTileZ * kTileY)), my_group = (int)(tid / (kTileZ * kTileY));
+    const int my_y = my_row % kTileY, my_z = my_row / kTileY;
+    for (uint32_t ti = blockIdx.x; ti < n_tiles; ti += gridDim.x) {
+        const uint32_t t = __ldg(&tiles[ti]);
+        const uint32_t tx = t % td.n[0], tyz = t / td.n[0], ty = tyz % td.n[1], tz = tyz / td.n[1];
+        const int t0[3] = {(int)tx * kTileX, (int)ty * kTileY, (int)tz * kTileZ};
+        const int t1[3] = {min(t0[0] + kTileX, (int)g.scres[0]) - 1, min(t0[1] + kTileY, (int)g.scres[1]) - 1,
+                           min(t0[2] + kTileZ, (int)g.scres[2]) - 1};
+        if (tid < kTileX) vxs[tid] = sc_coord_i(g, t0[0] + (int)tid, 0);
+        // this thread's tile row
+        const float vy = sc_coord_i(g, t0[1] + my_y, 1), vz = sc_coord_i(g, t0[2] + my_z, 2);
+        const bool row_in = t0[1] + my_y <= t1[1] && t0[2] + my_z <= t1[2];
+        uint32_t acc = 0u;
+        // spatial cells of the particles whose box can reach the tile
+        int slo[3], shi[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            c[k] = __float2int_rz(__fdiv_rn(__fsub_rn(p[k], g.scmin_pos[k]), g.sc_cs));
-            lo[k] = min(max(c[k] - ext, 0), res[k] - 1);
-            hi[k] = min(max(c[k] + ext, 0), res[k] - 1);
-            aa[k] = __fsub_rn(p[k], h);
-            bb[k] = __fadd_rn(p[k], h);
+            const float a = g.scmin_pos[k] + (float)(t0[k] - ext - 1) * g.sc_cs - g.min_pos[k];
+            const float b = g.scmin_pos[k] + (float)(t1[k] + ext + 2) * g.sc_cs - g.min_pos[k];
+            slo[k] = max((int)floorf(a / g.sp_cs) - 1, 0);
+            shi[k] = min((int)floorf(b / g.sp_cs) + 1, (int)g.spres[k] - 1);
         }
-        const int W = hi[0] - lo[0] + 1;            // row width
-        if (W <= 0 || hi[1] < lo[1] || hi[2] < lo[2]) continue;
-        const int ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-        const int nrows = ny * nz;
-        for (int x0 = 0; x0 < W; x0 += 32) {        // row chunks of at most 32 vertices
-            const int Wc = min(32, W - x0);
-            const int rpi = 32 / Wc;                 // rows per warp pass
-            const int my_row = lane / Wc, my_x = lane - my_row * Wc;
-            for (int r0 = 0; r0 < nrows; r0 += rpi) {
-                const int row = r0 + my_row;
-                bool pass = false;
-                int y = 0, z = 0;
-                if (my_row < rpi && row < nrows) {
-                    y = lo[1] + row % ny;
-                    z = lo[2] + row / ny;
-                    const int x = lo[0] + x0 + my_x;
-                    const float vx = sc_coord_i(g, x, 0), vy = sc_coord_i(g, y, 1), vz = sc_coord_i(g, z, 2);
-                    const bool outside = (vx < aa[0] || vy < aa[1] || vz < aa[2]) || (vx > bb[0] || vy > bb[1] || vz > bb[2]);
-                    if (!outside) {
-                        const float dx = __fsub_rn(vx, p[0]), dy = __fsub_rn(vy, p[1]), dz = __fsub_rn(vz, p[2]);
-                        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n4.x, dx), __fmul_rn(n4.y, dy)), __fmul_rn(n4.z, dz));
-                        pass = flag || dot > 0.f;
+        const int ny = shi[1] - slo[1] + 1, nz = shi[2] - slo[2] + 1;
+        const int nrow = (ny > 0 && nz > 0 && shi[0] >= slo[0]) ? ny * nz : 0;
+        for (int r0 = 0; r0 < nrow; r0 += kTileRows) {
+            const int nr = min(kTileRows, nrow - r0);
+            // each row's stretch of the surface list, and a block-wide exclusive scan of the lengths
+            uint32_t len = 0u;
+            if ((int)tid < nr) {
+                const int r = r0 + (int)tid;
+                const uint32_t row = ((uint32_t)(slo[2] + r / ny) * sry + (uint32_t)(slo[1] + r % ny)) * srx;
+                const uint32_t c0 = row + (uint32_t)slo[0], c1 = row + (uint32_t)shi[0];
+                const uint32_t a = __ldg(&surf_start[c0]);
+                len = __ldg(&surf_start[c1]) + __ldg(&surf_count[c1]) - a;
+                first[tid] = a;
+            }
+            uint32_t incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            if (lane == 31u) wsum[warp] = incl;
+            __syncthreads();
+            uint32_t wofs = 0u;
+            for (uint32_t w = 0; w < warp; ++w) wofs += wsum[w];
+            if ((int)tid < nr) pre[tid] = wofs + incl - len;
+            if (tid == kTileThreads - 1) {
+                uint32_t tot = 0u;
+                for (uint32_t w = 0; w < kTileThreads / 32; ++w) tot += wsum[w];
+                pre[nr] = tot;
+            }
+            __syncthreads();
+            const uint32_t total = pre[nr];
+            for (uint32_t c0 = 0; c0 < total; c0 += kTileChunk) {
+                const uint32_t nc = min((uint32_t)kTileChunk, total - c0);
+                // stage the chunk
+                if (tid < nc) {
+                    const uint32_t k = c0 + tid;
+                    int lo = 0, hi = nr - 1;     // the row holding entry k: the last row whose prefix is <= k
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (pre[mid] <= k) lo = mid; else hi = mid - 1;
+                    }
+                    const uint32_t j = __ldg(&slist[first[lo] + (k - pre[lo])]);
+                    const float4 p4 = __ldg(&spos[j]);
+                    const float4 n4 = __ldg(&nrm4[j]);
+                    const float p[3] = {p4.x, p4.y, p4.z};
+                    int blo[3], bhi[3];
+                    particle_box(g, ext, p, blo, bhi);
+                    const int x0 = max(blo[0], t0[0]), x1 = min(bhi[0], t1[0]);
+                    const int y0 = max(blo[1], t0[1]), y1 = min(bhi[1], t1[1]);
+                    const int z0 = max(blo[2], t0[2]), z1 = min(bhi[2], t1[2]);
+                    uint32_t xin = 0u;
+                    if (x0 <= x1 && y0 <= y1 && z0 <= z1) {
+                        const float ax = __fsub_rn(p[0], h), bx = __fadd_rn(p[0], h);
+                        for (int x = x0; x <= x1; ++x) {
+                            const float vx = vxs[x - t0[0]];
+                            if (!(vx < ax || vx > bx)) xin |= 1u << (x - t0[0]);
+                        }
+                    }
+                    sp[tid] = p4;
+                    sn[tid] = n4;
+                    sxin[tid] = xin;
+                    syz[tid] = xin ? (uint32_t)(y0 - t0[1]) | (uint32_t)(y1 - t0[1]) << 8 | (uint32_t)(z0 - t0[2]) << 16 |
+                                         (uint32_t)(z1 - t0[2]) << 24
+                                   : 0u;
+                }
+                __syncthreads();
+                // this thread's row against its share of the chunk
+                if (row_in) {
+                    for (uint32_t k = (uint32_t)my_group; k < nc; k += kTileGroups) {
+                        const uint32_t xin = sxin[k];
+                        const uint32_t yz = syz[k];
+                        if (!xin || my_y < (int)(yz & 0xffu) || my_y > (int)((yz >> 8) & 0xffu) ||
+                            my_z < (int)((yz >> 16) & 0xffu) || my_z > (int)(yz >> 24))
+                            continue;
+                        const float4 p4 = sp[k];
+                        const float4 n4 = sn[k];
+                        if (vy < __fsub_rn(p4.y, h) || vy > __fadd_rn(p4.y, h) || vz < __fsub_rn(p4.z, h) ||
+                            vz > __fadd_rn(p4.z, h))
+                            continue;
+                        if (n4.w != 0.f) { acc |= xin; continue; }     // flag: the whole AABB part
+                        const float by = __fmul_rn(n4.y, __fsub_rn(vy, p4.y));
+                        const float cz = __fmul_rn(n4.z, __fsub_rn(vz, p4.z));
+                        for (uint32_t m = xin & ~acc; m; m &= m - 1u) {
+                            const int i = __ffs(m) - 1;
+                            const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n4.x, __fsub_rn(vxs[i], p4.x)), by), cz);
+                            if (dot > 0.f) acc |= 1u << i;
+                        }
                     }
                 }
-                const uint32_t bal = __ballot_sync(0xffffffffu, pass);
-                if (my_row < rpi && row < nrows && my_x == 0) {
-                    const uint32_t mask = (Wc == 32) ? bal : ((bal >> (my_row * Wc)) & ((1u << Wc) - 1u));
-                    if (mask) {
-                        const uint64_t bit = (uint64_t)z * rxy + (uint64_t)y * (uint64_t)rx + (uint64_t)(lo[0] + x0);
-                        const uint64_t w = bit >> 5;
-                        const uint32_t sh = (uint32_t)(bit & 31u);
-                        if (bit < nbits) atomicOr(&bm0[w], mask << sh);
-                        if (sh && (mask >> (32u - sh)) && ((w + 1) << 5) < nbits) atomicOr(&bm0[w + 1], mask >> (32u - sh));
-                    }
-                }
+                __syncthreads();
             }
         }
+        red[my_group][my_row] = acc;
+        __syncthreads();
+        if (tid < kTileZ * kTileY) {
+            uint32_t m = 0u;
+#pragma unroll
+            for (int q = 0; q < kTileGroups; ++q) m |= red[q][tid];
+            if (m) {
+                const uint64_t bit = (uint64_t)(t0[2] + (int)tid / kTileY) * rxy +
+                                     (uint64_t)(t0[1] + (int)tid % kTileY) * g.scres[0] + (uint64_t)t0[0];
+                const uint64_t w = bit >> 5;
+                const uint32_t sh = (uint32_t)(bit & 31u);
+                atomicOr(&bm0[w], m << sh);
+                if (sh && (m >> (32u - sh))) atomicOr(&bm0[w + 1], m >> (32u - sh));
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -114,6 +265,13 @@ __global__ void __launch_bounds__(256) k_band_dilate(const uint32_t* __restrict_
     }
 }
 
+// popcount per word
+__global__ void __launch_bounds__(256) k_word_popc(const uint32_t* __restrict__ b, uint32_t* __restrict__ wcount,
+                                                   uint64_t nwords) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x)
+        wcount[w] = __popc(b[w]);
+}
+
 // ascending vertex list from the bitmap
 __global__ void __launch_bounds__(256) k_band_list(const uint32_t* __restrict__ bm, const uint32_t* __restrict__ wprefix,
                                                    uint64_t nwords, uint32_t* __restrict__ vlist) {
@@ -128,207 +286,42 @@ __global__ void __launch_bounds__(256) k_band_list(const uint32_t* __restrict__ 
     }
 }
 
-// ---------------------------------------------------------------------------
-// Plain-band membership of single vertices, for the learned band: a vertex
-// belongs to the band of k_band_mark + k_band_dilate when a surface particle
-// marks it or the vertex one step lower in linear order along x, y or z (the
-// dilation B0 | B0 << 1 | B0 << rx | B0 << rx*ry, row wrap included).  The
-// test looks from the vertex at the surface cells within h instead of marking
-// from every surface particle, and repeats k_band_mark's per-particle test
-// with the same roundings, so it answers exactly what the bitmap would hold.
-// ---------------------------------------------------------------------------
-
-// k_band_mark's test of one (particle, vertex) pair: the AABB p +- h, the
-// direction flag || n . (v - p) > 0, and the index box c +- ext clamped to the grid
-__device__ __forceinline__ bool marks(const KGrid& g, float h, int ext, float4 p, float4 n, int ix, int iy, int iz,
-                                      float vx, float vy, float vz) {
-    if (vx < __fsub_rn(p.x, h) || vy < __fsub_rn(p.y, h) || vz < __fsub_rn(p.z, h) || vx > __fadd_rn(p.x, h) ||
-        vy > __fadd_rn(p.y, h) || vz > __fadd_rn(p.z, h))
-        return false;
-    if (n.w == 0.f) {
-        const float dx = __fsub_rn(vx, p.x), dy = __fsub_rn(vy, p.y), dz = __fsub_rn(vz, p.z);
-        const float dot = __fadd_rn(__fadd_rn(__fmul_rn(n.x, dx), __fmul_rn(n.y, dy)), __fmul_rn(n.z, dz));
-        if (!(dot > 0.f)) return false;
-    }
-    const int cx = __float2int_rz(__fdiv_rn(__fsub_rn(p.x, g.scmin_pos[0]), g.sc_cs));
-    const int cy = __float2int_rz(__fdiv_rn(__fsub_rn(p.y, g.scmin_pos[1]), g.sc_cs));
-    const int cz = __float2int_rz(__fdiv_rn(__fsub_rn(p.z, g.scmin_pos[2]), g.sc_cs));
-    const int rx = (int)g.scres[0] - 1, ry = (int)g.scres[1] - 1, rz = (int)g.scres[2] - 1;
-    return ix >= min(max(cx - ext, 0), rx) && ix <= min(max(cx + ext, 0), rx) && iy >= min(max(cy - ext, 0), ry) &&
-           iy <= min(max(cy + ext, 0), ry) && iz >= min(max(cz - ext, 0), rz) && iz <= min(max(cz + ext, 0), rz);
-}
-
-// Does a particle of the surface cells [xa, xb) x [ya, yb) x [za, zb) mark one
-// of the NT (1 or 3) target vertices?  Targets t with bit t of `use` clear are skipped.
-template <int NT>
-__device__ bool scan_cells(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
-                           const float4* __restrict__ spos, const float4* __restrict__ nrm4, int xa, int xb, int ya,
-                           int yb, int za, int zb, const int (&ix)[NT], const int (&iy)[NT], const int (&iz)[NT],
-                           const float (&vx)[NT], const float (&vy)[NT], const float (&vz)[NT], uint32_t use) {
-    for (int cz = za; cz < zb; ++cz)
-        for (int cy = ya; cy < yb; ++cy) {
-            const uint32_t row = ((uint32_t)cz * g.spres[1] + (uint32_t)cy) * g.spres[0];
-            for (int cx = xa; cx < xb; ++cx) {
-                const uint2 ci = __ldg(&cell_info[row + (uint32_t)cx]);
-                if (!(ci.y & 0x80000000u)) continue;         // empty or not a surface cell
-                const uint32_t j1 = ci.x + (ci.y & 0x7fffffffu);
-                for (uint32_t j = ci.x; j < j1; ++j) {
-                    const float4 p = __ldg(&spos[j]), n = __ldg(&nrm4[j]);
-#pragma unroll
-                    for (int t = 0; t < NT; ++t)
-                        if (((use >> t) & 1u) && marks(g, h, ext, p, n, ix[t], iy[t], iz[t], vx[t], vy[t], vz[t]))
-                            return true;
-                }
-            }
-        }
-    return false;
-}
-
-// the surface cells within h of the box [lo, hi]: every particle that can mark a vertex of the box
-template <int NT>
-__device__ __forceinline__ bool scan_marks(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
-                                           const float4* __restrict__ spos, const float4* __restrict__ nrm4, float lox,
-                                           float loy, float loz, float hix, float hiy, float hiz, const int (&ix)[NT],
-                                           const int (&iy)[NT], const int (&iz)[NT], const float (&vx)[NT],
-                                           const float (&vy)[NT], const float (&vz)[NT], uint32_t use) {
-    const float inv = 1.f / g.sp_cs, r = h * inv + kRangeMargin;
-    return scan_cells<NT>(g, h, ext, cell_info, spos, nrm4, max((int)floorf((lox - g.min_pos[0]) * inv - r), 0),
-                          min((int)floorf((hix - g.min_pos[0]) * inv + r) + 1, (int)g.spres[0]),
-                          max((int)floorf((loy - g.min_pos[1]) * inv - r), 0),
-                          min((int)floorf((hiy - g.min_pos[1]) * inv + r) + 1, (int)g.spres[1]),
-                          max((int)floorf((loz - g.min_pos[2]) * inv - r), 0),
-                          min((int)floorf((hiz - g.min_pos[2]) * inv + r) + 1, (int)g.spres[2]), ix, iy, iz, vx, vy, vz, use);
-}
-
-// B0 at vertex (x, y, z)
-__device__ __forceinline__ bool in_b0(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
-                                      const float4* __restrict__ spos, const float4* __restrict__ nrm4, int x, int y, int z) {
-    const int ix[1] = {x}, iy[1] = {y}, iz[1] = {z};
-    const float vx[1] = {sc_coord_i(g, x, 0)}, vy[1] = {sc_coord_i(g, y, 1)}, vz[1] = {sc_coord_i(g, z, 2)};
-    return scan_marks<1>(g, h, ext, cell_info, spos, nrm4, vx[0], vy[0], vz[0], vx[0], vy[0], vz[0], ix, iy, iz, vx, vy, vz, 1u);
-}
-
-// The quick side of the test: B0 at v, then at its three lower neighbours (no
-// row wrap), from the 2 x 2 x 2 particle cells nearest to v -- most band
-// vertices are marked by a particle there.  A vertex it cannot confirm goes to
-// `rest` for the full test.
-__global__ void __launch_bounds__(128) k_plain_quick(KGrid g, float h, const uint32_t* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ list, const uint2* __restrict__ cell_info,
-                                                     const float4* __restrict__ spos, const float4* __restrict__ nrm4,
-                                                     uint32_t* __restrict__ rest, uint32_t* __restrict__ n_rest) {
-    const uint32_t n = *n_dev;
-    const int ext = (int)(uint32_t)ceilf(__fdiv_rn(h, g.sc_cs));   // as k_band_mark
-    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
-    const float inv = 1.f / g.sp_cs;
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {
-        const uint32_t t = t0 + threadIdx.x;
-        bool open = false;
-        uint32_t v = 0;
-        if (t < n) {
-            v = list[t];
-            const int z = (int)(v / rxy), y = (int)((v - (uint32_t)z * rxy) / rx), x = (int)(v - (uint32_t)z * rxy - (uint32_t)y * rx);
-            const int ix[1] = {x}, iy[1] = {y}, iz[1] = {z};
-            const float vx[1] = {sc_coord_i(g, x, 0)}, vy[1] = {sc_coord_i(g, y, 1)}, vz[1] = {sc_coord_i(g, z, 2)};
-            int a[3], b[3];
-            const float u[3] = {(vx[0] - g.min_pos[0]) * inv, (vy[0] - g.min_pos[1]) * inv, (vz[0] - g.min_pos[2]) * inv};
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int c = (int)floorf(u[k]);
-                const int lo = u[k] - (float)c < 0.5f ? c - 1 : c;
-                a[k] = max(lo, 0);
-                b[k] = min(lo + 2, (int)g.spres[k]);
-            }
-            open = !scan_cells<1>(g, h, ext, cell_info, spos, nrm4, a[0], b[0], a[1], b[1], a[2], b[2], ix, iy, iz, vx, vy,
-                                  vz, 1u);
-            const uint32_t use = (x > 0 ? 1u : 0u) | (y > 0 ? 2u : 0u) | (z > 0 ? 4u : 0u);
-            if (open && use) {
-                const int jx[3] = {x - 1, x, x}, jy[3] = {y, y - 1, y}, jz[3] = {z, z, z - 1};
-                const float qx = sc_coord_i(g, x - 1, 0), qy = sc_coord_i(g, y - 1, 1), qz = sc_coord_i(g, z - 1, 2);
-                const float wx[3] = {qx, vx[0], vx[0]}, wy[3] = {vy[0], qy, vy[0]}, wz[3] = {vz[0], vz[0], qz};
-                open = !scan_cells<3>(g, h, ext, cell_info, spos, nrm4, a[0], b[0], a[1], b[1], a[2], b[2], jx, jy, jz, wx, wy,
-                                      wz, use);
-            }
-        }
-        // warp-aggregated append of the open vertices
-        const uint32_t m = __ballot_sync(0xffffffffu, open);
-        uint32_t base = 0;
-        if (lane == 0 && m) base = atomicAdd(n_rest, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (open) rest[base + (uint32_t)__popc(m & ((1u << lane) - 1u))] = v;
-    }
-}
-
-// membership of vertex v = (x, y, z) in the dilated band
-__device__ bool in_plain_band(const KGrid& g, float h, int ext, const uint2* __restrict__ cell_info,
-                              const float4* __restrict__ spos, const float4* __restrict__ nrm4, uint32_t v) {
-    const uint32_t rx = g.scres[0], ry = g.scres[1], rxy = rx * ry;
-    const int z = (int)(v / rxy), y = (int)((v - (uint32_t)z * rxy) / rx), x = (int)(v - (uint32_t)z * rxy - (uint32_t)y * rx);
-    if (in_b0(g, h, ext, cell_info, spos, nrm4, x, y, z)) return true;
-    // the lower neighbours v - 1, v - rx, v - rx*ry where they do not wrap, in one scan
-    const uint32_t use = (x > 0 ? 1u : 0u) | (y > 0 ? 2u : 0u) | (z > 0 ? 4u : 0u);
-    if (use) {
-        const int ix[3] = {x - 1, x, x}, iy[3] = {y, y - 1, y}, iz[3] = {z, z, z - 1};
-        const float px = sc_coord_i(g, x, 0), py = sc_coord_i(g, y, 1), pz = sc_coord_i(g, z, 2);
-        const float qx = sc_coord_i(g, x - 1, 0), qy = sc_coord_i(g, y - 1, 1), qz = sc_coord_i(g, z - 1, 2);
-        const float vx[3] = {qx, px, px}, vy[3] = {py, qy, py}, vz[3] = {pz, pz, qz};
-        if (scan_marks<3>(g, h, ext, cell_info, spos, nrm4, (use & 1u) ? qx : px, (use & 2u) ? qy : py,
-                          (use & 4u) ? qz : pz, px, py, pz, ix, iy, iz, vx, vy, vz, use))
-            return true;
-    }
-    // at x == 0 (y == 0) the linear shift wraps to the row (slab) below; z == 0 has nothing below
-    if (x == 0 && v >= 1) {
-        const uint32_t u = v - 1, uz = u / rxy, uy = (u - uz * rxy) / rx;
-        if (in_b0(g, h, ext, cell_info, spos, nrm4, (int)(u - uz * rxy - uy * rx), (int)uy, (int)uz)) return true;
-    }
-    if (y == 0 && v >= rx) {
-        const uint32_t u = v - rx, uz = u / rxy, uy = (u - uz * rxy) / rx;
-        if (in_b0(g, h, ext, cell_info, spos, nrm4, (int)(u - uz * rxy - uy * rx), (int)uy, (int)uz)) return true;
-    }
-    (void)ry;
-    return false;
-}
-
-// The listed vertices outside the plain band leave the vertex set: the bit in
-// vbm is cleared, the dense field value set to 0 (what a vertex off the band
-// reads) and n_removed counts them.
-__global__ void __launch_bounds__(128) k_plain_member(KGrid g, float h, const uint32_t* __restrict__ n_dev,
-                                                      const uint32_t* __restrict__ list, const uint2* __restrict__ cell_info,
-                                                      const float4* __restrict__ spos, const float4* __restrict__ nrm4,
-                                                      uint32_t* __restrict__ vbm, float* __restrict__ fdense,
-                                                      uint32_t* __restrict__ n_removed) {
-    const uint32_t n = *n_dev;
-    const int ext = (int)(uint32_t)ceilf(__fdiv_rn(h, g.sc_cs));   // as k_band_mark
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint32_t v = list[t];
-        if (in_plain_band(g, h, ext, cell_info, spos, nrm4, v)) continue;
-        atomicAnd(&vbm[v >> 5], ~(1u << (v & 31u)));
-        fdense[v] = 0.f;
-        atomicAdd(n_removed, 1u);
-    }
-}
-
-pms_status launch_plain_member(pms_ctx* ctx, const uint32_t* list, const uint32_t* n_dev, uint32_t n_host, uint32_t* rest,
-                               uint32_t* n_rest, uint32_t* n_removed) {
-    const KGrid g = kgrid_of(ctx->grid);
-    PMS_CUDA(ctx, cudaMemsetAsync(n_rest, 0, sizeof(uint32_t), ctx->stream));
-    k_plain_quick<<<grid_for(n_host, 128), 128, 0, ctx->stream>>>(g, ctx->prm.h, n_dev, list, ctx->cell_info.as<uint2>(),
-                                                                  ctx->spos.as<float4>(), ctx->nrm4.as<float4>(), rest, n_rest);
-    PMS_LAUNCHED(ctx);
-    k_plain_member<<<grid_for(n_host, 128), 128, 0, ctx->stream>>>(
-        g, ctx->prm.h, n_rest, rest, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->nrm4.as<float4>(),
-        ctx->bm.as<uint32_t>(), ctx->fdense.as<float>(), n_removed);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
+static TileDims tile_dims(const KGrid& g) {
+    TileDims td;
+    td.n[0] = (g.scres[0] + kTileX - 1) / kTileX;
+    td.n[1] = (g.scres[1] + kTileY - 1) / kTileY;
+    td.n[2] = (g.scres[2] + kTileZ - 1) / kTileZ;
+    return td;
 }
 
 pms_status launch_band(pms_ctx* ctx) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
+    const TileDims td = tile_dims(g);
+    const uint64_t ntiles = (uint64_t)td.n[0] * td.n[1] * td.n[2];
+    const uint64_t tw = (ntiles + 31) / 32;
+    // sized with the grid (ensure_grid_buffers: a tile holds at least one vertex)
+    if (ctx->tile_list.cap < 4 * ntiles || ctx->tile_bits.cap < 4 * tw)
+        return pms_fail(ctx, PMS_ERR_STATE, "internal: band tile buffers not sized for the grid");
+    PMS_CUDA(ctx, cudaMemsetAsync(ctx->tile_bits.p, 0, 4 * tw, ctx->stream));
     PMS_CUDA(ctx, cudaMemsetAsync(ctx->bm0.p, 0, sizeof(uint32_t) * nwords, ctx->stream));
-    k_band_mark<<<grid_for((uint64_t)ctx->n * 32u, 256), 256, 0, ctx->stream>>>(
-        g, ctx->prm.h, ctx->slist.as<uint32_t>(), cnt, ctx->spos.as<float4>(), ctx->nrm4.as<float4>(), ctx->bm0.as<uint32_t>());
+    // extent = ceil(maxdistance / scGridSize) (Anisotropic_kernel.cuh:551), a correctly rounded float quotient
+    const int ext_dev = (int)(uint32_t)ceilf(ctx->prm.h / g.sc_cs);
+    k_band_tile_mark<<<grid_for(ctx->n, 256), 256, 0, ctx->stream>>>(g, ext_dev, td, ctx->slist.as<uint32_t>(), cnt,
+                                                                     ctx->spos.as<float4>(), ctx->tile_bits.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    k_word_popc<<<grid_for(tw, 256), 256, 0, ctx->stream>>>(ctx->tile_bits.as<uint32_t>(), ctx->tile_wc.as<uint32_t>(), tw);
+    PMS_LAUNCHED(ctx);
+    pms_status st = scan_u32(ctx, ctx->tile_wc.as<uint32_t>(), ctx->tile_wp.as<uint32_t>(), tw, &cnt->n_tiles);
+    if (st != PMS_OK) return st;
+    k_band_list<<<grid_for(tw, 256), 256, 0, ctx->stream>>>(ctx->tile_bits.as<uint32_t>(), ctx->tile_wp.as<uint32_t>(), tw,
+                                                            ctx->tile_list.as<uint32_t>());
+    PMS_LAUNCHED(ctx);
+    k_band_tiles<<<grid_for(ntiles, 1, 152u * 8u), kTileThreads, 0, ctx->stream>>>(
+        g, ctx->prm.h, ext_dev, td, &cnt->n_tiles, ctx->tile_list.as<uint32_t>(), ctx->surf_start.as<uint32_t>(),
+        ctx->surf_count.as<uint32_t>(), ctx->slist.as<uint32_t>(), ctx->spos.as<float4>(), ctx->nrm4.as<float4>(),
+        ctx->bm0.as<uint32_t>());
     PMS_LAUNCHED(ctx);
     const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
     k_band_dilate<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(ctx->bm0.as<uint32_t>(), ctx->bm.as<uint32_t>(),

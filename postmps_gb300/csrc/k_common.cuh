@@ -152,47 +152,6 @@ __device__ __forceinline__ void row_walk(const KGrid& g, float3 p, uint3 lo, uin
     }
 }
 
-// Border check of the learned band (no reference counterpart).  A valid cube
-// (origin x, y, z; case cs over the corner order {000,001,011,010,100,101,111,
-// 110} in (x, y, z)) whose face has corners on both sides of the iso-surface
-// shares that crossing with the cube across the face, so the neighbour is a
-// valid cube too; if not all of the neighbour's corners are in the vertex
-// bitmap vbm, it is queued once: its bit in qadd, the count, and (when qlist is
-// given) a list entry while the list has room (the count tells the caller).
-__device__ __forceinline__ void queue_cube(uint32_t nid, uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
-                                           uint32_t* __restrict__ qlist, uint32_t qcap) {
-    const uint32_t bit = 1u << (nid & 31u);
-    const uint32_t old = atomicOr(&qadd[nid >> 5], bit);
-    if (old & bit) return;
-    const uint32_t slot = atomicAdd(n_added, 1u);
-    if (qlist && slot < qcap) qlist[slot] = nid;
-}
-
-__device__ __forceinline__ void border_faces(const KGrid& g, int x, int y, int z, uint32_t cs,
-                                             const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
-                                             uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist, uint32_t qcap) {
-    const int rx = (int)g.scres[0], ry = (int)g.scres[1], rz = (int)g.scres[2];
-    const uint32_t rxy = g.scres[0] * g.scres[1];
-    const uint32_t mask[6] = {0x0Fu, 0xF0u, 0x33u, 0xCCu, 0x99u, 0x66u};
-    const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-        const uint32_t m = cs & mask[f];
-        if (m == 0u || m == mask[f]) continue;
-        const int X = x + dxs[f], Y = y + dys[f], Z = z + dzs[f];
-        if (X < 0 || Y < 0 || Z < 0 || X > rx - 2 || Y > ry - 2 || Z > rz - 2) continue;
-        const uint32_t nid = (uint32_t)Z * rxy + (uint32_t)Y * (uint32_t)rx + (uint32_t)X;
-        // corners (X, Y, Z) + {0,1}^3
-        bool all = true;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t c = nid + (uint32_t)(k & 1) + (uint32_t)((k >> 1) & 1) * (uint32_t)rx + (uint32_t)(k >> 2) * rxy;
-            all = all && ((vbm[c >> 5] >> (c & 31u)) & 1u);
-        }
-        if (!all) queue_cube(nid, qadd, n_added, qlist, qcap);
-    }
-}
-
 // rank of bit `id` among set bits of a bitmap with exclusive word prefix sums
 __device__ __forceinline__ uint32_t bit_rank(const uint32_t* bm, const uint32_t* wprefix, uint32_t id) {
     uint32_t w = id >> 5, b = id & 31u;

@@ -344,33 +344,57 @@ __device__ __forceinline__ float wendland(float rx, float ry, float rz, float h)
     return 0.f;
 }
 
-// updateDiffuseParticle, one diffuse particle of the previous frame per thread
+// Neighbours of x within hd (|s| <= hd, the advection's test), walking only the rows
+// and cells of the diffuse box that come within hd of x: a cell left out holds no
+// particle that the count would take, so the count is the reference's.
+__device__ __forceinline__ int count_within_near(const KGrid& g, const DiffuseParams& dp,
+                                                 const uint32_t* __restrict__ cell_start, const float4* __restrict__ spos,
+                                                 float px, float py, float pz) {
+    uint3 lo, hi;
+    diffuse_box(g, px, py, pz, lo, hi);
+    hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);          // row_walk takes [lo, hi)
+    const float r = dp.hd * kSupportGrow;
+    int count = 0;
+    row_walk(g, make_float3(px, py, pz), lo, hi, r * r, 1e-4f * g.sp_cs, cell_start, [&](uint32_t j) {
+        const float4 q = __ldg(&spos[j]);
+        const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
+        if (__fsqrt_rn(dot_rn(sx, sy, sz, sx, sy, sz)) <= dp.hd) ++count;
+    });
+    return count;
+}
+
+// updateDiffuseParticle (DiffuseGeneration_kernel.cuh:1036-1199), one diffuse
+// particle of the previous frame per thread.  The reference walks its cell box
+// three times (neighbour count, velocity average, neighbour count at the new
+// position); here the first two share one walk over the rows and cells within
+// 2 hd (the Wendland support: every particle farther adds exactly 0 to the
+// average, every particle the count takes lies within hd), in the reference's
+// cell and particle order, and the last walk covers only what lies within hd.
 __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParams dp, uint32_t n_old,
-                                                        const uint2* __restrict__ cell_info, const float4* __restrict__ spos,
+                                                        const uint32_t* __restrict__ cell_start,
+                                                        const float4* __restrict__ spos,
                                                         const float4* __restrict__ svel, DiffuseParticle* __restrict__ old) {
-    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_old; t += gridDim.x * blockDim.x) {
         DiffuseParticle d = old[t];
         const float px = d.px, py = d.py, pz = d.pz, vx = d.vx, vy = d.vy, vz = d.vz;
-        const int density = count_within(g, dp, cell_info, spos, px, py, pz, false);
+        int density = 0;
         float nx = 0.f, ny = 0.f, nz = 0.f, wsum = 0.f;
-        if (density >= kSpray) {
+        {
             uint3 lo, hi;
             diffuse_box(g, px, py, pz, lo, hi);
-            for (uint32_t z = lo.z; z <= hi.z; ++z)
-                for (uint32_t y = lo.y; y <= hi.y; ++y)
-                    for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                        const uint2 ci = cell_info[z * rxy + y * rx + x];
-                        const uint32_t m = ci.y & 0x7fffffffu;
-                        for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                            const float4 q = spos[j], w = svel[j];
-                            const float tv = wendland(__fsub_rn(px, q.x), __fsub_rn(py, q.y), __fsub_rn(pz, q.z), dp.hd);
-                            nx = __fadd_rn(nx, __fmul_rn(w.x, tv));
-                            ny = __fadd_rn(ny, __fmul_rn(w.y, tv));
-                            nz = __fadd_rn(nz, __fmul_rn(w.z, tv));
-                            wsum = __fadd_rn(wsum, tv);
-                        }
-                    }
+            hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
+            const float r = 2.f * dp.hd * kSupportGrow;
+            row_walk(g, make_float3(px, py, pz), lo, hi, r * r, 1e-4f * g.sp_cs, cell_start, [&](uint32_t j) {
+                const float4 q = __ldg(&spos[j]);
+                const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
+                if (__fsqrt_rn(dot_rn(sx, sy, sz, sx, sy, sz)) <= dp.hd) ++density;
+                const float4 w = __ldg(&svel[j]);
+                const float tv = wendland(sx, sy, sz, dp.hd);
+                nx = __fadd_rn(nx, __fmul_rn(w.x, tv));
+                ny = __fadd_rn(ny, __fmul_rn(w.y, tv));
+                nz = __fadd_rn(nz, __fmul_rn(w.z, tv));
+                wsum = __fadd_rn(wsum, tv);
+            });
         }
         const float gz = -9.81f, dt = dp.time_step;
         if (density < kSpray) {
@@ -405,21 +429,28 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParam
             d.type = 3;
             d.ttl = 0;
         } else {
-            d.type = type_of(count_within(g, dp, cell_info, spos, d.px, d.py, d.pz, false));
+            d.type = type_of(count_within_near(g, dp, cell_start, spos, d.px, d.py, d.pz));
         }
         old[t] = d;
     }
 }
 
-// delete and append: generated then old, dropping type 3; per-type counts
+// delete and append: generated then old, dropping type 3; per-type counts (summed per
+// thread, then per warp, one atomic per warp and type)
 __global__ void __launch_bounds__(256) k_df_keep(const DiffuseParticle* __restrict__ gen, uint32_t n_gen,
                                                  const DiffuseParticle* __restrict__ old, uint32_t n_old,
                                                  uint32_t* __restrict__ keep, Counters* __restrict__ cnt) {
     const uint32_t total = n_gen + n_old;
+    uint32_t c[4] = {0u, 0u, 0u, 0u};
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
         const int type = k < n_gen ? gen[k].type : old[k - n_gen].type;
         keep[k] = type != 3 ? 1u : 0u;
-        atomicAdd(&cnt->n_type[type == 0 ? 0 : (type == 2 ? 2 : (type == 3 ? 3 : 1))], 1u);
+        c[type == 0 ? 0 : (type == 2 ? 2 : (type == 3 ? 3 : 1))]++;
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t w = __reduce_add_sync(0xffffffffu, c[i]);
+        if ((threadIdx.x & 31u) == 0 && w) atomicAdd(&cnt->n_type[i], w);
     }
 }
 
@@ -473,6 +504,8 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     pms_status st;
     if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
     const size_t N = n;
+    // last frame's live particles (moved in place below) may still be on their way to the host
+    if (ctx->dout_pending) PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->diffuse_copied, 0));
     PMS_CUDA(ctx, ctx->d_isfree.ensure(4 * N));
     PMS_CUDA(ctx, ctx->d_freescan.ensure(4 * N));
     PMS_CUDA(ctx, ctx->d_freelist.ensure(4 * N));
@@ -526,7 +559,7 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     if (n_spawn) PMS_LAUNCHED(ctx);
     if (n_old) {
         k_df_update<<<grid_for(n_old, kThreads), kThreads, 0, ctx->stream>>>(
-            g, dp, n_old, ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
+            g, dp, n_old, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
             ctx->d_old.as<DiffuseParticle>());
         PMS_LAUNCHED(ctx);
     }
@@ -545,6 +578,18 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     if ((st = sync_counters(ctx))) return st;
     ctx->diffuse_old = total ? ctx->h_counters->n_live : 0;
     std::swap(ctx->d_all, ctx->d_old);               // the survivors are next frame's old particles
+    if (ctx->dout) {
+        // the live set to the registered host buffer, on the copy stream
+        ctx->dout_n = ctx->diffuse_old;
+        ctx->dout_overflow = ctx->dout_n > ctx->dout_cap;
+        PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_ready, ctx->stream));
+        PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->diffuse_ready, 0));
+        if (!ctx->dout_overflow && ctx->dout_n)
+            PMS_CUDA(ctx, cudaMemcpyAsync(ctx->dout, ctx->d_old.p, sizeof(DiffuseParticle) * ctx->dout_n,
+                                          cudaMemcpyDeviceToHost, ctx->copy_stream));
+        PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_copied, ctx->copy_stream));
+        ctx->dout_pending = true;
+    }
     return PMS_OK;
 }
 
@@ -579,6 +624,41 @@ static pms_status download_live(pms_ctx* ctx, std::vector<DiffuseParticle>& v) {
         PMS_CUDA(ctx, cudaMemcpyAsync(v.data(), ctx->d_old.p, sizeof(DiffuseParticle) * v.size(), cudaMemcpyDeviceToHost,
                                       ctx->stream));
     PMS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return PMS_OK;
+}
+
+static_assert(sizeof(DiffuseParticle) == sizeof(pms_diffuse_particle), "diffuse particle layout");
+
+extern "C" pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_particle* out, uint64_t cap) {
+    if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->dout_pending) PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
+    ctx->dout_pending = false;
+    if (out && !ctx->copy_stream) {
+        PMS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->mesh_ready, cudaEventDisableTiming));
+        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->mesh_copied, cudaEventDisableTiming));
+    }
+    if (out && !ctx->diffuse_ready) {
+        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->diffuse_ready, cudaEventDisableTiming));
+        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->diffuse_copied, cudaEventDisableTiming));
+    }
+    ctx->dout = out;
+    ctx->dout_cap = out ? cap : 0;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n) {
+    if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
+    if (!ctx->dout) return pms_fail(ctx, PMS_ERR_STATE, "pms_wait_diffuse without pms_stream_diffuse_to_host");
+    if (!ctx->dout_pending) return pms_fail(ctx, PMS_ERR_STATE, "no diffuse particles streamed since the last wait");
+    cudaSetDevice(ctx->device);
+    PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
+    ctx->dout_pending = false;
+    if (n) *n = ctx->dout_n;
+    if (ctx->dout_overflow)
+        return pms_fail(ctx, PMS_ERR_CAPACITY, "%llu diffuse particles, the host buffer holds %llu",
+                        (unsigned long long)ctx->dout_n, (unsigned long long)ctx->dout_cap);
     return PMS_OK;
 }
 

@@ -26,6 +26,21 @@
 // Adding a zero contribution leaves the sum unchanged, so no cut changes the
 // reference's sum or its early exit: the threshold test after a skipped cell
 // sees the same sum as the test before it.
+//
+// Sign certification (the learned band's exact fallback; no reference
+// counterpart).  Every term of the sum is >= 0 and float addition of a
+// non-negative term never decreases a sum, so a vertex is certainly above the
+// iso-value -- marching-cubes corner bit clear, whatever the rest of its walk
+// would add -- as soon as a part of its sum exceeds iso.  In this mode a vertex
+// (1) first sums the particles of the 2 x 2 x 2 spatial cells nearest to it (in
+// any order; the test then asks for iso * (1 + 2^-9), which covers the rounding
+// of two float sums in different orders of up to ~30,000 non-zero terms each);
+// (2) failing that, walks in the reference's order and stops as soon as its
+// running sum exceeds iso -- that prefix is the reference's own, since the
+// reference's early exit (2 * iso) cannot have fired before.  A vertex stopped
+// either way gets a placeholder above iso (its partial sum) and a bit in
+// `cert`; a vertex whose walk ran to the end has exactly the reference's value
+// (no early exit fired, the sum never exceeded iso).
 #include <type_traits>
 
 #include "pms_internal.h"
@@ -35,8 +50,9 @@ namespace pms {
 
 struct FieldParams {
     float h;                  // isotropic support, the smallest culling radius of a cell
-    float thr;                // 2 * iso: the early-exit threshold
+    float thr;                // 2 * iso: the early-exit threshold (certification: iso)
     float grow;               // relative margin on culling radii
+    float quick;              // certification: iso * (1 + 2^-9), the nearest-cells test
 };
 
 __device__ __forceinline__ float gap2_axis(float p, float lo, float cs, float pad) {
@@ -69,13 +85,17 @@ static constexpr uint32_t kItemShift = 29;
 // non-empty cell by its record: the bounding box of its particles and its
 // largest support.  The value goes to field[t] (band order; skipped when field
 // is null) and to fdense[id] (the whole scalar grid).
-template <int BT, int K>
+// CERT: sign certification (above); cert receives a bit per vertex stopped above
+// iso, n_cert their count.
+template <int BT, int K, bool CERT>
 __global__ void __launch_bounds__(BT, (K == 1 ? 1280 : 1024) / BT)
 k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_t* __restrict__ n_items_dev,
         const uint32_t* __restrict__ items, const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
         const float* __restrict__ cell_rad, const float4* __restrict__ rec, const float4* __restrict__ spos,
-        const float4* __restrict__ aniso, float* __restrict__ field, float* __restrict__ fdense) {
+        const float4* __restrict__ aniso, float* __restrict__ field, float* __restrict__ fdense,
+        uint32_t* __restrict__ cert, uint32_t* __restrict__ n_cert) {
     const uint32_t n_items = *n_items_dev;
+    uint32_t my_cert = 0;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], sry = g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
@@ -105,6 +125,75 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
             sum[k] = 0.f;
         }
         const float uy = (vy - g.min_pos[1]) * inv_cs, uz = (vz - g.min_pos[2]) * inv_cs;
+        bool done[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) done[k] = false;
+        if constexpr (CERT) {
+            // the 2 x 2 x 2 cells nearest to each vertex (inside its window): the run
+            // shares the two slabs and two rows, each vertex takes its own two x cells
+            const int cz = (int)floorf(uz), cy = (int)floorf(uy);
+            const int z2 = uz - (float)cz >= 0.5f ? cz + 1 : cz - 1, y2 = uy - (float)cy >= 0.5f ? cy + 1 : cy - 1;
+            int qa[K], qb[K];
+            int XA = 0x7fffffff, XB = -1;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int cx = (int)floorf(ux[k]);
+                const int x2 = ux[k] - (float)cx >= 0.5f ? cx + 1 : cx - 1;
+                qa[k] = max(min(cx, x2), wlo[k]);
+                qb[k] = min(max(cx, x2) + 1, whi[k]);
+                if (qa[k] < qb[k]) { XA = min(XA, qa[k]); XB = max(XB, qb[k]); }
+            }
+#pragma unroll
+            for (int s2 = 0; s2 < 4; ++s2) {
+                const int z = (s2 >> 1) ? z2 : cz, y = (s2 & 1) ? y2 : cy;
+                if (z < (int)lo.z || z >= (int)hi.z || y < (int)lo.y || y >= (int)hi.y) continue;
+                const uint32_t row = ((uint32_t)z * sry + (uint32_t)y) * srx;
+                for (int x = XA; x < XB; ++x) {
+                    bool use[K];
+#pragma unroll
+                    for (int k = 0; k < K; ++k) use[k] = x >= qa[k] && x < qb[k];
+                    const uint32_t j1 = __ldg(&cell_start[row + (uint32_t)x + 1u]);
+                    for (uint32_t j = __ldg(&cell_start[row + (uint32_t)x]); j < j1; ++j) {
+                        const float4 q = __ldg(&spos[j]);
+                        const float4 a0 = __ldg(&aniso[2 * (size_t)j]);
+                        const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);
+                        const float ry = __fsub_rn(q.y, vy), rz = __fsub_rn(q.z, vz);
+                        const float pyz = __fmaf_rn(rz, __fmul_rn(a1.z, rz), __fmul_rn(ry, __fmaf_rn(a1.x, ry, __fmul_rn(a1.y, rz))));
+                        const float cyz = __fmaf_rn(a0.y, ry, __fmul_rn(a0.z, rz));
+#pragma unroll
+                        for (int k = 0; k < K; ++k) {
+                            const float rxk = __fsub_rn(q.x, vx[k]);
+                            const float d2 = __fmaf_rn(rxk, __fmaf_rn(a0.x, rxk, cyz), pyz);
+                            const float xx = __fsub_rn(1.f, d2);
+                            const float w = (d2 < 1.f) ? __fmul_rn(a1.w, __fmul_rn(__fmul_rn(xx, xx), xx)) : 0.f;
+                            if (use[k]) sum[k] = __fadd_rn(sum[k], w);
+                        }
+                    }
+                }
+            }
+            bool all = true;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if (k < m && sum[k] > fp.quick) {
+                    done[k] = true;
+                    whi[k] = wlo[k];                 // nothing left to walk
+                } else {
+                    sum[k] = 0.f;                    // the walk starts over in the reference's order
+                    all = all && !(k < m);
+                }
+            }
+            if (all) {
+                uint32_t mask = 0u;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (k < m) { fdense[id + k] = sum[k]; mask |= 1u << k; }
+                const uint32_t w = id >> 5, sh = id & 31u;
+                atomicOr(&cert[w], mask << sh);
+                if (sh && (mask >> (32u - sh))) atomicOr(&cert[w + 1], mask >> (32u - sh));
+                my_cert += (uint32_t)m;
+                continue;
+            }
+        }
         int za, zb;
         cell_range(uz, rmax * inv_cs + kRangeMargin, lo.z, hi.z, za, zb);
         for (int z = za; z < zb; ++z) {
@@ -128,7 +217,7 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                 int X0 = 0x7fffffff, X1 = -1;
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
-                    if (sum[k] > fp.thr) {
+                    if (!CERT && sum[k] > fp.thr) {
                         xs[k] = wlo[k];
                         xe[k] = min(wlo[k] + 1, whi[k]);
                     } else {
@@ -202,7 +291,11 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                         uint32_t still = 0u;
 #pragma unroll
                         for (int k = 0; k < K; ++k) {
-                            if (use[k] && sum[k] > fp.thr) { reach[k] = 0u; live[k] = false; }
+                            if (use[k] && sum[k] > fp.thr) {
+                                reach[k] = 0u;
+                                live[k] = false;
+                                if constexpr (CERT) { done[k] = true; whi[k] = wlo[k]; }   // certified: stop for good
+                            }
                             still |= reach[k];
                         }
                         any = still & ~((bit << 1) - 1u);   // i = 31: bit << 1 = 0, nothing left
@@ -214,12 +307,24 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                 }
             }
         }
+        uint32_t mask = 0u;
 #pragma unroll
         for (int k = 0; k < K; ++k)
             if (k < m) {
                 if (field) field[t0 + k] = sum[k];
                 fdense[id + k] = sum[k];
+                if (done[k]) mask |= 1u << k;
             }
+        if (CERT && mask) {
+            const uint32_t w = id >> 5, sh = id & 31u;
+            atomicOr(&cert[w], mask << sh);
+            if (sh && (mask >> (32u - sh))) atomicOr(&cert[w + 1], mask >> (32u - sh));
+            my_cert += (uint32_t)__popc(mask);
+        }
+    }
+    if constexpr (CERT) {
+        const uint32_t tot = __reduce_add_sync(0xffffffffu, my_cert);
+        if ((threadIdx.x & 31u) == 0 && tot) atomicAdd(n_cert, tot);
     }
 }
 
@@ -249,13 +354,15 @@ __global__ void __launch_bounds__(256) k_field_items(const uint32_t* __restrict_
     }
 }
 
-pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out) {
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out,
+                           uint32_t* cert, uint32_t* n_cert) {
     const KGrid g = kgrid_of(ctx->grid);
     const pms_params& P = ctx->prm;
     FieldParams fp;
     fp.h = P.h;
-    fp.thr = 2.f * P.iso_value;
+    fp.thr = cert ? P.iso_value : 2.f * P.iso_value;
     fp.grow = kSupportGrow;
+    fp.quick = P.iso_value * (1.f + 1.f / 512.f);
     Counters* cnt = ctx->counters.as<Counters>();
     if ((uint64_t)n_host >= (1ull << kItemShift)) return pms_fail(ctx, PMS_ERR_UNSUPPORTED, "band above 2^29 vertices");
     const uint32_t K = (uint32_t)ctx->tune.field_vpt;
@@ -278,13 +385,19 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
         kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, &cnt->n_items, ctx->fitems.as<uint32_t>(), vlist,
                                              ctx->cell_start.as<uint32_t>(), ctx->cell_rad.as<float>(),
                                              ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out,
-                                             ctx->fdense.as<float>());
+                                             ctx->fdense.as<float>(), cert, n_cert);
     };
     auto by_vpt = [&](auto bt_tag) {
         constexpr int B = decltype(bt_tag)::value;
-        if (K == 1) go(k_field<B, 1>);
-        else if (K == 4) go(k_field<B, 4>);
-        else go(k_field<B, 2>);
+        if (cert) {
+            if (K == 1) go(k_field<B, 1, true>);
+            else if (K == 4) go(k_field<B, 4, true>);
+            else go(k_field<B, 2, true>);
+        } else {
+            if (K == 1) go(k_field<B, 1, false>);
+            else if (K == 4) go(k_field<B, 4, false>);
+            else go(k_field<B, 2, false>);
+        }
     };
     if (bt == 64) by_vpt(std::integral_constant<int, 64>());
     else if (bt == 256) by_vpt(std::integral_constant<int, 256>());

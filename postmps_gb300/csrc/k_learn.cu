@@ -561,7 +561,10 @@ __global__ void __launch_bounds__(kTcThreads, kTcBlocksPerSm) k_learn_mlp(LearnD
 }
 
 // ---------------------------------------------------------------------------
-// vertex bitmaps from cube bitmaps: a cube marks its 8 corners
+// The band split: a cube marks its 8 corners (cube c is a corner's cube when c
+// is the corner minus {0,1} along each axis), and the plain band U splits into
+// the corners of predicted cubes E (evaluated exactly at once) and the rest N
+// (certified); popcounts per word for the scans of both.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t shifted(const uint32_t* __restrict__ b, uint64_t w, uint64_t s) {
     const uint64_t q = s >> 5;
@@ -573,123 +576,43 @@ __device__ __forceinline__ uint32_t shifted(const uint32_t* __restrict__ b, uint
     return (hi << r) | (lo >> (32u - r));
 }
 
-// out = corners(cubes) & ~exclude (exclude may be null); popcount per word
-__global__ void __launch_bounds__(256) k_cube_corners(const uint32_t* __restrict__ cubes, const uint32_t* __restrict__ exclude,
-                                                      uint32_t* __restrict__ out, uint32_t* __restrict__ wcount,
-                                                      uint64_t nwords, uint64_t nbits, uint64_t sy, uint64_t sz) {
+// cubes null: no prediction, N = U
+__global__ void __launch_bounds__(256) k_band_split(const uint32_t* __restrict__ cubes, const uint32_t* __restrict__ band,
+                                                    uint32_t* __restrict__ e_bm, uint32_t* __restrict__ n_bm,
+                                                    uint32_t* __restrict__ e_wc, uint32_t* __restrict__ n_wc, uint64_t nwords,
+                                                    uint64_t nbits, uint64_t sy, uint64_t sz) {
     for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t v = cubes[w] | shifted(cubes, w, 1) | shifted(cubes, w, sy) | shifted(cubes, w, sy + 1) |
-                     shifted(cubes, w, sz) | shifted(cubes, w, sz + 1) | shifted(cubes, w, sz + sy) |
-                     shifted(cubes, w, sz + sy + 1);
-        if (w == nwords - 1 && (nbits & 31u)) v &= (1u << (nbits & 31u)) - 1u;
-        if (exclude) v &= ~exclude[w];
-        out[w] = v;
-        wcount[w] = __popc(v);
+        uint32_t v = 0u;
+        if (cubes)
+            v = cubes[w] | shifted(cubes, w, 1) | shifted(cubes, w, sy) | shifted(cubes, w, sy + 1) |
+                shifted(cubes, w, sz) | shifted(cubes, w, sz + 1) | shifted(cubes, w, sz + sy) | shifted(cubes, w, sz + sy + 1);
+        uint32_t u = band[w];
+        if (w == nwords - 1 && (nbits & 31u)) u &= (1u << (nbits & 31u)) - 1u;
+        const uint32_t e = u & v, n = u & ~v;
+        e_bm[w] = e;
+        n_bm[w] = n;
+        e_wc[w] = __popc(e);
+        n_wc[w] = __popc(n);
     }
 }
 
-// corners(cubes) appended to a list in no particular order (one atomic per warp)
-__global__ void __launch_bounds__(256) k_corner_list(const uint32_t* __restrict__ cubes, uint64_t nwords, uint64_t nbits,
-                                                     uint64_t sy, uint64_t sz, uint32_t* __restrict__ list,
-                                                     uint32_t* __restrict__ n_list) {
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint64_t w0 = blockIdx.x * (uint64_t)blockDim.x; w0 < nwords; w0 += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t w = w0 + threadIdx.x;
-        uint32_t v = 0;
-        if (w < nwords) {
-            v = cubes[w] | shifted(cubes, w, 1) | shifted(cubes, w, sy) | shifted(cubes, w, sy + 1) | shifted(cubes, w, sz) |
-                shifted(cubes, w, sz + 1) | shifted(cubes, w, sz + sy) | shifted(cubes, w, sz + sy + 1);
-            if (w == nwords - 1 && (nbits & 31u)) v &= (1u << (nbits & 31u)) - 1u;
-        }
-        const uint32_t c = __popc(v);
-        uint32_t incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
-        }
-        uint32_t base = 0;
-        if (lane == 31u && incl) base = atomicAdd(n_list, incl);
-        base = __shfl_sync(0xffffffffu, base, 31);
-        uint32_t o = base + incl - c;
-        while (v) {
-            list[o++] = (uint32_t)(w * 32u) + (uint32_t)(__ffs(v) - 1);
-            v &= v - 1u;
-        }
-    }
-}
-
-// a | b with popcount per word
-__global__ void __launch_bounds__(256) k_bits_or(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
-                                                 uint32_t* __restrict__ out, uint32_t* __restrict__ wcount, uint64_t nwords) {
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t v = a[w] | b[w];
-        out[w] = v;
-        wcount[w] = __popc(v);
-    }
-}
-
-// Border check: a valid cube whose face has corners on both sides of the
-// iso-surface shares that crossing with the cube across the face, so the
-// neighbour is a valid cube too; if not all of the neighbour's corners have a
-// field value yet, the neighbour cube is queued.  One thread per valid cube
-// of the classification ({vertex id, case} records of the compaction).
-__global__ void __launch_bounds__(256) k_border(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
-                                                const uint32_t* __restrict__ vbm, uint32_t* __restrict__ qadd,
-                                                uint32_t* __restrict__ n_added, uint32_t* __restrict__ qlist, uint32_t qcap) {
+// The certified corners of the valid cubes (compaction records {vertex id,
+// case, ...}): their bits go to `recheck`, whose vertices are then evaluated
+// exactly.  A cube's corners lie in 4 rows of 2 neighbouring vertices.
+__global__ void __launch_bounds__(256) k_recheck_bits(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
+                                                      const uint32_t* __restrict__ cert, uint32_t* __restrict__ recheck) {
     const uint32_t n = cnt->nvalid;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint4 cr = __ldg(&cube[t]);
-        const uint32_t cs = cr.y, id = cr.x;
-        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-        border_faces(g, x, y, z, cs, vbm, qadd, n_added, qlist, qcap);
-    }
-}
-
-// Border check of a list of cubes whose corners all have field values (the
-// cubes the last round queued): their cases are computed here from the field
-// (bit k set when corner k lies at or below iso, the corner order of
-// detectValidSurfaceCubes) and the crossed faces are checked as in k_border.
-__global__ void __launch_bounds__(256) k_border_list(KGrid g, float iso, const uint32_t* __restrict__ cubes,
-                                                     uint32_t n_host, const uint32_t* __restrict__ n_dev,
-                                                     const uint32_t* __restrict__ vbm, const float* __restrict__ fdense,
-                                                     uint32_t* __restrict__ qadd, uint32_t* __restrict__ n_added,
-                                                     uint32_t* __restrict__ qlist, uint32_t qcap) {
-    const uint32_t n = n_dev ? *n_dev : n_host;
-    const uint32_t rx = g.scres[0], rxy = rx * g.scres[1];
-    // corner order {000,001,011,010,100,101,111,110} as (x, y, z) offsets
-    const uint32_t cx[8] = {0, 0, 0, 0, 1, 1, 1, 1}, cy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, cz[8] = {0, 1, 1, 0, 0, 1, 1, 0};
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint32_t id = cubes[t];
-        uint32_t cs = 0;
-        bool all = true;
+        const uint32_t id = __ldg(&cube[t]).x;
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t c = id + cx[k] + cy[k] * rx + cz[k] * rxy;
-            if (!((vbm[c >> 5] >> (c & 31u)) & 1u)) { all = false; break; }
-            cs |= (__ldg(&fdense[c]) <= iso ? 1u : 0u) << k;
-        }
-        if (!all || cs == 0u || cs == 255u) continue;
-        const int z = (int)(id / rxy), rem = (int)(id - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
-        border_faces(g, x, y, z, cs, vbm, qadd, n_added, qlist, qcap);
-    }
-}
-
-// The corners of queued cubes that have no field value yet: set in the vertex
-// bitmap and appended to vnew (one entry per new vertex, in no fixed order).
-__global__ void __launch_bounds__(256) k_queue_corners(KGrid g, const uint32_t* __restrict__ cubes, uint32_t n,
-                                                       uint32_t* __restrict__ vbm, uint32_t* __restrict__ vnew,
-                                                       uint32_t* __restrict__ n_new) {
-    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint32_t id = cubes[t];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const uint32_t c = id + (uint32_t)(k & 1) + (uint32_t)((k >> 1) & 1) * rx + (uint32_t)(k >> 2) * rxy;
-            const uint32_t bit = 1u << (c & 31u);
-            if (atomicOr(&vbm[c >> 5], bit) & bit) continue;
-            vnew[atomicAdd(n_new, 1u)] = c;      // at most 8 n entries
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t c = id + (uint32_t)(r & 1) * rx + (uint32_t)(r >> 1) * rxy;   // corners c, c + 1
+            const uint32_t w = c >> 5, sh = c & 31u;
+            const uint32_t pair = (__ldg(&cert[w]) >> sh) & (sh == 31u ? 1u : 3u);
+            const uint32_t hi = sh == 31u ? (__ldg(&cert[w + 1]) & 1u) : 0u;
+            if (pair) atomicOr(&recheck[w], pair << sh);
+            if (hi) atomicOr(&recheck[w + 1], 1u);
         }
     }
 }
@@ -706,25 +629,6 @@ __global__ void __launch_bounds__(256) k_label_bits(const uint32_t* __restrict__
     const uint32_t n = *n_dev;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
         if (mc_key[t]) atomicOr(&lbm[vlist[t] >> 5], 1u << (vlist[t] & 31u));
-}
-
-// cube bitmap of the compacted valid-cube records (one atomic per warp and word)
-__global__ void __launch_bounds__(256) k_valid_bits(const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
-                                                    uint32_t* __restrict__ bits) {
-    const uint32_t n = cnt->nvalid;
-    const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t t0 = blockIdx.x * blockDim.x; t0 < n; t0 += gridDim.x * blockDim.x) {
-        const uint32_t t = t0 + threadIdx.x;
-        uint32_t w = 0xffffffffu, b = 0u;
-        if (t < n) {
-            const uint32_t id = cube[t].x;
-            w = id >> 5;
-            b = 1u << (id & 31u);
-        }
-        const uint32_t peers = __match_any_sync(0xffffffffu, w);
-        const uint32_t orv = __reduce_or_sync(peers, b);
-        if (t < n && (uint32_t)(__ffs(peers) - 1) == lane) atomicOr(&bits[w], orv);
-    }
 }
 
 // features of explicit cubes (bf16 bits, 64 per cube), for checks against the oracle
@@ -1024,58 +928,24 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
     return PMS_OK;
 }
 
-pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
-                               uint32_t* wcount) {
+pms_status launch_band_split(pms_ctx* ctx, const uint32_t* cubes, uint32_t* e_bm, uint32_t* n_bm, uint32_t* e_wc,
+                             uint32_t* n_wc) {
     const KGrid g = kgrid_of(ctx->grid);
     const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
     const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
-    k_cube_corners<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, exclude, out, wcount, nwords, nbits, sy, sz);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
-pms_status launch_corner_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t* list, uint32_t* n_list) {
-    const KGrid g = kgrid_of(ctx->grid);
-    const uint64_t nbits = g.sc_size, nwords = (nbits + 31) / 32;
-    const uint64_t sy = g.scres[0], sz = (uint64_t)g.scres[0] * g.scres[1];
-    PMS_CUDA(ctx, cudaMemsetAsync(n_list, 0, sizeof(uint32_t), ctx->stream));
-    k_corner_list<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, nwords, nbits, sy, sz, list, n_list);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
-pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount) {
-    const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
-    k_bits_or<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(a, b, out, wcount, nwords);
+    k_band_split<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(cubes, ctx->bm.as<uint32_t>(), e_bm, n_bm, e_wc, n_wc,
+                                                                 nwords, nbits, sy, sz);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 
-pms_status launch_border(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist, uint32_t qcap) {
+pms_status launch_recheck_bits(pms_ctx* ctx, const uint32_t* cert, uint32_t* recheck) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     // ctx->nv bounds the valid cubes; the kernel reads their count
-    k_border<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), ctx->bm.as<uint32_t>(), qadd,
-                                                              &cnt->l_added, qlist, qcap);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
-pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd, const uint32_t* n_dev,
-                              uint32_t* qlist, uint32_t qcap) {
-    const KGrid g = kgrid_of(ctx->grid);
-    Counters* cnt = ctx->counters.as<Counters>();
-    k_border_list<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, cubes, n, n_dev, ctx->bm.as<uint32_t>(),
-                                                              ctx->fdense.as<float>(), qadd, &cnt->l_added, qlist, qcap);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
-pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* vnew, uint32_t* n_new) {
-    const KGrid g = kgrid_of(ctx->grid);
-    k_queue_corners<<<grid_for(n, 256), 256, 0, ctx->stream>>>(g, cubes, n, ctx->bm.as<uint32_t>(), vnew, n_new);
+    k_recheck_bits<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), cert, recheck);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
@@ -1083,14 +953,6 @@ pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n,
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount) {
     const uint64_t nwords = ((uint64_t)ctx->grid.sc_size + 31) / 32;
     k_popc<<<grid_for(nwords, 256), 256, 0, ctx->stream>>>(b, wcount, nwords);
-    PMS_LAUNCHED(ctx);
-    return PMS_OK;
-}
-
-pms_status launch_valid_bits(pms_ctx* ctx, uint32_t* bits) {
-    Counters* cnt = ctx->counters.as<Counters>();
-    // ctx->nv bounds the valid cubes; the kernel reads their count
-    k_valid_bits<<<grid_for(ctx->nv, 256), 256, 0, ctx->stream>>>(cnt, ctx->cube.as<uint4>(), bits);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }

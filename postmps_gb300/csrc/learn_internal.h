@@ -37,26 +37,21 @@ struct TrainArgs {
 LearnDims learn_dims(const pms_ctx* ctx);
 pms_status launch_coarse_counts(pms_ctx* ctx);
 pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* cand, float* logit, uint32_t cand_cap);
-pms_status launch_cube_corners(pms_ctx* ctx, const uint32_t* cubes, const uint32_t* exclude, uint32_t* out,
-                               uint32_t* wcount);
-// the corners of the cubes of a bitmap, listed in no particular order; *n_list their count
-pms_status launch_corner_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t* list, uint32_t* n_list);
-pms_status launch_bits_or(pms_ctx* ctx, const uint32_t* a, const uint32_t* b, uint32_t* out, uint32_t* wcount);
-// border checks queue cubes in qadd (a bitmap) and, when qlist is given, in a
-// list of at most qcap entries; the count (l_added) may exceed qcap
-pms_status launch_border(pms_ctx* ctx, uint32_t* qadd, uint32_t* qlist = nullptr, uint32_t qcap = 0);
-// corners of n queued cubes not yet in the vertex bitmap: set there and appended to vnew
-pms_status launch_queue_corners(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* vnew, uint32_t* n_new);
-pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
-// cube bitmap of the compacted valid-cube records (bits: zeroed)
-pms_status launch_valid_bits(pms_ctx* ctx, uint32_t* bits);
-// n: the list length, or a bound when n_dev holds it on the device
-pms_status launch_border_list(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint32_t* qadd,
-                              const uint32_t* n_dev = nullptr, uint32_t* qlist = nullptr, uint32_t qcap = 0);
+// the plain band (ctx->bm) split into the corners of the cubes of a cube bitmap (E,
+// evaluated exactly at once) and the rest (N, certified); cubes null: E empty
+pms_status launch_band_split(pms_ctx* ctx, const uint32_t* cubes, uint32_t* e_bm, uint32_t* n_bm, uint32_t* e_wc,
+                             uint32_t* n_wc);
+// the certified corners (bits of cert) of the classified valid cubes, as bits of recheck
+pms_status launch_recheck_bits(pms_ctx* ctx, const uint32_t* cert, uint32_t* recheck);
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount);
-// corners of the classified valid cubes outside the plain band leave the vertex
-// set (bitmap and dense field); Counters::l_removed counts them
-pms_status plain_band_filter(pms_ctx* ctx);
+pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
+// the learned band after the plain band (ctx->bm, ctx->vlist; ctx->nv its count, or a
+// bound for batched frames): prediction and split, then the field stage (exact field
+// at E, certification of N, classification, exact field at the rechecked corners,
+// band-order field); no host synchronisation
+pms_status ensure_learned_buffers(pms_ctx* ctx, uint64_t sc_size, uint32_t nv);
+pms_status learned_split(pms_ctx* ctx, bool predict);
+pms_status learned_field(pms_ctx* ctx);
 pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x);
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,
                          float* loss_sum);

@@ -55,7 +55,10 @@ static void release_all(pms_ctx* c) {
                     &c->mc_key, &c->mc_off, &c->valid, &c->fdense, &c->cube, &c->fitems, &c->fitem_cnt, &c->fitem_off, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
-                    &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp};
+                    &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp,
+                    &c->l_dens, &c->l_clist, &c->l_counts, &c->l_model, &c->l_q, &c->l_cert, &c->l_e_bm, &c->l_e_wc,
+                    &c->l_e_wp, &c->l_e_list, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp, &c->l_n_list, &c->l_field_new,
+                    &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list};
     for (DBuf* b : bufs) b->release();
 }
 
@@ -104,6 +107,8 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (c->vel_ready) cudaEventDestroy(c->vel_ready);
     if (c->mesh_ready) cudaEventDestroy(c->mesh_ready);
     if (c->mesh_copied) cudaEventDestroy(c->mesh_copied);
+    if (c->diffuse_ready) cudaEventDestroy(c->diffuse_ready);
+    if (c->diffuse_copied) cudaEventDestroy(c->diffuse_copied);
     pms_batch_release(c);
     release_all(c);
     for (int i = 0; i <= kNumStages; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -176,12 +181,19 @@ pms_status pms::ensure_grid_buffers(pms_ctx* c, const pms_grid& g) {
     PMS_CUDA(c, c->bm.ensure(4 * W));
     PMS_CUDA(c, c->wcount.ensure(4 * W));
     PMS_CUDA(c, c->wprefix.ensure(4 * W));
+    // the band marking's tiles of the scalar grid: at most one per vertex
+    const size_t T = (size_t)g.sc_size + 1, TW = T / 32 + 2;
+    PMS_CUDA(c, c->tile_bits.ensure(4 * TW));
+    PMS_CUDA(c, c->tile_wc.ensure(4 * TW));
+    PMS_CUDA(c, c->tile_wp.ensure(4 * TW));
+    PMS_CUDA(c, c->tile_list.ensure(4 * T));
     return PMS_OK;
 }
 
 namespace pms {
 pms_status ensure_band_buffers(pms_ctx* c, uint32_t nv);
 void mark_stage(pms_ctx* c, int boundary);
+pms_status plain_band(pms_ctx* c);
 }  // namespace pms
 
 pms_status pms::ensure_band_buffers(pms_ctx* c, uint32_t nv) {
@@ -288,7 +300,7 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     c->have_particles = true;
     c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = false;
     c->band_learned = c->mc_classified = c->mc_compacted = false;
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
+    c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
     c->ns = c->nv = c->nvalid = 0;
     c->nmesh = 0;
     for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
@@ -350,13 +362,8 @@ extern "C" pms_status pms_anisotropy(pms_ctx* c) {
     return PMS_OK;
 }
 
-extern "C" pms_status pms_band(pms_ctx* c) {
-    if (!c) return PMS_ERR_INVALID_ARGUMENT;
-    if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
-    cudaSetDevice(c->device);
-    c->band_learned = c->mc_classified = c->mc_compacted = false;
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
-    if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
+// The plain band's bitmap, count and ascending vertex list (one synchronisation).
+pms_status pms::plain_band(pms_ctx* c) {
     pms_status st;
     if ((st = launch_band(c))) return st;
     if ((st = sync_counters(c))) return st;
@@ -364,7 +371,18 @@ extern "C" pms_status pms_band(pms_ctx* c) {
     c->ns = c->h_counters->ns;
     c->nv = c->h_counters->nv;
     if ((st = ensure_band(c, c->nv))) return st;
-    if ((st = launch_band_list(c))) return st;
+    return launch_band_list(c);
+}
+
+extern "C" pms_status pms_band(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band before pms_anisotropy");
+    cudaSetDevice(c->device);
+    c->band_learned = c->mc_classified = c->mc_compacted = false;
+    c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
+    if (c->n == 0) { c->nv = 0; c->have_band = true; return PMS_OK; }
+    pms_status st;
+    if ((st = plain_band(c))) return st;
     c->have_band = true;
     mark(c, kStageBand + 1);
     return PMS_OK;
@@ -484,7 +502,7 @@ extern "C" pms_status pms_run_frame(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     pms_status st;
     if ((st = pms_build_grid(c))) return st;
-    if (c->cfg.is_surface && (st = c->band_mode == PMS_BAND_LEARNED ? pms_surface_learned(c) : pms_surface(c))) return st;
+    if (c->cfg.is_surface && (st = c->band_mode != PMS_BAND_PLAIN ? pms_surface_learned(c) : pms_surface(c))) return st;
     if (c->cfg.is_diffuse && (st = pms_diffuse(c))) return st;
     c->frame_index++;
     return PMS_OK;
@@ -516,9 +534,9 @@ extern "C" pms_status pms_get_counts(pms_ctx* c, pms_counts* out) {
     if (c->band_learned) {
         out->n_band_candidates = c->l_ncand;
         out->n_band_predicted = c->l_npred;
-        out->n_band_fallback = c->l_nadded;
-        out->n_band_iterations = c->l_iters;
-        out->n_band_removed = c->l_nremoved;
+        out->n_band_exact = c->l_nexact;
+        out->n_band_certified = c->l_ncert;
+        out->n_band_rechecked = c->l_nrecheck;
     }
     return check_device_errors(c);
 }

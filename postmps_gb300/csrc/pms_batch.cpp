@@ -17,11 +17,12 @@
 // capture stream, so independent frames overlap on the GPU; a frame's mesh
 // claims its stretch of the arena with an atomic add.
 //
-// With the learned band, the graph holds the prediction, the field at the
-// predicted corners and one border check per frame; a frame whose border
-// check finds missing cubes, or whose valid cubes have corners outside the
-// plain band, is re-run alone on the exact learned path afterwards, so the
-// batched result equals the single-frame result.
+// With the learned band, the graph holds each frame's plain band, prediction,
+// split, exact field at the predicted corners, sign certification of the rest,
+// classification and exact field at the certified corners of valid cubes: the
+// same launches as a single learned frame, every size a bound and every count
+// on the device, so the batched result equals the single-frame result (and the
+// plain band's).
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
@@ -50,12 +51,10 @@ struct BatchState {
     std::vector<pms_ctx*> lanes;                 // sub-contexts (lane 0 is the context itself)
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr;
-    std::vector<std::vector<float>> rerun_mesh;   // frames re-run alone (learned band fallback)
-    std::vector<char> rerun;
     cudaGraphExec_t exec = nullptr;
     int flags = -1;
     uint64_t mesh_cap = 0;
-    uint32_t captures = 0, reruns = 0;
+    uint32_t captures = 0;
     uint64_t gen = 0;                 // buffer generation the graph was captured against
     uint32_t nlanes_captured = 0;
     uint32_t wait_captured = 0;       // the debug wait limit baked into the captured launches
@@ -108,58 +107,12 @@ struct FrameView {
     }
 };
 
-// Border-check rounds inside the graph: a fixed number per frame, every size a
-// bound and every count on the device (a round with an empty queue does no work).
-static constexpr int kGraphRounds = 3;
-
-// classify every cube of the vertex set, then queue the cubes across crossed faces
-static pms_status full_check(pms_ctx* c, uint64_t W) {
-    Counters* cnt = c->counters.as<Counters>();
-    pms_status st;
-    if ((st = launch_mc_classify(c))) return st;
-    PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
-    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-    return launch_border(c, c->l_qadd.as<uint32_t>());
-}
-
-// one round: field at the queued cubes' new corners (into the dense field), merged vertex set,
-// check the queued cubes
-static pms_status border_round(pms_ctx* c, uint64_t W) {
-    Counters* cnt = c->counters.as<Counters>();
-    const uint32_t S = c->grid.sc_size;
-    pms_status st;
-    if ((st = launch_popc(c, c->l_qadd.as<uint32_t>(), c->l_wc_new.as<uint32_t>()))) return st;
-    if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), W, &cnt->l_nq))) return st;
-    if ((st = launch_bits_list(c, c->l_qadd.as<uint32_t>(), c->l_wp_q.as<uint32_t>(), c->l_qlist.as<uint32_t>()))) return st;
-    if ((st = launch_cube_corners(c, c->l_qadd.as<uint32_t>(), c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(),
-                                  c->l_wc_new.as<uint32_t>())))
-        return st;
-    if ((st = scan_u32(c, c->l_wc_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), W, &cnt->l_nnew))) return st;
-    if ((st = launch_bits_list(c, c->l_bm_new.as<uint32_t>(), c->l_wp_new.as<uint32_t>(), c->l_vlist_new.as<uint32_t>())))
-        return st;
-    if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, S, nullptr))) return st;
-    if ((st = launch_bits_or(c, c->bm.as<uint32_t>(), c->l_bm_new.as<uint32_t>(), c->l_bm_m.as<uint32_t>(),
-                             c->wcount.as<uint32_t>())))
-        return st;
-    if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), W, &cnt->nv))) return st;
-    if ((st = launch_bits_list(c, c->l_bm_m.as<uint32_t>(), c->l_wp_m.as<uint32_t>(), c->l_vlist_m.as<uint32_t>())))
-        return st;
-    std::swap(c->bm, c->l_bm_m);
-    std::swap(c->wprefix, c->l_wp_m);
-    std::swap(c->vlist, c->l_vlist_m);
-    PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
-    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-    if ((st = launch_border_list(c, c->l_qlist.as<uint32_t>(), S, c->l_q.as<uint32_t>(), &cnt->l_nq))) return st;
-    std::swap(c->l_q, c->l_qadd);
-    return PMS_OK;
-}
-
 // Stages of one frame without host synchronisation (the context points at the frame).
-static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool learned) {
+// band: 0 plain, 1 learned (network + certification), 2 certification alone
+static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, int band) {
     pms_status st;
     Counters* cnt = c->counters.as<Counters>();
     const pms_grid& g = c->grid;
-    const uint64_t W = ((uint64_t)g.sc_size + 31) / 32;
     c->nv = g.sc_size;                       // bounds for launch grids; kernels read the device counts
     c->nvalid = g.sc_size;
     if ((st = launch_bbox(c))) return st;    // resets the frame's counters
@@ -167,24 +120,11 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, bool lear
     if ((st = launch_hash_sort(c))) return st;
     if ((st = launch_surface_cells(c))) return st;
     if ((st = launch_density_aniso(c))) return st;
-    if (learned) {
-        if ((st = launch_coarse_counts(c))) return st;
-        PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
-        if ((st = launch_predict(c, 1, c->l_q.as<uint32_t>(), nullptr, nullptr, 0))) return st;
-        if ((st = launch_cube_corners(c, c->l_q.as<uint32_t>(), nullptr, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>())))
-            return st;
-        if ((st = scan_u32(c, c->wcount.as<uint32_t>(), c->wprefix.as<uint32_t>(), W, &cnt->nv))) return st;
-        if ((st = launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>())))
-            return st;
-        if ((st = launch_field(c))) return st;
-        if ((st = full_check(c, W))) return st;
-        for (int r = 0; r < kGraphRounds; ++r)
-            if ((st = border_round(c, W))) return st;
-        // the band-order field of the final vertex set (the rounds work on the dense field)
-        if ((st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, g.sc_size, c->field.as<float>()))) return st;
-        if ((st = full_check(c, W))) return st;              // what is still missing: the frame runs again alone
-        // corners of valid cubes outside the plain band: the frame runs again alone too
-        if ((st = plain_band_filter(c))) return st;
+    if (band) {
+        if ((st = launch_band(c))) return st;
+        if ((st = launch_band_list(c))) return st;
+        if ((st = learned_split(c, band == 1))) return st;
+        if ((st = learned_field(c))) return st;
     } else {
         if ((st = launch_band(c))) return st;
         if ((st = launch_band_list(c))) return st;
@@ -201,7 +141,7 @@ static constexpr uint32_t kBatchLanes = 4;
 // lane l of the batch: the context itself for l = 0, else a sub-context
 static pms_ctx* lane_ctx(pms_ctx* c, BatchState* b, uint32_t l) { return l == 0 ? c : b->lanes[l - 1]; }
 
-static pms_status capture(pms_ctx* c, BatchState* b, bool learned, uint32_t nlanes) {
+static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     const uint32_t k = (uint32_t)b->n.size();
     // frames to lanes, largest first onto the least loaded lane
@@ -231,7 +171,7 @@ static pms_status capture(pms_ctx* c, BatchState* b, bool learned, uint32_t nlan
             view.point(b, f);
             // external: recorded when the graph runs (a plain record inside a capture only orders work)
             if (cudaEventRecordWithFlags(b->ev[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
-            if ((st = capture_frame(lc, b, f, learned))) break;
+            if ((st = capture_frame(lc, b, f, band))) break;
             if (cudaEventRecordWithFlags(b->ev_end[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) st = PMS_ERR_CUDA;
         }
     }
@@ -273,17 +213,8 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
     lc->tune = c->tune;
     lc->tc_wait_polls = c->tc_wait_polls;     // the debug wait limit holds on every lane
     if (!learned) return PMS_OK;
-    const uint64_t W = ((uint64_t)gmax.sc_size + 31) / 32;
     const size_t S = (size_t)gmax.sc_size + 1;
-    for (DBuf* d : {&lc->l_q, &lc->l_qadd, &lc->l_bm_new, &lc->l_wc_new, &lc->l_wp_new, &lc->l_bm_m, &lc->l_wp_m, &lc->l_wp_q})
-        PMS_CUDA(lc, d->ensure(4 * (W + 1)));
-    for (DBuf* d : {&lc->l_vlist_new, &lc->l_vlist_m, &lc->l_qlist})
-        PMS_CUDA(lc, d->ensure(4 * S));
-    // the buffers that trade places with these in the rounds must be as large
-    PMS_CUDA(lc, lc->bm.ensure(4 * (W + 1)));
-    PMS_CUDA(lc, lc->wprefix.ensure(4 * (W + 1)));
-    PMS_CUDA(lc, lc->vlist.ensure(4 * S));
-    PMS_CUDA(lc, lc->field.ensure(4 * S));
+    if ((st = ensure_learned_buffers(lc, gmax.sc_size, gmax.sc_size))) return st;
     size_t ncoarse = 1;
     for (const pms_grid& g : grid)
         ncoarse = std::max(ncoarse, (size_t)(g.scres[0] / 2 + 2) * (g.scres[1] / 2 + 2) * (g.scres[2] / 2 + 2));
@@ -293,7 +224,7 @@ static pms_status ensure_lane(pms_ctx* lc, pms_ctx* c, uint32_t nmax, const pms_
         npad = std::max(npad, (size_t)(g.scres[0] / 2 + 3) * (g.scres[1] / 2 + 3) * (g.scres[2] / 2 + 3));
     PMS_CUDA(lc, lc->l_dens.ensure(4 * npad));    // padded coarse grid: cres + 1 per axis
     PMS_CUDA(lc, lc->l_clist.ensure(8 * S));
-    if (lc != c) {
+    if (lc != c && c->have_model) {
         // the lane reads the context's model
         PMS_CUDA(lc, lc->l_model.ensure(sizeof(pms_band_model)));
         PMS_CUDA(lc, cudaMemcpyAsync(lc->l_model.p, c->l_model.p, sizeof(pms_band_model), cudaMemcpyDeviceToDevice, c->stream));
@@ -322,8 +253,9 @@ static inline float decode_ordered(uint32_t u) {
 
 extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_t k, int flags) {
     if (!c || (k && !frames)) return PMS_ERR_INVALID_ARGUMENT;
-    const bool learned = (flags & PMS_BATCH_LEARNED) != 0;
-    if (learned && !c->have_model) return pms_fail(c, PMS_ERR_STATE, "learned batch without a model");
+    const int band = (flags & PMS_BATCH_LEARNED) ? 1 : (flags & PMS_BATCH_CERTIFIED) ? 2 : 0;
+    const bool learned = band != 0;          // the learned band's buffers and launches
+    if (band == 1 && !c->have_model) return pms_fail(c, PMS_ERR_STATE, "learned batch without a model");
     for (uint32_t f = 0; f < k; ++f)
         if (frames[f].n && !frames[f].pos_xyz) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: no positions", f);
     cudaSetDevice(c->device);
@@ -334,7 +266,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         c->vel_pending = false;
     }
     BatchState* b = batch_of(c);
-    if (k == 0) { b->n.clear(); b->hcnt.clear(); b->rerun.clear(); b->rerun_mesh.clear(); return PMS_OK; }
+    if (k == 0) { b->n.clear(); b->hcnt.clear(); return PMS_OK; }
     // ---- pass 1: arena, uploads, bounding boxes
     uint64_t total = 0;
     std::vector<uint64_t> off(k);
@@ -425,7 +357,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     // ---- pass 2: the graph (captured again when the frames' grids or any buffer changed)
     for (int attempt = 0; attempt < 3; ++attempt) {
         if (!grids_same || !b->exec || b->gen != g_dbuf_generation) {
-            if ((st = capture(c, b, learned, nlanes))) return st;
+            if ((st = capture(c, b, band, nlanes))) return st;
             b->gen = g_dbuf_generation;
             b->nlanes_captured = nlanes;
             b->wait_captured = c->tc_wait_polls;
@@ -449,30 +381,6 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         grids_same = false;
         if (attempt == 2) return pms_fail(c, PMS_ERR_CAPACITY, "batch mesh arena overflow");
     }
-    // ---- learned band: frames whose border check found missing cubes run alone on the exact path
-    b->rerun.assign(k, 0);
-    b->rerun_mesh.assign(k, {});
-    if (learned) {
-        for (uint32_t f = 0; f < k; ++f) {
-            if (b->hcnt[f].l_added == 0 && b->hcnt[f].l_removed == 0) continue;
-            b->rerun[f] = 1;
-            b->reruns++;
-            if ((st = pms_upload_particles_device(c, b->pos.as<float>() + 3 * off[f], b->vel.as<float>() + 3 * off[f],
-                                                  b->rho.as<float>() + off[f], n[f])))
-                return st;
-            if ((st = pms_build_grid(c)) || (st = pms_surface_learned(c))) return st;
-            uint64_t nv = 0;
-            pms_download_mesh(c, nullptr, nullptr, 0, &nv);
-            b->rerun_mesh[f].resize(3 * nv);
-            if (nv && (st = pms_download_mesh(c, b->rerun_mesh[f].data(), nullptr, nv, &nv))) return st;
-            PMS_CUDA(c, cudaStreamSynchronize(c->stream));
-            pms::Counters h = *c->h_counters;
-            h.l_added = 0;
-            h.l_removed = 0;
-            b->hcnt[f] = h;
-            b->hcnt[f].nmesh = nv;
-        }
-    }
     return PMS_OK;
 }
 
@@ -489,15 +397,17 @@ extern "C" pms_status pms_batch_frame(pms_ctx* c, uint32_t f, pms_counts* out, f
         out->n_valid_cubes = h.nvalid;
         out->n_mesh_vertices = h.nmesh;
         out->n_fp64_svd = h.n_fp64;
-        if (b->flags & PMS_BATCH_LEARNED) {
+        if (b->flags & (PMS_BATCH_LEARNED | PMS_BATCH_CERTIFIED)) {
             out->n_band_candidates = h.l_cand;
             out->n_band_predicted = h.l_pred;
-            out->n_band_iterations = b->rerun[f] ? 1u : 0u;
+            out->n_band_exact = h.l_exact;
+            out->n_band_certified = h.l_cert;
+            out->n_band_rechecked = h.l_recheck;
         }
     }
     if (ms) {
         *ms = 0.f;
-        if (!b->rerun[f] && cudaEventElapsedTime(ms, b->ev[f], b->ev_end[f]) != cudaSuccess) {
+        if (cudaEventElapsedTime(ms, b->ev[f], b->ev_end[f]) != cudaSuccess) {
             *ms = 0.f;
             cudaGetLastError();                      // a missing time is not a failure of later calls
         }
@@ -509,14 +419,6 @@ extern "C" pms_status pms_batch_mesh(pms_ctx* c, uint32_t f, float* pos, uint64_
     if (!c || !c->batch || !n_out) return PMS_ERR_INVALID_ARGUMENT;
     BatchState* b = static_cast<BatchState*>(c->batch);
     if (f >= b->n.size()) return PMS_ERR_INVALID_ARGUMENT;
-    if (b->rerun[f]) {
-        const uint64_t m = b->rerun_mesh[f].size() / 3;
-        *n_out = m;
-        if (!pos) return PMS_OK;
-        if (cap < m) return PMS_ERR_CAPACITY;
-        memcpy(pos, b->rerun_mesh[f].data(), 12 * m);
-        return PMS_OK;
-    }
     const uint64_t m = b->hcnt[f].nmesh;
     *n_out = m;
     if (!pos) return PMS_OK;
@@ -527,11 +429,10 @@ extern "C" pms_status pms_batch_mesh(pms_ctx* c, uint32_t f, float* pos, uint64_
     return PMS_OK;
 }
 
-extern "C" pms_status pms_batch_info(pms_ctx* c, uint32_t* graph_kernels, uint32_t* captures, uint32_t* reruns) {
+extern "C" pms_status pms_batch_info(pms_ctx* c, uint32_t* graph_kernels, uint32_t* captures) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     BatchState* b = static_cast<BatchState*>(c->batch);
     if (graph_kernels) *graph_kernels = (uint32_t)c->batch_launches;
     if (captures) *captures = b ? b->captures : 0;
-    if (reruns) *reruns = b ? b->reruns : 0;
     return PMS_OK;
 }

@@ -60,16 +60,17 @@ struct Counters {
     uint32_t n_live;        // after delete/append
     uint32_t n_type[4];     // spray, foam, bubble, deleted
     uint32_t rad_max_bits;  // largest anisotropic support maxvalue * h (float bits)
-    // learned band
+    // learned band (the first kLearnCounters fields are zeroed per frame)
     uint32_t l_cand;        // candidate cubes evaluated by the network
     uint32_t l_pred;        // predicted cubes (or candidate slots written)
-    uint32_t l_added;       // cubes the last border check queued
-    uint32_t l_nnew;        // vertices those cubes add
-    uint32_t l_nq;          // cubes queued for a border-check round (batched frames)
+    uint32_t l_exact;       // band vertices evaluated exactly first (corners of predicted cubes)
+    uint32_t l_nlist;       // band vertices certified (the rest of the band)
+    uint32_t l_cert;        // ... of which stopped above iso without an exact value
+    uint32_t l_recheck;     // certified corners of valid cubes, evaluated exactly afterwards
     uint32_t n_items;       // work items of the last field launch
-    uint32_t l_removed;     // learned-band vertices outside the plain band
-    uint32_t l_open;        // vertices the quick plain-band test left open
+    uint32_t n_tiles;       // scalar-grid tiles the band marking visits
 };
+static constexpr int kLearnCounters = 6;
 
 enum : uint32_t {
     kErrNonFinite = 1u,     // NaN/Inf particle position
@@ -129,6 +130,11 @@ struct pms_ctx {
     float* out_nrm = nullptr;
     uint64_t out_cap = 0, out_n = 0;
     bool out_pending = false, out_overflow = false;
+    // live diffuse particles streamed to a registered host buffer on the copy stream
+    pms_diffuse_particle* dout = nullptr;
+    uint64_t dout_cap = 0, dout_n = 0;
+    bool dout_pending = false, dout_overflow = false;
+    cudaEvent_t diffuse_ready = nullptr, diffuse_copied = nullptr;
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;
@@ -147,8 +153,8 @@ struct pms_ctx {
     pms::DBuf cell_count, cell_start, cell_info, surf_count, surf_start, big_cells;
     // anisotropy
     pms::DBuf slist, moments, aniso, nrm4, mean4, gdebug, nnb, cell_rad, cell_rec;
-    // band
-    pms::DBuf bm0, bm, wcount, wprefix, vlist;
+    // band (and the tiles of the scalar grid its marking visits)
+    pms::DBuf bm0, bm, wcount, wprefix, vlist, tile_bits, tile_wc, tile_wp, tile_list;
     // field and marching cubes
     pms::DBuf field, mc_case, mc_key, mc_off, valid, vert, vnorm, sval;
     // the field over the whole scalar grid, 0 off the band (the marching cubes' lookups);
@@ -165,8 +171,10 @@ struct pms_ctx {
               d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
     // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
     pms::DBuf l_dens, l_clist;   // bf16 coarse density pairs (padded grid), candidate cube records
-    pms::DBuf l_counts, l_model, l_q, l_qadd, l_bm_new, l_wc_new, l_wp_new, l_bm_m, l_wp_m, l_vlist_new,
-              l_field_new, l_vlist_m, l_qnext, l_cand, l_logit, l_label, l_qlist, l_wp_q;
+    // l_q: predicted cubes; l_cert: certified vertices; E / N: vertices evaluated exactly first /
+    // certified (bitmaps, popcounts, prefixes, lists); the rechecked corners reuse E's buffers
+    pms::DBuf l_counts, l_model, l_q, l_cert, l_e_bm, l_e_wc, l_e_wp, l_e_list, l_n_bm, l_n_wc, l_n_wp, l_n_list,
+              l_field_new, l_cand, l_logit, l_label;
     bool have_model = false, band_learned = false, mc_classified = false, mc_compacted = false;
     // polls + 1 of the first bounded wait on the tensor cores (0: the default bound)
     uint32_t tc_wait_polls = 0;
@@ -175,7 +183,7 @@ struct pms_ctx {
     // batched frames (pms_batch.cpp)
     void* batch = nullptr;
     uint64_t batch_launches = 0;         // kernels in the batch graph
-    uint32_t l_ncand = 0, l_npred = 0, l_nadded = 0, l_iters = 0, l_nremoved = 0;
+    uint32_t l_ncand = 0, l_npred = 0, l_nexact = 0, l_ncert = 0, l_nrecheck = 0;
     uint32_t diffuse_old = 0;    // live diffuse particles carried to the next frame
     uint32_t frame_index = 0;
 
@@ -236,16 +244,13 @@ pms_status launch_density_aniso(pms_ctx* ctx);
 pms_status launch_band(pms_ctx* ctx);
 pms_status launch_band_list(pms_ctx* ctx);
 pms_status launch_field(pms_ctx* ctx);
-// field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid)
-pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
+// field at the vertices vlist[0 .. *n_dev) into out (n_host: a bound for the grid); with
+// cert, sign certification: vertices stopped above iso get a bit there, n_cert counts them
+pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out,
+                           uint32_t* cert = nullptr, uint32_t* n_cert = nullptr);
 pms_status launch_field_gather(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* n_dev, uint32_t n_host, float* out);
 // ascending list of the set bits of a bitmap over the scalar grid
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
-// the vertices list[0 .. *n_dev) outside the plain band leave ctx->bm / ctx->fdense
-// (n_host: a bound for the grid; rest: room for n_host vertices the quick pass
-// leaves open, counted in n_rest; n_removed: their count)
-pms_status launch_plain_member(pms_ctx* ctx, const uint32_t* list, const uint32_t* n_dev, uint32_t n_host, uint32_t* rest,
-                               uint32_t* n_rest, uint32_t* n_removed);
 // marching-cube cases of the band vertices, then the scan and compaction; classify = both
 pms_status launch_mc_cases(pms_ctx* ctx);
 pms_status launch_mc_compact(pms_ctx* ctx);

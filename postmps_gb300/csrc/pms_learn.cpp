@@ -1,6 +1,7 @@
 // pms_learn.cpp -- host side of the learned narrow band: the band + field
-// stage driven by the network with its border-check fallback, training-data
-// preparation, and the trainer.  No counterpart in the reference (see k_learn.cu).
+// stage driven by the network with the exact sign certification of the rest of
+// the band, training-data preparation, and the trainer.  No counterpart in the
+// reference (see k_learn.cu, k_field.cu).
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
@@ -15,13 +16,12 @@ using namespace pms;
 namespace pms {
 pms_status ensure_band_buffers(pms_ctx* c, uint32_t nv);
 void mark_stage(pms_ctx* c, int boundary);
+pms_status plain_band(pms_ctx* c);
 }  // namespace pms
-
-static constexpr uint32_t kMaxBorderRounds = 256;
 
 static pms_status zero_learn_counters(pms_ctx* c) {
     PMS_CUDA(c, cudaMemsetAsync(reinterpret_cast<char*>(c->counters.p) + offsetof(Counters, l_cand), 0,
-                                sizeof(uint32_t) * 5, c->stream));
+                                sizeof(uint32_t) * kLearnCounters, c->stream));
     return PMS_OK;
 }
 
@@ -38,7 +38,8 @@ extern "C" pms_status pms_set_band_model(pms_ctx* c, const pms_band_model* m) {
 }
 
 extern "C" pms_status pms_set_band_mode(pms_ctx* c, int mode) {
-    if (!c || (mode != PMS_BAND_PLAIN && mode != PMS_BAND_LEARNED)) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c || (mode != PMS_BAND_PLAIN && mode != PMS_BAND_LEARNED && mode != PMS_BAND_CERTIFIED))
+        return PMS_ERR_INVALID_ARGUMENT;
     if (mode == PMS_BAND_LEARNED && !c->have_model) return pms_fail(c, PMS_ERR_STATE, "learned band without a model");
     c->band_mode = mode;
     return PMS_OK;
@@ -73,159 +74,94 @@ extern "C" pms_status pms_load_band_model(const char* path, pms_band_model* out)
     return std::isfinite(out->b2) && !std::isnan(out->threshold) ? PMS_OK : PMS_ERR_IO;
 }
 
-// vertex list, nv and band buffers of the bitmap in c->bm (popcounts in c->wcount)
-static pms_status finish_vertex_set(pms_ctx* c) {
-    Counters* cnt = c->counters.as<Counters>();
-    const uint64_t W = words_of(c);
-    pms_status st = scan_u32(c, c->wcount.as<uint32_t>(), c->wprefix.as<uint32_t>(), W, &cnt->nv);
-    if (st) return st;
-    if ((st = sync_counters(c))) return st;
-    c->nv = c->h_counters->nv;
-    if ((st = ensure_band_buffers(c, c->nv))) return st;
-    return launch_bits_list(c, c->bm.as<uint32_t>(), c->wprefix.as<uint32_t>(), c->vlist.as<uint32_t>());
+// Buffers of the split and the certification: a scalar grid of sc_size vertices, a band
+// of at most nv of them.
+pms_status pms::ensure_learned_buffers(pms_ctx* c, uint64_t sc_size, uint32_t nv) {
+    const uint64_t W = (sc_size + 31) / 32 + 1;
+    for (DBuf* d : {&c->l_q, &c->l_cert, &c->l_e_bm, &c->l_e_wc, &c->l_e_wp, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp})
+        PMS_CUDA(c, d->ensure(4 * W));
+    for (DBuf* d : {&c->l_e_list, &c->l_n_list}) PMS_CUDA(c, d->ensure(4 * ((size_t)nv + 1)));
+    return PMS_OK;
 }
 
-// The corners of the compacted valid cubes (cube bitmap from their records,
-// then the list of its corners), each tested against the plain band's rule; those
-// outside leave the vertex set and l_removed counts them.  Corners of valid
-// cubes are band vertices, so c->nv bounds the list.
-pms_status pms::plain_band_filter(pms_ctx* c) {
+// The network's prediction (when asked) and the split of the plain band into the
+// corners of predicted cubes E and the rest N, both as ascending lists.
+pms_status pms::learned_split(pms_ctx* c, bool predict) {
     Counters* cnt = c->counters.as<Counters>();
     const uint64_t W = words_of(c);
     pms_status st;
-    PMS_CUDA(c, c->l_vlist_new.ensure(4 * ((size_t)c->nv + 1)));
-    PMS_CUDA(c, c->l_vlist_m.ensure(4 * ((size_t)c->nv + 1)));
-    PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
-    PMS_CUDA(c, cudaMemsetAsync(&cnt->l_removed, 0, sizeof(uint32_t), c->stream));
-    if ((st = launch_valid_bits(c, c->l_q.as<uint32_t>()))) return st;
-    if ((st = launch_corner_list(c, c->l_q.as<uint32_t>(), c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew))) return st;
-    return launch_plain_member(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, c->nv, c->l_vlist_m.as<uint32_t>(),
-                               &cnt->l_open, &cnt->l_removed);
+    if ((st = zero_learn_counters(c))) return st;
+    if (predict) {
+        if ((st = launch_coarse_counts(c))) return st;
+        PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
+        if ((st = launch_predict(c, 1, c->l_q.as<uint32_t>(), nullptr, nullptr, 0))) return st;
+    }
+    if ((st = launch_band_split(c, predict ? c->l_q.as<uint32_t>() : nullptr, c->l_e_bm.as<uint32_t>(),
+                                c->l_n_bm.as<uint32_t>(), c->l_e_wc.as<uint32_t>(), c->l_n_wc.as<uint32_t>())))
+        return st;
+    if ((st = scan_u32(c, c->l_e_wc.as<uint32_t>(), c->l_e_wp.as<uint32_t>(), W, &cnt->l_exact))) return st;
+    if ((st = scan_u32(c, c->l_n_wc.as<uint32_t>(), c->l_n_wp.as<uint32_t>(), W, &cnt->l_nlist))) return st;
+    if ((st = launch_bits_list(c, c->l_e_bm.as<uint32_t>(), c->l_e_wp.as<uint32_t>(), c->l_e_list.as<uint32_t>()))) return st;
+    return launch_bits_list(c, c->l_n_bm.as<uint32_t>(), c->l_n_wp.as<uint32_t>(), c->l_n_list.as<uint32_t>());
+}
+
+// The field stage of the learned band: the exact field at E, signs at N, the
+// classification of every band cube (the signs are those of the exact field
+// everywhere), the exact field at the certified corners of the valid cubes, and
+// the band-order field.  c->nv bounds every list.
+pms_status pms::learned_field(pms_ctx* c) {
+    Counters* cnt = c->counters.as<Counters>();
+    const uint64_t W = words_of(c);
+    const uint32_t nvb = c->nv;
+    pms_status st;
+    PMS_CUDA(c, cudaMemsetAsync(c->fdense.p, 0, 4 * (size_t)c->grid.sc_size, c->stream));
+    PMS_CUDA(c, cudaMemsetAsync(c->l_cert.p, 0, 4 * W, c->stream));
+    if ((st = launch_field_on(c, c->l_e_list.as<uint32_t>(), &cnt->l_exact, nvb, nullptr))) return st;
+    if ((st = launch_field_on(c, c->l_n_list.as<uint32_t>(), &cnt->l_nlist, nvb, nullptr, c->l_cert.as<uint32_t>(),
+                              &cnt->l_cert)))
+        return st;
+    if ((st = launch_mc_classify(c))) return st;
+    // the certified corners of valid cubes: E's buffers hold them from here on
+    PMS_CUDA(c, cudaMemsetAsync(c->l_e_bm.p, 0, 4 * W, c->stream));
+    if ((st = launch_recheck_bits(c, c->l_cert.as<uint32_t>(), c->l_e_bm.as<uint32_t>()))) return st;
+    if ((st = launch_popc(c, c->l_e_bm.as<uint32_t>(), c->l_e_wc.as<uint32_t>()))) return st;
+    if ((st = scan_u32(c, c->l_e_wc.as<uint32_t>(), c->l_e_wp.as<uint32_t>(), W, &cnt->l_recheck))) return st;
+    if ((st = launch_bits_list(c, c->l_e_bm.as<uint32_t>(), c->l_e_wp.as<uint32_t>(), c->l_e_list.as<uint32_t>()))) return st;
+    if ((st = launch_field_on(c, c->l_e_list.as<uint32_t>(), &cnt->l_recheck, nvb, nullptr))) return st;
+    return launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, nvb, c->field.as<float>());
 }
 
 extern "C" pms_status pms_band_learned(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     if (!c->have_aniso) return pms_fail(c, PMS_ERR_STATE, "pms_band_learned before pms_anisotropy");
-    if (!c->have_model) return pms_fail(c, PMS_ERR_STATE, "pms_band_learned without a model (pms_set_band_model)");
+    const bool predict = c->band_mode != PMS_BAND_CERTIFIED;
+    if (predict && !c->have_model)
+        return pms_fail(c, PMS_ERR_STATE, "pms_band_learned without a model (pms_set_band_model)");
     cudaSetDevice(c->device);
-    c->l_ncand = c->l_npred = c->l_nadded = c->l_iters = c->l_nremoved = 0;
+    c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
     c->band_learned = true;
     c->mc_classified = c->mc_compacted = false;
     if (c->n == 0) { c->nv = 0; c->have_band = c->have_field = true; return PMS_OK; }
-    Counters* cnt = c->counters.as<Counters>();
-    const uint64_t W = words_of(c);
     pms_status st;
-    PMS_CUDA(c, c->l_q.ensure(4 * (W + 1)));
-    PMS_CUDA(c, c->l_qadd.ensure(4 * (W + 1)));
-    if ((st = zero_learn_counters(c))) return st;
-    // predicted cubes -> their corners -> vertex list
-    if ((st = launch_coarse_counts(c))) return st;
-    PMS_CUDA(c, cudaMemsetAsync(c->l_q.p, 0, 4 * W, c->stream));
-    if ((st = launch_predict(c, 1, c->l_q.as<uint32_t>(), nullptr, nullptr, 0))) return st;
-    if ((st = launch_cube_corners(c, c->l_q.as<uint32_t>(), nullptr, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>())))
-        return st;
-    if ((st = finish_vertex_set(c))) return st;
-    c->l_ncand = c->h_counters->l_cand;
-    c->l_npred = c->h_counters->l_pred;
+    // the plain band: where the field exists (a cube with a corner off it is never valid)
+    if ((st = plain_band(c))) return st;
+    if ((st = ensure_learned_buffers(c, c->grid.sc_size, c->nv))) return st;
+    if (c->nv && (st = learned_split(c, predict))) return st;
     c->have_band = true;
     mark_stage(c, kStageBand + 1);
-    // exact field at those vertices, then the border check until no cube is missing:
-    // a full check over every valid cube queues the cubes across crossed faces whose
-    // corners lack a value; each round evaluates the queued cubes' new corners (set in
-    // the vertex bitmap and listed as they are found) and checks only those cubes, one
-    // synchronisation per round; when a round queues nothing, the sorted vertex list
-    // is rebuilt from the bitmap and one more full check catches cubes whose corners
-    // other cubes' rounds completed
-    if (c->nv && (st = launch_field(c))) return st;
-    uint64_t nv_bound = c->nv;                 // host bound on the vertex count while rounds run
-    uint32_t added = 0;
-    // queue lists: grow-only; a check whose queue overflowed its list runs again
-    auto qcap_of = [](const DBuf& d) { return (uint32_t)std::min<size_t>(d.cap / 4, 0xffffffffu); };
-    PMS_CUDA(c, c->l_qlist.ensure(4 * std::max<size_t>(1u << 16, nv_bound / 16)));
-    PMS_CUDA(c, c->l_qnext.ensure(c->l_qlist.cap));
-    auto run_check = [&](auto&& launch) -> pms_status {
-        pms_status s2;
-        for (int pass = 0; pass < 2; ++pass) {
-            PMS_CUDA(c, cudaMemsetAsync(c->l_qadd.p, 0, 4 * W, c->stream));
-            PMS_CUDA(c, cudaMemsetAsync(&cnt->l_added, 0, sizeof(uint32_t), c->stream));
-            if ((s2 = launch())) return s2;
-            if ((s2 = sync_counters(c))) return s2;
-            added = c->h_counters->l_added;
-            if (added <= qcap_of(c->l_qnext)) return PMS_OK;
-            PMS_CUDA(c, c->l_qnext.ensure(4 * (size_t)added));
-        }
-        return pms_fail(c, PMS_ERR_CAPACITY, "border queue outgrew its list");
-    };
-    auto full_check = [&]() -> pms_status {
-        pms_status s2;
-        c->nv = (uint32_t)nv_bound;
-        // classification (cases, scan, compaction: the valid-cube records), then the
-        // border check over those records
-        if ((s2 = launch_mc_classify(c))) return s2;
-        if ((s2 = run_check([&] { return launch_border(c, c->l_qadd.as<uint32_t>(), c->l_qnext.as<uint32_t>(),
-                                                       qcap_of(c->l_qnext)); })))
-            return s2;
-        c->mc_compacted = true;
-        c->nv = c->h_counters->nv;
-        nv_bound = c->nv;
-        std::swap(c->l_qlist, c->l_qnext);
-        return PMS_OK;
-    };
-    if (c->nv && (st = full_check())) return st;
-    for (uint32_t round = 0; added && round < kMaxBorderRounds; ++round) {
-        c->l_nadded += added;
-        c->l_iters++;
-        const uint32_t nq = added;
-        // the queued cubes' corners without a value, and the field there
-        const uint64_t nnew_bound = std::min<uint64_t>(8ull * nq, (uint64_t)c->grid.sc_size);
-        PMS_CUDA(c, c->l_vlist_new.ensure(4 * (nnew_bound + 1)));
-        PMS_CUDA(c, cudaMemsetAsync(&cnt->l_nnew, 0, sizeof(uint32_t), c->stream));
-        if ((st = launch_queue_corners(c, c->l_qlist.as<uint32_t>(), nq, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew)))
-            return st;
-        if ((st = launch_field_on(c, c->l_vlist_new.as<uint32_t>(), &cnt->l_nnew, (uint32_t)nnew_bound, nullptr)))
-            return st;
-        nv_bound = std::min<uint64_t>(nv_bound + nnew_bound, (uint64_t)c->grid.sc_size);
-        // border check of the queued cubes, now evaluated
-        if ((st = run_check([&] { return launch_border_list(c, c->l_qlist.as<uint32_t>(), nq, c->l_qadd.as<uint32_t>(),
-                                                            nullptr, c->l_qnext.as<uint32_t>(), qcap_of(c->l_qnext)); })))
-            return st;
-        std::swap(c->l_qlist, c->l_qnext);
-        if (!added) {
-            // the sorted vertex list of the grown set, then one full check
-            if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
-            if ((st = finish_vertex_set(c))) return st;
-            nv_bound = c->nv;
-            if ((st = full_check())) return st;
-        }
-    }
-    if (added) {
-        // round limit reached: the vertex list still covers every value computed
-        if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
-        if ((st = finish_vertex_set(c))) return st;
-        if (c->nv && (st = launch_mc_classify(c))) return st;
-    }
-    // the plain band's membership test of the valid cubes' corners: a corner the
-    // plain band lacks leaves the set, so that every cube classified valid is one
-    // the plain band holds; the set then gets its sorted list again
-    uint32_t removed = 0;
-    if (c->nv) {
-        if ((st = plain_band_filter(c))) return st;
-        if ((st = sync_counters(c))) return st;
-        removed = c->l_nremoved = c->h_counters->l_removed;
-        if (removed) {
-            if ((st = launch_popc(c, c->bm.as<uint32_t>(), c->wcount.as<uint32_t>()))) return st;
-            if ((st = finish_vertex_set(c))) return st;
-        }
-    }
-    c->nv = c->h_counters->nv;
-    if ((st = ensure_band_buffers(c, c->nv))) return st;
-    // the band-order field of the final vertex set (the rounds work on the dense field)
-    if ((c->l_iters || removed) && c->nv && (st = launch_field_gather(c, c->vlist.as<uint32_t>(), &cnt->nv, c->nv, c->field.as<float>())))
-        return st;
-    // the last full check (or classification) computed the final vertex set's cases
-    // unless corners were removed since
-    c->mc_classified = removed == 0;
-    c->mc_compacted = c->mc_classified;
+    if (c->nv && (st = learned_field(c))) return st;
+    // the classification and compaction are the marching cubes' own
+    if ((st = sync_counters(c))) return st;
+    const Counters& h = *c->h_counters;
+    c->l_ncand = h.l_cand;
+    c->l_npred = h.l_pred;
+    c->l_nexact = h.l_exact;
+    c->l_ncert = h.l_cert;
+    c->l_nrecheck = h.l_recheck;
+    if (h.err & kErrTcLost)
+        return pms_fail(c, PMS_ERR_CUDA, "a tensor-core operation outlived two bounded waits; destroy this context");
+    if (h.err & kErrTimeout) return pms_fail(c, PMS_ERR_CUDA, "internal: a wait on the tensor cores timed out");
+    c->mc_classified = c->mc_compacted = c->nv != 0;
     c->have_field = true;
     mark_stage(c, kStageField + 1);
     return PMS_OK;
@@ -283,20 +219,20 @@ extern "C" pms_status pms_learn_candidates(pms_ctx* c, uint32_t* ids, float* log
     if (nc > cap) return PMS_ERR_CAPACITY;
     const size_t NC = nc ? nc : 1;
     PMS_CUDA(c, c->l_logit.ensure(4 * NC));
-    PMS_CUDA(c, c->l_vlist_new.ensure(4 * NC));
+    PMS_CUDA(c, c->l_e_list.ensure(4 * NC));
     pms_status st;
     if ((st = zero_learn_counters(c))) return st;
     if (logits) {
         if (!c->have_model) return pms_fail(c, PMS_ERR_STATE, "logits need a model (pms_set_band_model)");
-        if ((st = launch_predict(c, 1, nullptr, c->l_vlist_new.as<uint32_t>(), c->l_logit.as<float>(), nc))) return st;
+        if ((st = launch_predict(c, 1, nullptr, c->l_e_list.as<uint32_t>(), c->l_logit.as<float>(), nc))) return st;
     } else {
-        if ((st = launch_predict(c, 0, nullptr, c->l_vlist_new.as<uint32_t>(), nullptr, nc))) return st;
+        if ((st = launch_predict(c, 0, nullptr, c->l_e_list.as<uint32_t>(), nullptr, nc))) return st;
     }
     // candidates come back in the order the tiles finished: sort by cube id
     std::vector<uint32_t> id(nc);
     std::vector<float> lg(logits ? nc : 0);
     if (nc) {
-        PMS_CUDA(c, cudaMemcpyAsync(id.data(), c->l_vlist_new.p, 4 * (size_t)nc, cudaMemcpyDeviceToHost, c->stream));
+        PMS_CUDA(c, cudaMemcpyAsync(id.data(), c->l_e_list.p, 4 * (size_t)nc, cudaMemcpyDeviceToHost, c->stream));
         if (logits) PMS_CUDA(c, cudaMemcpyAsync(lg.data(), c->l_logit.p, 4 * (size_t)nc, cudaMemcpyDeviceToHost, c->stream));
     }
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -321,10 +257,10 @@ extern "C" pms_status pms_learn_features(pms_ctx* c, const uint32_t* ids, uint32
         if (ids[i] >= c->grid.sc_size) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "cube id outside the scalar grid");
     if (!n) return PMS_OK;
     cudaSetDevice(c->device);
-    PMS_CUDA(c, c->l_vlist_new.ensure(4 * (size_t)n));
+    PMS_CUDA(c, c->l_e_list.ensure(4 * (size_t)n));
     PMS_CUDA(c, c->l_field_new.ensure(128 * (size_t)n));
-    PMS_CUDA(c, cudaMemcpyAsync(c->l_vlist_new.p, ids, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
-    pms_status st = launch_features(c, c->l_vlist_new.as<uint32_t>(), n, c->l_field_new.as<uint16_t>());
+    PMS_CUDA(c, cudaMemcpyAsync(c->l_e_list.p, ids, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    pms_status st = launch_features(c, c->l_e_list.as<uint32_t>(), n, c->l_field_new.as<uint16_t>());
     if (st) return st;
     PMS_CUDA(c, cudaMemcpyAsync(x, c->l_field_new.p, 128 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));

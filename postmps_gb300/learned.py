@@ -168,18 +168,34 @@ def hausdorff(mesh_a: np.ndarray, cubes_a, mesh_b: np.ndarray, cubes_b) -> dict:
     return out
 
 
-def compare(ctx: "pms.Context", model: "pms.BandModel", h: float, pos, vel=None, rho=None) -> dict:
-    """Plain and learned surface of one frame on one context: counts, stage
-    times, triangle delta, Hausdorff distance (also in units of h)."""
-    ctx.set_band_model(model)
+def band_stats(c: "pms.Counts") -> dict:
+    """Work of a learned or certified band: full field walks (exact values) and
+    sign certificates (walks stopped above iso)."""
+    return {"band_vertices": c.n_band_vertices, "valid_cubes": c.n_valid_cubes, "triangles": c.n_mesh_vertices // 3,
+            "candidates": c.n_band_candidates, "predicted": c.n_band_predicted, "exact_first": c.n_band_exact,
+            "certified": c.n_band_certified, "rechecked": c.n_band_rechecked,
+            "full_walks": c.n_band_vertices - c.n_band_certified + c.n_band_rechecked}
+
+
+def compare(ctx: "pms.Context", model: "pms.BandModel", h: float, pos, vel=None, rho=None,
+            mode: str = "learned") -> dict:
+    """Plain and learned (or certified) surface of one frame on one context:
+    counts, stage times, whether the two triangle soups are identical, triangle
+    delta and Hausdorff distance (also in units of h)."""
+    if model is not None:
+        ctx.set_band_model(model)
     plain_frame(ctx, pos, vel, rho)
     tp = ctx.stage_times()
     cp = ctx.counts()
     mesh_p, _ = ctx.mesh(normals=False)
     cubes_p = cube_vertex_ranges(ctx)
-    ctx.upload(pos, vel, rho)
-    ctx.build_grid()
-    ctx.surface_learned()
+    ctx.set_band_mode(mode)
+    try:
+        ctx.upload(pos, vel, rho)
+        ctx.build_grid()
+        ctx.surface_learned()
+    finally:
+        ctx.set_band_mode("plain")
     tl = ctx.stage_times()
     cl = ctx.counts()
     mesh_l, _ = ctx.mesh(normals=False)
@@ -187,10 +203,8 @@ def compare(ctx: "pms.Context", model: "pms.BandModel", h: float, pos, vel=None,
     hd = hausdorff(mesh_p, cubes_p, mesh_l, cubes_l)
     res = {"particles": int(len(pos)), "plain": {"band_vertices": cp.n_band_vertices, "valid_cubes": cp.n_valid_cubes,
                                                  "triangles": cp.n_mesh_vertices // 3, "ms": tp},
-           "learned": {"band_vertices": cl.n_band_vertices, "valid_cubes": cl.n_valid_cubes,
-                       "triangles": cl.n_mesh_vertices // 3, "candidates": cl.n_band_candidates,
-                       "predicted": cl.n_band_predicted, "fallback_cubes": cl.n_band_fallback,
-                       "fallback_rounds": cl.n_band_iterations, "removed": cl.n_band_removed, "ms": tl},
+           "learned": dict(band_stats(cl), ms=tl), "mode": mode,
+           "identical": bool(mesh_p.shape == mesh_l.shape and np.array_equal(mesh_p, mesh_l)),
            "triangle_delta": int(cl.n_mesh_vertices // 3) - int(cp.n_mesh_vertices // 3)}
     res.update(hd)
     res["hausdorff_h"] = hd["hausdorff"] / h

@@ -94,8 +94,8 @@ class Counts(C.Structure):
         ("n_valid_cubes", C.c_uint32), ("n_mesh_vertices", C.c_uint64), ("n_free_surface", C.c_uint32),
         ("n_generated_diffuse", C.c_uint32), ("n_spawning", C.c_uint32), ("n_diffuse", C.c_uint32),
         ("n_spray", C.c_uint32), ("n_foam", C.c_uint32), ("n_bubble", C.c_uint32), ("n_fp64_svd", C.c_uint32),
-        ("n_band_candidates", C.c_uint32), ("n_band_predicted", C.c_uint32), ("n_band_fallback", C.c_uint32),
-        ("n_band_iterations", C.c_uint32), ("n_band_removed", C.c_uint32),
+        ("n_band_candidates", C.c_uint32), ("n_band_predicted", C.c_uint32), ("n_band_exact", C.c_uint32),
+        ("n_band_certified", C.c_uint32), ("n_band_rechecked", C.c_uint32),
     ]
 
     def as_dict(self) -> dict:
@@ -117,7 +117,8 @@ class Frame(C.Structure):
     _fields_ = [("pos_xyz", C.c_void_p), ("vel_xyz", C.c_void_p), ("rhop", C.c_void_p), ("n", C.c_uint32)]
 
 
-BATCH_LEARNED = 1
+BATCH_LEARNED, BATCH_CERTIFIED = 1, 2
+BAND_PLAIN, BAND_LEARNED, BAND_CERTIFIED = 0, 1, 2
 MLP_INPUTS, MLP_HIDDEN, MLP_PARAMS = 64, 64, 4225
 
 
@@ -204,7 +205,7 @@ def lib() -> C.CDLL:
         L.pms_get_tune.argtypes = [vp, C.POINTER(Tune)]
         L.pms_batch_frame.argtypes = [vp, C.c_uint32, C.POINTER(Counts), C.POINTER(C.c_float)]
         L.pms_batch_mesh.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
-        L.pms_batch_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.pms_batch_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.pms_save_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel), C.c_char_p]
         L.pms_load_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel)]
         L.pms_band_learned.argtypes = [vp]
@@ -382,8 +383,12 @@ class Context:
     def set_band_model(self, model: BandModel) -> None:
         self._call("pms_set_band_model", C.byref(model))
 
-    def set_band_mode(self, learned: bool) -> None:
-        self._call("pms_set_band_mode", 1 if learned else 0)
+    def set_band_mode(self, mode) -> None:
+        """False / "plain": the reference's band; True / "learned": the network plus
+        the exact sign certification; "certified": the certification alone."""
+        m = {False: BAND_PLAIN, True: BAND_LEARNED, "plain": BAND_PLAIN, "learned": BAND_LEARNED,
+             "certified": BAND_CERTIFIED}[mode]
+        self._call("pms_set_band_mode", m)
 
     def band_learned(self): self._call("pms_band_learned")
     def surface_learned(self): self._call("pms_surface_learned")
@@ -422,7 +427,7 @@ class Context:
         return t.as_dict()
 
     # batched frames
-    def run_batch(self, frames, learned: bool = False) -> None:
+    def run_batch(self, frames, learned=False) -> None:
         """frames: sequence of (pos, vel, rho) numpy arrays (vel / rho may be None),
         or of pms_frame-like (pos_ptr, vel_ptr, rho_ptr, n) tuples of raw pointers."""
         arr = (Frame * max(1, len(frames)))()
@@ -437,7 +442,8 @@ class Context:
             rho = None if rho is None else np.ascontiguousarray(rho, np.float32)
             self._keep += [pos, vel, rho]
             arr[i] = Frame(_ptr(pos), _ptr(vel), _ptr(rho), len(pos))
-        self._call("pms_run_batch", arr, len(frames), BATCH_LEARNED if learned else 0)
+        flag = {False: 0, True: BATCH_LEARNED, "plain": 0, "learned": BATCH_LEARNED, "certified": BATCH_CERTIFIED}[learned]
+        self._call("pms_run_batch", arr, len(frames), flag)
 
     def batch_frame(self, f: int) -> tuple[Counts, float]:
         c = Counts()
@@ -454,9 +460,9 @@ class Context:
         return out
 
     def batch_info(self) -> dict:
-        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
-        self._call("pms_batch_info", C.byref(a), C.byref(b), C.byref(c))
-        return {"graph_kernels": a.value, "captures": b.value, "reruns": c.value}
+        a, b = C.c_uint32(), C.c_uint32()
+        self._call("pms_batch_info", C.byref(a), C.byref(b))
+        return {"graph_kernels": a.value, "captures": b.value}
 
     def learn_features(self, cubes) -> np.ndarray:
         cubes = np.ascontiguousarray(cubes, np.uint32)
@@ -498,6 +504,18 @@ class Context:
         """Wait for the streamed mesh of the last frame; returns its vertex count."""
         n = C.c_uint64()
         self._call("pms_wait_mesh", C.byref(n))
+        return n.value
+
+    def stream_diffuse_to_host(self, ptr: int, cap: int) -> None:
+        """Register a page-locked host buffer (raw address) of `cap` 32-byte
+        pms_diffuse_particle records that each frame's diffuse stage fills on a
+        copy stream; ptr 0 unregisters."""
+        self._call("pms_stream_diffuse_to_host", C.c_void_p(ptr or None), C.c_uint64(cap))
+
+    def wait_diffuse(self) -> int:
+        """Wait for the streamed live diffuse particles of the last frame; returns their count."""
+        n = C.c_uint64()
+        self._call("pms_wait_diffuse", C.byref(n))
         return n.value
 
     def diffuse_particles(self, type_: int = -1) -> dict:

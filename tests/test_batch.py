@@ -77,7 +77,7 @@ def test_learned_batch_equals_learned_single_frames(pms_lib):
     pms = pms_lib
     frames = _frames(4)
     with _ctx(pms, 0.02) as ctx:
-        # a quickly trained model on the first frame is enough: the fallback makes results exact
+        # a quickly trained model on the first frame is enough: the certification makes results exact
         ctx.upload(*frames[0])
         ctx.build_grid()
         ctx.surface()
@@ -88,9 +88,15 @@ def test_learned_batch_equals_learned_single_frames(pms_lib):
         ctx.set_band_model(t.model(0.0))
         ctx.run_batch(frames, learned=True)
         got = [ctx.batch_mesh(f) for f in range(len(frames))]
+        cert = [ctx.batch_frame(f)[0] for f in range(len(frames))]
         for f, fr in enumerate(frames):
             cs, ms_ = _single(ctx, fr, learned=True)
             assert np.array_equal(got[f], ms_), f
+            assert (cert[f].n_band_exact, cert[f].n_band_certified, cert[f].n_band_rechecked) == \
+                   (cs.n_band_exact, cs.n_band_certified, cs.n_band_rechecked), f
+            # ... and equals the plain band's soup
+            cp, mp = _single(ctx, fr, learned=False)
+            assert np.array_equal(got[f], mp), f
         t.close()
 
 

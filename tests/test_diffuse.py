@@ -162,3 +162,40 @@ def test_diffuse_files_written(pms_lib, tmp_path):
             assert p.exists()
             pos, vel, _ = pms_lib.read_vtk(str(p))
             assert pos.shape[1] == 3
+
+
+@pytest.mark.gpu
+def test_streamed_diffuse_particles_equal_downloaded(pms_lib, tmp_config):
+    """pms_stream_diffuse_to_host: each frame's live set lands in the registered
+    host buffer, record for record what pms_download_diffuse returns, and the
+    next frame (whose update moves those particles) waits for the copy."""
+    import ctypes as C
+    from postmps_gb300 import synth
+    pms = pms_lib
+    pos, vel, rho = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"})))
+    cap = 1 << 18
+    buf = (C.c_uint8 * (32 * cap))()
+    rec = np.frombuffer(buf, dtype=np.dtype([("pos", np.float32, 3), ("ttl", np.int32), ("vel", np.float32, 3),
+                                             ("type", np.int32)]))
+    with pms.Context(cfg, 0) as ctx:
+        ctx.stream_diffuse_to_host(C.addressof(buf), cap)
+        for fr in range(3):
+            p = (pos + np.float32(0.004 * fr) * vel).astype(np.float32)
+            ctx.upload(p, vel, rho)
+            ctx.run_frame()
+            n = ctx.wait_diffuse()
+            live = ctx.diffuse_particles(-1)
+            assert n == len(live["pos"]) > 0
+            np.testing.assert_array_equal(rec["pos"][:n], live["pos"])
+            np.testing.assert_array_equal(rec["vel"][:n], live["vel"])
+            np.testing.assert_array_equal(rec["ttl"][:n], live["ttl"])
+            np.testing.assert_array_equal(rec["type"][:n], live["type"])
+        # too small a buffer: the count comes back with PMS_ERR_CAPACITY
+        ctx.stream_diffuse_to_host(C.addressof(buf), 1)
+        ctx.upload(pos, vel, rho)
+        ctx.run_frame()
+        with pytest.raises(pms.PmsError) as ei:
+            ctx.wait_diffuse()
+        assert ei.value.status == 4
+        ctx.stream_diffuse_to_host(0, 0)

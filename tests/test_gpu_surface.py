@@ -223,15 +223,17 @@ def test_scalar_values_match_oracle(pms_lib, oracle, tmp_config, tmp_path, case)
 @pytest.mark.parametrize("case", ["drops_sheet", "block12_ratio4"])
 def test_fp64_eigen_branch_matches_oracle(pms_lib, oracle, tmp_config, case):
     """Covariances whose condition number exceeds [GB300] Fp64SvdCondition are
-    re-solved in float64.  With the limit lowered to 2 nearly every surface
-    particle takes that branch; G, the band, field, cases and mesh still meet
-    the float32 branch's bounds against the float64 oracle, and the mesh equals
-    the float32 branch's mesh within 1e-4 cell."""
+    re-solved in float64.  The reference seeds every covariance with h^2 I, so
+    even a flat sheet's condition number stays near 1.2; a limit of 1 sends
+    every covariance that is not exactly isotropic down that branch.  G, the
+    band, field, cases and mesh still meet the float32 branch's bounds against
+    the float64 oracle, and the mesh equals the float32 branch's within 1e-4 cell."""
     d = load_golden(case)
-    text = d["config"] + "\n[GB300]\nFp64SvdCondition = 2\n"
+    text = d["config"] + "\n[GB300]\nFp64SvdCondition = 1\n"
     out = run_gpu(pms_lib, tmp_config(text), d["pos"], d["vel"], d["rho_in"])
     c = out["counts"]
-    assert c["n_fp64_svd"] > 0.5 * c["n_surface_particles"] > 0, c
+    # (isolated particles take the isotropic kernel and never reach the solver)
+    assert c["n_fp64_svd"] >= min(100, c["n_surface_particles"] // 10) > 0, c
     check_against_oracle(oracle, pms_lib, d["config"], d["pos"], out)
     base = run_gpu(pms_lib, tmp_config(d["config"]), d["pos"], d["vel"], d["rho_in"])
     assert base["counts"]["n_fp64_svd"] < c["n_fp64_svd"]
