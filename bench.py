@@ -192,6 +192,115 @@ def cpu_baseline(pos, keys: dict, frac: float = 0.25) -> dict:
             "sample": f"x-slab with {len(sub)} of {len(pos)} particles, float64 oracle, surface path, {dt:.2f} s"}
 
 
+def _cube_ranges(band, nvert):
+    """Valid cubes (origin ids), their cases' vertex counts and first mesh vertex."""
+    nv = np.asarray(nvert, np.int64)
+    off = np.concatenate([[0], np.cumsum(nv)])[:-1]
+    sel = nv > 0
+    return np.asarray(band)[sel], off[sel], nv[sel]
+
+
+def fp64_judge(ctx, frame, keys: dict, arms, model, h: float) -> dict:
+    """Every arm's frame against the float64 oracle at the benchmark configuration
+    (outside the timed region): integer stages bit for bit, the field on the band
+    vertices both hold (relative to max(|f|, iso), below the 2 iso early exit),
+    mesh vertices of the cubes both classify alike (in cells), and the symmetric
+    Hausdorff distance between the GPU and the float64 meshes (in h): vertex for
+    vertex on those cubes, point to surface for the others."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from postmps_gb300 import synth
+    O.build()
+    pos = frame[0]
+    t0 = time.perf_counter()
+    p = O.derive_params(O.config_from_keys(synth.keys_of(**keys)))
+    g = O.grid_from_positions(p, pos)
+    r = O.run_surface(p, pos, g)
+    from postmps_gb300 import pms
+    e, tt, nvt, ev, _ = pms.mc_tables()
+    O.set_mc_tables(e, tt, nvt, ev)
+    iso = float(p.iso_value)
+    cases_o, nvert_o, _ = O.mc_classify(g, iso, r.bitmap, r.band, r.field.astype(np.float32))
+    mesh_o, _ = O.mc_emit(g, iso, r.bitmap, r.band, r.field, cases_o, nvert_o)
+    t_oracle = time.perf_counter() - t0
+    cs = float(g.sc_grid_size)
+    ids_o, off_o, cnt_o = _cube_ranges(r.band, nvert_o)
+    case_o = np.asarray(cases_o)[np.asarray(nvert_o) > 0]
+    out = {"oracle_seconds": round(t_oracle, 2), "cores": os.cpu_count(), "triangles_fp64": int(len(mesh_o) // 3)}
+    first = True
+    for arm in arms:
+        ctx.set_band_mode(arm)
+        ctx.upload(*frame)
+        ctx.build_grid()
+        if arm == "plain":
+            ctx.surface()
+        else:
+            ctx.surface_learned()
+        ctx.set_band_mode("plain")
+        if first:
+            # integer stages: identical for every arm (computed before the band)
+            ok = {k: bool(np.array_equal(ctx.debug(k), ref)) for k, ref in
+                  (("keys_sorted", r.keys_sorted), ("perm", r.perm), ("cell_start", r.cell_start),
+                   ("cell_end", r.cell_end), ("surf_list", r.surf_list))}
+            out["integer_stages_bit_exact"] = ok
+            first = False
+        band = ctx.debug("band_list")
+        field = ctx.debug("field").astype(np.float64)
+        nvert = ctx.debug("cube_nvert")
+        case = ctx.debug("cube_case")
+        mesh = ctx.mesh(normals=False)[0].astype(np.float64)
+        # field on the common band vertices (a learned or certified band keeps only a sign,
+        # a placeholder above iso, at the vertices it certified: those are left out)
+        common, ig, io = np.intersect1d(band, r.band, assume_unique=True, return_indices=True)
+        fg, fo = field[ig], r.field[io]
+        below = (fo < 2 * iso * 0.999) & (fg < 2 * iso * 0.999)
+        certified = 0
+        if arm != "plain":
+            cb = ctx.debug("band_certified")
+            held = ((cb[band[ig] >> 5] >> (band[ig] & 31)) & 1).astype(bool)
+            certified = int(held.sum())
+            below &= ~held
+        ferr = float((np.abs(fg - fo) / np.maximum(np.abs(fo), iso))[below].max(initial=0.0))
+        # cubes classified alike: vertex for vertex
+        ids_g, off_g, cnt_g = _cube_ranges(band, nvert)
+        case_g = case[nvert > 0]
+        cc, jg, jo = np.intersect1d(ids_g, ids_o, assume_unique=True, return_indices=True)
+        same = case_g[jg] == case_o[jo]
+        vmax = 0.0
+        if same.any():
+            a_first = np.repeat(off_g[jg][same], cnt_g[jg][same])
+            b_first = np.repeat(off_o[jo][same], cnt_o[jo][same])
+            k = np.arange(len(a_first)) - np.repeat(np.cumsum(cnt_g[jg][same]) - cnt_g[jg][same], cnt_g[jg][same])
+            vmax = float(np.abs(mesh[a_first + k] - mesh_o[b_first + k]).max(initial=0.0))
+        # the rest (cubes in one set only, or classified differently): point to surface
+        only_g = np.ones(len(ids_g), bool)
+        only_g[jg[same]] = False
+        only_o = np.ones(len(ids_o), bool)
+        only_o[jo[same]] = False
+
+        def verts(m, off, cnt, sel):
+            if not sel.any():
+                return np.zeros((0, 3))
+            f = np.repeat(off[sel], cnt[sel])
+            k = np.arange(len(f)) - np.repeat(np.cumsum(cnt[sel]) - cnt[sel], cnt[sel])
+            return np.ascontiguousarray(m[f + k])
+
+        qa, qb = verts(mesh, off_g, cnt_g, only_g), verts(mesh_o, off_o, cnt_o, only_o)
+        da = O.lib().orc_hausdorff_vertices_to_mesh(qa.reshape(-1), len(qa), np.ascontiguousarray(mesh_o).reshape(-1),
+                                                    len(mesh_o), cs) if len(qa) else 0.0
+        db = O.lib().orc_hausdorff_vertices_to_mesh(qb.reshape(-1), len(qb), np.ascontiguousarray(mesh).reshape(-1),
+                                                    len(mesh), cs) if len(qb) else 0.0
+        hd = max(vmax, da, db)
+        out[arm] = {"hausdorff_h_vs_fp64": hd / h, "max_vertex_err_cells": vmax / cs, "max_field_rel_err": ferr,
+                    "field_placeholders": certified,
+                    "band_vertices_differing": int(len(band) + len(r.band) - 2 * len(common)),
+                    "valid_cubes_differing": int(only_g.sum() + only_o.sum()),
+                    "cases_bit_exact_on_common_cubes": bool(same.all()),
+                    "triangle_delta_vs_fp64": int(len(mesh) // 3 - len(mesh_o) // 3)}
+    out["seconds"] = round(time.perf_counter() - t0, 2)
+    return out
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -463,11 +572,18 @@ def run_pms(args) -> None:
                                    for k in ("band_vertices", "exact_first", "certified", "rechecked", "full_walks",
                                              "predicted")},
                           "seconds": time.perf_counter() - t0}
-    # headline: the learned band when its meshes are the plain ones on every frame and it is faster
+    # every arm against the float64 oracle at this configuration (single-frame workloads)
+    fp64 = None
+    if not batched and not args.no_fp64 and rank == 0:
+        fp64 = fp64_judge(ctx, frames[0], keys, arms, model, h)
+    # headline: the learned band when it is within 0.05 h of the float64 mesh, its meshes
+    # are the plain ones on every frame, and it is faster end to end
     head_arm = arms[0]
     if "learned" in arms and "plain" in arms:
         j = judge.get("learned")
         ok = j is not None and j["identical_frames"] == j["frames"]
+        if fp64 is not None:
+            ok = ok and fp64["learned"]["hausdorff_h_vs_fp64"] <= 0.05
         head_arm = "learned" if ok and res["learned"]["ms_e2e"] < res["plain"]["ms_e2e"] else "plain"
     head = res[head_arm]
     n_total = sum(len(fr[0]) for fr in frames)
@@ -528,10 +644,24 @@ def run_pms(args) -> None:
         line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                             "algorithmic_bytes": alg[dom], "peak_source": peak_src}
+        # the field's own work: (band vertex, particle) pairs it evaluated, against the FP32
+        # rate of the SMs (about 10 FP32 operations per pair: the r^T M r form, (1 - d2)^3 w, the sum)
+        pairs = int(head["counts"].get("n_field_pairs", 0))
+        fms = stage_ms.get("field", 0.0)
+        if pairs and fms > 0:
+            sm_mhz = (head["clocks"] or {}).get("sm_mhz") or 2070.0
+            peak_fp32 = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12      # TFLOP/s, FMA = 2
+            rate = pairs / (fms / 1e3)
+            line["field_compute"] = {"pair_evals": pairs, "pair_evals_per_s": rate, "flops_per_pair": 10,
+                                     "achieved_tflops": rate * 10 / 1e12, "peak_tflops_fp32": peak_fp32,
+                                     "frac": rate * 10 / 1e12 / peak_fp32,
+                                     "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x the sampled SM clock"}
         line["stage_ms"] = stage_ms
         line["counts"] = head["counts"]
     if judge:
         line["judge"] = judge
+    if fp64 is not None:
+        line["fp64"] = fp64
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(frames[0][0], keys, args.cpu_fraction)
     if rank == 0:
@@ -555,6 +685,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diffuse", action="store_true")
     ap.add_argument("--no-judge", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the float64 oracle judge")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -134,6 +134,7 @@ typedef struct pms_counts {
     uint32_t n_band_exact;             /* band vertices evaluated exactly first (corners of predicted cubes) */
     uint32_t n_band_certified;         /* band vertices certified above iso without an exact value */
     uint32_t n_band_rechecked;         /* ... of those, corners of valid cubes, then evaluated exactly */
+    uint64_t n_field_pairs;            /* (band vertex, particle) pairs the field evaluated this frame */
 } pms_counts;
 
 typedef struct pms_ctx pms_ctx;
@@ -269,7 +270,9 @@ typedef enum pms_array {
     PMS_ARRAY_NEIGHBORS = 18,    /* uint32[ns] neighbours within h of each surface particle */
     PMS_ARRAY_DIFFUSE_POTENTIAL = 19, /* float[3 n] waveCrest, Ita, energy after the phi clamps */
     PMS_ARRAY_DIFFUSE_COUNT = 20,     /* int32[n] spawned diffuse particles per sorted particle */
-    PMS_ARRAY_FREE_NORMAL = 21        /* float[3 n] particle normals after the diffuse colour-gradient pass */
+    PMS_ARRAY_FREE_NORMAL = 21,       /* float[3 n] particle normals after the diffuse colour-gradient pass */
+    PMS_ARRAY_BAND_CERTIFIED = 22     /* uint32 bitmap over the scalar grid: band vertices of a learned or
+                                         certified band whose field value is a placeholder above iso */
 } pms_array;
 pms_status pms_debug_download(pms_ctx* ctx, int array_id, void* dst, uint64_t cap_bytes, uint64_t* needed);
 /* Tests of the failure path: the first bounded wait of the band network on the

@@ -93,9 +93,10 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
         const uint32_t* __restrict__ items, const uint32_t* __restrict__ vlist, const uint32_t* __restrict__ cell_start,
         const float* __restrict__ cell_rad, const float4* __restrict__ rec, const float4* __restrict__ spos,
         const float4* __restrict__ aniso, float* __restrict__ field, float* __restrict__ fdense,
-        uint32_t* __restrict__ cert, uint32_t* __restrict__ n_cert) {
+        uint32_t* __restrict__ cert, uint32_t* __restrict__ n_cert, Counters* __restrict__ cnt_w) {
     const uint32_t n_items = *n_items_dev;
     uint32_t my_cert = 0;
+    unsigned long long my_pairs = 0;         // (vertex, particle) pairs evaluated
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     const uint32_t srx = g.spres[0], sry = g.spres[1];
     const uint32_t e2 = 2u * (uint32_t)g.spexpand;
@@ -152,8 +153,14 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                     bool use[K];
 #pragma unroll
                     for (int k = 0; k < K; ++k) use[k] = x >= qa[k] && x < qb[k];
-                    const uint32_t j1 = __ldg(&cell_start[row + (uint32_t)x + 1u]);
-                    for (uint32_t j = __ldg(&cell_start[row + (uint32_t)x]); j < j1; ++j) {
+                    const uint32_t j0 = __ldg(&cell_start[row + (uint32_t)x]), j1 = __ldg(&cell_start[row + (uint32_t)x + 1u]);
+                    {
+                        uint32_t nu = 0u;
+#pragma unroll
+                        for (int k = 0; k < K; ++k) nu += use[k] ? 1u : 0u;
+                        my_pairs += (unsigned long long)(j1 - j0) * nu;
+                    }
+                    for (uint32_t j = j0; j < j1; ++j) {
                         const float4 q = __ldg(&spos[j]);
                         const float4 a0 = __ldg(&aniso[2 * (size_t)j]);
                         const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);
@@ -268,9 +275,15 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                         bool use[K];
 #pragma unroll
                         for (int k = 0; k < K; ++k) use[k] = (reach[k] & bit) != 0u;
-                        const uint32_t j1 = __ldg(&cell_start[c + 1u]);
+                        const uint32_t j0 = __ldg(&cell_start[c]), j1 = __ldg(&cell_start[c + 1u]);
+                        {
+                            uint32_t nu = 0u;
+#pragma unroll
+                            for (int k = 0; k < K; ++k) nu += use[k] ? 1u : 0u;
+                            my_pairs += (unsigned long long)(j1 - j0) * nu;
+                        }
 #pragma unroll 2
-                        for (uint32_t j = __ldg(&cell_start[c]); j < j1; ++j) {
+                        for (uint32_t j = j0; j < j1; ++j) {
                             const float4 q = __ldg(&spos[j]);
                             const float4 a0 = __ldg(&aniso[2 * (size_t)j]);      // {m00, 2 m01, 2 m02, h_s^2}
                             const float4 a1 = __ldg(&aniso[2 * (size_t)j + 1]);  // {m11, 2 m12, m22, w}
@@ -326,6 +339,9 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
         const uint32_t tot = __reduce_add_sync(0xffffffffu, my_cert);
         if ((threadIdx.x & 31u) == 0 && tot) atomicAdd(n_cert, tot);
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) my_pairs += __shfl_xor_sync(0xffffffffu, my_pairs, o);
+    if ((threadIdx.x & 31u) == 0 && my_pairs) atomicAdd(&cnt_w->n_pairs, my_pairs);
 }
 
 // Work items over vlist[0 .. *n_dev): group g = entries [g K, g K + K) splits
@@ -385,7 +401,7 @@ pms_status launch_field_on(pms_ctx* ctx, const uint32_t* vlist, const uint32_t* 
         kern<<<blocks, bt, 0, ctx->stream>>>(g, fp, cnt, &cnt->n_items, ctx->fitems.as<uint32_t>(), vlist,
                                              ctx->cell_start.as<uint32_t>(), ctx->cell_rad.as<float>(),
                                              ctx->cell_rec.as<float4>(), ctx->spos.as<float4>(), ctx->aniso.as<float4>(), out,
-                                             ctx->fdense.as<float>(), cert, n_cert);
+                                             ctx->fdense.as<float>(), cert, n_cert, cnt);
     };
     auto by_vpt = [&](auto bt_tag) {
         constexpr int B = decltype(bt_tag)::value;

@@ -597,10 +597,12 @@ __global__ void __launch_bounds__(256) k_band_split(const uint32_t* __restrict__
 }
 
 // The certified corners of the valid cubes (compaction records {vertex id,
-// case, ...}): their bits go to `recheck`, whose vertices are then evaluated
-// exactly.  A cube's corners lie in 4 rows of 2 neighbouring vertices.
+// case, ...}): their bits move from `cert` to `recheck`, whose vertices are
+// then evaluated exactly, so that `cert` ends holding the band vertices whose
+// field is a placeholder.  A cube's corners lie in 4 rows of 2 neighbouring
+// vertices.
 __global__ void __launch_bounds__(256) k_recheck_bits(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
-                                                      const uint32_t* __restrict__ cert, uint32_t* __restrict__ recheck) {
+                                                      uint32_t* __restrict__ cert, uint32_t* __restrict__ recheck) {
     const uint32_t n = cnt->nvalid;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -609,10 +611,13 @@ __global__ void __launch_bounds__(256) k_recheck_bits(KGrid g, const Counters* _
         for (int r = 0; r < 4; ++r) {
             const uint32_t c = id + (uint32_t)(r & 1) * rx + (uint32_t)(r >> 1) * rxy;   // corners c, c + 1
             const uint32_t w = c >> 5, sh = c & 31u;
-            const uint32_t pair = (__ldg(&cert[w]) >> sh) & (sh == 31u ? 1u : 3u);
-            const uint32_t hi = sh == 31u ? (__ldg(&cert[w + 1]) & 1u) : 0u;
+            const uint32_t pair = (cert[w] >> sh) & (sh == 31u ? 1u : 3u);
+            const uint32_t hi = sh == 31u ? (cert[w + 1] & 1u) : 0u;
             if (pair) atomicOr(&recheck[w], pair << sh);
             if (hi) atomicOr(&recheck[w + 1], 1u);
+            // those vertices get exact values: they leave the certified set
+            if (pair) atomicAnd(&cert[w], ~(pair << sh));
+            if (hi) atomicAnd(&cert[w + 1], ~1u);
         }
     }
 }
@@ -941,7 +946,7 @@ pms_status launch_band_split(pms_ctx* ctx, const uint32_t* cubes, uint32_t* e_bm
 
 pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wprefix, uint32_t* vlist);
 
-pms_status launch_recheck_bits(pms_ctx* ctx, const uint32_t* cert, uint32_t* recheck) {
+pms_status launch_recheck_bits(pms_ctx* ctx, uint32_t* cert, uint32_t* recheck) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
     // ctx->nv bounds the valid cubes; the kernel reads their count

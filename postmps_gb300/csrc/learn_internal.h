@@ -41,8 +41,8 @@ pms_status launch_predict(pms_ctx* ctx, int use_model, uint32_t* q, uint32_t* ca
 // evaluated exactly at once) and the rest (N, certified); cubes null: E empty
 pms_status launch_band_split(pms_ctx* ctx, const uint32_t* cubes, uint32_t* e_bm, uint32_t* n_bm, uint32_t* e_wc,
                              uint32_t* n_wc);
-// the certified corners (bits of cert) of the classified valid cubes, as bits of recheck
-pms_status launch_recheck_bits(pms_ctx* ctx, const uint32_t* cert, uint32_t* recheck);
+// the certified corners (bits of cert) of the classified valid cubes move to recheck
+pms_status launch_recheck_bits(pms_ctx* ctx, uint32_t* cert, uint32_t* recheck);
 pms_status launch_popc(pms_ctx* ctx, const uint32_t* b, uint32_t* wcount);
 pms_status launch_label_bits(pms_ctx* ctx, uint32_t* lbm);
 // the learned band after the plain band (ctx->bm, ctx->vlist; ctx->nv its count, or a

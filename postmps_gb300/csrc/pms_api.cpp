@@ -524,6 +524,7 @@ extern "C" pms_status pms_get_counts(pms_ctx* c, pms_counts* out) {
     out->n_valid_cubes = c->have_mc ? h.nvalid : 0;
     out->n_mesh_vertices = c->have_mc ? h.nmesh : 0;
     out->n_fp64_svd = h.n_fp64;
+    out->n_field_pairs = c->have_field ? h.n_pairs : 0;
     out->n_free_surface = h.n_free;
     out->n_generated_diffuse = h.n_generated;
     out->n_spawning = h.n_spawning;
@@ -712,6 +713,13 @@ extern "C" pms_status pms_debug_download(pms_ctx* c, int id, void* dst, uint64_t
                 for (size_t s = 0; s < ns; ++s) o[s] = nr[4 * (size_t)sl[s] + 3] != 0.f;
                 put(o.data(), o.size());
             }
+            break;
+        }
+        case PMS_ARRAY_BAND_CERTIFIED: {
+            if (!c->have_field) return PMS_ERR_STATE;
+            std::vector<uint32_t> v(((uint64_t)c->grid.sc_size + 31) / 32, 0u);
+            if (c->band_learned && c->nv && (st = d2h(c, v, c->l_cert.p, v.size()))) return st;
+            put(v.data(), 4 * v.size());
             break;
         }
         case PMS_ARRAY_BAND_BITMAP: {

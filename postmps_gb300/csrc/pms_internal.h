@@ -47,6 +47,7 @@ struct Counters {
     uint32_t nv;            // band vertices
     uint32_t nvalid;        // valid cubes
     unsigned long long nmesh;  // mesh vertices
+    unsigned long long n_pairs;  // (vertex, particle) pairs the field launches evaluated
     uint32_t n_fp64;        // covariances solved in FP64
     uint32_t n_big_cells;   // cells with more particles than the per-thread sort handles
     uint32_t err;           // error bits (kErr*)

@@ -31,6 +31,7 @@ ARRAY = {
     "band_list": (13, np.uint32), "field": (14, np.float32), "cube_case": (15, np.uint32),
     "cube_nvert": (16, np.uint32), "pos_sorted": (17, np.float32), "neighbors": (18, np.uint32),
     "diffuse_potential": (19, np.float32), "diffuse_count": (20, np.int32), "free_normal": (21, np.float32),
+    "band_certified": (22, np.uint32),
 }
 
 
@@ -95,7 +96,7 @@ class Counts(C.Structure):
         ("n_generated_diffuse", C.c_uint32), ("n_spawning", C.c_uint32), ("n_diffuse", C.c_uint32),
         ("n_spray", C.c_uint32), ("n_foam", C.c_uint32), ("n_bubble", C.c_uint32), ("n_fp64_svd", C.c_uint32),
         ("n_band_candidates", C.c_uint32), ("n_band_predicted", C.c_uint32), ("n_band_exact", C.c_uint32),
-        ("n_band_certified", C.c_uint32), ("n_band_rechecked", C.c_uint32),
+        ("n_band_certified", C.c_uint32), ("n_band_rechecked", C.c_uint32), ("n_field_pairs", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

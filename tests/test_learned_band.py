@@ -240,6 +240,36 @@ def test_certified_band_without_network_gives_the_plain_mesh(pms_lib, tmp_config
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scale", [0.05, 0.3])
+def test_certificates_hold_and_exact_values_are_the_plain_ones(pms_lib, scale):
+    """Every vertex the certified band left with a placeholder has an exact value
+    above iso in the plain band (the certificate is right), the placeholder is
+    above iso too, and every other band vertex carries the plain band's value bit
+    for bit; the marching-cubes cases agree everywhere."""
+    pms = pms_lib
+    ctx, cfg, pos, vel, rho = _crown_ctx(pms, scale, seed=205)
+    iso = float(pms.derive_params(cfg).iso_value)
+    with ctx:
+        ctx.upload(pos, vel, rho)
+        ctx.build_grid()
+        ctx.surface()
+        band_p, field_p, case_p = ctx.debug("band_list"), ctx.debug("field"), ctx.debug("cube_case")
+        ctx.set_band_mode("certified")
+        ctx.upload(pos, vel, rho)
+        ctx.build_grid()
+        ctx.surface_learned()
+        band_c, field_c, case_c = ctx.debug("band_list"), ctx.debug("field"), ctx.debug("cube_case")
+        cert = ctx.debug("band_certified")
+        c = ctx.counts()
+    np.testing.assert_array_equal(band_c, band_p)
+    np.testing.assert_array_equal(case_c, case_p)
+    held = ((cert[band_c >> 5] >> (band_c & 31)) & 1).astype(bool)
+    assert held.sum() == c.n_band_certified - c.n_band_rechecked > 0
+    assert np.all(field_p[held] > iso) and np.all(field_c[held] > iso)
+    np.testing.assert_array_equal(field_c[~held], field_p[~held])
+
+
+@pytest.mark.gpu
 def test_all_held_out_frames_match_the_plain_mesh(pms_lib):
     """The committed model on the ten full-size held-out crown frames (seeds
     200-209, 1.3-1.75M particles, never trained on): every learned triangle soup
