@@ -344,6 +344,33 @@ __device__ __forceinline__ float wendland(float rx, float ry, float rz, float h)
     return 0.f;
 }
 
+// The previous frame's particles grouped by their type (spray, foam, bubble; each
+// group in stored order), as a permutation: spray particles in air walk almost
+// empty cells while foam and bubbles walk dense ones, and a warp that mixes them
+// runs at the pace of its slowest lane.  The particles stay where they are (the
+// live set keeps the reference's generated-then-old order).
+__global__ void __launch_bounds__(256) k_df_type_keys(const DiffuseParticle* __restrict__ old, uint32_t n_old,
+                                                      unsigned long long* __restrict__ key) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
+        const int t = old[i].type;
+        key[i] = t == 0 ? 1ull : (t == 1 ? (1ull << 32) : 0ull);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_df_type_perm(const unsigned long long* __restrict__ key,
+                                                      const unsigned long long* __restrict__ scan,
+                                                      const unsigned long long* __restrict__ total, uint32_t n_old,
+                                                      uint32_t* __restrict__ perm) {
+    const unsigned long long tot = *total;
+    const uint32_t n0 = (uint32_t)(tot & 0xffffffffull), n1 = (uint32_t)(tot >> 32);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
+        const unsigned long long k = key[i], sc = scan[i];
+        const uint32_t s0 = (uint32_t)(sc & 0xffffffffull), s1 = (uint32_t)(sc >> 32);
+        const uint32_t dest = (k & 1ull) ? s0 : (k ? n0 + s1 : n0 + n1 + (i - s0 - s1));
+        perm[dest] = i;
+    }
+}
+
 // Neighbours of x within hd (|s| <= hd, the advection's test), walking only the rows
 // and cells of the diffuse box that come within hd of x: a cell left out holds no
 // particle that the count would take, so the count is the reference's.
@@ -373,8 +400,10 @@ __device__ __forceinline__ int count_within_near(const KGrid& g, const DiffusePa
 __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParams dp, uint32_t n_old,
                                                         const uint32_t* __restrict__ cell_start,
                                                         const float4* __restrict__ spos,
-                                                        const float4* __restrict__ svel, DiffuseParticle* __restrict__ old) {
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n_old; t += gridDim.x * blockDim.x) {
+                                                        const float4* __restrict__ svel, const uint32_t* __restrict__ perm,
+                                                        DiffuseParticle* __restrict__ old) {
+    for (uint32_t tt = blockIdx.x * blockDim.x + threadIdx.x; tt < n_old; tt += gridDim.x * blockDim.x) {
+        const uint32_t t = perm[tt];
         DiffuseParticle d = old[t];
         const float px = d.px, py = d.py, pz = d.pz, vx = d.vx, vy = d.vy, vz = d.vz;
         int density = 0;
@@ -558,9 +587,23 @@ pms_status launch_diffuse(pms_ctx* ctx) {
             ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>());
     if (n_spawn) PMS_LAUNCHED(ctx);
     if (n_old) {
+        PMS_CUDA(ctx, ctx->d_tkey.ensure(8 * (size_t)n_old));
+        PMS_CUDA(ctx, ctx->d_tscan.ensure(8 * (size_t)n_old));
+        PMS_CUDA(ctx, ctx->d_perm.ensure(4 * (size_t)n_old));
+        const unsigned go = grid_for(n_old, 256);
+        k_df_type_keys<<<go, 256, 0, ctx->stream>>>(ctx->d_old.as<DiffuseParticle>(), n_old,
+                                                    ctx->d_tkey.as<unsigned long long>());
+        PMS_LAUNCHED(ctx);
+        if ((st = scan_u64(ctx, ctx->d_tkey.as<unsigned long long>(), ctx->d_tscan.as<unsigned long long>(), n_old,
+                           ctx->tmp.as<unsigned long long>())))
+            return st;
+        k_df_type_perm<<<go, 256, 0, ctx->stream>>>(ctx->d_tkey.as<unsigned long long>(),
+                                                    ctx->d_tscan.as<unsigned long long>(),
+                                                    ctx->tmp.as<unsigned long long>(), n_old, ctx->d_perm.as<uint32_t>());
+        PMS_LAUNCHED(ctx);
         k_df_update<<<grid_for(n_old, kThreads), kThreads, 0, ctx->stream>>>(
             g, dp, n_old, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
-            ctx->d_old.as<DiffuseParticle>());
+            ctx->d_perm.as<uint32_t>(), ctx->d_old.as<DiffuseParticle>());
         PMS_LAUNCHED(ctx);
     }
     uint32_t* keep = ctx->d_typescan.as<uint32_t>();

@@ -55,7 +55,7 @@ static void release_all(pms_ctx* c) {
                     &c->mc_key, &c->mc_off, &c->valid, &c->fdense, &c->cube, &c->fitems, &c->fitem_cnt, &c->fitem_off, &c->vert, &c->vnorm, &c->sval, &c->d_isfree, &c->d_freescan,
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
-                    &c->d_nrm_free, &c->counters, &c->scan.partial, &c->tmp,
+                    &c->d_nrm_free, &c->d_tkey, &c->d_tscan, &c->d_perm, &c->counters, &c->scan.partial, &c->tmp,
                     &c->l_dens, &c->l_clist, &c->l_counts, &c->l_model, &c->l_q, &c->l_cert, &c->l_e_bm, &c->l_e_wc,
                     &c->l_e_wp, &c->l_e_list, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp, &c->l_n_list, &c->l_field_new,
                     &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list};

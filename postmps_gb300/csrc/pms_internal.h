@@ -169,7 +169,7 @@ struct pms_ctx {
     bool mesh_normals = false;
     // diffuse
     pms::DBuf d_isfree, d_freescan, d_freelist, d_pot, d_num, d_numscan, d_isdiff, d_isdiffscan,
-              d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free;
+              d_difflist, d_gen, d_old, d_all, d_rand, d_typescan, d_nrm_free, d_tkey, d_tscan, d_perm;
     // learned band: coarse counts, model, cube bitmaps, merge buffers, training data
     pms::DBuf l_dens, l_clist;   // bf16 coarse density pairs (padded grid), candidate cube records
     // l_q: predicted cubes; l_cert: certified vertices; E / N: vertices evaluated exactly first /
