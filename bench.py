@@ -301,6 +301,50 @@ def fp64_judge(ctx, frame, keys: dict, arms, model, h: float) -> dict:
     return out
 
 
+class RefCudaResult(C.Structure):
+    _fields_ = [("seconds_per_frame", C.c_double), ("mesh_vertices", C.c_uint64), ("spray", C.c_uint64),
+                ("foam", C.c_uint64), ("bubble", C.c_uint64), ("frames", C.c_int)]
+
+
+def reference_cuda(frame, keys: dict, diffuse: bool, frames: int = 5) -> dict:
+    """The reference's own CUDA code (its GPUPOST frame loop, compiled unmodified
+    for this GPU by oracle/ref_cuda from the sources build() copied to
+    baseline/_ref/src) on `frames` copies of the frame: particles from host
+    memory, mesh (and diffuse particles) read back as the reference does, no file
+    I/O.  Wall time per frame of its whole host + device loop."""
+    lib_path = os.path.join(ROOT, "baseline", "_ref", "libref_cuda.so")
+    src = os.path.join(ROOT, "baseline", "_ref", "src", "cuda")
+    if not os.path.isdir(src):
+        return {"unavailable": "the reference's sources were not copied to baseline/_ref/src (no reference checkout at build time)"}
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref_cuda"), f"-j{os.cpu_count() or 4}"],
+                       capture_output=True, text=True)
+    if r.returncode != 0 or not os.path.exists(lib_path):
+        return {"unavailable": "the reference's CUDA sources did not build: " + (r.stderr or r.stdout)[-300:]}
+    from postmps_gb300 import synth
+    pos, vel, rho = (np.ascontiguousarray(a, np.float32) for a in frame)
+    lib = C.CDLL(lib_path)
+    lib.ref_cuda_run.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.POINTER(RefCudaResult)]
+    res = RefCudaResult()
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "config.txt"), "w") as f:
+            f.write(synth.config_text(**keys, **{"config.framefrom": 0, "config.frameto": frames - 1,
+                                                "config.issurfacereconstruct": "true",
+                                                "config.isdiffusegeneration": "true" if diffuse else "false"}))
+        os.chdir(td)
+        try:
+            rc = lib.ref_cuda_run(pos.ctypes.data, vel.ctypes.data, rho.ctypes.data, len(pos), frames, 1, C.byref(res))
+        finally:
+            os.chdir(cwd)
+    if rc != 0:
+        return {"unavailable": f"ref_cuda_run returned {rc}"}
+    return {"ms_per_frame": 1e3 * res.seconds_per_frame, "particles_per_s": len(pos) / res.seconds_per_frame,
+            "mesh_vertices": int(res.mesh_vertices), "spray": int(res.spray), "foam": int(res.foam),
+            "bubble": int(res.bubble), "frames": int(res.frames),
+            "what": "the reference's GPUPOST frame loop compiled unmodified for sm_103a (texture references as "
+                    "device pointers, FileData served from memory): host arrays in, mesh read back, no file I/O"}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -662,6 +706,8 @@ def run_pms(args) -> None:
         line["judge"] = judge
     if fp64 is not None:
         line["fp64"] = fp64
+    if rank == 0 and not batched and not args.no_ref_cuda:
+        line["reference_cuda"] = reference_cuda(frames[0], keys, diffuse)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(frames[0][0], keys, args.cpu_fraction)
     if rank == 0:
@@ -686,6 +732,7 @@ def main() -> None:
     ap.add_argument("--no-diffuse", action="store_true")
     ap.add_argument("--no-judge", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 oracle judge")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA build")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
