@@ -7,14 +7,13 @@
 // file _build/gen/mc_tables.inc, so the mesh comes out in the reference's
 // exact triangle order.  Without it, the tables are derived here from first
 // principles: the edges a case crosses are the edges whose end corners lie on
-// different sides of the iso value; on each cube face the crossings are joined
-// into segments (a face with four crossings joins them so that the corners on
-// the "inside" side -- bit set, field <= iso -- are cut off individually when
-// fewer than half of the cube's corners are set, and the outside ones
-// otherwise), segments chain into closed loops, and every loop is fanned into
-// triangles wound with their normal pointing away from the set corners.  Both
-// variants give the same crossed edges; the derived one may split polygons
-// along other diagonals.
+// different sides of the iso value; on each cube face (its corners taken
+// counter-clockwise seen from outside) the crossings are joined into segments
+// -- a face with four crossings joins them so that each set corner (bit set,
+// field <= iso) is cut off on its own --, segments chain into closed loops, and
+// every loop is fanned into triangles.  Both variants cross the same edges,
+// emit the same number of vertices in every case and wind their triangles the
+// same way; the derived one splits some polygons along other diagonals.
 #include "pms_internal.h"
 
 #if defined(__has_include)
@@ -50,7 +49,16 @@ static void derive_tables(McTables& T) {
             for (int i = 1; i < 4; ++i)
                 for (int j = 0; j < 4; ++j)
                     if (!used[j] && edge_between(cyc[i - 1], cs[j]) >= 0) { cyc[i] = cs[j]; used[j] = true; break; }
-            for (int i = 0; i < 4; ++i) faces[nf][i] = cyc[i];
+            // counter-clockwise seen from outside the cube, so that an edge shared by two
+            // faces is walked in opposite directions by their cycles
+            int d1[3], d2[3];
+            for (int a = 0; a < 3; ++a) {
+                d1[a] = kCorner[cyc[1]][a] - kCorner[cyc[0]][a];
+                d2[a] = kCorner[cyc[2]][a] - kCorner[cyc[1]][a];
+            }
+            const int cr = d1[(axis + 1) % 3] * d2[(axis + 2) % 3] - d1[(axis + 2) % 3] * d2[(axis + 1) % 3];
+            const bool ccw = side ? cr > 0 : cr < 0;
+            for (int i = 0; i < 4; ++i) faces[nf][i] = ccw ? cyc[i] : cyc[(4 - i) & 3];
             ++nf;
         }
     for (int e = 0; e < 12; ++e) { T.edge_vertex[e][0] = kEdge[e][0]; T.edge_vertex[e][1] = kEdge[e][1]; }
@@ -59,8 +67,10 @@ static void derive_tables(McTables& T) {
         uint32_t ef = 0;
         for (int e = 0; e < 12; ++e) if (in(kEdge[e][0]) != in(kEdge[e][1])) ef |= 1u << e;
         T.edge_flags[cse] = ef;
-        int nset = __builtin_popcount(cse);
-        bool cut_set = nset <= 4;            // which side is separated on ambiguous faces
+        // on a face with four crossings the set corners are always the ones cut off
+        // (whatever their number): the rule that gives the reference's vertex count
+        // in every one of the 256 cases
+        const bool cut_set = true;
         // next[e]: successor of crossed edge e along its loop
         int next[12];
         for (int e = 0; e < 12; ++e) next[e] = -1;

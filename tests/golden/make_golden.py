@@ -7,7 +7,7 @@ Params.cpp, compiled unmodified for the CPU by ``make -C oracle ref`` (see
 oracle/ref_emu/).  Needs the reference tree, named by $PMS_REFERENCE_DIR; the
 committed .npz files are what the tests read.
 
-    PMS_REFERENCE_DIR=path/to/PostMPS python tests/golden/make_golden.py
+    PMS_REFERENCE_DIR=path/to/PostMPS python tests/golden/make_golden.py [mc]   (mc: the table counts only)
 """
 from __future__ import annotations
 
@@ -124,6 +124,15 @@ def make_diffuse() -> str:
     return path
 
 
+def make_mc_counts() -> str:
+    """The reference's marching-cubes edge flags and vertex counts per case
+    (MarchingCubesHelper.cpp), for the check of the tables libpms derives."""
+    e, tri, nv, ev = O.ref_mc_tables()
+    path = os.path.join(HERE, "mc_tables_counts.npz")
+    np.savez_compressed(path, edge_flags=np.asarray(e, np.uint32), num_vertices=np.asarray(nv, np.uint32))
+    return path
+
+
 def main() -> int:
     if not os.environ.get("PMS_REFERENCE_DIR"):
         print("set PMS_REFERENCE_DIR to the reference checkout: the fixtures come from its own kernels",
@@ -133,6 +142,10 @@ def main() -> int:
     if not O.ref_available():
         print("the reference's kernels did not build from PMS_REFERENCE_DIR: cannot generate fixtures", file=sys.stderr)
         return 1
+    p = make_mc_counts()
+    print(f"{p}: {os.path.getsize(p) / 1024:.0f} KiB")
+    if sys.argv[1:] == ["mc"]:
+        return 0
     for name in CASES:
         p = make(name)
         print(f"{p}: {os.path.getsize(p) / 1024:.0f} KiB")

