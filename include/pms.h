@@ -86,6 +86,8 @@ typedef struct pms_config {
     double fp64_svd_cond;              /* covariances with condition number above this use the FP64 eigen solver (1e6) */
     uint64_t rng_seed;                 /* seed of the diffuse spawn uniforms (replaces std::random_device) */
     char band_model[512];              /* [GB300] BandModel: learned-band model file; empty = plain band */
+    int ply_binary;                    /* [GB300] PlyBinary: pms_run_config writes binary PLY (false: ASCII) */
+    int weld_mesh;                     /* [GB300] WeldMesh: ... an indexed mesh (false: the reference's soup) */
 } pms_config;
 
 /* Derived float32 parameters (SimParams, SurfaceParams, DiffuseParams, Define.h:85-139). */
@@ -217,6 +219,18 @@ pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint6
  * cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
 pms_status pms_stream_mesh_to_host(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices);
 pms_status pms_wait_mesh(pms_ctx* ctx, uint64_t* n_vertices);
+/* Welded (indexed) mesh of the current frame, after pms_marching_cubes: one vertex
+ * per crossed grid edge and a triangle index list in the soup's triangle order
+ * (3 indices per triangle, n_indices = the soup's vertex count).  Each edge point is
+ * interpolated once, from the edge's lower to its upper corner; the soup interpolates
+ * it in every cube that uses it from the end that cube's table names first, so the
+ * two agree up to that rounding.  With normals != 0 the vertex normals are made too
+ * (as the soup's, from central differences of the field).  No counterpart in the
+ * reference, whose PLY and VTK surface files hold the triangle soup
+ * (FileData.cpp:677-773, 1277-1332); a welded mesh is about 2.4x smaller. */
+pms_status pms_weld_mesh(pms_ctx* ctx, int normals);
+pms_status pms_download_welded_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices,
+                                    uint32_t* indices, uint64_t cap_indices, uint64_t* n_vertices, uint64_t* n_indices);
 /* The scalar values of the mesh vertices (any array may be NULL): velocity xyz,
  * its length and the density (the reference's ScalarValue). */
 pms_status pms_download_scalar_values(pms_ctx* ctx, float* vel_xyz, float* vel_len, float* rhop, uint64_t cap,
@@ -451,6 +465,13 @@ pms_status pms_write_surface_vtk(const char* path, const float* pos_xyz, const f
                                  const float* vel_len, const float* rhop, uint64_t n_vertices);
 /* ASCII PLY triangle soup in tinyply 2.3's layout (FileData.cpp:1277-1332). */
 pms_status pms_write_ply(const char* path, const float* pos_xyz, uint64_t n_vertices);
+/* PLY with a face list: indices NULL writes the soup (faces 3k, 3k+1, 3k+2), else
+ * n_indices / 3 triangles over the n_vertices vertices; binary != 0 writes
+ * binary_little_endian (12 bytes per vertex, 13 per face), else ASCII (9 significant
+ * digits, so the float32 positions read back exactly).  The soup in ASCII is
+ * pms_write_ply's layout. */
+pms_status pms_write_ply_mesh(const char* path, const float* pos_xyz, uint64_t n_vertices, const uint32_t* indices,
+                              uint64_t n_indices, int binary);
 /* Diffuse particles as BINARY legacy VTK with Velocity, Size, energy, Ita and
  * waveCrest arrays (FileData.cpp:945-1036). */
 pms_status pms_write_diffuse_vtk(const char* path, const float* pos_xyz, const float* vel_xyz,

@@ -211,6 +211,8 @@ extern "C" pms_status pms_config_load(const char* path, pms_config* c) {
     c->fp64_svd_cond = ini.real("GB300", "Fp64SvdCondition", 1e6);
     c->rng_seed = (uint64_t)ini.real("GB300", "RandomSeed", 4);
     copy_str(c->band_model, sizeof(c->band_model), ini.get("GB300", "BandModel", ""));
+    c->ply_binary = ini.boolean("GB300", "PlyBinary", false) ? 1 : 0;
+    c->weld_mesh = ini.boolean("GB300", "WeldMesh", false) ? 1 : 0;
     return PMS_OK;
 }
 
@@ -372,22 +374,77 @@ double load_be(const char* p, const std::string& t) {
     { uint64_t v; memcpy(&v, b, 8); return (double)v; }
 }
 
-// reads count values of type t as doubles (ascii or big-endian binary)
+// f(begin, end) over [0, n) split across the host's threads (one chunk when small)
+template <class F>
+void parallel_ranges(size_t n, F&& f) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, n / 262144 + 1));
+    if (T == 1) { f(0, n); return; }
+    std::vector<std::thread> th;
+    for (size_t c = 0; c < T; ++c) th.emplace_back([&, c]() { f(n * c / T, n * (c + 1) / T); });
+    for (std::thread& t : th) t.join();
+}
+
+// reads count values of type t as doubles (ascii or big-endian binary); the binary
+// decode and the ASCII number parsing run on all host threads
 bool read_values(Reader& r, const std::string& t, size_t count, std::vector<double>* out) {
     if (out) out->resize(count);
     if (r.binary) {
-        size_t ts = type_size(t);
+        const size_t ts = type_size(t);
         if (!ts) return false;
         r.to_payload();
         if (r.pos + ts * count > r.buf.size()) return false;
-        if (out) for (size_t i = 0; i < count; ++i) (*out)[i] = load_be(r.buf.data() + r.pos + ts * i, t);
+        if (out) {
+            const char* base = r.buf.data() + r.pos;
+            double* o = out->data();
+            if (t == "float")
+                parallel_ranges(count, [&](size_t a, size_t b) {
+                    for (size_t i = a; i < b; ++i) {
+                        const unsigned char* q = reinterpret_cast<const unsigned char*>(base + 4 * i);
+                        const uint32_t u = (uint32_t)q[0] << 24 | (uint32_t)q[1] << 16 | (uint32_t)q[2] << 8 | q[3];
+                        float f;
+                        memcpy(&f, &u, 4);
+                        o[i] = f;
+                    }
+                });
+            else if (t == "double")
+                parallel_ranges(count, [&](size_t a, size_t b) {
+                    for (size_t i = a; i < b; ++i) {
+                        const unsigned char* q = reinterpret_cast<const unsigned char*>(base + 8 * i);
+                        uint64_t u = 0;
+                        for (int k = 0; k < 8; ++k) u = u << 8 | q[k];
+                        double d;
+                        memcpy(&d, &u, 8);
+                        o[i] = d;
+                    }
+                });
+            else
+                parallel_ranges(count, [&](size_t a, size_t b) {
+                    for (size_t i = a; i < b; ++i) o[i] = load_be(base + ts * i, t);
+                });
+        }
         r.pos += ts * count;
         return true;
     }
+    // ASCII: the token starts in one pass, then the numbers in parallel
+    std::vector<size_t> starts(count);
     for (size_t i = 0; i < count; ++i) {
-        std::string tok = r.token();
-        if (tok.empty()) return false;
-        if (out) (*out)[i] = std::strtod(tok.c_str(), nullptr);
+        while (r.pos < r.buf.size() && std::isspace((unsigned char)r.buf[r.pos])) ++r.pos;
+        if (r.pos >= r.buf.size()) return false;
+        starts[i] = r.pos;
+        while (r.pos < r.buf.size() && !std::isspace((unsigned char)r.buf[r.pos])) ++r.pos;
+    }
+    if (out) {
+        double* o = out->data();
+        parallel_ranges(count, [&](size_t a, size_t b) {
+            std::string tok;
+            for (size_t i = a; i < b; ++i) {
+                size_t e = starts[i];
+                while (e < r.buf.size() && !std::isspace((unsigned char)r.buf[e])) ++e;
+                tok.assign(r.buf.data() + starts[i], e - starts[i]);
+                o[i] = std::strtod(tok.c_str(), nullptr);
+            }
+        });
     }
     return true;
 }
@@ -619,6 +676,54 @@ extern "C" pms_status pms_write_ply(const char* path, const float* pos, uint64_t
     return ok ? PMS_OK : PMS_ERR_IO;
 }
 
+extern "C" pms_status pms_write_ply_mesh(const char* path, const float* pos, uint64_t nv, const uint32_t* indices,
+                                         uint64_t ni, int binary) {
+    if (!path || (nv && !pos) || (indices && ni % 3)) return PMS_ERR_INVALID_ARGUMENT;
+    if (!indices && !binary) return pms_write_ply(path, pos, nv);      // the reference's ASCII soup
+    if (!indices) ni = nv - nv % 3;
+    if (indices)
+        for (uint64_t i = 0; i < ni; ++i)
+            if (indices[i] >= nv) return PMS_ERR_INVALID_ARGUMENT;
+    const uint64_t nf = ni / 3;
+    FILE* f = fopen(path, "wb");
+    if (!f) return PMS_ERR_IO;
+    fprintf(f, "ply\nformat %s 1.0\ncomment generated by libpms\n", binary ? "binary_little_endian" : "ascii");
+    fprintf(f, "element vertex %llu\nproperty float x\nproperty float y\nproperty float z\n", (unsigned long long)nv);
+    fprintf(f, "element face %llu\nproperty list uchar uint vertex_indices\nend_header\n", (unsigned long long)nf);
+    bool ok = true;
+    if (binary) {
+        // little-endian records: 12 bytes per vertex, 13 per face (count, then three uint32)
+        std::vector<unsigned char> buf;
+        buf.reserve(12 * nv);
+        auto put32 = [&](uint32_t u) { for (int k = 0; k < 4; ++k) buf.push_back((unsigned char)(u >> (8 * k))); };
+        for (uint64_t i = 0; i < 3 * nv; ++i) { uint32_t u; memcpy(&u, &pos[i], 4); put32(u); }
+        ok = fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+        buf.clear();
+        buf.reserve(13 * nf);
+        for (uint64_t t = 0; t < nf; ++t) {
+            buf.push_back(3);
+            for (int k = 0; k < 3; ++k) put32(indices ? indices[3 * t + k] : (uint32_t)(3 * t + k));
+        }
+        ok = ok && fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+    } else {
+        std::string out;
+        char line[96];
+        for (uint64_t i = 0; i < nv; ++i) {
+            // 9 significant digits: the float32 values read back exactly
+            const int k = snprintf(line, sizeof(line), "%.9g %.9g %.9g \n", pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+            out.append(line, (size_t)k);
+        }
+        for (uint64_t t = 0; t < nf; ++t) {
+            const int k = snprintf(line, sizeof(line), "3 %u %u %u \n", indices[3 * t], indices[3 * t + 1], indices[3 * t + 2]);
+            out.append(line, (size_t)k);
+        }
+        ok = fwrite(out.data(), 1, out.size(), f) == out.size();
+    }
+    ok = ferror(f) == 0 && ok;
+    ok = fclose(f) == 0 && ok;
+    return ok ? PMS_OK : PMS_ERR_IO;
+}
+
 extern "C" pms_status pms_write_diffuse_vtk(const char* path, const float* pos, const float* vel, const float* energy,
                                             const float* ita, const float* wave_crest, uint32_t n, float size) {
     if (!path || (n && !pos)) return PMS_ERR_INVALID_ARGUMENT;
@@ -657,39 +762,106 @@ static std::string frame_name(const char* dir, const char* prefix, int nzeros, i
     return d + prefix + num + ext;
 }
 
+// One frame's input, parsed on the reader thread.
+struct FrameIn {
+    float *pos = nullptr, *vel = nullptr, *rho = nullptr;
+    uint32_t n = 0;
+    pms_status st = PMS_OK;
+    std::string path;
+    void release() { pms_free_host(pos); pms_free_host(vel); pms_free_host(rho); pos = vel = rho = nullptr; }
+};
+
+// One frame's output, written on the writer thread.
+struct FrameOut {
+    std::string ply, dir;
+    std::vector<float> pos;            // soup or welded vertices
+    std::vector<uint32_t> idx;         // welded triangle indices (empty: soup)
+    bool binary = false, surface = false;
+    std::vector<std::vector<float>> dpos, dvel;   // diffuse spray, foam, bubble
+    std::vector<std::string> dpaths;
+    float dsize = 0.f;
+};
+
+static pms_status write_frame(const FrameOut& o) {
+    pms_status st = PMS_OK;
+    if (o.surface) {
+        const uint64_t nv = o.pos.size() / 3;
+        if (nv == 0) fprintf(stderr, "Nothing produced.\n");
+        else if (o.idx.empty() && !o.binary) st = pms_write_ply(o.ply.c_str(), o.pos.data(), nv);
+        else st = pms_write_ply_mesh(o.ply.c_str(), o.pos.data(), nv, o.idx.empty() ? nullptr : o.idx.data(),
+                                     o.idx.size(), o.binary ? 1 : 0);
+        if (st) { fprintf(stderr, "error: cannot write %s\n", o.ply.c_str()); return st; }
+    }
+    for (size_t k = 0; k < o.dpaths.size() && !st; ++k) {
+        const uint32_t m = (uint32_t)(o.dpos[k].size() / 3);
+        std::vector<float> zeros(m, 0.f);
+        st = pms_write_diffuse_vtk(o.dpaths[k].c_str(), o.dpos[k].data(), o.dvel[k].data(), zeros.data(), zeros.data(),
+                                   zeros.data(), m, o.dsize);
+        if (st) fprintf(stderr, "error: cannot write %s\n", o.dpaths[k].c_str());
+    }
+    return st;
+}
+
+// The VisGPU frame loop as a pipeline: while the GPU reconstructs frame k, a reader
+// thread parses frame k + 1 and a writer thread writes frame k - 1's files (the
+// reference does the three one after another, GPUPOST.cpp:51-82).
 extern "C" pms_status pms_run_config(const char* config_path, int verbose) {
     pms_config cfg;
     pms_status st = pms_config_load(config_path, &cfg);
     if (st) { fprintf(stderr, "error: cannot load %s\n", config_path ? config_path : "(null)"); return st; }
     pms_ctx* ctx = nullptr;
     if ((st = pms_create(&cfg, -1, &ctx))) { fprintf(stderr, "error: pms_create: %s\n", pms_status_string(st)); return st; }
-    std::vector<float> mesh;
-    for (int frame = cfg.frame_start; frame <= cfg.frame_end; frame += (cfg.frame_step > 0 ? cfg.frame_step : 1)) {
-        std::string in = frame_name(cfg.fluid_path, cfg.fluid_prefix, cfg.num_zeros, frame, ".vtk");
-        float *pos = nullptr, *vel = nullptr, *rho = nullptr;
-        uint32_t n = 0;
-        if ((st = pms_read_vtk_particles(in.c_str(), &pos, &vel, &rho, &n))) {
-            fprintf(stderr, "error: cannot read %s\n", in.c_str());
+    const int step = cfg.frame_step > 0 ? cfg.frame_step : 1;
+    auto read = [&](int frame, FrameIn* in) {
+        in->path = frame_name(cfg.fluid_path, cfg.fluid_prefix, cfg.num_zeros, frame, ".vtk");
+        in->st = pms_read_vtk_particles(in->path.c_str(), &in->pos, &in->vel, &in->rho, &in->n);
+    };
+    FrameIn cur, next;
+    std::thread reader, writer;
+    pms_status wst = PMS_OK;
+    if (cfg.frame_start <= cfg.frame_end) read(cfg.frame_start, &cur);
+    for (int frame = cfg.frame_start; frame <= cfg.frame_end; frame += step) {
+        if (cur.st) { fprintf(stderr, "error: cannot read %s\n", cur.path.c_str()); st = cur.st; break; }
+        const bool more = frame + step <= cfg.frame_end;
+        if (more) reader = std::thread(read, frame + step, &next);
+        if (verbose) printf("frame %d: %u particles from %s\n", frame, cur.n, cur.path.c_str());
+        st = pms_upload_particles(ctx, cur.pos, cur.vel, cur.rho, cur.n);
+        if (!st) st = pms_run_frame(ctx);
+        FrameOut out;
+        if (!st && cfg.is_surface) {
+            out.surface = true;
+            out.binary = cfg.ply_binary != 0;
+            out.ply = frame_name(cfg.surface_path, cfg.surface_prefix, cfg.num_zeros, frame, ".ply");
+            uint64_t nv = 0, ni = 0;
+            if (cfg.weld_mesh) {
+                if (!(st = pms_weld_mesh(ctx, 0)) && !(st = pms_download_welded_mesh(ctx, nullptr, nullptr, 0, nullptr, 0, &nv, &ni))) {
+                    out.pos.resize(3 * (size_t)nv);
+                    out.idx.resize((size_t)ni);
+                    st = pms_download_welded_mesh(ctx, out.pos.data(), nullptr, nv, out.idx.data(), ni, &nv, &ni);
+                }
+            } else {
+                pms_download_mesh(ctx, nullptr, nullptr, 0, &nv);
+                out.pos.resize(3 * (size_t)nv);
+                st = nv ? pms_download_mesh(ctx, out.pos.data(), nullptr, nv, &nv) : PMS_OK;
+            }
+            if (verbose && !st) printf("  %llu mesh vertices -> %s\n", (unsigned long long)(out.pos.size() / 3), out.ply.c_str());
+        }
+        if (!st && cfg.is_diffuse) st = pms::diffuse_frame_output(ctx, cfg, frame, out.dpos, out.dvel, out.dpaths, out.dsize);
+        if (st) {
+            fprintf(stderr, "error: frame %d: %s\n", frame, pms_last_error(ctx));
+            if (reader.joinable()) reader.join();
+            next.release();
             break;
         }
-        if (verbose) printf("frame %d: %u particles from %s\n", frame, n, in.c_str());
-        st = pms_upload_particles(ctx, pos, vel, rho, n);
-        pms_free_host(pos); pms_free_host(vel); pms_free_host(rho);
-        if (st || (st = pms_run_frame(ctx))) { fprintf(stderr, "error: frame %d: %s\n", frame, pms_last_error(ctx)); break; }
-        if (cfg.is_surface) {
-            uint64_t nv = 0;
-            pms_download_mesh(ctx, nullptr, nullptr, 0, &nv);
-            mesh.resize(3 * (size_t)(nv ? nv : 1));
-            if ((st = pms_download_mesh(ctx, mesh.data(), nullptr, nv, &nv))) break;
-            std::string out = frame_name(cfg.surface_path, cfg.surface_prefix, cfg.num_zeros, frame, ".ply");
-            if (nv == 0) fprintf(stderr, "Nothing produced.\n");
-            else if ((st = pms_write_ply(out.c_str(), mesh.data(), nv))) { fprintf(stderr, "error: cannot write %s\n", out.c_str()); break; }
-            if (verbose) printf("  %llu mesh vertices -> %s\n", (unsigned long long)nv, out.c_str());
-        }
-        if (cfg.is_diffuse) {
-            if ((st = pms::write_diffuse_frame(ctx, cfg, frame))) break;
-        }
+        if (writer.joinable()) writer.join();
+        if (wst) { st = wst; if (reader.joinable()) reader.join(); next.release(); break; }
+        writer = std::thread([o = std::move(out), &wst]() { wst = write_frame(o); });
+        cur.release();
+        if (more) { reader.join(); cur = next; next = FrameIn(); }
     }
+    cur.release();
+    if (writer.joinable()) writer.join();
+    if (!st) st = wst;
     pms_destroy(ctx);
     return st;
 }

@@ -736,29 +736,26 @@ extern "C" pms_status pms_download_diffuse(pms_ctx* ctx, int type, float* pos, f
     return PMS_OK;
 }
 
-pms_status pms::write_diffuse_frame(pms_ctx* ctx, const pms_config& cfg, int frame) {
+pms_status pms::diffuse_frame_output(pms_ctx* ctx, const pms_config& cfg, int frame, std::vector<std::vector<float>>& pos,
+                                     std::vector<std::vector<float>>& vel, std::vector<std::string>& paths, float& size) {
     std::vector<DiffuseParticle> v;
     pms_status st = download_live(ctx, v);
     if (st) return st;
     static const char* prefixes[3] = {"PartSpary_", "PartFoam_", "PartBubble_"};
-    for (int cls = 0; cls < 3; ++cls) {
-        std::vector<float> pos, vel;
-        for (const DiffuseParticle& d : v) {
-            const int c = d.type == 0 ? 0 : (d.type == 2 ? 2 : 1);
-            if (c != cls) continue;
-            pos.insert(pos.end(), {d.px, d.py, d.pz});
-            vel.insert(vel.end(), {d.vx, d.vy, d.vz});
-        }
-        const uint32_t m = (uint32_t)(pos.size() / 3);
-        std::vector<float> zeros(m, 0.f);
-        char num[64];
-        snprintf(num, sizeof(num), "%.*d", cfg.num_zeros, frame);
-        std::string dir = cfg.diffuse_path;
-        if (!dir.empty() && dir.back() != '/') dir += "/";
-        std::string path = dir + prefixes[cls] + num + ".vtk";
-        st = pms_write_diffuse_vtk(path.c_str(), pos.data(), vel.data(), zeros.data(), zeros.data(), zeros.data(), m,
-                                   ctx->prm.hd / 10.f);
-        if (st) return pms_fail(ctx, st, "cannot write %s", path.c_str());
+    pos.assign(3, {});
+    vel.assign(3, {});
+    paths.assign(3, {});
+    for (const DiffuseParticle& d : v) {
+        // the reference's split: 0 spray, 2 bubble, anything else foam (DiffuseGeneration.cu:808-826)
+        const int c = d.type == 0 ? 0 : (d.type == 2 ? 2 : 1);
+        pos[c].insert(pos[c].end(), {d.px, d.py, d.pz});
+        vel[c].insert(vel[c].end(), {d.vx, d.vy, d.vz});
     }
+    char num[64];
+    snprintf(num, sizeof(num), "%.*d", cfg.num_zeros, frame);
+    std::string dir = cfg.diffuse_path;
+    if (!dir.empty() && dir.back() != '/') dir += "/";
+    for (int cls = 0; cls < 3; ++cls) paths[cls] = dir + prefixes[cls] + num + ".vtk";
+    size = ctx->prm.hd / 10.f;
     return PMS_OK;
 }

@@ -372,6 +372,134 @@ pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsi
     return PMS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Welded mesh (no counterpart in the reference, whose PLY and VTK surface files
+// hold the triangle soup, FileData.cpp:677-773 and 1277-1332).  Neighbouring
+// cubes share their crossed grid edges; the welded mesh keeps one vertex per
+// crossed edge and a triangle index list in the soup's order.  A grid edge is
+// keyed by its lower corner and its axis, 3 * vertex id + axis.  Its point is
+// interpolated once, from the lower to the upper corner; the soup interpolates
+// it in every cube that uses it, from whichever end that cube's table names
+// first, so the two agree up to the rounding of that choice.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t edge_key(uint32_t id, uint32_t rx, uint32_t rxy, int e) {
+    const int a = edge_end(e, 0), b = edge_end(e, 1);
+    const int axis = corner_off(a, 0) != corner_off(b, 0) ? 0 : (corner_off(a, 1) != corner_off(b, 1) ? 1 : 2);
+    const int lo = corner_off(a, axis) < corner_off(b, axis) ? a : b;
+    const uint32_t v = id + (uint32_t)corner_off(lo, 0) + (uint32_t)corner_off(lo, 1) * rx + (uint32_t)corner_off(lo, 2) * rxy;
+    return 3ull * v + (uint64_t)axis;
+}
+
+__global__ void __launch_bounds__(256) k_weld_mark(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
+                                                   uint32_t* __restrict__ ebits) {
+    const uint32_t n = cnt->nvalid;
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint4 cr = __ldg(&cube[t]);
+        const uint32_t ef = __ldg(&g_case[cr.y]) & 0xfffu;
+        for (uint32_t m = ef; m; m &= m - 1u) {
+            const uint64_t key = edge_key(cr.x, rx, rxy, __ffs(m) - 1);
+            const uint32_t bit = 1u << (key & 31u);
+            if (!(ebits[key >> 5] & bit)) atomicOr(&ebits[key >> 5], bit);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_weld_popc(const uint32_t* __restrict__ b, uint32_t* __restrict__ wc, uint64_t nw) {
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw; w += (uint64_t)gridDim.x * blockDim.x)
+        wc[w] = __popc(b[w]);
+}
+
+// the negative field gradient at a scalar vertex (central differences, 0 outside the grid
+// and the band), the vertex normal of getVertexNorm (myCuda.cuh:259-289)
+__device__ __forceinline__ float3 vertex_normal(const KGrid& g, const float* __restrict__ fdense, int x, int y, int z) {
+    return normalized(make_float3(grid_value(g, fdense, x - 1, y, z) - grid_value(g, fdense, x + 1, y, z),
+                                  grid_value(g, fdense, x, y - 1, z) - grid_value(g, fdense, x, y + 1, z),
+                                  grid_value(g, fdense, x, y, z - 1) - grid_value(g, fdense, x, y, z + 1)));
+}
+
+// one welded vertex per set edge bit, at the edge's rank
+__global__ void __launch_bounds__(256) k_weld_vertices(KGrid g, float iso, const uint32_t* __restrict__ ebits,
+                                                       const uint32_t* __restrict__ wprefix, uint64_t nw,
+                                                       const float* __restrict__ fdense, uint64_t cap,
+                                                       float* __restrict__ vert, float* __restrict__ vnorm) {
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    const float sgn = (iso < 0.f) ? -1.f : 1.f;
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nw; w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t bits = ebits[w], r = wprefix[w];
+        while (bits) {
+            const uint32_t bi = (uint32_t)(__ffs(bits) - 1);
+            bits &= bits - 1u;
+            if (r >= cap) break;   // the host sizes vert for every soup vertex; never reached
+            const uint64_t key = 32ull * w + bi;
+            const uint32_t v = (uint32_t)(key / 3ull), axis = (uint32_t)(key - 3ull * v);
+            const int z = (int)(v / rxy), rem = (int)(v - (uint32_t)z * rxy), y = rem / (int)rx, x = rem - y * (int)rx;
+            const int X = x + (axis == 0), Y = y + (axis == 1), Z = z + (axis == 2);
+            const float fa = grid_value(g, fdense, x, y, z), fb = grid_value(g, fdense, X, Y, Z);
+            const float d = fb - fa;
+            const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - fa) / d;
+            const float ax = sc_coord_i(g, x, 0), ay = sc_coord_i(g, y, 1), az = sc_coord_i(g, z, 2);
+            const float bx = sc_coord_i(g, X, 0), by = sc_coord_i(g, Y, 1), bz = sc_coord_i(g, Z, 2);
+            vert[3 * (size_t)r + 0] = ax + tt * (bx - ax);
+            vert[3 * (size_t)r + 1] = ay + tt * (by - ay);
+            vert[3 * (size_t)r + 2] = az + tt * (bz - az);
+            if (vnorm) {
+                const float3 na = vertex_normal(g, fdense, x, y, z), nb = vertex_normal(g, fdense, X, Y, Z);
+                const float3 nn = normalized(make_float3(na.x + tt * (nb.x - na.x), na.y + tt * (nb.y - na.y),
+                                                         na.z + tt * (nb.z - na.z)));
+                vnorm[3 * (size_t)r + 0] = sgn * nn.x;
+                vnorm[3 * (size_t)r + 1] = sgn * nn.y;
+                vnorm[3 * (size_t)r + 2] = sgn * nn.z;
+            }
+            ++r;
+        }
+    }
+}
+
+// the triangle index list, in the soup's order: mesh vertex base + slot of a valid cube
+// takes the rank of the edge its table entry names
+__global__ void __launch_bounds__(256) k_weld_indices(KGrid g, const Counters* __restrict__ cnt, const uint4* __restrict__ cube,
+                                                      const uint32_t* __restrict__ ebits, const uint32_t* __restrict__ wprefix,
+                                                      uint32_t* __restrict__ idx) {
+    const uint32_t n = cnt->nvalid;
+    const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint4 cr = __ldg(&cube[t]);
+        const uint32_t ef = __ldg(&g_case[cr.y]) & 0xfffu;
+        for (uint32_t m = ef; m; m &= m - 1u) {
+            const int e = __ffs(m) - 1;
+            const uint64_t key = edge_key(cr.x, rx, rxy, e);
+            const uint32_t w = (uint32_t)(key >> 5), bi = (uint32_t)(key & 31u);
+            const uint32_t rank = wprefix[w] + __popc(ebits[w] & ((1u << bi) - 1u));
+            for (uint32_t sl = __ldg(&g_slots[cr.y][e]); sl; sl &= sl - 1u)
+                idx[(size_t)cr.z + (uint32_t)(__ffs(sl) - 1)] = rank;
+        }
+    }
+}
+
+pms_status launch_weld(pms_ctx* ctx, uint32_t* ebits, uint32_t* wc, uint32_t* wprefix, uint64_t nw, uint32_t* n_unique,
+                       uint64_t cap, float* vert, float* vnorm, uint32_t* idx) {
+    const KGrid g = kgrid_of(ctx->grid);
+    Counters* cnt = ctx->counters.as<Counters>();
+    PMS_CUDA(ctx, cudaMemsetAsync(ebits, 0, 4 * nw, ctx->stream));
+    k_weld_mark<<<grid_for(ctx->nvalid, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), ebits);
+    PMS_LAUNCHED(ctx);
+    k_weld_popc<<<grid_for(nw, 256), 256, 0, ctx->stream>>>(ebits, wc, nw);
+    PMS_LAUNCHED(ctx);
+    pms_status st = scan_u32(ctx, wc, wprefix, nw, n_unique);
+    if (st) return st;
+    if (vert) {
+        k_weld_vertices<<<grid_for(nw, 256), 256, 0, ctx->stream>>>(g, ctx->prm.iso_value, ebits, wprefix, nw,
+                                                                    ctx->fdense.as<float>(), cap, vert, vnorm);
+        PMS_LAUNCHED(ctx);
+    }
+    if (idx) {
+        k_weld_indices<<<grid_for(ctx->nvalid, 256), 256, 0, ctx->stream>>>(g, cnt, ctx->cube.as<uint4>(), ebits, wprefix, idx);
+        PMS_LAUNCHED(ctx);
+    }
+    return PMS_OK;
+}
+
 pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo, uint32_t v_hi) {
     return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->mesh_normals ? ctx->vnorm.as<float>() : nullptr, nullptr,
                              ~0ull, v_lo, v_hi);

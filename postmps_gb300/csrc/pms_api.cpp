@@ -58,7 +58,8 @@ static void release_all(pms_ctx* c) {
                     &c->d_nrm_free, &c->d_tkey, &c->d_tscan, &c->d_perm, &c->counters, &c->scan.partial, &c->tmp,
                     &c->l_dens, &c->l_clist, &c->l_counts, &c->l_model, &c->l_q, &c->l_cert, &c->l_e_bm, &c->l_e_wc,
                     &c->l_e_wp, &c->l_e_list, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp, &c->l_n_list, &c->l_field_new,
-                    &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list};
+                    &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list,
+                    &c->w_bits, &c->w_wc, &c->w_wp, &c->w_vert, &c->w_vnorm, &c->w_idx};
     for (DBuf* b : bufs) b->release();
 }
 
@@ -298,7 +299,7 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
     }
     c->n = n;
     c->have_particles = true;
-    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = false;
+    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = c->have_weld = false;
     c->band_learned = c->mc_classified = c->mc_compacted = false;
     c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
     c->ns = c->nv = c->nvalid = 0;
@@ -404,6 +405,7 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     cudaSetDevice(c->device);
     c->nvalid = 0;
     c->nmesh = 0;
+    c->have_weld = false;
     if (c->nv) {
         pms_status st;
         // the learned band's last border check already computed the final vertex set's cases
@@ -566,6 +568,53 @@ extern "C" pms_status pms_download_mesh(pms_ctx* c, float* pos, float* nrm, uint
     }
     PMS_CUDA(c, cudaMemcpyAsync(pos, c->vert.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     if (nrm) PMS_CUDA(c, cudaMemcpyAsync(nrm, c->vnorm.p, 12 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_weld_mesh(pms_ctx* c, int normals) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_mc) return pms_fail(c, PMS_ERR_STATE, "pms_weld_mesh before pms_marching_cubes");
+    cudaSetDevice(c->device);
+    c->w_nvert = 0;
+    c->weld_normals = normals != 0;
+    if (c->nmesh) {
+        const uint64_t nw = (3ull * c->grid.sc_size + 31) / 32;
+        PMS_CUDA(c, c->w_bits.ensure(4 * (nw + 1)));
+        PMS_CUDA(c, c->w_wc.ensure(4 * (nw + 1)));
+        PMS_CUDA(c, c->w_wp.ensure(4 * (nw + 1)));
+        // at most one welded vertex per soup vertex
+        PMS_CUDA(c, c->w_vert.ensure(12 * c->nmesh));
+        if (normals) PMS_CUDA(c, c->w_vnorm.ensure(12 * c->nmesh));
+        PMS_CUDA(c, c->w_idx.ensure(4 * c->nmesh));
+        Counters* cnt = c->counters.as<Counters>();
+        pms_status st = launch_weld(c, c->w_bits.as<uint32_t>(), c->w_wc.as<uint32_t>(), c->w_wp.as<uint32_t>(), nw,
+                                    &cnt->n_weld, c->nmesh, c->w_vert.as<float>(), normals ? c->w_vnorm.as<float>() : nullptr,
+                                    c->w_idx.as<uint32_t>());
+        if (st) return st;
+        if ((st = sync_counters(c))) return st;
+        c->w_nvert = c->h_counters->n_weld;
+        if (c->w_nvert > c->nmesh) return pms_fail(c, PMS_ERR_CAPACITY, "welded mesh has more vertices than the soup");
+    }
+    c->have_weld = true;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_download_welded_mesh(pms_ctx* c, float* pos, float* nrm, uint64_t cap_vertices, uint32_t* indices,
+                                               uint64_t cap_indices, uint64_t* n_vertices, uint64_t* n_indices) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    if (!c->have_weld) return pms_fail(c, PMS_ERR_STATE, "pms_download_welded_mesh before pms_weld_mesh");
+    if (nrm && !c->weld_normals) return pms_fail(c, PMS_ERR_STATE, "the welded mesh was made without normals");
+    cudaSetDevice(c->device);
+    if (n_vertices) *n_vertices = c->w_nvert;
+    if (n_indices) *n_indices = c->nmesh;
+    if ((pos || nrm) && cap_vertices < c->w_nvert)
+        return pms_fail(c, PMS_ERR_CAPACITY, "welded mesh has %llu vertices", (unsigned long long)c->w_nvert);
+    if (indices && cap_indices < c->nmesh)
+        return pms_fail(c, PMS_ERR_CAPACITY, "welded mesh has %llu indices", (unsigned long long)c->nmesh);
+    if (pos && c->w_nvert) PMS_CUDA(c, cudaMemcpyAsync(pos, c->w_vert.p, 12 * c->w_nvert, cudaMemcpyDeviceToHost, c->stream));
+    if (nrm && c->w_nvert) PMS_CUDA(c, cudaMemcpyAsync(nrm, c->w_vnorm.p, 12 * c->w_nvert, cudaMemcpyDeviceToHost, c->stream));
+    if (indices && c->nmesh) PMS_CUDA(c, cudaMemcpyAsync(indices, c->w_idx.p, 4 * c->nmesh, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PMS_OK;
 }

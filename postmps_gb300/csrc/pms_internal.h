@@ -70,6 +70,7 @@ struct Counters {
     uint32_t l_recheck;     // certified corners of valid cubes, evaluated exactly afterwards
     uint32_t n_items;       // work items of the last field launch
     uint32_t n_tiles;       // scalar-grid tiles the band marking visits
+    uint32_t n_weld;        // vertices of the welded mesh (crossed grid edges)
 };
 static constexpr int kLearnCounters = 6;
 
@@ -161,6 +162,11 @@ struct pms_ctx {
     // the field over the whole scalar grid, 0 off the band (the marching cubes' lookups);
     // per valid cube {vertex id, case, first mesh vertex, 0}
     pms::DBuf fdense, cube;
+    // welded mesh: crossed-edge bitmap (3 bits per scalar vertex), its word popcounts and
+    // prefix, vertices, normals, triangle indices
+    pms::DBuf w_bits, w_wc, w_wp, w_vert, w_vnorm, w_idx;
+    uint64_t w_nvert = 0;
+    bool have_weld = false, weld_normals = false;
     // field work items (runs of x-neighbouring band vertices)
     pms::DBuf fitems, fitem_cnt, fitem_off;
     bool have_values = false;
@@ -260,6 +266,10 @@ pms_status launch_mc_classify(pms_ctx* ctx);
 pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo = 0,
                           uint32_t v_hi = 0xffffffffu);
 pms_status launch_scalar_values(pms_ctx* ctx);
+// welded mesh from the valid-cube records (k_mc.cu): ebits of nw words zeroed and set,
+// n_unique its vertex count; vert / vnorm / idx may be null
+pms_status launch_weld(pms_ctx* ctx, uint32_t* ebits, uint32_t* wc, uint32_t* wprefix, uint64_t nw, uint32_t* n_unique,
+                       uint64_t cap, float* vert, float* vnorm, uint32_t* idx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
                              unsigned long long cap, uint32_t v_lo = 0,
@@ -274,5 +284,8 @@ void pms_batch_release(pms_ctx* c);   // pms_batch.cpp
 namespace pms {
 // diffuse results (k_diffuse.cu)
 pms_status diffuse_debug(pms_ctx* ctx, int array_id, std::vector<uint8_t>& out);
-pms_status write_diffuse_frame(pms_ctx* ctx, const pms_config& cfg, int frame);
+// the live diffuse particles split into the three files of a frame (FileData.cpp:945-1036):
+// positions and velocities per class (spray, foam, bubble), their paths, the size value
+pms_status diffuse_frame_output(pms_ctx* ctx, const pms_config& cfg, int frame, std::vector<std::vector<float>>& pos,
+                                std::vector<std::vector<float>>& vel, std::vector<std::string>& paths, float& size);
 }  // namespace pms

@@ -59,6 +59,7 @@ class Config(C.Structure):
         ("surface_path", C.c_char * 512), ("surface_prefix", C.c_char * 128),
         ("diffuse_path", C.c_char * 512), ("diffuse_prefix", C.c_char * 128),
         ("fp64_svd_cond", C.c_double), ("rng_seed", C.c_uint64), ("band_model", C.c_char * 512),
+        ("ply_binary", C.c_int), ("weld_mesh", C.c_int),
     ]
 
 
@@ -200,6 +201,10 @@ def lib() -> C.CDLL:
         L.pms_write_surface_vtk.argtypes = [C.c_char_p, vp, vp, vp, vp, vp, C.c_uint64]
         L.pms_set_band_model.argtypes = [vp, C.POINTER(BandModel)]
         L.pms_set_band_mode.argtypes = [vp, C.c_int]
+        L.pms_weld_mesh.argtypes = [vp, C.c_int]
+        L.pms_download_welded_mesh.argtypes = [vp, vp, vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64),
+                                               C.POINTER(C.c_uint64)]
+        L.pms_write_ply_mesh.argtypes = [C.c_char_p, vp, C.c_uint64, vp, C.c_uint64, C.c_int]
         L.pms_run_batch.argtypes = [vp, C.POINTER(Frame), C.c_uint32, C.c_int]
         L.pms_autotune.argtypes = [vp, C.POINTER(Tune)]
         L.pms_set_tune.argtypes = [vp, C.POINTER(Tune)]
@@ -272,6 +277,13 @@ def mc_tables(derived: bool = False):
 # ---------------------------------------------------------------------------
 # files
 # ---------------------------------------------------------------------------
+def write_ply_mesh(path: str, pos, indices=None, binary: bool = False) -> None:
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    idx = None if indices is None else np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    _check(lib().pms_write_ply_mesh(str(path).encode(), _ptr(pos), C.c_uint64(len(pos)), _ptr(idx),
+                                    C.c_uint64(0 if idx is None else len(idx)), 1 if binary else 0))
+
+
 def read_vtk(path: str):
     p, v, r = C.c_void_p(), C.c_void_p(), C.c_void_p()
     n = C.c_uint32()
@@ -506,6 +518,19 @@ class Context:
         n = C.c_uint64()
         self._call("pms_wait_mesh", C.byref(n))
         return n.value
+
+    def weld(self, normals: bool = False):
+        """The welded mesh of the current frame: (positions (m, 3), normals or None,
+        triangle indices (t, 3))."""
+        self._call("pms_weld_mesh", 1 if normals else 0)
+        nv, ni = C.c_uint64(), C.c_uint64()
+        self._call("pms_download_welded_mesh", None, None, C.c_uint64(0), None, C.c_uint64(0), C.byref(nv), C.byref(ni))
+        pos = np.zeros((nv.value, 3), np.float32)
+        nrm = np.zeros((nv.value, 3), np.float32) if normals else None
+        idx = np.zeros(ni.value, np.uint32)
+        self._call("pms_download_welded_mesh", _ptr(pos), _ptr(nrm), C.c_uint64(nv.value), _ptr(idx), C.c_uint64(ni.value),
+                   C.byref(nv), C.byref(ni))
+        return pos, nrm, idx.reshape(-1, 3)
 
     def stream_diffuse_to_host(self, ptr: int, cap: int) -> None:
         """Register a page-locked host buffer (raw address) of `cap` 32-byte

@@ -95,11 +95,13 @@ def test_grid_matches_reference_fixture(pms_lib, tmp_config, case):
     np.testing.assert_array_equal(np.array(g.scres[:]), d["scres"])
 
 
-def test_vtk_round_trip_binary(pms_lib, tmp_path):
+@pytest.mark.parametrize("n", [1000, 400_000])
+def test_vtk_round_trip_binary(pms_lib, tmp_path, n):
+    # 400k particles take the threaded decode (more than 262144 values per array)
     rng = np.random.default_rng(0)
-    pos = rng.random((1000, 3)).astype(np.float32)
-    vel = rng.standard_normal((1000, 3)).astype(np.float32)
-    rho = (1000 + rng.random(1000)).astype(np.float32)
+    pos = rng.random((n, 3)).astype(np.float32)
+    vel = rng.standard_normal((n, 3)).astype(np.float32)
+    rho = (1000 + rng.random(n)).astype(np.float32)
     path = str(tmp_path / "PartFluid_0001.vtk")
     pms_lib.write_vtk(path, pos, vel, rho)
     p2, v2, r2 = pms_lib.read_vtk(path)
@@ -204,3 +206,45 @@ def test_derived_mc_tables_match_reference_counts_and_close_their_loops(pms_lib)
                 sides[key] = sides.get(key, 0) + (1 if x < y else -1)
         # interior diagonals cancel in direction; boundary sides (on faces) appear once
         assert all(v in (-1, 0, 1) for v in sides.values()), c
+
+
+def _read_ply(path):
+    """A small PLY reader (ascii / binary_little_endian; float xyz, uchar-uint faces)."""
+    raw = open(path, "rb").read()
+    end = raw.index(b"end_header\n") + len(b"end_header\n")
+    head = raw[:end].decode().splitlines()
+    fmt = head[1].split()[1]
+    nv = int([h for h in head if h.startswith("element vertex")][0].split()[2])
+    nf = int([h for h in head if h.startswith("element face")][0].split()[2])
+    body = raw[end:]
+    if fmt == "ascii":
+        toks = body.decode().split()
+        v = np.array(toks[: 3 * nv], np.float32).reshape(-1, 3)
+        f = np.array(toks[3 * nv:], np.int64).reshape(-1, 4)
+        assert np.all(f[:, 0] == 3)
+        return fmt, v, f[:, 1:]
+    v = np.frombuffer(body[: 12 * nv], "<f4").reshape(-1, 3)
+    rec = np.frombuffer(body[12 * nv: 12 * nv + 13 * nf], np.dtype([("n", "u1"), ("i", "<u4", 3)]))
+    assert np.all(rec["n"] == 3) and len(body) == 12 * nv + 13 * nf
+    return fmt, v, rec["i"].astype(np.int64)
+
+
+@pytest.mark.parametrize("binary", [False, True])
+def test_ply_indexed_and_binary_layouts(pms_lib, tmp_path, binary):
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(-1, 1, (10, 3)).astype(np.float32)
+    idx = np.array([[0, 1, 2], [2, 3, 4], [9, 8, 7]], np.uint32)
+    p = tmp_path / "m.ply"
+    pms_lib.write_ply_mesh(str(p), pos, idx, binary=binary)
+    fmt, v, f = _read_ply(str(p))
+    assert fmt == ("binary_little_endian" if binary else "ascii")
+    np.testing.assert_array_equal(v, pos)
+    np.testing.assert_array_equal(f, idx)
+    # the soup in binary: faces 3k, 3k+1, 3k+2
+    q = tmp_path / "s.ply"
+    pms_lib.write_ply_mesh(str(q), pos[:9], None, binary=True)
+    fmt, v, f = _read_ply(str(q))
+    np.testing.assert_array_equal(f, np.arange(9).reshape(-1, 3))
+    # an index past the vertices is refused
+    with pytest.raises(pms_lib.PmsError):
+        pms_lib.write_ply_mesh(str(p), pos, np.array([[0, 1, 10]], np.uint32))
