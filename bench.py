@@ -477,6 +477,10 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         for s, v in ctx.stage_times().items():
             stage_sum[s] += v
 
+    # every arm and both timings run the same sequence: the diffuse set carried between
+    # frames starts empty, so step i of each timing carries the particles of the
+    # warm-up frames and of the i steps before it
+    ctx.reset_diffuse()
     for _ in range(args.warmup):
         step_device()
     torch.cuda.synchronize()
@@ -488,16 +492,23 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
     ms = timer(step_device, args.steps, collect)
     launches = (ctx.launches - l0) // max(1, args.steps)
     clk = clocks.stop() if clocks else None
+    if diffuse:
+        # the carried set grows over the timed steps: its mean stands for the steps
+        end = ctx.counts().as_dict()
+        counts["n_diffuse_first_last"] = [int(counts["n_diffuse"]), int(end["n_diffuse"])]
+        counts["n_diffuse"] = (int(counts["n_diffuse"]) + int(end["n_diffuse"])) // 2
     # the host mesh buffer (pinned), sized from the frame's mesh
     host["mesh"] = torch.empty(max(3, int(3 * counts["n_mesh_vertices"] * 1.25)), dtype=torch.float32).pin_memory()
     ctx.stream_mesh_to_host(host["mesh"].data_ptr(), None, host["mesh"].numel() // 3)
     if diffuse:
-        # 32-byte records; the live set grows while the same frame repeats (particles live
-        # LifefimeMultiplier frames), so the buffer has room for several times the current set
-        cap = 4 * int(counts["n_diffuse"]) + 4 * int(counts["n_generated_diffuse"]) + (1 << 20)
+        # 32-byte records; the live set grows while the same frame repeats (a spawned
+        # particle lives LifefimeMultiplier frames per sibling), so the buffer has room for
+        # every particle the warm-up and timed frames spawn
+        cap = int(counts["n_generated_diffuse"]) * (args.warmup + args.steps + 2) + (1 << 20)
         host["dbuf"] = torch.empty(32 * cap, dtype=torch.uint8).pin_memory()
         ctx.stream_diffuse_to_host(host["dbuf"].data_ptr(), cap)
-    for _ in range(max(1, args.warmup // 2)):
+    ctx.reset_diffuse()
+    for _ in range(args.warmup):
         step_e2e()
     ms_e2e = timer(step_e2e, args.steps)
     ctx.stream_mesh_to_host(0, None, 0)
@@ -506,6 +517,38 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
     return {"ms": ms, "ms_e2e": ms_e2e, "counts": counts, "sp_size": grid.sp_size, "sc_size": grid.sc_size,
             "launches": launches, "clocks": clk, "stage_ms": {k: v / args.steps for k, v in stage_sum.items()},
             "h2d": 24 * n, "d2h": 12 * int(counts["n_mesh_vertices"]) + 32 * int(host.get("n_diffuse", 0))}
+
+
+def training_rate(pms, ctx, frame, stream, torch, batch: int = 8192, steps: int = 50) -> dict:
+    """Band-MLP training throughput on this frame's candidates (outside every timed
+    region): Adam steps of `batch` sampled cubes, forward and backward on the tensor
+    cores (k_learn_train, tcgen05) plus the Adam kernel, CUDA events on the stream."""
+    ctx.set_band_mode("plain")
+    ctx.upload(*frame)
+    ctx.build_grid()
+    ctx.surface()
+    n_cand, _ = ctx.learn_prepare()
+    tr = pms.Trainer(torch.cuda.current_device(), 1)
+    try:
+        for i in range(3):
+            tr.step(ctx, batch, i, 1e-3, 4.0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for i in range(steps):
+            tr.step(ctx, batch, 100 + i, 1e-3, 4.0, want_loss=False)
+        b.record(stream)
+        b.synchronize()
+        loss = tr.step(ctx, batch, 1000, 0.0, 4.0)
+        ms = a.elapsed_time(b) / steps
+    finally:
+        tr.close()
+    # forward 2*64*64 and backward 2*80*128 (M = 128 rows of dh and h over each sample)
+    # multiply-adds per sample on the tensor cores
+    flops = 2 * 64 * 64 + 2 * 128 * 80
+    return {"samples_per_s": batch / (ms / 1e3), "ms_per_step": ms, "batch": batch, "steps": steps,
+            "candidates": int(n_cand), "loss": loss, "tensor_flops_per_sample": flops,
+            "kernel": "k_learn_train (tcgen05.mma kind::f16, accumulators in tensor memory) + k_adam"}
 
 
 def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None) -> dict:
@@ -734,6 +777,8 @@ def run_pms(args) -> None:
                                      "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x the sampled SM clock"}
         line["stage_ms"] = stage_ms
         line["counts"] = head["counts"]
+    if not batched and not args.no_train and rank == 0:
+        line["training"] = training_rate(pms, ctx, frames[0], stream, torch)
     if judge:
         line["judge"] = judge
     if fp64 is not None:
@@ -761,6 +806,7 @@ def main() -> None:
     ap.add_argument("--model", default=LN.DEFAULT_MODEL)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-diffuse", action="store_true")
+    ap.add_argument("--no-train", action="store_true", help="skip timing the band-MLP training step")
     ap.add_argument("--no-judge", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the float64 oracle judge")
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference's own CUDA build")

@@ -261,6 +261,12 @@ typedef struct pms_diffuse_particle {
 pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_particle* out, uint64_t cap);
 pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n);
 
+/* Drops the diffuse particles carried between frames and restarts the frame
+ * counter that seeds the spawn, so the next frame starts a sequence as a fresh
+ * run does (the reference's DiffuseGeneration starts empty and has no reset;
+ * DiffuseGeneration.cu:21-87).  Waits for a streamed copy still in flight. */
+pms_status pms_reset_diffuse(pms_ctx* ctx);
+
 /* Intermediate arrays, for parity tests.  Bytes needed are written to *needed;
  * nothing is copied when dst is NULL or cap_bytes is too small. */
 typedef enum pms_array {

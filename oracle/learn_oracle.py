@@ -20,7 +20,8 @@ Definitions (the same as postmps_gb300/csrc/k_learn.cu):
     vertex above 0 and one below 0.5 (vertices outside the grid are 0);
   * network: h = relu(x W1 + b1), z = h.w2 + b2 with bf16 W1, w2;
   * loss: mean of pw*y*softplus(-z) + (1-y)*softplus(z);
-  * gradients with dh rounded to bf16 before dW1 = X^T dh.
+  * gradients from one bf16 product: dW1 = X^T dh, db1 = sum dh, dw2 = h^T dz with
+    dh, h and dz rounded to bf16.
 """
 from __future__ import annotations
 
@@ -175,8 +176,11 @@ def loss_and_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray, pos_weight: 
     dhq = bf16_round(dh.astype(np.float32)).astype(np.float64)
     g = np.zeros(N_PARAMS)
     g[:OFF_B1] = (np.asarray(x, np.float64).T @ dhq).reshape(-1)
-    g[OFF_B1:OFF_W2] = dh.sum(axis=0)
-    g[OFF_W2:OFF_B2] = (dz[:, None] * h).sum(axis=0)
+    # the kernel forms db1 and dw2 on the tensor cores too: dh, h and dz rounded to bf16
+    g[OFF_B1:OFF_W2] = dhq.sum(axis=0)
+    hq = bf16_round(h.astype(np.float32)).astype(np.float64)
+    dzq = bf16_round(dz.astype(np.float32)).astype(np.float64)
+    g[OFF_W2:OFF_B2] = (dzq[:, None] * hq).sum(axis=0)
     g[OFF_B2] = dz.sum()
     return loss, g
 

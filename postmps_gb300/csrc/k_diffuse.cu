@@ -61,6 +61,7 @@ struct DiffuseParams {
     float d2_eps;    // sqrt(x) > EPSILON_     <=>  x > d2_eps
     float d2_hd;     // sqrt(x) <= hd          <=>  x <= d2_hd
     float d2_q1;     // sqrt(x) / hd < 1       <=>  x <= d2_q1
+    float w_ad;      // the Wendland kernel's factor 21 / (16 pi hd^3), rounded to float
     uint64_t seed;
     uint32_t frame;
 };
@@ -71,7 +72,8 @@ __host__ __device__ __forceinline__ float spawn_uniform(uint64_t seed, uint32_t 
     x ^= x >> 30; x *= 0xBF58476D1CE4E5B9ull;
     x ^= x >> 27; x *= 0x94D049BB133111EBull;
     x ^= x >> 31;
-    return (float)((double)(x >> 40) * (1.0 / 16777216.0));
+    // a 24-bit integer times 2^-24: exact in float
+    return (float)(uint32_t)(x >> 40) * 0x1p-24f;
 }
 
 // a.b with every product and sum rounded on its own (x, y, z order)
@@ -317,7 +319,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
             const float u2 = spawn_uniform(dp.seed, dp.frame, 3 * idif + 2);
             const float r = dp.hd * sqrtf(u1);
             const float theta = u2 * 2.f * kPiF;
-            const float ct = (float)cos((double)theta), st = (float)sin((double)theta);
+            // cos(theta) and sin(theta) of a float theta are the single-precision
+            // functions in the reference's device code
+            float st, ct;
+            sincosf(theta, &st, &ct);
             DiffuseParticle d;
             d.px = p.x; d.py = p.y; d.pz = p.z;      // the reference overwrites the offset position with the parent's
             d.vx = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(r, ct), e1x), __fmul_rn(__fmul_rn(r, st), e2x)), v.x);
@@ -330,16 +335,73 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
     }
 }
 
+// The last factor of Wwendland, (float)((double)d * ((double)t + 1.0)) with d >= 0 and
+// t = 2q in [0, 4] floats, without the FP64 pipe (GB300 runs FP64 at a small fraction
+// of the FP32 rate, and this runs once per neighbour pair).  r = fma(d, t, d) is the
+// exact product P = d (1 + t) rounded once.  The double form rounds P to 53 bits and
+// then to 24; the two agree unless the 53-bit rounding lands exactly on a midpoint
+// between two floats, which needs P within 2^-53 |P| of that midpoint.  The residual
+// P - r is formed exactly from error-free transforms (TwoProduct by fma, Knuth's
+// TwoSum) and summed in float (error below 2^-21 ulp(r)); when it lies within
+// 2^-18 ulp(r) of half an ulp, or r is not a normal float well above the underflow
+// range, the double form is evaluated instead.  For t < 2^-29 the double sum t + 1
+// is itself rounded, but then P lies within 2^-29 |d| of the float d, far from any
+// midpoint, and both forms return d.
+#ifndef __CUDA_ARCH__
+// host forms of the rounded operations that no compiler may contract into an fma
+static inline float host_mul(float a, float b) { volatile float r = a * b; return r; }
+static inline float host_add(float a, float b) { volatile float r = a + b; return r; }
+static inline float host_sub(float a, float b) { volatile float r = a - b; return r; }
+#endif
+
+__host__ __device__ __forceinline__ float wendland_tail(float d, float t) {
+#ifdef __CUDA_ARCH__
+#define PMS_FMA(a, b, c) __fmaf_rn(a, b, c)
+#define PMS_MUL(a, b) __fmul_rn(a, b)
+#define PMS_ADD(a, b) __fadd_rn(a, b)
+#define PMS_SUB(a, b) __fsub_rn(a, b)
+#else
+#define PMS_FMA(a, b, c) std::fma(a, b, c)
+#define PMS_MUL(a, b) host_mul(a, b)
+#define PMS_ADD(a, b) host_add(a, b)
+#define PMS_SUB(a, b) host_sub(a, b)
+#endif
+    const float r = PMS_FMA(d, t, d);
+    const float ph = PMS_MUL(d, t), pl = PMS_FMA(d, t, -ph);          // d t = ph + pl
+    const float sm = PMS_ADD(d, ph), bb = PMS_SUB(sm, d);
+    const float e = PMS_ADD(PMS_SUB(d, PMS_SUB(sm, bb)), PMS_SUB(ph, bb));   // d + ph = sm + e
+    const float eps = PMS_ADD(PMS_ADD(PMS_SUB(sm, r), e), pl);              // P - r
+    uint32_t rb;
+    memcpy(&rb, &r, 4);
+    const uint32_t ex = (rb >> 23) & 0xffu;
+    bool exact_enough = ex >= 40u && ex < 255u && d >= 1.0e-30f;
+    if (exact_enough) {
+        const uint32_t hb = (ex - 24u) << 23;                            // half an ulp of r
+        float half;
+        memcpy(&half, &hb, 4);
+        const float gap = PMS_SUB(eps < 0.f ? -eps : eps, half);
+        exact_enough = (gap < 0.f ? -gap : gap) > PMS_MUL(half, 0x1p-17f);
+    }
+#undef PMS_FMA
+#undef PMS_MUL
+#undef PMS_ADD
+#undef PMS_SUB
+    return exact_enough ? r : (float)((double)d * ((double)t + 1.0));
+}
+
 // Wwendland, myCuda.cuh:391-401: ad and e1 are float variables set from double
-// expressions; ad*e1^4 runs in float, the last factor (2q + 1.) in double
-__device__ __forceinline__ float wendland(float rx, float ry, float rz, float h) {
+// expressions; ad*e1^4 runs in float, the last factor (2q + 1.) in double.  ad is a
+// constant of the frame (dp.w_ad, the same double expression evaluated on the host).
+// e1 = (float)(1.0 - q/2.0) is computed in float: for q in [0, 2] the double
+// difference is exact whenever q/2 >= 2^-30, and below that both forms give 1.0f, so
+// the one float rounding is the double form's.
+__device__ __forceinline__ float wendland(float rx, float ry, float rz, float h, float ad) {
     const float mx = __fsqrt_rn(dot_rn(rx, ry, rz, rx, ry, rz));
     const float q = __fdiv_rn(mx, h);
     if (q >= 0.f && q <= 2.f) {
-        const float ad = (float)(21.0 / (16.0 * (double)kPiF * (double)h * (double)h * (double)h));
-        const float e1 = (float)(1.0 - ((double)q / 2.0));
+        const float e1 = __fsub_rn(1.f, __fmul_rn(q, 0.5f));
         const float d = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(ad, e1), e1), e1), e1);
-        return (float)((double)d * ((double)__fmul_rn(2.0f, q) + 1.0));
+        return wendland_tail(d, __fmul_rn(2.0f, q));
     }
     return 0.f;
 }
@@ -385,7 +447,7 @@ __device__ __forceinline__ int count_within_near(const KGrid& g, const DiffusePa
     row_walk(g, make_float3(px, py, pz), lo, hi, r * r, 1e-4f * g.sp_cs, cell_start, [&](uint32_t j) {
         const float4 q = __ldg(&spos[j]);
         const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
-        if (__fsqrt_rn(dot_rn(sx, sy, sz, sx, sy, sz)) <= dp.hd) ++count;
+        if (dot_rn(sx, sy, sz, sx, sy, sz) <= dp.d2_hd) ++count;   // |s| <= hd
     });
     return count;
 }
@@ -406,9 +468,14 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParam
         const uint32_t t = perm[tt];
         DiffuseParticle d = old[t];
         const float px = d.px, py = d.py, pz = d.pz, vx = d.vx, vy = d.vy, vz = d.vz;
-        int density = 0;
+        // a particle that was spray last frame most likely still is, and spray moves with
+        // gravity alone: its neighbours within hd are counted first, and the walk over
+        // 2 hd that the velocity average needs runs only when that count says foam or
+        // bubble (then it counts again, the same particles in the same order)
+        int density = d.type == 0 ? count_within_near(g, dp, cell_start, spos, px, py, pz) : kSpray;
         float nx = 0.f, ny = 0.f, nz = 0.f, wsum = 0.f;
-        {
+        if (density >= kSpray) {
+            density = 0;
             uint3 lo, hi;
             diffuse_box(g, px, py, pz, lo, hi);
             hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
@@ -416,9 +483,9 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParam
             row_walk(g, make_float3(px, py, pz), lo, hi, r * r, 1e-4f * g.sp_cs, cell_start, [&](uint32_t j) {
                 const float4 q = __ldg(&spos[j]);
                 const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
-                if (__fsqrt_rn(dot_rn(sx, sy, sz, sx, sy, sz)) <= dp.hd) ++density;
+                if (dot_rn(sx, sy, sz, sx, sy, sz) <= dp.d2_hd) ++density;   // |s| <= hd
                 const float4 w = __ldg(&svel[j]);
-                const float tv = wendland(sx, sy, sz, dp.hd);
+                const float tv = wendland(sx, sy, sz, dp.hd, dp.w_ad);
                 nx = __fadd_rn(nx, __fmul_rn(w.x, tv));
                 ny = __fadd_rn(ny, __fmul_rn(w.y, tv));
                 nz = __fadd_rn(nz, __fmul_rn(w.z, tv));
@@ -519,6 +586,7 @@ static DiffuseParams diffuse_params(const pms_ctx* ctx) {
     d.d2_eps = largest_float_where(kEpsDown * kEpsDown, [](float x) { return std::sqrt(x) <= kEpsDown; });
     d.d2_hd = largest_float_where(d.hd * d.hd, [&](float x) { return std::sqrt(x) <= d.hd; });
     d.d2_q1 = largest_float_where(d.hd * d.hd, [&](float x) { return std::sqrt(x) / d.hd < 1.f; });
+    d.w_ad = (float)(21.0 / (16.0 * (double)kPiF * (double)d.hd * (double)d.hd * (double)d.hd));
     d.seed = ctx->cfg.rng_seed;
     d.frame = ctx->frame_index;
     return d;
@@ -702,6 +770,25 @@ extern "C" pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n) {
     if (ctx->dout_overflow)
         return pms_fail(ctx, PMS_ERR_CAPACITY, "%llu diffuse particles, the host buffer holds %llu",
                         (unsigned long long)ctx->dout_n, (unsigned long long)ctx->dout_cap);
+    return PMS_OK;
+}
+
+// The float form of Wwendland's last factor evaluated on the host, for tests (exported,
+// not part of pms.h's stable surface).
+extern "C" void pms_debug_wendland_tail(const float* d, const float* t, float* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = pms::wendland_tail(d[i], t[i]);
+}
+
+extern "C" pms_status pms_reset_diffuse(pms_ctx* ctx) {
+    if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    // the carried set is the source of a streamed copy until diffuse_copied fires
+    if (ctx->dout) PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
+    PMS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->diffuse_old = 0;
+    ctx->frame_index = 0;
+    ctx->dout_pending = false;
+    ctx->have_diffuse = false;
     return PMS_OK;
 }
 

@@ -658,9 +658,33 @@ __global__ void __launch_bounds__(256) k_features(KGrid g, LearnDims ld, const u
 }
 
 // ---------------------------------------------------------------------------
-// training: one block = 128 samples (8 groups of 16), 4 warps
+// Training on the fifth-generation tensor cores: one block = 128 samples, one
+// thread per sample (its tensor-memory lane).
+//   forward   D1 (128 x 64, fp32, tensor memory) = X (128 x 64, bf16, tensor
+//             memory, written by each thread to its own lane) . W1 (shared memory,
+//             the inference kernel's K-major layout); each thread reads its row back
+//             and forms pre, h, z, the loss and dz, dh = dz w2 [pre > 0].
+//   backward  D2 (128 x 80) = A2 (128 x 128 samples) . B2 (128 samples x 80), both
+//             K-major in shared memory (each thread writes its sample's column):
+//             A2 rows j < 64 hold dh[:, j], rows 64 + j hold h[:, j]; B2 columns
+//             f < 64 hold X[:, f], column 64 holds 1, column 65 dz, the rest 0.  So
+//             D2[j][f] = sum_s dh[s][j] X[s][f] (dW1 transposed), D2[j][64] =
+//             sum_s dh[s][j] (db1) and D2[64 + j][65] = sum_s h[s][j] dz[s] (dw2):
+//             all three gradients from one accumulator (dh, h, dz rounded to bf16,
+//             fp32 accumulation).  db2 and the loss are warp reductions.
+// One thread issues the MMAs; their completion arrives on an mbarrier whose waits
+// are bounded (a wait that runs out sets an error bit, waits once more for the
+// MMA in flight and frees the tensor memory).
 // ---------------------------------------------------------------------------
 static constexpr int kTrainThreads = 128, kBlockSamples = 128;
+static constexpr uint32_t kTrCols = 256;                 // tensor-memory columns of a block
+static constexpr uint32_t kTrColA = 64, kTrColD2 = 128;  // X (32 columns), D2 (80 columns)
+static constexpr uint32_t kTrN2 = 80;                     // D2 columns: 64 features, ones, dz, zero padding
+static constexpr uint32_t kTrBytesA2 = 128u * 128u * 2u, kTrBytesB2 = kTrN2 * 128u * 2u;
+static constexpr uint32_t kTrSmem = 1024u + kTcBytesB + kTrBytesA2 + kTrBytesB2 + kBlockSamples * kIn * 2 +
+                                    kBlockSamples * 4 + 2 * kHid * 4 + 64;
+constexpr uint32_t kTrIdesc2 = (1u << 4) | (1u << 7) | (1u << 10) | ((kTrN2 >> 3) << 17) | ((128u >> 4) << 24);
+static_assert(kTrN2 % 16 == 0 && kTrColD2 + kTrN2 <= kTrCols && kTrColA + 32 <= kTrColD2, "tensor-memory plan");
 
 struct TrainIn {
     // source A: sampled candidates of a frame
@@ -676,21 +700,65 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
+// byte offset of element (row r, k) of a K-major operand with 128 K elements (bf16)
+__device__ __forceinline__ uint32_t umma_off128(uint32_t r, uint32_t k) {
+    return ((((r >> 3) << 4) + (k >> 3)) << 7) + ((r & 7u) << 4) + ((k & 7u) << 1);
+}
+// the descriptor of such an operand: core matrices 128 bytes apart along K, 8-row
+// groups 2048 bytes apart
+__device__ __forceinline__ uint64_t umma_desc128(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(2048u >> 4) << 32) |
+           (1ull << 46);
+}
+// A and B from shared memory
+__device__ __forceinline__ void tc_mma_ss(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// a bounded wait on the mbarrier phase, block-wide; false when it ran out (then the
+// MMA in flight had a second bounded wait and err holds the reason)
+__device__ bool tr_wait(uint32_t bar, uint32_t parity, uint32_t* err) {
+    bool done = false;
+    for (uint32_t spins = 0; spins < kTcSpin && !(done = mbar_try(bar, parity)); ++spins) {
+    }
+    if (__syncthreads_and(done)) return true;
+    if (threadIdx.x == 0) {
+        uint32_t again = 0;
+        bool landed = false;
+        while (!(landed = mbar_try(bar, parity)) && ++again < kTcSpin) {
+        }
+        atomicOr(err, landed ? kErrTimeout : (kErrTimeout | kErrTcLost));
+    }
+    __syncthreads();
+    return false;
+}
+
 __global__ void __launch_bounds__(kTrainThreads) k_learn_train(KGrid g, LearnDims ld, TrainIn in,
                                                                const DevModel* __restrict__ model, float* __restrict__ grad,
-                                                               float* __restrict__ loss_sum) {
-    __shared__ uint16_t s_x[kBlockSamples][kIn];
-    __shared__ uint16_t s_dh[kBlockSamples][kHid];
-    __shared__ float s_y[kBlockSamples];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+                                                               float* __restrict__ loss_sum, uint32_t* __restrict__ err) {
+    extern __shared__ uint8_t tr_smem[];
+    uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(tr_smem) + 1023u) & ~(uintptr_t)1023u);
+    uint8_t* sW1 = sm;
+    uint8_t* sA2 = sW1 + kTcBytesB;
+    uint8_t* sB2 = sA2 + kTrBytesA2;
+    uint16_t* s_x = reinterpret_cast<uint16_t*>(sB2 + kTrBytesB2);        // [sample][feature]
+    float* s_y = reinterpret_cast<float*>(s_x + kBlockSamples * kIn);
+    float* s_b1 = s_y + kBlockSamples;
+    float* s_w2 = s_b1 + kHid;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_w2 + kHid);
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(s_bar + 1);
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t s_base = blockIdx.x * kBlockSamples;
     const float inv_batch = 1.f / (float)in.batch;
-    // gather features and labels of the block's samples (invalid rows: zero, weight 0)
-    for (int e = tid; e < kBlockSamples * kIn; e += kTrainThreads) {
-        const int r = e / kIn, f = e % kIn;
+    // features and labels of the block's samples (rows past the batch: zero, label -1)
+    for (uint32_t e = tid; e < (uint32_t)(kBlockSamples * kIn); e += kTrainThreads) {
+        const uint32_t r = e / kIn, f = e % kIn;
         const uint32_t s = s_base + r;
         uint16_t v = 0;
-        float y = -1.f;                               // -1 marks a padding row
+        float y = -1.f;
         if (s < in.batch) {
             if (in.x) {
                 v = in.x[(size_t)s * kIn + f];
@@ -700,7 +768,7 @@ __global__ void __launch_bounds__(kTrainThreads) k_learn_train(KGrid g, LearnDim
                 const uint32_t id = in.cand[slot];
                 const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
                 const int c[3] = {(int)(id % rx), (int)((id / rx) % g.scres[1]), (int)(id / rxy)};
-                const int d[3] = {f & 3, (f >> 2) & 3, f >> 4};
+                const int d[3] = {(int)(f & 3u), (int)((f >> 2) & 3u), (int)(f >> 4)};
                 int cc[3];
                 bool inside = true;
 #pragma unroll
@@ -713,145 +781,142 @@ __global__ void __launch_bounds__(kTrainThreads) k_learn_train(KGrid g, LearnDim
                 y = ((in.labels[id >> 5] >> (id & 31u)) & 1u) ? 1.f : 0.f;
             }
         }
-        s_x[r][f] = v;
+        s_x[r * kIn + f] = v;
         if (f == 0) s_y[r] = y;
     }
+    // W1 as the forward's B operand (row j = hidden unit, K = input feature i)
+    for (uint32_t e = tid; e < (uint32_t)(kHid * kIn / 2); e += kTrainThreads) {
+        const uint32_t j = e / (kIn / 2), i = (e % (kIn / 2)) * 2;
+        *reinterpret_cast<uint32_t*>(sW1 + umma_off(j, i)) = pack_raw(model->w1[i * kHid + j], model->w1[(i + 1) * kHid + j]);
+    }
+    if (tid < (uint32_t)kHid) {
+        s_b1[tid] = model->b1[tid];
+        s_w2[tid] = bf16_to_f(model->w2[tid]);
+    }
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(s_bar);
+    if (tid == 0) mbar_init(bar, 1);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(s_tmem)),
+                     "r"(kTrCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_before_sync();
     __syncthreads();
-    uint32_t b[4][8][2];
-    load_w1_frags(model, b, lane);
-    const int kq = (lane & 3) * 2;
-    float b1v[8][2], w2v[8][2], g_w2[8][2], g_b1[8][2];
+    tc_after_sync();
+    const uint32_t tmem = *s_tmem;
+    const uint32_t t_row = tmem + ((warp * 32u) << 16);
+    // forward: this sample's features into its lane, then D1 = X W1
+    {
+        uint32_t xr[32];
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
+        for (int i = 0; i < 32; ++i) xr[i] = pack_raw(s_x[tid * kIn + 2 * i], s_x[tid * kIn + 2 * i + 1]);
+        tc_st32(t_row + kTrColA, xr);
+    }
+    tc_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+        tc_after_sync();
+        const uint32_t w_saddr = (uint32_t)__cvta_generic_to_shared(sW1);
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int j = nt * 8 + kq + e;
-            b1v[nt][e] = model->b1[j];
-            w2v[nt][e] = bf16_to_f(model->w2[j]);
-            g_w2[nt][e] = g_b1[nt][e] = 0.f;
+        for (uint32_t kk = 0; kk < 4; ++kk) tc_mma_ts(tmem, tmem + kTrColA + 8u * kk, umma_desc(w_saddr + kk * 256u), kk);
+        tc_commit(bar);
+    }
+    bool ok = tr_wait(bar, 0, err);
+    float dz = 0.f, lsum = 0.f;
+    if (ok) {
+        tc_after_sync();
+        float acc[kHid];
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            float v[16];
+            tc_ld16(t_row + q * 16u, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc[q * 16 + i] = v[i] + s_b1[q * 16 + i];
         }
-    float g_b2 = 0.f, lsum = 0.f;
-    const float b2 = model->b2;
-    // phase 1: forward and the per-sample backward, two groups of 16 per warp
-    for (int grp = warp; grp < kBlockSamples / 16; grp += kTrainThreads / 32) {
-        const int r0 = grp * 16 + (lane >> 2), r1 = r0 + 8;
-        float acc[8][4];
+        float z = model->b2;
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-            const int c = kk * 16 + kq;
-            uint32_t a[4];
-            a[0] = pack_raw(s_x[r0][c], s_x[r0][c + 1]);
-            a[1] = pack_raw(s_x[r1][c], s_x[r1][c + 1]);
-            a[2] = pack_raw(s_x[r0][c + 8], s_x[r0][c + 9]);
-            a[3] = pack_raw(s_x[r1][c + 8], s_x[r1][c + 9]);
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) mma_bf16(acc[nt], a, b[kk][nt][0], b[kk][nt][1]);
-        }
-        float z0 = 0.f, z1 = 0.f;
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                acc[nt][e] += b1v[nt][e];
-                acc[nt][2 + e] += b1v[nt][e];
-                z0 += fmaxf(acc[nt][e], 0.f) * w2v[nt][e];
-                z1 += fmaxf(acc[nt][2 + e], 0.f) * w2v[nt][e];
-            }
-        z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
-        z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
-        z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
-        z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
-        z0 += b2;
-        z1 += b2;
-        float dz[2];
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float z = r ? z1 : z0, y = s_y[r ? r1 : r0];
-            if (y < 0.f) { dz[r] = 0.f; continue; }
+        for (int j = 0; j < kHid; ++j) z += fmaxf(acc[j], 0.f) * s_w2[j];
+        const float y = s_y[tid];
+        if (y >= 0.f) {
             const float p = 1.f / (1.f + expf(-z));
             const float wy = in.pos_weight * y;
-            dz[r] = (p * (wy + 1.f - y) - wy) * inv_batch;
+            dz = (p * (wy + 1.f - y) - wy) * inv_batch;
             // softplus(-z) = -log sigmoid(z), softplus(z) = -log(1 - sigmoid(z))
             const float sp_pos = fmaxf(-z, 0.f) + log1pf(expf(-fabsf(z)));
             const float sp_neg = fmaxf(z, 0.f) + log1pf(expf(-fabsf(z)));
-            if ((lane & 3) == 0) lsum += (wy * sp_pos + (1.f - y) * sp_neg) * inv_batch;
+            lsum = (wy * sp_pos + (1.f - y) * sp_neg) * inv_batch;
         }
+        // this sample's column of A2 (dh, then h) and of B2 (x, 1, dz, 0)
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int j = nt * 8 + kq + e;
-#pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const float pre = acc[nt][2 * r + e];
-                    const float h = fmaxf(pre, 0.f);
-                    const float dh = pre > 0.f ? dz[r] * w2v[nt][e] : 0.f;
-                    g_w2[nt][e] += dz[r] * h;
-                    g_b1[nt][e] += dh;
-                    s_dh[r ? r1 : r0][j] = __bfloat16_as_ushort(__float2bfloat16_rn(dh));
-                }
-            }
-        if ((lane & 3) == 0) g_b2 += dz[0] + dz[1];
+        for (int j = 0; j < kHid; ++j) {
+            const float dh = acc[j] > 0.f ? dz * s_w2[j] : 0.f;
+            *reinterpret_cast<uint16_t*>(sA2 + umma_off128((uint32_t)j, tid)) = __bfloat16_as_ushort(__float2bfloat16_rn(dh));
+            *reinterpret_cast<uint16_t*>(sA2 + umma_off128((uint32_t)(kHid + j), tid)) =
+                __bfloat16_as_ushort(__float2bfloat16_rn(fmaxf(acc[j], 0.f)));
+        }
     }
-    __syncthreads();
-    // phase 2: dW1 rows 16*warp .. 16*warp+15 = X^T dh over the block's 128 samples
-    {
-        float acc[8][4];
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-        const int i0 = warp * 16 + (lane >> 2);
-        for (int ks = 0; ks < kBlockSamples / 16; ++ks) {
-            const int s0 = ks * 16 + kq;
-            uint32_t a[4];
-            a[0] = pack_raw(s_x[s0][i0], s_x[s0 + 1][i0]);
-            a[1] = pack_raw(s_x[s0][i0 + 8], s_x[s0 + 1][i0 + 8]);
-            a[2] = pack_raw(s_x[s0 + 8][i0], s_x[s0 + 9][i0]);
-            a[3] = pack_raw(s_x[s0 + 8][i0 + 8], s_x[s0 + 9][i0 + 8]);
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                const int j = nt * 8 + (lane >> 2);
-                const uint32_t b0 = pack_raw(s_dh[s0][j], s_dh[s0 + 1][j]);
-                const uint32_t b1 = pack_raw(s_dh[s0 + 8][j], s_dh[s0 + 9][j]);
-                mma_bf16(acc[nt], a, b0, b1);
-            }
-        }
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int j = nt * 8 + kq + e;
-                atomicAdd(&grad[i0 * kHid + j], acc[nt][e]);
-                atomicAdd(&grad[(i0 + 8) * kHid + j], acc[nt][2 + e]);
-            }
+#pragma unroll 8
+    for (uint32_t n = 0; n < kTrN2; ++n) {
+        const uint16_t v = n < (uint32_t)kIn ? s_x[tid * kIn + n]
+                                             : (n == (uint32_t)kIn ? (uint16_t)0x3F80u
+                                                                   : (n == (uint32_t)kIn + 1u ? __bfloat16_as_ushort(__float2bfloat16_rn(dz))
+                                                                                              : (uint16_t)0u));
+        *reinterpret_cast<uint16_t*>(sB2 + umma_off128(n, tid)) = v;
     }
-    // the per-column sums: lanes with equal (lane & 3) hold the same columns
+    // db2 and the loss, one atomic per warp
+    float gb2 = dz;
 #pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            float a = g_w2[nt][e], c = g_b1[nt][e];
-#pragma unroll
-            for (int o = 4; o < 32; o <<= 1) {
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                c += __shfl_xor_sync(0xffffffffu, c, o);
-            }
-            if (lane < 4) {
-                const int j = nt * 8 + kq + e;
-                atomicAdd(&grad[kOffW2 + j], a);
-                atomicAdd(&grad[kOffB1 + j], c);
-            }
-        }
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        g_b2 += __shfl_xor_sync(0xffffffffu, g_b2, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        gb2 += __shfl_xor_sync(0xffffffffu, gb2, o);
         lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
     }
-    if (lane == 0) {
-        atomicAdd(&grad[kOffB2], g_b2);
+    if (ok && lane == 0) {
+        atomicAdd(&grad[kOffB2], gb2);
         atomicAdd(loss_sum, lsum);
     }
+    // backward: D2 = A2 B2 over the block's 128 samples
+    fence_async_smem();
+    tc_before_sync();
+    __syncthreads();
+    if (ok) {
+        if (tid == 0) {
+            tc_after_sync();
+            const uint32_t a_saddr = (uint32_t)__cvta_generic_to_shared(sA2), b_saddr = (uint32_t)__cvta_generic_to_shared(sB2);
+#pragma unroll
+            for (uint32_t kk = 0; kk < 8; ++kk)
+                tc_mma_ss(tmem + kTrColD2, umma_desc128(a_saddr + kk * 256u), umma_desc128(b_saddr + kk * 256u), kTrIdesc2, kk);
+            tc_commit(bar);
+        }
+        ok = tr_wait(bar, 1, err);
+    }
+    if (ok) {
+        tc_after_sync();
+        if (warp < 2) {
+            // row j = tid: dW1[f][j] for f < 64 and db1[j]
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) {
+                float v[16];
+                tc_ld16(t_row + kTrColD2 + q * 16u, v);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) atomicAdd(&grad[(q * 16 + i) * kHid + tid], v[i]);
+            }
+            float v[16];
+            tc_ld16(t_row + kTrColD2 + 64u, v);
+            atomicAdd(&grad[kOffB1 + tid], v[0]);
+        } else {
+            // row 64 + j: dw2[j] in column 65
+            float v[16];
+            tc_ld16(t_row + kTrColD2 + 64u, v);
+            atomicAdd(&grad[kOffW2 + tid - kHid], v[1]);
+        }
+    }
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTrCols) : "memory");
 }
 
 // Adam on the fp32 master parameters, then the bf16 / fp32 model copy
@@ -979,7 +1044,7 @@ pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint
 }
 
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,
-                         float* loss_sum) {
+                         float* loss_sum, uint32_t* err) {
     KGrid g = {};
     LearnDims ld = {};
     TrainIn in = {};
@@ -997,7 +1062,9 @@ cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainAr
     in.seed = a.seed;
     in.pos_weight = a.pos_weight;
     const unsigned blocks = (a.batch + kBlockSamples - 1) / kBlockSamples;
-    k_learn_train<<<blocks, kTrainThreads, 0, stream>>>(g, ld, in, model, grad, loss_sum);
+    const cudaError_t e = cudaFuncSetAttribute(k_learn_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrSmem);
+    if (e != cudaSuccess) return e;
+    k_learn_train<<<blocks, kTrainThreads, kTrSmem, stream>>>(g, ld, in, model, grad, loss_sum, err);
     return cudaGetLastError();
 }
 

@@ -217,8 +217,11 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                 if (!(ef & (1u << e))) continue;
                 const int a = edge_end(e, 0), b = edge_end(e, 1);
                 const float d = cf[b] - cf[a];
-                // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5
-                const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - cf[a]) / d;
+                // getLerpFac: |delta| < 1e-7 (a double literal) -> 0.5.  1e-7f, the float
+                // nearest 1e-7, lies above it and no float lies between them, so for a float
+                // delta the double test is |delta| < 1e-7f: the same decision without the
+                // FP64 pipe
+                const float tt = fabsf(d) < 1.0e-7f ? 0.5f : (iso - cf[a]) / d;
                 const float ax = px[corner_off(a, 0)], ay = py[corner_off(a, 1)], az = pz[corner_off(a, 2)];
                 const float bx = px[corner_off(b, 0)], by = py[corner_off(b, 1)], bz = pz[corner_off(b, 2)];
                 float q[kS];
@@ -437,7 +440,7 @@ __global__ void __launch_bounds__(256) k_weld_vertices(KGrid g, float iso, const
             const int X = x + (axis == 0), Y = y + (axis == 1), Z = z + (axis == 2);
             const float fa = grid_value(g, fdense, x, y, z), fb = grid_value(g, fdense, X, Y, Z);
             const float d = fb - fa;
-            const float tt = ((double)d > -1.0e-7 && (double)d < 1.0e-7) ? 0.5f : (iso - fa) / d;
+            const float tt = fabsf(d) < 1.0e-7f ? 0.5f : (iso - fa) / d;   // getLerpFac's test, as above
             const float ax = sc_coord_i(g, x, 0), ay = sc_coord_i(g, y, 1), az = sc_coord_i(g, z, 2);
             const float bx = sc_coord_i(g, X, 0), by = sc_coord_i(g, Y, 1), bz = sc_coord_i(g, Z, 2);
             vert[3 * (size_t)r + 0] = ax + tt * (bx - ax);

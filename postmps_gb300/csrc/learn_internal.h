@@ -53,8 +53,10 @@ pms_status ensure_learned_buffers(pms_ctx* ctx, uint64_t sc_size, uint32_t nv);
 pms_status learned_split(pms_ctx* ctx, bool predict);
 pms_status learned_field(pms_ctx* ctx);
 pms_status launch_features(pms_ctx* ctx, const uint32_t* cubes, uint32_t n, uint16_t* x);
+// one training pass over a batch on the tensor cores; err collects kErrTimeout /
+// kErrTcLost when a bounded wait on the MMAs ran out
 cudaError_t launch_train(const pms_ctx* data, cudaStream_t stream, const TrainArgs& a, const DevModel* model, float* grad,
-                         float* loss_sum);
+                         float* loss_sum, uint32_t* err);
 cudaError_t launch_adam(cudaStream_t stream, float* w, const float* grad, float* m, float* v, const AdamParams& ap,
                         DevModel* model);
 

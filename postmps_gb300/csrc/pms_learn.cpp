@@ -273,7 +273,7 @@ extern "C" pms_status pms_learn_features(pms_ctx* c, const uint32_t* ids, uint32
 struct pms_trainer {
     int device = 0;
     cudaStream_t stream = nullptr;
-    DBuf w, m, v, grad, model, loss, x, y;
+    DBuf w, m, v, grad, model, loss, x, y, err;
     uint64_t step = 0;
 };
 
@@ -301,7 +301,8 @@ extern "C" pms_status pms_trainer_create(int device, uint64_t seed, pms_trainer*
     const size_t P = sizeof(float) * kNumParams;
     bool ok = cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) == cudaSuccess && t->w.ensure(P) == cudaSuccess &&
               t->m.ensure(P) == cudaSuccess && t->v.ensure(P) == cudaSuccess && t->grad.ensure(P) == cudaSuccess &&
-              t->model.ensure(sizeof(DevModel)) == cudaSuccess && t->loss.ensure(sizeof(float)) == cudaSuccess;
+              t->model.ensure(sizeof(DevModel)) == cudaSuccess && t->loss.ensure(sizeof(float)) == cudaSuccess &&
+              t->err.ensure(sizeof(uint32_t)) == cudaSuccess;
     if (ok) {
         // He-uniform first layer, small second layer, zero biases
         std::vector<float> w(kNumParams, 0.f);
@@ -312,6 +313,7 @@ extern "C" pms_status pms_trainer_create(int device, uint64_t seed, pms_trainer*
         ok = cudaMemcpy(t->w.p, w.data(), P, cudaMemcpyHostToDevice) == cudaSuccess &&
              cudaMemset(t->m.p, 0, P) == cudaSuccess && cudaMemset(t->v.p, 0, P) == cudaSuccess &&
              cudaMemset(t->grad.p, 0, P) == cudaSuccess && cudaMemset(t->model.p, 0, sizeof(DevModel)) == cudaSuccess &&
+             cudaMemset(t->err.p, 0, sizeof(uint32_t)) == cudaSuccess &&
              refresh_model(t) == PMS_OK;
     }
     if (!ok) { pms_trainer_destroy(t); return PMS_ERR_CUDA; }
@@ -323,7 +325,7 @@ extern "C" void pms_trainer_destroy(pms_trainer* t) {
     if (!t) return;
     cudaSetDevice(t->device);
     if (t->stream) cudaStreamSynchronize(t->stream);
-    for (DBuf* b : {&t->w, &t->m, &t->v, &t->grad, &t->model, &t->loss, &t->x, &t->y}) b->release();
+    for (DBuf* b : {&t->w, &t->m, &t->v, &t->grad, &t->model, &t->loss, &t->x, &t->y, &t->err}) b->release();
     if (t->stream) cudaStreamDestroy(t->stream);
     delete t;
 }
@@ -342,7 +344,8 @@ extern "C" pms_status pms_trainer_step(pms_trainer* t, pms_ctx* c, uint32_t batc
     a.batch = batch;
     a.seed = seed;
     a.pos_weight = pos_weight;
-    PMS_CUDA(c, launch_train(c, c->stream, a, t->model.as<DevModel>(), t->grad.as<float>(), t->loss.as<float>()));
+    PMS_CUDA(c, launch_train(c, c->stream, a, t->model.as<DevModel>(), t->grad.as<float>(), t->loss.as<float>(),
+                             t->err.as<uint32_t>()));
     c->launches++;
     t->step++;
     AdamParams ap;
@@ -354,7 +357,11 @@ extern "C" pms_status pms_trainer_step(pms_trainer* t, pms_ctx* c, uint32_t batc
     c->launches++;
     if (loss) {
         PMS_CUDA(c, cudaMemcpyAsync(loss, t->loss.p, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        uint32_t e = 0;
+        PMS_CUDA(c, cudaMemcpyAsync(&e, t->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
         PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (e) return pms_fail(c, PMS_ERR_CUDA, "a wait on the tensor cores timed out in a training step%s",
+                               (e & kErrTcLost) ? "; destroy this context" : "");
     }
     return PMS_OK;
 }
@@ -371,15 +378,19 @@ extern "C" pms_status pms_trainer_grad(pms_trainer* t, const uint16_t* x, const 
     a.batch = batch;
     a.pos_weight = pos_weight;
     float l = 0.f;
+    uint32_t e = 0;
     if (cudaMemcpyAsync(t->x.p, x, 128 * (size_t)batch, cudaMemcpyHostToDevice, t->stream) != cudaSuccess ||
         cudaMemcpyAsync(t->y.p, y, batch, cudaMemcpyHostToDevice, t->stream) != cudaSuccess ||
         cudaMemsetAsync(t->grad.p, 0, P, t->stream) != cudaSuccess ||
         cudaMemsetAsync(t->loss.p, 0, sizeof(float), t->stream) != cudaSuccess ||
-        launch_train(nullptr, t->stream, a, t->model.as<DevModel>(), t->grad.as<float>(), t->loss.as<float>()) != cudaSuccess ||
+        launch_train(nullptr, t->stream, a, t->model.as<DevModel>(), t->grad.as<float>(), t->loss.as<float>(),
+                     t->err.as<uint32_t>()) != cudaSuccess ||
         cudaMemcpyAsync(grad, t->grad.p, P, cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
         cudaMemcpyAsync(&l, t->loss.p, sizeof(float), cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
+        cudaMemcpyAsync(&e, t->err.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, t->stream) != cudaSuccess ||
         cudaStreamSynchronize(t->stream) != cudaSuccess)
         return PMS_ERR_CUDA;
+    if (e) return PMS_ERR_TIMEOUT;
     if (loss) *loss = l;
     return PMS_OK;
 }

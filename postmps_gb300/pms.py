@@ -544,6 +544,10 @@ class Context:
         self._call("pms_wait_diffuse", C.byref(n))
         return n.value
 
+    def reset_diffuse(self) -> None:
+        """Drop the carried diffuse particles and restart the spawn's frame counter."""
+        self._call("pms_reset_diffuse")
+
     def diffuse_particles(self, type_: int = -1) -> dict:
         n = C.c_uint32()
         st = lib().pms_download_diffuse(self._h, type_, None, None, None, None, None, None, None, 0, C.byref(n))
@@ -617,10 +621,13 @@ class Trainer:
         except Exception:
             pass
 
-    def step(self, ctx: "Context", batch: int, seed: int, lr: float, pos_weight: float) -> float:
+    def step(self, ctx: "Context", batch: int, seed: int, lr: float, pos_weight: float, want_loss: bool = True):
+        """One Adam step on a batch sampled from ctx's prepared candidates, on ctx's
+        stream; returns the batch loss (a synchronisation), or None without waiting."""
         loss = C.c_float()
-        _check(lib().pms_trainer_step(self._h, ctx.handle, batch, seed, lr, pos_weight, C.byref(loss)), ctx.handle)
-        return float(loss.value)
+        _check(lib().pms_trainer_step(self._h, ctx.handle, batch, seed, lr, pos_weight,
+                                      C.byref(loss) if want_loss else None), ctx.handle)
+        return float(loss.value) if want_loss else None
 
     def grad(self, x_bf16: np.ndarray, y: np.ndarray, pos_weight: float) -> tuple[np.ndarray, float]:
         x = np.ascontiguousarray(x_bf16, np.uint16)

@@ -191,6 +191,20 @@ def test_streamed_diffuse_particles_equal_downloaded(pms_lib, tmp_config):
             np.testing.assert_array_equal(rec["vel"][:n], live["vel"])
             np.testing.assert_array_equal(rec["ttl"][:n], live["ttl"])
             np.testing.assert_array_equal(rec["type"][:n], live["type"])
+        # a reset starts the sequence again: the first frame's live set comes back
+        ctx.reset_diffuse()
+        first = []
+        for fr in range(2):
+            ctx.upload((pos + np.float32(0.004 * fr) * vel).astype(np.float32), vel, rho)
+            ctx.run_frame()
+            first.append(rec[: ctx.wait_diffuse()].copy())
+        with pms.Context(cfg, 0) as fresh:
+            for fr in range(2):
+                fresh.upload((pos + np.float32(0.004 * fr) * vel).astype(np.float32), vel, rho)
+                fresh.run_frame()
+                live = fresh.diffuse_particles(-1)
+                np.testing.assert_array_equal(first[fr]["pos"], live["pos"])
+                np.testing.assert_array_equal(first[fr]["ttl"], live["ttl"])
         # too small a buffer: the count comes back with PMS_ERR_CAPACITY
         ctx.stream_diffuse_to_host(C.addressof(buf), 1)
         ctx.upload(pos, vel, rho)

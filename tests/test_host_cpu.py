@@ -248,3 +248,64 @@ def test_ply_indexed_and_binary_layouts(pms_lib, tmp_path, binary):
     # an index past the vertices is refused
     with pytest.raises(pms_lib.PmsError):
         pms_lib.write_ply_mesh(str(p), pos, np.array([[0, 1, 10]], np.uint32))
+
+
+def test_float_form_of_the_double_lerp_threshold():
+    """The emission decides getLerpFac's |delta| < 1e-7 (a double literal) on the float
+    delta as |delta| < 1e-7f; both give the same answer for every float, checked on the
+    floats around the threshold and on a spread of magnitudes."""
+    t = np.float32(1e-7)
+    near = [t]
+    for _ in range(64):
+        near.append(np.nextafter(near[-1], np.float32(1)))
+    lo = [t]
+    for _ in range(64):
+        lo.append(np.nextafter(lo[-1], np.float32(0)))
+    rng = np.random.default_rng(5)
+    d = np.concatenate([np.array(near + lo, np.float32),
+                        (10.0 ** rng.uniform(-12, 2, 100000)).astype(np.float32),
+                        np.array([0.0, np.float32(1e-45)], np.float32)])
+    d = np.concatenate([d, -d])
+    ref = (d.astype(np.float64) > -1.0e-7) & (d.astype(np.float64) < 1.0e-7)
+    np.testing.assert_array_equal(ref, np.abs(d) < np.float32(1e-7))
+
+
+def test_float_form_of_the_wendland_tail(pms_lib):
+    """The diffuse update evaluates Wwendland's last factor (float)((double)d *
+    ((double)(2q) + 1.0)) in float (one fma, an exact residual and a midpoint test
+    that falls back to the double form); it returns the double form's bits for every
+    input, here over log-uniform and integer-valued d, the whole t = 2q range, tiny t
+    and the floats next to 0, 1, 2 and 4."""
+    rng = np.random.default_rng(11)
+    n = 1 << 20
+    d = np.concatenate([(10.0 ** rng.uniform(-30, 6, n)).astype(np.float32),
+                        rng.integers(1, 1 << 24, n).astype(np.float32),
+                        np.array([0.0, 1e-45, 1e-38, 1.0, 3.0, 16777215.0], np.float32)])
+    t = np.concatenate([rng.uniform(0, 4, n).astype(np.float32),
+                        (10.0 ** rng.uniform(-14, 0.6, n)).astype(np.float32),
+                        np.array([0.0, 1e-45, 2.0 ** -29, 2.0 ** -30, 1.0, 4.0], np.float32)])
+    edge = []
+    for c in (0.0, 1.0, 2.0, 4.0):
+        x = np.float32(c)
+        for _ in range(200):
+            x = np.nextafter(x, np.float32(-1))
+            if x >= 0:
+                edge.append(x)
+        x = np.float32(c)
+        for _ in range(200):
+            x = np.nextafter(x, np.float32(5))
+            if x <= 4:
+                edge.append(x)
+    edge = np.array(edge, np.float32)
+    d = np.concatenate([d, rng.choice(d, len(edge))]).astype(np.float32)
+    t = np.concatenate([t, edge]).astype(np.float32)
+    d, t = np.ascontiguousarray(d), np.ascontiguousarray(t)
+    out = np.empty_like(d)
+    L = pms_lib.lib()
+    f = L.pms_debug_wendland_tail
+    f.restype = None
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]
+    f(d.ctypes.data, t.ctypes.data, out.ctypes.data, len(d))
+    want = (d.astype(np.float64) * (t.astype(np.float64) + 1.0)).astype(np.float32)
+    bad = np.flatnonzero(out.view(np.uint32) != want.view(np.uint32))
+    assert bad.size == 0, (d[bad[:5]], t[bad[:5]], out[bad[:5]], want[bad[:5]])
