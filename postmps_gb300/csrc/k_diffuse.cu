@@ -177,7 +177,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
             }
         });
         pot[i].y = ita;
-        pot[i].z = (float)(0.5 * (double)dp.mass * (double)(v.x * v.x + v.y * v.y + v.z * v.z));
+        // 0.5 * (double)m * (double)|v|^2 rounded to float: the double product of two floats
+        // is exact and the halving too, so it is the float product rounded once, halved (the
+        // two could differ only for energies below the normal float range, ~1e-38)
+        pot[i].z = 0.5f * __fmul_rn(dp.mass, v.x * v.x + v.y * v.y + v.z * v.z);
     }
 }
 

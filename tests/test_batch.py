@@ -124,6 +124,7 @@ def test_autotune_keeps_results_and_shapes_agree(pms_lib):
             ctx.set_tune(shape)
             cs, mesh = _single(ctx, frames[1])
             assert np.array_equal(mesh, ref_mesh)
+            assert np.array_equal(ctx.debug("field"), ref_field), shape
         with pytest.raises(pms.PmsError):
             ctx.set_tune({"field_threads": 96, "field_waves": 1, "density_threads": 64, "moments_threads": 64})
 
