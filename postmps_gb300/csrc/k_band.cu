@@ -205,6 +205,9 @@ __global__ void __launch_bounds__(kTileThreads) k_band_tiles(KGrid g, float h, i
                         if (!xin || my_y < (int)(yz & 0xffu) || my_y > (int)((yz >> 8) & 0xffu) ||
                             my_z < (int)((yz >> 16) & 0xffu) || my_z > (int)(yz >> 24))
                             continue;
+                        // marks are an OR: a particle whose x positions in this row are all
+                        // marked already (each band vertex is marked by dozens) adds nothing
+                        if (!(xin & ~acc)) continue;
                         const float4 p4 = sp[k];
                         const float4 n4 = sn[k];
                         if (vy < __fsub_rn(p4.y, h) || vy > __fadd_rn(p4.y, h) || vz < __fsub_rn(p4.z, h) ||
