@@ -179,6 +179,21 @@ pms_status pms_upload_particles(pms_ctx* ctx, const float* pos_xyz, const float*
 pms_status pms_upload_particles_device(pms_ctx* ctx, const float* d_pos_xyz, const float* d_vel_xyz,
                                        const float* d_rhop, uint32_t n);
 
+/* Staged upload (no counterpart in the reference, whose loadFluidFile reads and
+ * copies each frame after the last one finished, FileData.cpp:177-305).
+ * pms_stage_particles copies the next frame's host arrays into pinned staging
+ * (split over the host's threads) and from there, on a stream of its own, into a
+ * second pair of device input buffers; it may run on another host thread while
+ * pms_run_frame runs the current frame on this context, so the parse and the
+ * host-to-device copy of frame k + 1 overlap frame k.  pms_upload_staged then
+ * makes the staged frame the context's input (a buffer swap and a device-side
+ * wait, no copy), in place of pms_upload_particles.  One frame is staged at a
+ * time (PMS_ERR_STATE while one waits); stage the next one only after
+ * pms_upload_staged of the last returned.  Staging reports errors by status
+ * only; pms_last_error belongs to the thread running the frames. */
+pms_status pms_stage_particles(pms_ctx* ctx, const float* pos_xyz, const float* vel_xyz, const float* rhop, uint32_t n);
+pms_status pms_upload_staged(pms_ctx* ctx);
+
 /* Stages (asynchronous on the context stream unless stated). */
 pms_status pms_build_grid(pms_ctx* ctx);        /* NeighborSearch::SpatialGridBuilding, NeighborSearch.cu:37-76 */
 pms_status pms_anisotropy(pms_ctx* ctx);        /* Anisotropic::processingOfParticles, Anisotropic.cu:30-40 */

@@ -812,20 +812,30 @@ extern "C" pms_status pms_run_config(const char* config_path, int verbose) {
     pms_ctx* ctx = nullptr;
     if ((st = pms_create(&cfg, -1, &ctx))) { fprintf(stderr, "error: pms_create: %s\n", pms_status_string(st)); return st; }
     const int step = cfg.frame_step > 0 ? cfg.frame_step : 1;
+    // parse a frame and stage it: pinned copy and host-to-device copy into the
+    // context's second input buffers (on the reader thread, while the GPU runs the
+    // frame before it)
     auto read = [&](int frame, FrameIn* in) {
         in->path = frame_name(cfg.fluid_path, cfg.fluid_prefix, cfg.num_zeros, frame, ".vtk");
         in->st = pms_read_vtk_particles(in->path.c_str(), &in->pos, &in->vel, &in->rho, &in->n);
+        if (!in->st) in->st = pms_stage_particles(ctx, in->pos, in->vel, in->rho, in->n);
+        in->release();
     };
     FrameIn cur, next;
     std::thread reader, writer;
     pms_status wst = PMS_OK;
     if (cfg.frame_start <= cfg.frame_end) read(cfg.frame_start, &cur);
     for (int frame = cfg.frame_start; frame <= cfg.frame_end; frame += step) {
-        if (cur.st) { fprintf(stderr, "error: cannot read %s\n", cur.path.c_str()); st = cur.st; break; }
+        if (cur.st) {
+            fprintf(stderr, "error: cannot read or stage %s: %s\n", cur.path.c_str(), pms_status_string(cur.st));
+            st = cur.st;
+            break;
+        }
         const bool more = frame + step <= cfg.frame_end;
-        if (more) reader = std::thread(read, frame + step, &next);
         if (verbose) printf("frame %d: %u particles from %s\n", frame, cur.n, cur.path.c_str());
-        st = pms_upload_particles(ctx, cur.pos, cur.vel, cur.rho, cur.n);
+        st = pms_upload_staged(ctx);
+        // the next frame is staged only after this one took the staged buffers
+        if (more) reader = std::thread(read, frame + step, &next);
         if (!st) st = pms_run_frame(ctx);
         FrameOut out;
         if (!st && cfg.is_surface) {
@@ -856,10 +866,8 @@ extern "C" pms_status pms_run_config(const char* config_path, int verbose) {
         if (writer.joinable()) writer.join();
         if (wst) { st = wst; if (reader.joinable()) reader.join(); next.release(); break; }
         writer = std::thread([o = std::move(out), &wst]() { wst = write_frame(o); });
-        cur.release();
         if (more) { reader.join(); cur = next; next = FrameIn(); }
     }
-    cur.release();
     if (writer.joinable()) writer.join();
     if (!st) st = wst;
     pms_destroy(ctx);

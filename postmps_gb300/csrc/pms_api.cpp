@@ -7,6 +7,8 @@
 //   * counts stay on the device; the host reads them only where it must size
 //     the next buffers (grid, band, mesh) or return results;
 //   * every failure is a returned pms_status with a message, never an abort.
+#include <thread>
+
 #include "pms_internal.h"
 
 #include <cstdarg>
@@ -110,6 +112,13 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (c->mesh_copied) cudaEventDestroy(c->mesh_copied);
     if (c->diffuse_ready) cudaEventDestroy(c->diffuse_ready);
     if (c->diffuse_copied) cudaEventDestroy(c->diffuse_copied);
+    if (c->stage_stream) { cudaStreamSynchronize(c->stage_stream); cudaStreamDestroy(c->stage_stream); }
+    if (c->stage_ready) cudaEventDestroy(c->stage_ready);
+    if (c->stage_free) cudaEventDestroy(c->stage_free);
+    if (c->stage_hpos) cudaFreeHost(c->stage_hpos);
+    if (c->stage_hvel) cudaFreeHost(c->stage_hvel);
+    c->st_pos.release();
+    c->st_vel.release();
     pms_batch_release(c);
     release_all(c);
     for (int i = 0; i <= kNumStages; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
@@ -267,6 +276,18 @@ static pms_status ensure_band(pms_ctx* c, uint32_t nv) { return ensure_band_buff
 // ---------------------------------------------------------------------------
 // upload (FileData::loadFluidFile + GPUmemory::memAlcandCpy_fluid)
 // ---------------------------------------------------------------------------
+// a new frame's inputs are in place: every result of the last frame is stale
+static void begin_frame(pms_ctx* c, uint32_t n) {
+    c->n = n;
+    c->have_particles = true;
+    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = c->have_weld = false;
+    c->band_learned = c->mc_classified = c->mc_compacted = false;
+    c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
+    c->ns = c->nv = c->nvalid = 0;
+    c->nmesh = 0;
+    for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
+}
+
 static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n,
                                 cudaMemcpyKind kind) {
     if (!c || (n && !pos)) return PMS_ERR_INVALID_ARGUMENT;
@@ -297,14 +318,7 @@ static pms_status upload_common(pms_ctx* c, const float* pos, const float* vel, 
         // Anisotropic_kernel.cuh:212), so it is not copied
         (void)rho;
     }
-    c->n = n;
-    c->have_particles = true;
-    c->have_grid = c->have_aniso = c->have_band = c->have_field = c->have_mc = c->have_values = c->have_weld = false;
-    c->band_learned = c->mc_classified = c->mc_compacted = false;
-    c->l_ncand = c->l_npred = c->l_nexact = c->l_ncert = c->l_nrecheck = 0;
-    c->ns = c->nv = c->nvalid = 0;
-    c->nmesh = 0;
-    for (int i = 0; i < kNumStages; ++i) c->ev_recorded[i] = false;
+    begin_frame(c, n);
     return PMS_OK;
 }
 
@@ -313,6 +327,91 @@ extern "C" pms_status pms_upload_particles(pms_ctx* c, const float* pos, const f
 }
 extern "C" pms_status pms_upload_particles_device(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n) {
     return upload_common(c, pos, vel, rho, n, cudaMemcpyDeviceToDevice);
+}
+
+// host copy split over the host's threads (the staging copy of a multi-megabyte frame)
+static void copy_parallel(void* dst, const void* src, size_t bytes) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const size_t T = std::max<size_t>(1, std::min<size_t>(hw ? hw : 1, bytes >> 22));
+    if (T == 1) { memcpy(dst, src, bytes); return; }
+    std::vector<std::thread> th;
+    for (size_t k = 0; k < T; ++k)
+        th.emplace_back([=]() {
+            const size_t a = bytes * k / T, b = bytes * (k + 1) / T;
+            memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, b - a);
+        });
+    for (std::thread& t : th) t.join();
+}
+
+// The staged upload.  Staging touches only its own members (pinned host buffers, a
+// second pair of device input buffers, its stream and events, under stage_mu), so a
+// thread may stage frame k + 1 while another runs frame k on the same context; it
+// reports failures by status only (the message slot belongs to the frame's thread).
+extern "C" pms_status pms_stage_particles(pms_ctx* c, const float* pos, const float* vel, const float* rho, uint32_t n) {
+    if (!c || (n && !pos)) return PMS_ERR_INVALID_ARGUMENT;
+    (void)rho;                                   // recomputed, as for pms_upload_particles
+    if (cudaSetDevice(c->device) != cudaSuccess) return PMS_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(c->stage_mu);
+    if (c->staged) return PMS_ERR_STATE;         // the frame staged before was not taken yet
+    if (!c->stage_stream) {
+        if (cudaStreamCreateWithFlags(&c->stage_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->stage_ready, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->stage_free, cudaEventDisableTiming) != cudaSuccess)
+            return PMS_ERR_CUDA;
+    }
+    const size_t bytes = 12 * (size_t)n;
+    // the previous staged copy has left the pinned buffers before they are refilled
+    if (cudaStreamSynchronize(c->stage_stream) != cudaSuccess) return PMS_ERR_CUDA;
+    if (c->stage_hcap < bytes) {
+        if (c->stage_hpos) cudaFreeHost(c->stage_hpos);
+        if (c->stage_hvel) cudaFreeHost(c->stage_hvel);
+        c->stage_hpos = c->stage_hvel = nullptr;
+        c->stage_hcap = 0;
+        if (cudaMallocHost(&c->stage_hpos, bytes) != cudaSuccess || cudaMallocHost(&c->stage_hvel, bytes) != cudaSuccess)
+            return PMS_ERR_OUT_OF_MEMORY;
+        c->stage_hcap = bytes;
+    }
+    if (c->st_pos.ensure(bytes ? bytes : 12) != cudaSuccess || c->st_vel.ensure(bytes ? bytes : 12) != cudaSuccess)
+        return PMS_ERR_OUT_OF_MEMORY;
+    // the device buffers held the inputs of a frame that pms_upload_staged retired
+    if (c->stage_free_recorded && cudaStreamWaitEvent(c->stage_stream, c->stage_free, 0) != cudaSuccess) return PMS_ERR_CUDA;
+    if (n) {
+        copy_parallel(c->stage_hpos, pos, bytes);
+        if (vel) copy_parallel(c->stage_hvel, vel, bytes);
+        else memset(c->stage_hvel, 0, bytes);
+        if (cudaMemcpyAsync(c->st_pos.p, c->stage_hpos, bytes, cudaMemcpyHostToDevice, c->stage_stream) != cudaSuccess ||
+            cudaMemcpyAsync(c->st_vel.p, c->stage_hvel, bytes, cudaMemcpyHostToDevice, c->stage_stream) != cudaSuccess)
+            return PMS_ERR_CUDA;
+    }
+    if (cudaEventRecord(c->stage_ready, c->stage_stream) != cudaSuccess) return PMS_ERR_CUDA;
+    c->staged_n = n;
+    c->staged = true;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_upload_staged(pms_ctx* c) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(c->stage_mu);
+    if (!c->staged) return pms_fail(c, PMS_ERR_STATE, "pms_upload_staged without a frame from pms_stage_particles");
+    cudaSetDevice(c->device);
+    const uint32_t n = c->staged_n;
+    // a velocity copy of a direct upload may still be in flight into the buffer retired below
+    if (c->vel_pending) {
+        PMS_CUDA(c, cudaStreamWaitEvent(c->stream, c->vel_ready, 0));
+        c->vel_pending = false;
+    }
+    // the staged buffers become the inputs (they hold n particles, so nothing regrows them)
+    std::swap(c->in_pos, c->st_pos);
+    std::swap(c->in_vel, c->st_vel);
+    c->staged = false;
+    pms_status st = ensure_particles(c, n);
+    if (st) return st;
+    PMS_CUDA(c, cudaStreamWaitEvent(c->stream, c->stage_ready, 0));
+    // the retired buffers are free once the work enqueued before this point has run
+    PMS_CUDA(c, cudaEventRecord(c->stage_free, c->stream));
+    c->stage_free_recorded = true;
+    begin_frame(c, n);
+    return PMS_OK;
 }
 
 // ---------------------------------------------------------------------------

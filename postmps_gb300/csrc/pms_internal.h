@@ -3,7 +3,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -18,7 +20,7 @@ namespace pms {
 // ---------------------------------------------------------------------------
 // Every (re)allocation or release bumps this generation: a captured CUDA graph
 // holds raw buffer addresses and is captured again when it has changed.
-inline uint64_t g_dbuf_generation = 0;
+inline std::atomic<uint64_t> g_dbuf_generation{0};
 
 struct DBuf {
     void* p = nullptr;
@@ -124,6 +126,16 @@ struct pms_ctx {
     // gather waits for them)
     cudaStream_t up_stream = nullptr;
     cudaEvent_t up_start = nullptr, vel_ready = nullptr;
+    // staged upload (pms_stage_particles / pms_upload_staged): the next frame's inputs in a
+    // second pair of device buffers, copied from pinned host staging on stage_stream
+    std::mutex stage_mu;
+    pms::DBuf st_pos, st_vel;
+    float *stage_hpos = nullptr, *stage_hvel = nullptr;
+    size_t stage_hcap = 0;
+    cudaStream_t stage_stream = nullptr;
+    cudaEvent_t stage_ready = nullptr, stage_free = nullptr;
+    bool staged = false, stage_free_recorded = false;
+    uint32_t staged_n = 0;
     bool vel_pending = false;
     // mesh streamed to registered host buffers on a copy stream while later stages run
     cudaStream_t copy_stream = nullptr;

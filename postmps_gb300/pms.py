@@ -176,6 +176,8 @@ def lib() -> C.CDLL:
         L.pms_reserve.argtypes = [vp, C.c_uint32, C.c_uint64]
         L.pms_upload_particles.argtypes = [vp, vp, vp, vp, C.c_uint32]
         L.pms_upload_particles_device.argtypes = [vp, vp, vp, vp, C.c_uint32]
+        L.pms_stage_particles.argtypes = [vp, vp, vp, vp, C.c_uint32]
+        L.pms_upload_staged.argtypes = [vp]
         for name in ("pms_build_grid", "pms_anisotropy", "pms_band", "pms_field", "pms_marching_cubes", "pms_surface",
                      "pms_diffuse", "pms_run_frame"):
             getattr(L, name).argtypes = [vp]
@@ -361,6 +363,17 @@ class Context:
         rho = None if rho is None else np.ascontiguousarray(rho, np.float32)
         self._keep = (pos, vel, rho)
         self._call("pms_upload_particles", _ptr(pos), _ptr(vel), _ptr(rho), len(pos))
+
+    def stage(self, pos, vel=None, rho=None) -> None:
+        """pms_stage_particles: the next frame's inputs, staged while a frame may run on
+        another thread (the arrays are copied before the call returns)."""
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        rho = None if rho is None else np.ascontiguousarray(rho, np.float32)
+        _check(lib().pms_stage_particles(self._h, _ptr(pos), _ptr(vel), _ptr(rho), len(pos)))
+
+    def upload_staged(self) -> None:
+        self._call("pms_upload_staged")
 
     def upload_device(self, d_pos: int, d_vel: int | None, d_rho: int | None, n: int) -> None:
         self._call("pms_upload_particles_device", d_pos, d_vel, d_rho, n)

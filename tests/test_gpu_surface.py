@@ -268,3 +268,44 @@ def test_welded_mesh_reproduces_the_soup(pms_lib, tmp_config, tmp_path, case):
     p = tmp_path / "w.ply"
     pms_lib.write_ply_mesh(str(p), pos, idx, binary=True)
     assert p.stat().st_size < 12 * len(soup) + 13 * len(idx)
+
+
+@pytest.mark.gpu
+def test_staged_upload_equals_direct_upload(pms_lib, tmp_config):
+    """pms_stage_particles on another thread while the frame before runs, then
+    pms_upload_staged: every frame's mesh is the one pms_upload_particles gives;
+    a second staging before the first is taken, or taking none, is a state error."""
+    import threading
+    from postmps_gb300 import synth
+    pms = pms_lib
+    a = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    b = tuple(np.ascontiguousarray(x[::-1]) for x in synth.crown_splash(n_slab=(50, 64, 10), n_ring=30000, radius=0.08, seed=5))
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS)))
+    with pms.Context(cfg, 0) as ctx:
+        want = []
+        for fr in (a, b, a):
+            ctx.upload(*fr)
+            ctx.run_frame()
+            want.append(ctx.mesh(normals=False)[0].copy())
+        ctx.stage(*a)
+        got = []
+        for nxt in (b, a, None):
+            ctx.upload_staged()
+            err = []
+            t = threading.Thread(target=lambda: err.append(None) if nxt is None else ctx.stage(*nxt))
+            t.start()
+            ctx.run_frame()
+            got.append(ctx.mesh(normals=False)[0].copy())
+            t.join()
+        for w, g in zip(want, got):
+            np.testing.assert_array_equal(g, w)
+        with pytest.raises(pms.PmsError) as ei:
+            ctx.upload_staged()
+        assert ei.value.status == 7
+        ctx.stage(*b)
+        with pytest.raises(pms.PmsError) as ei:
+            ctx.stage(*a)
+        assert ei.value.status == 7
+        ctx.upload_staged()
+        ctx.run_frame()
+        np.testing.assert_array_equal(ctx.mesh(normals=False)[0], want[1])
