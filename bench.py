@@ -10,6 +10,9 @@ Workloads (seeded synthetic data; --workload):
            spacing 0.01, reconstructed by one pms_run_batch call (one CUDA
            graph launch); a step is the whole batch.
   dam      the 8M-particle dam break (400x100x200, spacing 0.005), diffuse off.
+  crown4   four consecutive crown frames (8M particles), diffuse generation on
+           and carried from frame to frame, one pms_run_batch call; a step is
+           the whole batch (the carried particles dropped between steps).
 
 Bands (--band): "learned" runs the learned narrow band (the network picks the
 band vertices evaluated exactly at once, the exact sign certification covers
@@ -21,10 +24,12 @@ against the plain mesh (identical soups, triangle-count delta, Hausdorff
 distance in units of h).
 
 `value` is measured with the inputs already on the device (device-to-device
-upload inside the step); `e2e` goes through the C ABI from pinned host
-buffers and reads the triangle soup (and live diffuse particles) back into
-pinned host memory inside the timed region.  L2 is flushed (a 256 MiB write)
-between timed steps.
+upload inside the step); `e2e` goes through the C ABI as a pipelined frame
+loop: each step takes the frame staged during the step before, stages the next
+frame from pinned host buffers (pms_stage_particles, on another thread, while
+its own frame runs) and reads its triangle soup (and live diffuse particles)
+back into pinned host memory, all inside the timed region.  L2 is flushed (a
+256 MiB write) between timed steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pms|reference]
 
@@ -79,6 +84,15 @@ def workload(name: str):
         desc = {"workload": "sloshing_tank_16_frames", "frames": 16, "particles": int(sum(ns)),
                 "particles_per_frame": [min(ns), max(ns)], "h": 0.02, "grid_cell": 0.005, "iso": 0.5}
         return frames, {}, desc, False
+    if name == "crown4":
+        # four consecutive frames of the crown (the ring advected 4 ms per frame), diffuse
+        # particles carried from frame to frame: one batch, diffuse inside the graph
+        base = synth.crown_splash()
+        frames = [((base[0] + np.float32(0.004 * i) * base[1]).astype(np.float32), base[1], base[2]) for i in range(4)]
+        keys = dict(synth.CROWN_KEYS)
+        desc = {"workload": "crown_splash_4_frames", "frames": 4, "particles": int(sum(len(f[0]) for f in frames)),
+                "h": 0.01, "grid_cell": 0.0025, "iso": 0.5, "clamp_ratio": 4}
+        return frames, keys, desc, True
     if name == "dam":
         frames = [synth.dam_break()]
         keys = {"sim.particlespacing": 0.005}
@@ -135,7 +149,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -461,15 +475,31 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         ctx.upload_device(d_pos.data_ptr(), d_vel.data_ptr(), d_rho.data_ptr(), n)
         ctx.run_frame()
 
+    stage_err = []
+
+    def stage_next():
+        st = pms.lib().pms_stage_particles(ctx.handle, h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
+        if st:
+            stage_err.append(st)
+
     def step_e2e():
-        # the user's calls: upload from pinned host memory, reconstruct with the
-        # triangle soup streamed into pinned host memory while the diffuse stage
-        # runs and the live diffuse particles streamed after it, wait for both
-        ctx._call("pms_upload_particles", h_pos.data_ptr(), h_vel.data_ptr(), h_rho.data_ptr(), n)
+        # the user's calls of a pipelined frame loop: take the frame staged during the
+        # step before (its pinned copy and host-to-device copy ran while that frame
+        # computed), stage the next frame from another thread while this one runs,
+        # reconstruct with the triangle soup streamed into pinned host memory while the
+        # diffuse stage runs and the live diffuse particles streamed after it, wait for
+        # both.  Every step moves one frame's inputs host to device inside the timed
+        # region (the frame it stages) and reads its own results back.
+        ctx.upload_staged()
+        t = threading.Thread(target=stage_next)
+        t.start()
         ctx.run_frame()
         host["n_mesh"] = ctx.wait_mesh()
         if diffuse:
             host["n_diffuse"] = ctx.wait_diffuse()
+        t.join()
+        if stage_err:
+            raise RuntimeError(f"pms_stage_particles failed: status {stage_err[0]}")
 
     stage_sum = {k: 0.0 for k in STAGES}
 
@@ -480,18 +510,19 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
     # every arm and both timings run the same sequence: the diffuse set carried between
     # frames starts empty, so step i of each timing carries the particles of the
     # warm-up frames and of the i steps before it
+    # the clock record covers the warm-up and both timings (nvidia-smi needs a moment to
+    # deliver its first sample)
+    if clocks:
+        clocks.start()
     ctx.reset_diffuse()
     for _ in range(args.warmup):
         step_device()
     torch.cuda.synchronize()
     counts = ctx.counts().as_dict()
     grid = ctx.grid()
-    if clocks:
-        clocks.start()
     l0 = ctx.launches
     ms = timer(step_device, args.steps, collect)
     launches = (ctx.launches - l0) // max(1, args.steps)
-    clk = clocks.stop() if clocks else None
     if diffuse:
         # the carried set grows over the timed steps: its mean stands for the steps
         end = ctx.counts().as_dict()
@@ -508,9 +539,12 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         host["dbuf"] = torch.empty(32 * cap, dtype=torch.uint8).pin_memory()
         ctx.stream_diffuse_to_host(host["dbuf"].data_ptr(), cap)
     ctx.reset_diffuse()
+    stage_next()                              # the first frame of the pipelined loop
     for _ in range(args.warmup):
         step_e2e()
     ms_e2e = timer(step_e2e, args.steps)
+    clk = clocks.stop() if clocks else None
+    ctx.upload_staged()                       # the frame staged by the last step
     ctx.stream_mesh_to_host(0, None, 0)
     if diffuse:
         ctx.stream_diffuse_to_host(0, 0)
@@ -551,18 +585,23 @@ def training_rate(pms, ctx, frame, stream, torch, batch: int = 8192, steps: int 
             "kernel": "k_learn_train (tcgen05.mma kind::f16, accumulators in tensor memory) + k_adam"}
 
 
-def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None) -> dict:
+def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None, diffuse: bool = False) -> dict:
     dev = [tuple(torch.from_numpy(a).cuda() for a in fr) for fr in frames]
     pin = [tuple(torch.from_numpy(a).pin_memory() for a in fr) for fr in frames]
     dframes = [(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0])) for (p, v, r), fr in zip(dev, frames)]
     hframes = [(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0])) for (p, v, r), fr in zip(pin, frames)]
     host = {}
+    # with diffuse generation every step is the same sequence: the carried particles are
+    # dropped after each step, outside the timed region
+    reset = ctx.reset_diffuse if diffuse else None
+    read = {"diffuse": 0}
 
     def step_device():
         ctx.run_batch(dframes, learned=mode)
 
     def step_e2e():
         ctx.run_batch(hframes, learned=mode)
+        nd = 0
         for f in range(len(frames)):
             nv = C.c_uint64()
             pms.lib().pms_batch_mesh(ctx.handle, f, None, 0, C.byref(nv))
@@ -570,14 +609,24 @@ def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None) -> d
             if buf is None or buf.numel() < 3 * nv.value:
                 buf = host[f] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
             ctx._call("pms_batch_mesh", f, buf.data_ptr(), buf.numel() // 3, C.byref(nv))
+            if diffuse:
+                pms.lib().pms_batch_diffuse(ctx.handle, f, None, 0, C.byref(nv))
+                dbuf = host.get(("d", f))
+                if dbuf is None or dbuf.numel() < 32 * nv.value:
+                    dbuf = host[("d", f)] = torch.empty(max(32, int(32 * nv.value * 1.25)), dtype=torch.uint8).pin_memory()
+                ctx._call("pms_batch_diffuse", f, dbuf.data_ptr(), dbuf.numel() // 32, C.byref(nv))
+                nd += nv.value
+        read["diffuse"] = nd
 
     for _ in range(args.warmup):
         step_device()
+        if reset:
+            reset()
     torch.cuda.synchronize()
     if clocks:
         clocks.start()
     l0 = ctx.launches
-    ms = timer(step_device, args.steps)
+    ms = timer(step_device, args.steps, reset)
     launches = (ctx.launches - l0) // max(1, args.steps)
     clk = clocks.stop() if clocks else None
     per_frame = []
@@ -588,10 +637,13 @@ def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None) -> d
         counts.append(c.as_dict())
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
-    ms_e2e = timer(step_e2e, args.steps)
+        if reset:
+            reset()
+    ms_e2e = timer(step_e2e, args.steps, reset)
     mesh = sum(int(c["n_mesh_vertices"]) for c in counts)
     return {"ms": ms, "ms_e2e": ms_e2e, "launches": launches, "clocks": clk, "frame_ms": per_frame,
-            "counts": counts, "info": ctx.batch_info(), "h2d": sum(28 * len(fr[0]) for fr in frames), "d2h": 12 * mesh}
+            "counts": counts, "info": ctx.batch_info(), "h2d": sum(28 * len(fr[0]) for fr in frames),
+            "d2h": 12 * mesh + 32 * read["diffuse"]}
 
 
 def unbatched_ms(ctx, frames, mode: str, args, timer, torch) -> float:
@@ -604,9 +656,11 @@ def unbatched_ms(ctx, frames, mode: str, args, timer, torch) -> float:
             ctx.upload_device(p.data_ptr(), v.data_ptr(), r.data_ptr(), len(fr[0]))
             ctx.run_frame()
 
+    ctx.reset_diffuse()
     step()
+    ctx.reset_diffuse()
     torch.cuda.synchronize()
-    return timer(step, max(1, args.steps // 2))
+    return timer(step, max(1, args.steps // 2), ctx.reset_diffuse)
 
 
 def run_pms(args) -> None:
@@ -649,7 +703,7 @@ def run_pms(args) -> None:
         arms = [args.band]
     if "learned" in arms and model is None:
         raise SystemExit(f"--band learned needs a model ({args.model})")
-    batched = args.workload == "slosh16"
+    batched = args.workload in ("slosh16", "crown4")
     tune = None
     if not args.no_tune:
         # autotune the launch shapes on the largest frame, as the first (headline) arm
@@ -667,7 +721,7 @@ def run_pms(args) -> None:
     res = {}
     for i, arm in enumerate(arms):
         if batched:
-            res[arm] = batch_arm(pms, ctx, frames, arm, args, timer, torch, ClockSampler(local))
+            res[arm] = batch_arm(pms, ctx, frames, arm, args, timer, torch, ClockSampler(local), diffuse)
         else:
             res[arm] = single_frame_arm(pms, ctx, frames[0], arm, args, timer, torch, diffuse, ClockSampler(local))
     ctx.set_band_mode("plain")
@@ -744,8 +798,8 @@ def run_pms(args) -> None:
         # whole-path bytes of every frame over the whole batch time
         tot = 0.0
         for fr_c in head["counts"]:
-            tot += sum(algorithmic_bytes(dict(fr_c, n_generated_diffuse=0, n_diffuse=0), fr_c["n_particles"],
-                                         fr_c["n_band_vertices"], False, head_arm != "plain").values())
+            tot += sum(algorithmic_bytes(fr_c if diffuse else dict(fr_c, n_generated_diffuse=0, n_diffuse=0),
+                                         fr_c["n_particles"], fr_c["n_band_vertices"], diffuse, head_arm != "plain").values())
         achieved = tot / (head["ms"] / 1e3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": "whole batch", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": None, "algorithmic_bytes": tot, "peak_source": peak_src}
@@ -801,7 +855,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="pms", choices=["pms", "reference"])
-    ap.add_argument("--workload", default="crown", choices=["crown", "block", "slosh16", "dam"])
+    ap.add_argument("--workload", default="crown", choices=["crown", "block", "slosh16", "dam", "crown4"])
     ap.add_argument("--band", default="both", choices=["both", "learned", "certified", "plain"])
     ap.add_argument("--model", default=LN.DEFAULT_MODEL)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -418,10 +418,15 @@ pms_status pms_trainer_get_model(pms_trainer* t, pms_band_model* out);
  * between stages.  pms_run_batch copies k frames (host or device pointers) into
  * one device arena, finds their grids with one synchronisation, and runs the
  * surface path of all of them in one CUDA graph launch (captured on first use
- * and relaunched while the frames' grids stay the same).  Diffuse particles
- * are not generated in a batch.  With PMS_BATCH_LEARNED the learned band is
- * used (PMS_BATCH_CERTIFIED: its sign certification without the network); every
- * frame's result equals its single-frame run, and the plain band's.
+ * and relaunched while the frames' grids stay the same).  When the context's
+ * config has diffuse generation on, the frames are consecutive frames of one
+ * sequence: each frame's diffuse stage runs inside the graph in frame order,
+ * carrying the particles from frame to frame (starting from, and leaving, the
+ * context's carried set and frame counter, so batches and single frames
+ * continue one sequence); pms_batch_diffuse reads a frame's live particles.
+ * With PMS_BATCH_LEARNED the learned band is used (PMS_BATCH_CERTIFIED: its
+ * sign certification without the network); every frame's result equals its
+ * single-frame run, and the plain band's.
  * ------------------------------------------------------------------------- */
 typedef struct pms_frame {
     const float* pos_xyz;
@@ -436,6 +441,10 @@ pms_status pms_run_batch(pms_ctx* ctx, const pms_frame* frames, uint32_t k, int 
 pms_status pms_batch_frame(pms_ctx* ctx, uint32_t f, pms_counts* counts, float* ms);
 /* Triangle soup of frame f (positions, 3 vertices per triangle). */
 pms_status pms_batch_mesh(pms_ctx* ctx, uint32_t f, float* pos_xyz, uint64_t cap, uint64_t* n_vertices);
+/* Live diffuse particles of frame f of the last batch (after its delete/append),
+ * as the 32-byte records of pms_stream_diffuse_to_host; *n receives the count
+ * (PMS_ERR_CAPACITY, with the count, when cap is too small; out NULL: count only). */
+pms_status pms_batch_diffuse(pms_ctx* ctx, uint32_t f, pms_diffuse_particle* out, uint64_t cap, uint64_t* n);
 /* Kernels per graph launch, graph captures so far. */
 pms_status pms_batch_info(pms_ctx* ctx, uint32_t* graph_kernels, uint32_t* captures);
 

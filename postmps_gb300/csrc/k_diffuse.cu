@@ -66,6 +66,20 @@ struct DiffuseParams {
     uint32_t frame;
 };
 
+// Counts of the delete/append step: given on the host (a single frame: exact, and the
+// buffers sized to them) or read from the device and clamped to the buffers'
+// capacities (a batched frame, captured into a graph); a count past a capacity sets
+// kErrCapacity and the batch runs again with larger buffers.
+struct DfN {
+    uint32_t gen, old;                 // host counts, or the capacities when read from the device
+    const uint32_t* gen_dev;           // generated particles (Counters::n_generated), or null
+    const uint32_t* old_dev;           // carried particles, or null
+    uint32_t out_cap;                  // capacity of the delete/append output
+    uint32_t* err;                     // the frame's error word
+};
+__device__ __forceinline__ uint32_t df_gen(const DfN& c) { return c.gen_dev ? min(*c.gen_dev, c.gen) : c.gen; }
+__device__ __forceinline__ uint32_t df_old(const DfN& c) { return c.old_dev ? min(*c.old_dev, c.old) : c.old; }
+
 // counter-based uniform in [0, 1): splitmix64 finaliser of (seed, frame, index)
 __host__ __device__ __forceinline__ float spawn_uniform(uint64_t seed, uint32_t frame, uint64_t idx) {
     uint64_t x = seed * 0x9E3779B97F4A7C15ull + (uint64_t)frame * 0xD1B54A32D192ED03ull + idx;
@@ -294,8 +308,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
                                                        const unsigned long long* __restrict__ off,
                                                        const int32_t* __restrict__ num, const uint2* __restrict__ cell_info,
                                                        const float4* __restrict__ spos, const float4* __restrict__ svel,
-                                                       DiffuseParticle* __restrict__ gen) {
+                                                       DiffuseParticle* __restrict__ gen, uint32_t gen_cap,
+                                                       const uint32_t* __restrict__ frame_dev, uint32_t frame_off,
+                                                       uint32_t* __restrict__ err) {
     const uint32_t ns = cnt->n_spawning;
+    // a batched frame reads its number (the batch's first frame plus its place) from the device
+    const uint32_t frame = frame_dev ? *frame_dev + frame_off : dp.frame;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ns; t += gridDim.x * blockDim.x) {
         const uint32_t i = spawnlist[t];
         const float4 p = spos[i], v = svel[i];
@@ -318,8 +336,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
         const int type = type_of(count_within(g, dp, cell_info, spos, p.x, p.y, p.z, true));
         for (int c = 0; c < k; ++c) {
             const uint64_t idif = (uint64_t)start + (uint64_t)c;
-            const float u1 = spawn_uniform(dp.seed, dp.frame, 3 * idif + 1);
-            const float u2 = spawn_uniform(dp.seed, dp.frame, 3 * idif + 2);
+            const float u1 = spawn_uniform(dp.seed, frame, 3 * idif + 1);
+            const float u2 = spawn_uniform(dp.seed, frame, 3 * idif + 2);
             const float r = dp.hd * sqrtf(u1);
             const float theta = u2 * 2.f * kPiF;
             // cos(theta) and sin(theta) of a float theta are the single-precision
@@ -333,7 +351,8 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
             d.vz = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(r, ct), e1z), __fmul_rn(__fmul_rn(r, st), e2z)), v.z);
             d.ttl = k * dp.life_time;
             d.type = type;
-            gen[idif] = d;
+            if (idif < gen_cap) gen[idif] = d;
+            else atomicOr(err, kErrCapacity);
         }
     }
 }
@@ -414,8 +433,9 @@ __device__ __forceinline__ float wendland(float rx, float ry, float rz, float h,
 // empty cells while foam and bubbles walk dense ones, and a warp that mixes them
 // runs at the pace of its slowest lane.  The particles stay where they are (the
 // live set keeps the reference's generated-then-old order).
-__global__ void __launch_bounds__(256) k_df_type_keys(const DiffuseParticle* __restrict__ old, uint32_t n_old,
+__global__ void __launch_bounds__(256) k_df_type_keys(const DiffuseParticle* __restrict__ old, DfN dn,
                                                       unsigned long long* __restrict__ key) {
+    const uint32_t n_old = df_old(dn);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
         const int t = old[i].type;
         key[i] = t == 0 ? 1ull : (t == 1 ? (1ull << 32) : 0ull);
@@ -424,8 +444,9 @@ __global__ void __launch_bounds__(256) k_df_type_keys(const DiffuseParticle* __r
 
 __global__ void __launch_bounds__(256) k_df_type_perm(const unsigned long long* __restrict__ key,
                                                       const unsigned long long* __restrict__ scan,
-                                                      const unsigned long long* __restrict__ total, uint32_t n_old,
+                                                      const unsigned long long* __restrict__ total, DfN dn,
                                                       uint32_t* __restrict__ perm) {
+    const uint32_t n_old = df_old(dn);
     const unsigned long long tot = *total;
     const uint32_t n0 = (uint32_t)(tot & 0xffffffffull), n1 = (uint32_t)(tot >> 32);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_old; i += gridDim.x * blockDim.x) {
@@ -462,11 +483,12 @@ __device__ __forceinline__ int count_within_near(const KGrid& g, const DiffusePa
 // 2 hd (the Wendland support: every particle farther adds exactly 0 to the
 // average, every particle the count takes lies within hd), in the reference's
 // cell and particle order, and the last walk covers only what lies within hd.
-__global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParams dp, uint32_t n_old,
+__global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParams dp, DfN dn,
                                                         const uint32_t* __restrict__ cell_start,
                                                         const float4* __restrict__ spos,
                                                         const float4* __restrict__ svel, const uint32_t* __restrict__ perm,
                                                         DiffuseParticle* __restrict__ old) {
+    const uint32_t n_old = df_old(dn);
     for (uint32_t tt = blockIdx.x * blockDim.x + threadIdx.x; tt < n_old; tt += gridDim.x * blockDim.x) {
         const uint32_t t = perm[tt];
         DiffuseParticle d = old[t];
@@ -536,10 +558,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_update(KGrid g, DiffuseParam
 
 // delete and append: generated then old, dropping type 3; per-type counts (summed per
 // thread, then per warp, one atomic per warp and type)
-__global__ void __launch_bounds__(256) k_df_keep(const DiffuseParticle* __restrict__ gen, uint32_t n_gen,
-                                                 const DiffuseParticle* __restrict__ old, uint32_t n_old,
+__global__ void __launch_bounds__(256) k_df_keep(const DiffuseParticle* __restrict__ gen,
+                                                 const DiffuseParticle* __restrict__ old, DfN dn,
                                                  uint32_t* __restrict__ keep, Counters* __restrict__ cnt) {
-    const uint32_t total = n_gen + n_old;
+    const uint32_t n_gen = df_gen(dn), total = n_gen + df_old(dn);
     uint32_t c[4] = {0u, 0u, 0u, 0u};
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
         const int type = k < n_gen ? gen[k].type : old[k - n_gen].type;
@@ -553,13 +575,49 @@ __global__ void __launch_bounds__(256) k_df_keep(const DiffuseParticle* __restri
     }
 }
 
-__global__ void __launch_bounds__(256) k_df_append(const DiffuseParticle* __restrict__ gen, uint32_t n_gen,
-                                                   const DiffuseParticle* __restrict__ old, uint32_t n_old,
+__global__ void __launch_bounds__(256) k_df_append(const DiffuseParticle* __restrict__ gen,
+                                                   const DiffuseParticle* __restrict__ old, DfN dn,
                                                    const uint32_t* __restrict__ keep, const uint32_t* __restrict__ scan,
                                                    DiffuseParticle* __restrict__ out) {
-    const uint32_t total = n_gen + n_old;
+    const uint32_t n_gen = df_gen(dn), total = n_gen + df_old(dn);
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x)
-        if (keep[k]) out[scan[k]] = k < n_gen ? gen[k] : old[k - n_gen];
+        if (keep[k]) {
+            const uint32_t dest = scan[k];
+            if (dest < dn.out_cap) out[dest] = k < n_gen ? gen[k] : old[k - n_gen];
+            else atomicOr(dn.err, kErrCapacity);
+        }
+}
+
+// A batched frame's counts before delete/append: the carried count clamped to its
+// buffer and the step's total (generated + carried).
+__global__ void k_df_frame_counts(const uint32_t* __restrict__ old_dev, uint32_t old_cap, uint32_t gen_cap,
+                                  Counters* __restrict__ cnt) {
+    const uint32_t o = *old_dev, gnr = cnt->n_generated;
+    cnt->n_old = min(o, old_cap);
+    cnt->n_df_total = min(o, old_cap) + min(gnr, gen_cap);
+    if (o > old_cap || gnr > gen_cap) atomicOr(&cnt->err, kErrCapacity);
+}
+
+// A batched frame's survivors: their count becomes the next frame's carried count and
+// they take the next stretch of the batch's diffuse arena.
+__global__ void k_df_carry(const Counters* __restrict__ cnt, uint32_t out_cap, uint32_t* __restrict__ old_dev,
+                           unsigned long long* __restrict__ running, unsigned long long* __restrict__ base) {
+    const uint32_t live = min(cnt->n_live, out_cap);
+    *old_dev = live;
+    *base = *running;
+    *running += live;
+}
+
+__global__ void __launch_bounds__(256) k_df_export(const DiffuseParticle* __restrict__ live,
+                                                   const uint32_t* __restrict__ n_dev,
+                                                   const unsigned long long* __restrict__ base, uint64_t cap,
+                                                   DiffuseParticle* __restrict__ arena, uint32_t* __restrict__ err) {
+    const uint32_t n = *n_dev;
+    const unsigned long long b = *base;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        if (b + k < cap) arena[b + k] = live[k];
+        else if (k == 0 || b + k == cap) atomicOr(err, kErrCapacity);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -595,17 +653,12 @@ static DiffuseParams diffuse_params(const pms_ctx* ctx) {
     return d;
 }
 
-pms_status launch_diffuse(pms_ctx* ctx) {
+// Potentials, spawn counts and the spawn list of a frame: sizes from the frame's
+// particle count (on the host for single and batched frames alike).
+static pms_status diffuse_front(pms_ctx* ctx, const KGrid& g, const DiffuseParams& dp, Counters* cnt) {
     const uint32_t n = ctx->n;
-    if (n == 0) { ctx->diffuse_old = 0; return PMS_OK; }
-    const KGrid g = kgrid_of(ctx->grid);
-    const DiffuseParams dp = diffuse_params(ctx);
-    Counters* cnt = ctx->counters.as<Counters>();
-    pms_status st;
-    if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
     const size_t N = n;
-    // last frame's live particles (moved in place below) may still be on their way to the host
-    if (ctx->dout_pending) PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->diffuse_copied, 0));
+    pms_status st;
     PMS_CUDA(ctx, ctx->d_isfree.ensure(4 * N));
     PMS_CUDA(ctx, ctx->d_freescan.ensure(4 * N));
     PMS_CUDA(ctx, ctx->d_freelist.ensure(4 * N));
@@ -645,6 +698,66 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     k_df_spawnlist<<<gb, 256, 0, ctx->stream>>>(ctx->d_isdiff.as<unsigned long long>(),
                                                 ctx->d_isdiffscan.as<unsigned long long>(), n, ctx->d_difflist.as<uint32_t>());
     PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
+// Spawn, the carried particles' update and delete/append.  Single frames pass the exact
+// counts (dn.gen_dev, dn.old_dev null), batched frames the capacities and device counts;
+// launch grids follow the host values, kernels stop at the device counts.
+static pms_status diffuse_tail(pms_ctx* ctx, const KGrid& g, const DiffuseParams& dp, Counters* cnt, const DfN& dn,
+                               uint32_t spawn_bound, const uint32_t* frame_dev, uint32_t frame_off, uint32_t* live_out) {
+    pms_status st;
+    const uint32_t total = dn.gen + dn.old;
+    if (spawn_bound)
+        k_df_spawn<<<grid_for(spawn_bound, kThreads), kThreads, 0, ctx->stream>>>(
+            g, dp, cnt, ctx->d_difflist.as<uint32_t>(), ctx->d_isdiffscan.as<unsigned long long>(), ctx->d_num.as<int32_t>(),
+            ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>(),
+            dn.gen, frame_dev, frame_off, &cnt->err);
+    if (spawn_bound) PMS_LAUNCHED(ctx);
+    if (dn.old) {
+        const unsigned go = grid_for(dn.old, 256);
+        k_df_type_keys<<<go, 256, 0, ctx->stream>>>(ctx->d_old.as<DiffuseParticle>(), dn, ctx->d_tkey.as<unsigned long long>());
+        PMS_LAUNCHED(ctx);
+        if ((st = scan_u64(ctx, ctx->d_tkey.as<unsigned long long>(), ctx->d_tscan.as<unsigned long long>(), dn.old,
+                           ctx->tmp.as<unsigned long long>(), dn.old_dev ? &cnt->n_old : nullptr)))
+            return st;
+        k_df_type_perm<<<go, 256, 0, ctx->stream>>>(ctx->d_tkey.as<unsigned long long>(),
+                                                    ctx->d_tscan.as<unsigned long long>(),
+                                                    ctx->tmp.as<unsigned long long>(), dn, ctx->d_perm.as<uint32_t>());
+        PMS_LAUNCHED(ctx);
+        k_df_update<<<grid_for(dn.old, kThreads), kThreads, 0, ctx->stream>>>(
+            g, dp, dn, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
+            ctx->d_perm.as<uint32_t>(), ctx->d_old.as<DiffuseParticle>());
+        PMS_LAUNCHED(ctx);
+    }
+    uint32_t* keep = ctx->d_typescan.as<uint32_t>();
+    uint32_t* kscan = keep + (total ? total : 1);
+    if (total) {
+        k_df_keep<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(),
+                                                                 ctx->d_old.as<DiffuseParticle>(), dn, keep, cnt);
+        PMS_LAUNCHED(ctx);
+        if ((st = scan_u32(ctx, keep, kscan, total, live_out, dn.gen_dev ? &cnt->n_df_total : nullptr))) return st;
+        k_df_append<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(),
+                                                                   ctx->d_old.as<DiffuseParticle>(), dn, keep, kscan,
+                                                                   ctx->d_all.as<DiffuseParticle>());
+        PMS_LAUNCHED(ctx);
+    } else {
+        PMS_CUDA(ctx, cudaMemsetAsync(live_out, 0, sizeof(uint32_t), ctx->stream));
+    }
+    return PMS_OK;
+}
+
+pms_status launch_diffuse(pms_ctx* ctx) {
+    const uint32_t n = ctx->n;
+    if (n == 0) { ctx->diffuse_old = 0; return PMS_OK; }
+    const KGrid g = kgrid_of(ctx->grid);
+    const DiffuseParams dp = diffuse_params(ctx);
+    Counters* cnt = ctx->counters.as<Counters>();
+    pms_status st;
+    if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
+    // last frame's live particles (moved in place below) may still be on their way to the host
+    if (ctx->dout_pending) PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->diffuse_copied, 0));
+    if ((st = diffuse_front(ctx, g, dp, cnt))) return st;
     if ((st = sync_counters(ctx))) return st;
     const uint32_t n_gen = ctx->h_counters->n_generated, n_spawn = ctx->h_counters->n_spawning;
     const uint32_t n_old = ctx->diffuse_old;
@@ -652,43 +765,13 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     PMS_CUDA(ctx, ctx->d_gen.ensure(sizeof(DiffuseParticle) * (n_gen ? n_gen : 1)));
     PMS_CUDA(ctx, ctx->d_all.ensure(sizeof(DiffuseParticle) * (total ? total : 1)));
     PMS_CUDA(ctx, ctx->d_typescan.ensure(8 * (total ? total : 1)));
-    if (n_spawn)
-        k_df_spawn<<<grid_for(n_spawn, kThreads), kThreads, 0, ctx->stream>>>(
-            g, dp, cnt, ctx->d_difflist.as<uint32_t>(), ctx->d_isdiffscan.as<unsigned long long>(), ctx->d_num.as<int32_t>(),
-            ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>());
-    if (n_spawn) PMS_LAUNCHED(ctx);
     if (n_old) {
         PMS_CUDA(ctx, ctx->d_tkey.ensure(8 * (size_t)n_old));
         PMS_CUDA(ctx, ctx->d_tscan.ensure(8 * (size_t)n_old));
         PMS_CUDA(ctx, ctx->d_perm.ensure(4 * (size_t)n_old));
-        const unsigned go = grid_for(n_old, 256);
-        k_df_type_keys<<<go, 256, 0, ctx->stream>>>(ctx->d_old.as<DiffuseParticle>(), n_old,
-                                                    ctx->d_tkey.as<unsigned long long>());
-        PMS_LAUNCHED(ctx);
-        if ((st = scan_u64(ctx, ctx->d_tkey.as<unsigned long long>(), ctx->d_tscan.as<unsigned long long>(), n_old,
-                           ctx->tmp.as<unsigned long long>())))
-            return st;
-        k_df_type_perm<<<go, 256, 0, ctx->stream>>>(ctx->d_tkey.as<unsigned long long>(),
-                                                    ctx->d_tscan.as<unsigned long long>(),
-                                                    ctx->tmp.as<unsigned long long>(), n_old, ctx->d_perm.as<uint32_t>());
-        PMS_LAUNCHED(ctx);
-        k_df_update<<<grid_for(n_old, kThreads), kThreads, 0, ctx->stream>>>(
-            g, dp, n_old, ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(),
-            ctx->d_perm.as<uint32_t>(), ctx->d_old.as<DiffuseParticle>());
-        PMS_LAUNCHED(ctx);
     }
-    uint32_t* keep = ctx->d_typescan.as<uint32_t>();
-    uint32_t* kscan = keep + (total ? total : 1);
-    if (total) {
-        k_df_keep<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(), n_gen,
-                                                                 ctx->d_old.as<DiffuseParticle>(), n_old, keep, cnt);
-        PMS_LAUNCHED(ctx);
-        if ((st = scan_u32(ctx, keep, kscan, total, &cnt->n_live))) return st;
-        k_df_append<<<grid_for(total, 256), 256, 0, ctx->stream>>>(ctx->d_gen.as<DiffuseParticle>(), n_gen,
-                                                                   ctx->d_old.as<DiffuseParticle>(), n_old, keep, kscan,
-                                                                   ctx->d_all.as<DiffuseParticle>());
-        PMS_LAUNCHED(ctx);
-    }
+    const DfN dn = {n_gen, n_old, nullptr, nullptr, (uint32_t)(total ? total : 1), &cnt->err};
+    if ((st = diffuse_tail(ctx, g, dp, cnt, dn, n_spawn, nullptr, 0, &cnt->n_live))) return st;
     if ((st = sync_counters(ctx))) return st;
     ctx->diffuse_old = total ? ctx->h_counters->n_live : 0;
     std::swap(ctx->d_all, ctx->d_old);               // the survivors are next frame's old particles
@@ -704,6 +787,45 @@ pms_status launch_diffuse(pms_ctx* ctx) {
         PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_copied, ctx->copy_stream));
         ctx->dout_pending = true;
     }
+    return PMS_OK;
+}
+
+// every buffer of a batched frame's diffuse stage, for frames of up to nmax particles
+pms_status ensure_diffuse_batch_buffers(pms_ctx* ctx, uint32_t nmax, uint32_t gen_cap, uint32_t old_cap) {
+    const size_t N = nmax ? nmax : 1, G = gen_cap ? gen_cap : 1, O = old_cap ? old_cap : 1;
+    for (DBuf* b : {&ctx->d_isfree, &ctx->d_freescan, &ctx->d_freelist, &ctx->d_num, &ctx->d_difflist})
+        PMS_CUDA(ctx, b->ensure(4 * N));
+    for (DBuf* b : {&ctx->d_nrm_free, &ctx->d_pot}) PMS_CUDA(ctx, b->ensure(16 * N));
+    for (DBuf* b : {&ctx->d_isdiff, &ctx->d_isdiffscan}) PMS_CUDA(ctx, b->ensure(8 * N));
+    PMS_CUDA(ctx, ctx->d_gen.ensure(sizeof(DiffuseParticle) * G));
+    PMS_CUDA(ctx, ctx->d_all.ensure(sizeof(DiffuseParticle) * O));
+    PMS_CUDA(ctx, ctx->d_old.ensure(sizeof(DiffuseParticle) * O));
+    PMS_CUDA(ctx, ctx->d_typescan.ensure(8 * (G + O)));
+    PMS_CUDA(ctx, ctx->d_tkey.ensure(8 * O));
+    PMS_CUDA(ctx, ctx->d_tscan.ensure(8 * O));
+    PMS_CUDA(ctx, ctx->d_perm.ensure(4 * O));
+    return PMS_OK;
+}
+
+pms_status launch_diffuse_bounded(pms_ctx* ctx, const DiffuseBatch& db) {
+    const uint32_t n = ctx->n;
+    const KGrid g = kgrid_of(ctx->grid);
+    const DiffuseParams dp = diffuse_params(ctx);
+    Counters* cnt = ctx->counters.as<Counters>();
+    pms_status st;
+    if (n && (st = diffuse_front(ctx, g, dp, cnt))) return st;
+    if (!n) PMS_CUDA(ctx, cudaMemsetAsync(&cnt->n_generated, 0, sizeof(uint32_t), ctx->stream));
+    k_df_frame_counts<<<1, 1, 0, ctx->stream>>>(db.old_dev, db.old_cap, db.gen_cap, cnt);
+    PMS_LAUNCHED(ctx);
+    const DfN dn = {db.gen_cap, db.old_cap, &cnt->n_generated, &cnt->n_old, db.old_cap, &cnt->err};
+    if ((st = diffuse_tail(ctx, g, dp, cnt, dn, n, db.frame_dev, db.frame_off, &cnt->n_live))) return st;
+    std::swap(ctx->d_all, ctx->d_old);               // at capture: the next frame reads this frame's survivors
+    k_df_carry<<<1, 1, 0, ctx->stream>>>(cnt, db.old_cap, db.old_dev, db.running, db.base);
+    PMS_LAUNCHED(ctx);
+    k_df_export<<<grid_for(db.old_cap, 256), 256, 0, ctx->stream>>>(ctx->d_old.as<DiffuseParticle>(), db.old_dev, db.base,
+                                                                     db.arena_cap, static_cast<DiffuseParticle*>(db.arena),
+                                                                     &cnt->err);
+    PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
 

@@ -49,7 +49,10 @@ extern "C" uint64_t pms_kernel_launches(const pms_ctx* ctx) { return ctx ? ctx->
 // ---------------------------------------------------------------------------
 // lifetime
 // ---------------------------------------------------------------------------
-static void release_all(pms_ctx* c) {
+// every device buffer of a context: released together, and their addresses sign a
+// captured batch graph (the staging pair, swapped with the inputs, is released apart)
+template <class F>
+static void for_each_dbuf(pms_ctx* c, F f) {
     DBuf* bufs[] = {&c->in_pos, &c->in_vel, &c->in_rho, &c->keys, &c->slot, &c->order, &c->skeys, &c->spos,
                     &c->svel, &c->rho, &c->cell_count, &c->cell_start, &c->cell_info, &c->surf_count,
                     &c->surf_start, &c->big_cells, &c->slist, &c->moments, &c->cell_rad, &c->cell_rec, &c->aniso, &c->nrm4, &c->mean4, &c->gdebug,
@@ -62,7 +65,27 @@ static void release_all(pms_ctx* c) {
                     &c->l_e_wp, &c->l_e_list, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp, &c->l_n_list, &c->l_field_new,
                     &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list,
                     &c->w_bits, &c->w_wc, &c->w_wp, &c->w_vert, &c->w_vnorm, &c->w_idx};
-    for (DBuf* b : bufs) b->release();
+    for (DBuf* b : bufs) f(*b);
+}
+
+static void release_all(pms_ctx* c) {
+    for_each_dbuf(c, [](DBuf& b) { b.release(); });
+}
+
+uint64_t pms::dbuf_signature(pms_ctx* c, bool diffuse) {
+    // the diffuse stage's buffers (d_*): used by a graph only on its diffuse lane
+    const DBuf* dfirst[] = {&c->d_isfree, &c->d_freescan, &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan,
+                            &c->d_isdiff, &c->d_isdiffscan, &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all,
+                            &c->d_rand, &c->d_typescan, &c->d_nrm_free, &c->d_tkey, &c->d_tscan, &c->d_perm};
+    uint64_t h = 1469598103934665603ull;
+    for_each_dbuf(c, [&](DBuf& b) {
+        if (!diffuse)
+            for (const DBuf* d : dfirst)
+                if (d == &b) return;
+        h = (h ^ (uint64_t)(uintptr_t)b.p) * 1099511628211ull;
+        h = (h ^ (uint64_t)b.cap) * 1099511628211ull;
+    });
+    return h;
 }
 
 extern "C" pms_status pms_create(const pms_config* cfg, int device, pms_ctx** out) {

@@ -23,7 +23,19 @@
 // same launches as a single learned frame, every size a bound and every count
 // on the device, so the batched result equals the single-frame result (and the
 // plain band's).
+//
+// With diffuse generation on, a diffuse lane -- a further sub-context with its
+// own stream -- runs every frame's diffuse stage in frame order, as the carried
+// particles demand: frame f's stage waits for frame f's surface stages on their
+// lane and reads that lane's grid buffers, and the lane's next frame waits for it
+// before it overwrites them.  Sizes are capacities (generated and carried
+// particles per frame), counts live on the device, the carried set alternates
+// between two buffers, and each frame's survivors land in a diffuse arena; a
+// count past a capacity sets an error bit and the batch runs again, from the
+// same carried particles, with larger buffers.  The carried set enters from and
+// returns to the context, so batches and single frames continue one sequence.
 #include <algorithm>
+#include <memory>
 #include <cstdint>
 #include <cstring>
 #include <utility>
@@ -55,9 +67,18 @@ struct BatchState {
     int flags = -1;
     uint64_t mesh_cap = 0;
     uint32_t captures = 0;
-    uint64_t gen = 0;                 // buffer generation the graph was captured against
+    uint64_t sig = 0;                 // signature of the buffers the graph was captured against
     uint32_t nlanes_captured = 0;
     uint32_t wait_captured = 0;       // the debug wait limit baked into the captured launches
+    // diffuse generation
+    pms_ctx* dlane = nullptr;                    // the diffuse lane
+    cudaEvent_t djoin = nullptr;
+    std::vector<cudaEvent_t> ev_surf, ev_diff;   // per frame: surface stages done, diffuse stage done
+    DBuf dcnt, drun, dbase, darena;              // {carried count, first frame's number}, arena fill, offsets, arena
+    uint64_t darena_cap = 0;
+    uint32_t gen_cap = 0, old_cap = 0;
+    void *d_in = nullptr, *d_out = nullptr;      // carried buffer the graph reads first / holds the survivors last
+    std::vector<unsigned long long> hdbase;
     ~BatchState() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -65,7 +86,11 @@ struct BatchState {
         for (cudaEvent_t e : join) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         for (pms_ctx* l : lanes) pms_destroy(l);
-        for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh}) b->release();
+        for (cudaEvent_t e : ev_surf) cudaEventDestroy(e);
+        for (cudaEvent_t e : ev_diff) cudaEventDestroy(e);
+        if (djoin) cudaEventDestroy(djoin);
+        if (dlane) pms_destroy(dlane);
+        for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh, &dcnt, &drun, &dbase, &darena}) b->release();
     }
 };
 
@@ -107,6 +132,33 @@ struct FrameView {
     }
 };
 
+// Points the diffuse lane at frame f: the grid buffers of the lane that built the
+// frame, the frame's counters, size and grid (borrowed; restored on destruction).
+struct DiffuseLaneView {
+    pms_ctx* d;
+    DBuf skeys, cell_info, nrm4, cell_start, spos, svel, cnt;
+    uint32_t n;
+    pms_grid grid;
+    bool have_aniso;
+    explicit DiffuseLaneView(pms_ctx* dl)
+        : d(dl), skeys(dl->skeys), cell_info(dl->cell_info), nrm4(dl->nrm4), cell_start(dl->cell_start), spos(dl->spos),
+          svel(dl->svel), cnt(dl->counters), n(dl->n), grid(dl->grid), have_aniso(dl->have_aniso) {}
+    void point(const pms_ctx* lc, BatchState* b, uint32_t f) {
+        d->skeys = lc->skeys; d->cell_info = lc->cell_info; d->nrm4 = lc->nrm4;
+        d->cell_start = lc->cell_start; d->spos = lc->spos; d->svel = lc->svel;
+        for (DBuf* x : {&d->skeys, &d->cell_info, &d->nrm4, &d->cell_start, &d->spos, &d->svel}) x->cap = SIZE_MAX;
+        d->counters.p = b->cnt.as<Counters>() + f;
+        d->counters.cap = SIZE_MAX;
+        d->n = b->n[f];
+        d->grid = b->grid[f];
+        d->have_aniso = true;
+    }
+    ~DiffuseLaneView() {
+        d->skeys = skeys; d->cell_info = cell_info; d->nrm4 = nrm4; d->cell_start = cell_start; d->spos = spos;
+        d->svel = svel; d->counters = cnt; d->n = n; d->grid = grid; d->have_aniso = have_aniso;
+    }
+};
+
 // Stages of one frame without host synchronisation (the context points at the frame).
 // band: 0 plain, 1 learned (network + certification), 2 certification alone
 static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, int band) {
@@ -141,7 +193,7 @@ static constexpr uint32_t kBatchLanes = 4;
 // lane l of the batch: the context itself for l = 0, else a sub-context
 static pms_ctx* lane_ctx(pms_ctx* c, BatchState* b, uint32_t l) { return l == 0 ? c : b->lanes[l - 1]; }
 
-static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes) {
+static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes, bool diffuse) {
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     const uint32_t k = (uint32_t)b->n.size();
     // frames to lanes, largest first onto the least loaded lane
@@ -155,36 +207,78 @@ static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes) 
         load[l] += b->n[f] + 1;
     }
     cudaGraph_t graph = nullptr;
+    pms_ctx* dl = diffuse ? b->dlane : nullptr;
     std::vector<uint64_t> launches0(nlanes);
     for (uint32_t l = 0; l < nlanes; ++l) launches0[l] = lane_ctx(c, b, l)->launches;
+    const uint64_t dlaunches0 = dl ? dl->launches : 0;
     PMS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
     pms_status st = PMS_OK;
     cudaError_t e = cudaMemsetAsync(b->base.as<unsigned long long>() + k, 0, sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess && dl) e = cudaMemsetAsync(b->drun.p, 0, sizeof(unsigned long long), c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(b->fork, c->stream);
     for (uint32_t l = 1; l < nlanes && e == cudaSuccess; ++l) e = cudaStreamWaitEvent(lane_ctx(c, b, l)->stream, b->fork, 0);
+    if (e == cudaSuccess && dl) e = cudaStreamWaitEvent(dl->stream, b->fork, 0);
     if (e != cudaSuccess) st = PMS_ERR_CUDA;
-    for (uint32_t l = 0; l < nlanes && !st; ++l) {
-        pms_ctx* lc = lane_ctx(c, b, l);
-        FrameView view(lc);
+    {
+        // frames in order, each on its lane; with diffuse generation each frame's diffuse
+        // stage follows on the diffuse lane, and the lane's next frame waits for it
+        std::vector<std::unique_ptr<FrameView>> views;
+        for (uint32_t l = 0; l < nlanes; ++l) views.emplace_back(new FrameView(lane_ctx(c, b, l)));
+        std::unique_ptr<DiffuseLaneView> dview(dl ? new DiffuseLaneView(dl) : nullptr);
+        std::vector<int> last(nlanes, -1);
+        if (dl) b->d_in = dl->d_old.p;
         for (uint32_t f = 0; f < k && !st; ++f) {
-            if (lane_of[f] != l) continue;
-            view.point(b, f);
+            const uint32_t l = lane_of[f];
+            pms_ctx* lc = lane_ctx(c, b, l);
+            if (dl && last[l] >= 0 && cudaStreamWaitEvent(lc->stream, b->ev_diff[(uint32_t)last[l]], 0) != cudaSuccess) {
+                st = PMS_ERR_CUDA;
+                break;
+            }
+            views[l]->point(b, f);
             // external: recorded when the graph runs (a plain record inside a capture only orders work)
             if (cudaEventRecordWithFlags(b->ev[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
             if ((st = capture_frame(lc, b, f, band))) break;
-            if (cudaEventRecordWithFlags(b->ev_end[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) st = PMS_ERR_CUDA;
+            if (cudaEventRecordWithFlags(b->ev_end[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
+            last[l] = (int)f;
+            if (!dl) continue;
+            if (cudaEventRecord(b->ev_surf[f], lc->stream) != cudaSuccess ||
+                cudaStreamWaitEvent(dl->stream, b->ev_surf[f], 0) != cudaSuccess) {
+                st = PMS_ERR_CUDA;
+                break;
+            }
+            dview->point(lc, b, f);
+            DiffuseBatch db;
+            db.gen_cap = b->gen_cap;
+            db.old_cap = b->old_cap;
+            db.old_dev = b->dcnt.as<uint32_t>();
+            db.frame_dev = b->dcnt.as<uint32_t>() + 1;
+            db.frame_off = f;
+            db.running = b->drun.as<unsigned long long>();
+            db.base = b->dbase.as<unsigned long long>() + f;
+            db.arena = b->darena.p;
+            db.arena_cap = b->darena_cap;
+            if ((st = launch_diffuse_bounded(dl, db))) break;
+            if (cudaEventRecord(b->ev_diff[f], dl->stream) != cudaSuccess) st = PMS_ERR_CUDA;
         }
+        if (dl) b->d_out = dl->d_old.p;
     }
     for (uint32_t l = 1; l < nlanes && !st; ++l) {
         if (cudaEventRecord(b->join[l - 1], lane_ctx(c, b, l)->stream) != cudaSuccess ||
             cudaStreamWaitEvent(c->stream, b->join[l - 1], 0) != cudaSuccess)
             st = PMS_ERR_CUDA;
     }
+    if (dl && !st &&
+        (cudaEventRecord(b->djoin, dl->stream) != cudaSuccess || cudaStreamWaitEvent(c->stream, b->djoin, 0) != cudaSuccess))
+        st = PMS_ERR_CUDA;
     c->batch_launches = 0;
     for (uint32_t l = 0; l < nlanes; ++l) {
         pms_ctx* lc = lane_ctx(c, b, l);
         c->batch_launches += lc->launches - launches0[l];
         lc->launches = launches0[l];          // counted when the graph runs
+    }
+    if (dl) {
+        c->batch_launches += dl->launches - dlaunches0;
+        dl->launches = dlaunches0;
     }
     e = cudaStreamEndCapture(c->stream, &graph);
     if (st) {
@@ -192,6 +286,7 @@ static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes) 
         // a lane's failure message lives on the lane
         for (uint32_t l = 1; l < nlanes; ++l)
             if (!lane_ctx(c, b, l)->last_error.empty()) c->last_error = lane_ctx(c, b, l)->last_error;
+        if (dl && !dl->last_error.empty()) c->last_error = dl->last_error;
         return st;
     }
     if (e != cudaSuccess) return pms_fail(c, PMS_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
@@ -251,10 +346,22 @@ static inline float decode_ordered(uint32_t u) {
     return f;
 }
 
+// the buffers a batch graph holds: every lane's, the diffuse lane's and the batch's own
+static uint64_t batch_signature(pms_ctx* c, BatchState* b, uint32_t nlanes, bool diffuse) {
+    uint64_t h = 0;
+    for (uint32_t l = 0; l < nlanes; ++l) h = h * 31u + dbuf_signature(lane_ctx(c, b, l), false);
+    if (diffuse && b->dlane) h = h * 31u + dbuf_signature(b->dlane, true);
+    for (DBuf* x : {&b->pos, &b->vel, &b->rho, &b->cnt, &b->base, &b->mesh, &b->dcnt, &b->drun, &b->dbase, &b->darena})
+        h = (h * 1099511628211ull) ^ (uint64_t)(uintptr_t)x->p ^ ((uint64_t)x->cap << 1);
+    return h;
+}
+
 extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_t k, int flags) {
     if (!c || (k && !frames)) return PMS_ERR_INVALID_ARGUMENT;
     const int band = (flags & PMS_BATCH_LEARNED) ? 1 : (flags & PMS_BATCH_CERTIFIED) ? 2 : 0;
     const bool learned = band != 0;          // the learned band's buffers and launches
+    const bool diffuse = c->cfg.is_diffuse != 0;
+    const int shape_flags = flags | (diffuse ? (1 << 16) : 0);
     if (band == 1 && !c->have_model) return pms_fail(c, PMS_ERR_STATE, "learned batch without a model");
     for (uint32_t f = 0; f < k; ++f)
         if (frames[f].n && !frames[f].pos_xyz) return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "frame %u: no positions", f);
@@ -279,7 +386,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     PMS_CUDA(c, b->rho.ensure(4 * T));
     PMS_CUDA(c, b->cnt.ensure(sizeof(Counters) * (k ? k : 1)));
     PMS_CUDA(c, b->base.ensure(sizeof(unsigned long long) * (k + 1)));
-    const bool shape_same = b->n == n && b->flags == flags;
+    const bool shape_same = b->n == n && b->flags == shape_flags;
     for (uint32_t f = 0; f < k; ++f) {
         const size_t m = n[f];
         if (!m) continue;
@@ -295,7 +402,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     }
     b->n = n;
     b->off = off;
-    b->flags = flags;
+    b->flags = shape_flags;
     pms_status st;
     {
         FrameView view(c);
@@ -339,6 +446,26 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
     if (!b->fork) PMS_CUDA(c, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     for (uint32_t l = 0; l < nlanes; ++l)
         if ((st = ensure_lane(lane_ctx(c, b, l), c, nmax, gmax, grid, learned))) return st;
+    if (diffuse) {
+        if (!b->dlane) {
+            pms_config lcfg = c->cfg;
+            lcfg.band_model[0] = 0;
+            if ((st = pms_create(&lcfg, c->device, &b->dlane))) return pms_fail(c, st, "batch diffuse lane context");
+            PMS_CUDA(c, cudaEventCreateWithFlags(&b->djoin, cudaEventDisableTiming));
+        }
+        while (b->ev_surf.size() < k) {
+            cudaEvent_t e0, e1;
+            PMS_CUDA(c, cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+            PMS_CUDA(c, cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+            b->ev_surf.push_back(e0);
+            b->ev_diff.push_back(e1);
+        }
+        // capacities: generated and carried particles per frame, and the arena of every
+        // frame's survivors (grown, and the batch run again, when a frame exceeds them)
+        b->gen_cap = std::max(b->gen_cap, std::max<uint32_t>(1u << 18, nmax / 4));
+        b->old_cap = std::max(b->old_cap, std::max<uint32_t>(1u << 20, 2 * c->diffuse_old));
+        b->darena_cap = std::max<uint64_t>(b->darena_cap, (uint64_t)k * (b->old_cap / 2));
+    }
     if (nlanes != b->nlanes_captured || c->tc_wait_polls != b->wait_captured) grids_same = false;
     uint64_t want_cap = 0;
     for (uint32_t f = 0; f < k; ++f) {
@@ -355,13 +482,30 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         b->ev_end.push_back(e1);
     }
     // ---- pass 2: the graph (captured again when the frames' grids or any buffer changed)
-    for (int attempt = 0; attempt < 3; ++attempt) {
-        if (!grids_same || !b->exec || b->gen != g_dbuf_generation) {
-            if ((st = capture(c, b, band, nlanes))) return st;
-            b->gen = g_dbuf_generation;
+    const int attempts = diffuse ? 8 : 3;
+    for (int attempt = 0; attempt < attempts; ++attempt) {
+        if (diffuse) {
+            pms_ctx* dl = b->dlane;
+            if ((st = ensure_diffuse_batch_buffers(dl, nmax, b->gen_cap, b->old_cap))) return st;
+            PMS_CUDA(c, dl->scan.partial.ensure(sizeof(unsigned long long) * 1024));
+            PMS_CUDA(c, b->dcnt.ensure(2 * sizeof(uint32_t)));
+            PMS_CUDA(c, b->drun.ensure(sizeof(unsigned long long)));
+            PMS_CUDA(c, b->dbase.ensure(sizeof(unsigned long long) * k));
+            PMS_CUDA(c, b->darena.ensure(32 * (b->darena_cap ? b->darena_cap : 1)));
+        }
+        if (!grids_same || !b->exec || b->sig != batch_signature(c, b, nlanes, diffuse)) {
+            if ((st = capture(c, b, band, nlanes, diffuse))) return st;
+            b->sig = batch_signature(c, b, nlanes, diffuse);
             b->nlanes_captured = nlanes;
             b->wait_captured = c->tc_wait_polls;
             grids_same = true;
+        }
+        if (diffuse) {
+            // the context's carried particles and frame counter enter the batch
+            const uint32_t in[2] = {c->diffuse_old, c->frame_index};
+            if (c->diffuse_old)
+                PMS_CUDA(c, cudaMemcpyAsync(b->d_in, c->d_old.p, 32 * (size_t)c->diffuse_old, cudaMemcpyDeviceToDevice, c->stream));
+            PMS_CUDA(c, cudaMemcpyAsync(b->dcnt.p, in, sizeof(in), cudaMemcpyHostToDevice, c->stream));
         }
         PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
         c->launches += c->batch_launches;
@@ -375,11 +519,44 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
             if ((st = check_frame_errors(c, b->hcnt[f], f))) return st;
             overflow |= (b->hcnt[f].err & kErrCapacity) != 0;
         }
+        unsigned long long dfill = 0;
+        if (diffuse) PMS_CUDA(c, cudaMemcpy(&dfill, b->drun.p, sizeof(dfill), cudaMemcpyDeviceToHost));
         if (!overflow) break;
-        b->mesh_cap = std::max<uint64_t>(2 * b->mesh_cap, b->hbase[k] + (b->hbase[k] >> 2));
-        PMS_CUDA(c, b->mesh.ensure(12 * b->mesh_cap));
+        if (attempt == attempts - 1) return pms_fail(c, PMS_ERR_CAPACITY, "batch capacity overflow");
+        if (b->hbase[k] > b->mesh_cap) {
+            b->mesh_cap = std::max<uint64_t>(2 * b->mesh_cap, b->hbase[k] + (b->hbase[k] >> 2));
+            PMS_CUDA(c, b->mesh.ensure(12 * b->mesh_cap));
+        }
+        if (diffuse) {
+            // a frame past a capacity: its count (and every later frame's) is a lower bound
+            uint32_t gmax_seen = 0, omax_seen = 0;
+            bool hit = false;
+            for (uint32_t f = 0; f < k; ++f) {
+                const Counters& h = b->hcnt[f];
+                gmax_seen = std::max(gmax_seen, h.n_generated);
+                omax_seen = std::max(omax_seen, h.n_live);
+                hit |= (h.err & kErrCapacity) != 0 && h.n_generated > b->gen_cap;
+            }
+            if (hit) b->gen_cap = std::max<uint32_t>(2 * b->gen_cap, gmax_seen + (gmax_seen >> 2));
+            if (omax_seen >= b->old_cap || hit) b->old_cap = std::max<uint32_t>(2 * b->old_cap, omax_seen + (omax_seen >> 2));
+            if (dfill >= b->darena_cap || hit || omax_seen >= b->old_cap)
+                b->darena_cap = std::max<uint64_t>(2 * b->darena_cap, dfill + (dfill >> 2));
+            b->darena_cap = std::max<uint64_t>(b->darena_cap, (uint64_t)k * (b->old_cap / 2));
+        }
         grids_same = false;
-        if (attempt == 2) return pms_fail(c, PMS_ERR_CAPACITY, "batch mesh arena overflow");
+    }
+    if (diffuse) {
+        // the last frame's survivors leave the batch: the context's carried particles and
+        // frame counter continue the sequence
+        b->hdbase.resize(k);
+        PMS_CUDA(c, cudaMemcpy(b->hdbase.data(), b->dbase.p, sizeof(unsigned long long) * k, cudaMemcpyDeviceToHost));
+        const uint32_t last = std::min(b->hcnt[k - 1].n_live, b->old_cap);
+        PMS_CUDA(c, c->d_old.ensure(32 * (size_t)(last ? last : 1)));
+        if (last) PMS_CUDA(c, cudaMemcpyAsync(c->d_old.p, b->d_out, 32 * (size_t)last, cudaMemcpyDeviceToDevice, c->stream));
+        PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+        c->diffuse_old = last;
+        c->frame_index += k;
+        c->have_diffuse = true;
     }
     return PMS_OK;
 }
@@ -397,6 +574,15 @@ extern "C" pms_status pms_batch_frame(pms_ctx* c, uint32_t f, pms_counts* out, f
         out->n_valid_cubes = h.nvalid;
         out->n_mesh_vertices = h.nmesh;
         out->n_fp64_svd = h.n_fp64;
+        if (b->flags & (1 << 16)) {
+            out->n_free_surface = h.n_free;
+            out->n_spawning = h.n_spawning;
+            out->n_generated_diffuse = h.n_generated;
+            out->n_diffuse = h.n_live;
+            out->n_spray = h.n_type[0];
+            out->n_foam = h.n_type[1];
+            out->n_bubble = h.n_type[2];
+        }
         if (b->flags & (PMS_BATCH_LEARNED | PMS_BATCH_CERTIFIED)) {
             out->n_band_candidates = h.l_cand;
             out->n_band_predicted = h.l_pred;
@@ -425,6 +611,22 @@ extern "C" pms_status pms_batch_mesh(pms_ctx* c, uint32_t f, float* pos, uint64_
     if (cap < m) return PMS_ERR_CAPACITY;
     cudaSetDevice(c->device);
     if (m) PMS_CUDA(c, cudaMemcpyAsync(pos, b->mesh.as<float>() + 3 * b->hbase[f], 12 * m, cudaMemcpyDeviceToHost, c->stream));
+    PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_diffuse(pms_ctx* c, uint32_t f, pms_diffuse_particle* out, uint64_t cap, uint64_t* n_out) {
+    if (!c || !c->batch || !n_out) return PMS_ERR_INVALID_ARGUMENT;
+    BatchState* b = static_cast<BatchState*>(c->batch);
+    if (f >= b->n.size()) return PMS_ERR_INVALID_ARGUMENT;
+    if (!(b->flags & (1 << 16)) || b->hdbase.size() != b->n.size())
+        return pms_fail(c, PMS_ERR_STATE, "the last batch ran without diffuse generation");
+    const uint64_t m = b->hcnt[f].n_live;
+    *n_out = m;
+    if (!out) return PMS_OK;
+    if (cap < m) return PMS_ERR_CAPACITY;
+    cudaSetDevice(c->device);
+    if (m) PMS_CUDA(c, cudaMemcpyAsync(out, b->darena.as<char>() + 32 * b->hdbase[f], 32 * m, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PMS_OK;
 }

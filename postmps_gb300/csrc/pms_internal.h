@@ -18,16 +18,13 @@ namespace pms {
 // ---------------------------------------------------------------------------
 // device buffers: grow-only, contents not preserved across growth
 // ---------------------------------------------------------------------------
-// Every (re)allocation or release bumps this generation: a captured CUDA graph
-// holds raw buffer addresses and is captured again when it has changed.
-inline std::atomic<uint64_t> g_dbuf_generation{0};
-
+// A captured CUDA graph holds raw buffer addresses: it is captured again when the
+// signature of the buffers it uses (dbuf_signature) has changed.
 struct DBuf {
     void* p = nullptr;
     size_t cap = 0;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap && p) return cudaSuccess;
-        ++g_dbuf_generation;
         if (p) { cudaFree(p); p = nullptr; cap = 0; }
         size_t want = bytes < 256 ? 256 : bytes;
         cudaError_t e = cudaMalloc(&p, want);
@@ -35,7 +32,7 @@ struct DBuf {
         return e;
     }
     void release() {
-        if (p) { ++g_dbuf_generation; cudaFree(p); }
+        if (p) cudaFree(p);
         p = nullptr;
         cap = 0;
     }
@@ -59,7 +56,7 @@ struct Counters {
     uint32_t n_free;        // free-surface particles
     uint32_t n_spawning;    // particles that spawn diffuse particles
     uint32_t n_generated;   // generated diffuse particles
-    uint32_t n_old;         // live diffuse particles carried from the last frame
+    uint32_t n_old;         // live diffuse particles carried from the last frame (batched frames)
     uint32_t n_live;        // after delete/append
     uint32_t n_type[4];     // spray, foam, bubble, deleted
     uint32_t rad_max_bits;  // largest anisotropic support maxvalue * h (float bits)
@@ -73,6 +70,7 @@ struct Counters {
     uint32_t n_items;       // work items of the last field launch
     uint32_t n_tiles;       // scalar-grid tiles the band marking visits
     uint32_t n_weld;        // vertices of the welded mesh (crossed grid edges)
+    uint32_t n_df_total;    // generated + carried diffuse particles of a batched frame
 };
 static constexpr int kLearnCounters = 6;
 
@@ -287,10 +285,30 @@ pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsi
                              unsigned long long cap, uint32_t v_lo = 0,
                              uint32_t v_hi = 0xffffffffu);
 pms_status launch_diffuse(pms_ctx* ctx);
+// A batched frame's diffuse stage: every size is a capacity and every count lives on the
+// device, so it can be captured into a graph.  The carried particles come from ctx->d_old
+// (their count at *old_dev, set by the frame before), the survivors go to ctx->d_all and
+// (the buffers then swap, on the host, at capture) their count to *old_dev, and a copy of
+// them lands in the arena at a running offset.
+struct DiffuseBatch {
+    uint32_t gen_cap = 0, old_cap = 0;       // generated and carried particles a frame may hold
+    uint32_t* old_dev = nullptr;             // carried count (in: this frame's; out: the next frame's)
+    const uint32_t* frame_dev = nullptr;     // frame counter of the batch's first frame
+    uint32_t frame_off = 0;                  // this frame's place in the batch
+    unsigned long long* running = nullptr;   // arena fill (device)
+    unsigned long long* base = nullptr;      // this frame's arena offset (device)
+    void* arena = nullptr;                   // 32-byte diffuse records
+    uint64_t arena_cap = 0;                  // records the arena holds
+};
+pms_status ensure_diffuse_batch_buffers(pms_ctx* ctx, uint32_t nmax, uint32_t gen_cap, uint32_t old_cap);
+pms_status launch_diffuse_bounded(pms_ctx* ctx, const DiffuseBatch& db);
 pms_status upload_mc_tables(pms_ctx* ctx);
 
 // host utilities
 pms_status sync_counters(pms_ctx* ctx);
+// a hash of the addresses and sizes of a context's device buffers (without the
+// diffuse stage's unless asked for)
+uint64_t dbuf_signature(pms_ctx* c, bool diffuse);
 }  // namespace pms
 void pms_batch_release(pms_ctx* c);   // pms_batch.cpp
 namespace pms {

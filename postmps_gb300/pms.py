@@ -104,6 +104,10 @@ class Counts(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+# pms_diffuse_particle, the streamed and batched diffuse records
+DIFFUSE_RECORD = np.dtype([("pos", np.float32, 3), ("ttl", np.int32), ("vel", np.float32, 3), ("type", np.int32)])
+
+
 class Tune(C.Structure):
     """pms_tune: launch shapes of the neighbour walks."""
     _fields_ = [("field_threads", C.c_int), ("field_waves", C.c_int), ("density_threads", C.c_int),
@@ -213,6 +217,7 @@ def lib() -> C.CDLL:
         L.pms_get_tune.argtypes = [vp, C.POINTER(Tune)]
         L.pms_batch_frame.argtypes = [vp, C.c_uint32, C.POINTER(Counts), C.POINTER(C.c_float)]
         L.pms_batch_mesh.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.pms_batch_diffuse.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
         L.pms_batch_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.pms_save_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel), C.c_char_p]
         L.pms_load_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel)]
@@ -483,6 +488,16 @@ class Context:
         out = np.zeros((n.value, 3), np.float32)
         if n.value:
             self._call("pms_batch_mesh", f, _ptr(out), n.value, C.byref(n))
+        return out
+
+    def batch_diffuse(self, f: int) -> np.ndarray:
+        """Live diffuse particles of frame f of the last batch: records of pos (3 float),
+        ttl (int32), vel (3 float), type (int32)."""
+        n = C.c_uint64()
+        self._call("pms_batch_diffuse", f, None, 0, C.byref(n))
+        out = np.zeros(n.value, DIFFUSE_RECORD)
+        if n.value:
+            self._call("pms_batch_diffuse", f, out.ctypes.data, n.value, C.byref(n))
         return out
 
     def batch_info(self) -> dict:

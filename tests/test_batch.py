@@ -191,3 +191,59 @@ def test_streamed_mesh_equals_download(pms_lib, diffuse):
         ctx.stream_mesh_to_host(0, None, 0)
         with pytest.raises(pms.PmsError):
             ctx.wait_mesh()
+
+
+@pytest.mark.gpu
+def test_batch_with_diffuse_equals_single_frames(pms_lib, tmp_config):
+    """Diffuse generation inside the batch graph: consecutive crown frames (one of them
+    smaller) batched give, frame by frame, the live diffuse particles, counts and meshes
+    of running them one by one, and leave the context where the single frames leave
+    theirs -- a single frame after the batch, and a second batch (the graph relaunched),
+    continue the same sequence."""
+    from postmps_gb300 import synth
+    pms = pms_lib
+    pos, vel, rho = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    small = synth.crown_splash(n_slab=(40, 40, 10), n_ring=20000, radius=0.07, seed=9)
+
+    def frame(i):
+        if i == 2:
+            return small
+        return ((pos + np.float32(0.004 * i) * vel).astype(np.float32), vel, rho)
+
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"})))
+    with pms.Context(cfg, 0) as single, pms.Context(cfg, 0) as batch:
+        def run_single(i):
+            single.upload(*frame(i))
+            single.run_frame()
+            live = single.diffuse_particles(-1)
+            return live, single.counts().as_dict(), single.mesh(normals=False)[0].copy()
+
+        def check_batch(idx):
+            batch.run_batch([frame(i) for i in idx])
+            for f, i in enumerate(idx):
+                live, c, mesh = run_single(i)
+                got = batch.batch_diffuse(f)
+                assert len(got) == len(live["pos"]), (i, len(got), len(live["pos"]))
+                np.testing.assert_array_equal(got["pos"], live["pos"])
+                np.testing.assert_array_equal(got["vel"], live["vel"])
+                np.testing.assert_array_equal(got["ttl"], live["ttl"])
+                np.testing.assert_array_equal(got["type"], live["type"])
+                bc = batch.batch_frame(f)[0].as_dict()
+                for key in ("n_generated_diffuse", "n_spawning", "n_diffuse", "n_spray", "n_foam", "n_bubble",
+                            "n_free_surface", "n_mesh_vertices"):
+                    assert bc[key] == c[key], (i, key, bc[key], c[key])
+                np.testing.assert_array_equal(batch.batch_mesh(f), mesh)
+
+        check_batch([0, 1, 2, 3, 4])
+        assert batch.batch_frame(4)[0].as_dict()["n_diffuse"] > 0
+        # one frame alone on the batched context continues the sequence
+        batch.upload(*frame(5))
+        batch.run_frame()
+        live, _, _ = run_single(5)
+        np.testing.assert_array_equal(batch.diffuse_particles(-1)["pos"], live["pos"])
+        # a second batch (other grids: captured again) continues it, and the same frames
+        # once more relaunch that graph from the carried particles the context now holds
+        check_batch([6, 7, 8, 9, 10])
+        caps = batch.batch_info()["captures"]
+        check_batch([6, 7, 8, 9, 10])
+        assert batch.batch_info()["captures"] == caps
