@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(kTileThreads) k_band_tiles(KGrid g, float h, i
     __shared__ uint32_t sxin[kTileChunk];        // tile x positions inside its box and AABB (0: nothing to mark)
     __shared__ uint32_t syz[kTileChunk];         // its box inside the tile: y0 | y1 << 8 | z0 << 16 | z1 << 24
     __shared__ uint32_t red[kTileGroups][kTileZ * kTileY];
+    __shared__ uint32_t s_nrel;                  // staged particles of the chunk whose box reaches the tile
     const uint32_t n_tiles = *n_tiles_dev;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t srx = g.spres[0], sry = g.spres[1];
@@ -164,7 +165,11 @@ __global__ void __launch_bounds__(kTileThreads) k_band_tiles(KGrid g, float h, i
             const uint32_t total = pre[nr];
             for (uint32_t c0 = 0; c0 < total; c0 += kTileChunk) {
                 const uint32_t nc = min((uint32_t)kTileChunk, total - c0);
-                // stage the chunk
+                if (tid == 0) s_nrel = 0u;
+                __syncthreads();
+                // stage the chunk: only particles whose box reaches the tile take a slot (the
+                // cell rows around the tile hold about twice as many), so the rows' loops below
+                // see no particle that marks nothing; marks are an OR, the slot order is free
                 if (tid < nc) {
                     const uint32_t k = c0 + tid;
                     int lo = 0, hi = nr - 1;     // the row holding entry k: the last row whose prefix is <= k
@@ -189,17 +194,28 @@ __global__ void __launch_bounds__(kTileThreads) k_band_tiles(KGrid g, float h, i
                             if (!(vx < ax || vx > bx)) xin |= 1u << (x - t0[0]);
                         }
                     }
-                    sp[tid] = p4;
-                    sn[tid] = n4;
-                    sxin[tid] = xin;
-                    syz[tid] = xin ? (uint32_t)(y0 - t0[1]) | (uint32_t)(y1 - t0[1]) << 8 | (uint32_t)(z0 - t0[2]) << 16 |
-                                         (uint32_t)(z1 - t0[2]) << 24
-                                   : 0u;
+                    // the warp's lanes staging this chunk (tid < nc), named for the ballot
+                    const uint32_t nin = min(32u, nc - (tid & ~31u));
+                    const unsigned act = nin == 32u ? 0xffffffffu : ((1u << nin) - 1u);
+                    const unsigned want = __ballot_sync(act, xin != 0u);
+                    uint32_t slot0 = 0u;
+                    const int leader = __ffs(act) - 1;
+                    if ((int)lane == leader && want) slot0 = atomicAdd(&s_nrel, (uint32_t)__popc(want));
+                    slot0 = __shfl_sync(act, slot0, leader);
+                    if (xin) {
+                        const uint32_t slot = slot0 + (uint32_t)__popc(want & ((1u << lane) - 1u));
+                        sp[slot] = p4;
+                        sn[slot] = n4;
+                        sxin[slot] = xin;
+                        syz[slot] = (uint32_t)(y0 - t0[1]) | (uint32_t)(y1 - t0[1]) << 8 | (uint32_t)(z0 - t0[2]) << 16 |
+                                    (uint32_t)(z1 - t0[2]) << 24;
+                    }
                 }
                 __syncthreads();
+                const uint32_t nrel = s_nrel;
                 // this thread's row against its share of the chunk
                 if (row_in) {
-                    for (uint32_t k = (uint32_t)my_group; k < nc; k += kTileGroups) {
+                    for (uint32_t k = (uint32_t)my_group; k < nrel; k += kTileGroups) {
                         const uint32_t xin = sxin[k];
                         const uint32_t yz = syz[k];
                         if (!xin || my_y < (int)(yz & 0xffu) || my_y > (int)((yz >> 8) & 0xffu) ||

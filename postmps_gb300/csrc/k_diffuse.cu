@@ -762,13 +762,13 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     const uint32_t n_gen = ctx->h_counters->n_generated, n_spawn = ctx->h_counters->n_spawning;
     const uint32_t n_old = ctx->diffuse_old;
     const size_t total = (size_t)n_gen + n_old;
-    PMS_CUDA(ctx, ctx->d_gen.ensure(sizeof(DiffuseParticle) * (n_gen ? n_gen : 1)));
-    PMS_CUDA(ctx, ctx->d_all.ensure(sizeof(DiffuseParticle) * (total ? total : 1)));
-    PMS_CUDA(ctx, ctx->d_typescan.ensure(8 * (total ? total : 1)));
+    PMS_CUDA(ctx, ctx->d_gen.ensure_grow(sizeof(DiffuseParticle) * (n_gen ? n_gen : 1)));
+    PMS_CUDA(ctx, ctx->d_all.ensure_grow(sizeof(DiffuseParticle) * (total ? total : 1)));
+    PMS_CUDA(ctx, ctx->d_typescan.ensure_grow(8 * (total ? total : 1)));
     if (n_old) {
-        PMS_CUDA(ctx, ctx->d_tkey.ensure(8 * (size_t)n_old));
-        PMS_CUDA(ctx, ctx->d_tscan.ensure(8 * (size_t)n_old));
-        PMS_CUDA(ctx, ctx->d_perm.ensure(4 * (size_t)n_old));
+        PMS_CUDA(ctx, ctx->d_tkey.ensure_grow(8 * (size_t)n_old));
+        PMS_CUDA(ctx, ctx->d_tscan.ensure_grow(8 * (size_t)n_old));
+        PMS_CUDA(ctx, ctx->d_perm.ensure_grow(4 * (size_t)n_old));
     }
     const DfN dn = {n_gen, n_old, nullptr, nullptr, (uint32_t)(total ? total : 1), &cnt->err};
     if ((st = diffuse_tail(ctx, g, dp, cnt, dn, n_spawn, nullptr, 0, &cnt->n_live))) return st;

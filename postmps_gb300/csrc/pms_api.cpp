@@ -229,18 +229,19 @@ void mark_stage(pms_ctx* c, int boundary);
 pms_status plain_band(pms_ctx* c);
 }  // namespace pms
 
+// the band's size changes from frame to frame: its buffers grow with headroom
 pms_status pms::ensure_band_buffers(pms_ctx* c, uint32_t nv) {
     const size_t V = nv ? nv : 1;
-    PMS_CUDA(c, c->vlist.ensure(4 * V));
-    PMS_CUDA(c, c->field.ensure(4 * V));
-    PMS_CUDA(c, c->mc_case.ensure(4 * V));
-    PMS_CUDA(c, c->mc_key.ensure(8 * V));
-    PMS_CUDA(c, c->mc_off.ensure(8 * V));
-    PMS_CUDA(c, c->valid.ensure(4 * V));
-    PMS_CUDA(c, c->cube.ensure(16 * V));
-    PMS_CUDA(c, c->fitems.ensure(4 * (V + 1)));
-    PMS_CUDA(c, c->fitem_cnt.ensure(4 * (V + 1)));
-    PMS_CUDA(c, c->fitem_off.ensure(4 * (V + 1)));
+    PMS_CUDA(c, c->vlist.ensure_grow(4 * V));
+    PMS_CUDA(c, c->field.ensure_grow(4 * V));
+    PMS_CUDA(c, c->mc_case.ensure_grow(4 * V));
+    PMS_CUDA(c, c->mc_key.ensure_grow(8 * V));
+    PMS_CUDA(c, c->mc_off.ensure_grow(8 * V));
+    PMS_CUDA(c, c->valid.ensure_grow(4 * V));
+    PMS_CUDA(c, c->cube.ensure_grow(16 * V));
+    PMS_CUDA(c, c->fitems.ensure_grow(4 * (V + 1)));
+    PMS_CUDA(c, c->fitem_cnt.ensure_grow(4 * (V + 1)));
+    PMS_CUDA(c, c->fitem_off.ensure_grow(4 * (V + 1)));
     return PMS_OK;
 }
 
@@ -541,9 +542,9 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         const size_t M = c->nmesh ? c->nmesh : 1;
         // the previous frame's mesh may still be on its way to the host
         if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
-        PMS_CUDA(c, c->vert.ensure(12 * M));
+        PMS_CUDA(c, c->vert.ensure_grow(12 * M));
         c->mesh_normals = c->out_pos && c->out_nrm;
-        if (c->mesh_normals) PMS_CUDA(c, c->vnorm.ensure(12 * M));
+        if (c->mesh_normals) PMS_CUDA(c, c->vnorm.ensure_grow(12 * M));
         // a streamed mesh goes in pieces: the emission runs in vertex ranges and each
         // piece travels on the copy stream while the next is made and the stages after run
         const bool copy = c->out_pos && c->nmesh <= c->out_cap;

@@ -31,6 +31,12 @@ struct DBuf {
         if (e == cudaSuccess) cap = want;
         return e;
     }
+    // for sizes that grow from frame to frame (the carried diffuse set): half again as
+    // much room, so that a slowly growing need does not reallocate (and synchronise) every frame
+    cudaError_t ensure_grow(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        return ensure(bytes + bytes / 2);
+    }
     void release() {
         if (p) cudaFree(p);
         p = nullptr;
