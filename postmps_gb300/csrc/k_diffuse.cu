@@ -158,7 +158,15 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_normal(KGrid g, DiffuseParam
 // ---------------------------------------------------------------------------
 // potentials
 // ---------------------------------------------------------------------------
-// calculationofTrappedairpotential: every particle
+__device__ __forceinline__ float phi_clamp(float I, float tmin, float tmax) {
+    return __fdiv_rn(__fsub_rn(fminf(I, tmax), fminf(I, tmin)), __fsub_rn(tmax, tmin));
+}
+
+// calculationofTrappedairpotential: every particle.  A particle spawns
+// floor(ke (ta_mult TA + wc_mult WC) dt) diffuse particles with ke its clamped kinetic
+// energy: where ke clamps to 0 (a particle at rest) the count is 0 whatever its
+// trapped air and wave crest, so those walks are skipped and the potentials left 0;
+// every count, and so every output, is the reference's.
 __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffuseParams dp, const uint32_t* __restrict__ cell_start,
                                                          const float4* __restrict__ spos, const float4* __restrict__ svel,
                                                          uint32_t n, float4* __restrict__ pot) {
@@ -166,6 +174,15 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 p4 = spos[i], v = svel[i];
         const float3 p = make_float3(p4.x, p4.y, p4.z);
+        // 0.5 * (double)m * (double)|v|^2 rounded to float: the double product of two floats
+        // is exact and the halving too, so it is the float product rounded once, halved (the
+        // two could differ only for energies below the normal float range, ~1e-38)
+        const float ke = 0.5f * __fmul_rn(dp.mass, v.x * v.x + v.y * v.y + v.z * v.z);
+        pot[i].z = ke;
+        if (phi_clamp(ke, dp.min_ke, dp.max_ke) == 0.f) {
+            pot[i].y = 0.f;
+            continue;
+        }
         uint3 lo, hi;
         diffuse_box(g, p.x, p.y, p.z, lo, hi);
         hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);
@@ -191,10 +208,6 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_trapped(KGrid g, DiffusePara
             }
         });
         pot[i].y = ita;
-        // 0.5 * (double)m * (double)|v|^2 rounded to float: the double product of two floats
-        // is exact and the halving too, so it is the float product rounded once, halved (the
-        // two could differ only for energies below the normal float range, ~1e-38)
-        pot[i].z = 0.5f * __fmul_rn(dp.mass, v.x * v.x + v.y * v.y + v.z * v.z);
     }
 }
 
@@ -212,7 +225,10 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
         const float3 p = make_float3(p4.x, p4.y, p4.z);
         const float nn = dot_rn(ni.x, ni.y, ni.z, ni.x, ni.y, ni.z);
         const float vv = dot_rn(v.x, v.y, v.z, v.x, v.y, v.z);
-        if (nn <= kEpsDown || vv <= kEpsDown || dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < k06Up) {
+        // the reference's zero cases, and a particle that spawns nothing (its clamped kinetic
+        // energy, from the trapped-air pass, is 0)
+        if (nn <= kEpsDown || vv <= kEpsDown || dot_rn(v.x, v.y, v.z, ni.x, ni.y, ni.z) < k06Up ||
+            phi_clamp(pot[i].z, dp.min_ke, dp.max_ke) == 0.f) {
             pot[i].x = 0.f;
             continue;
         }
@@ -243,9 +259,6 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_crests(KGrid g, DiffuseParam
     }
 }
 
-__device__ __forceinline__ float phi_clamp(float I, float tmin, float tmax) {
-    return __fdiv_rn(__fsub_rn(fminf(I, tmax), fminf(I, tmin)), __fsub_rn(tmax, tmin));
-}
 
 // calculateofNumberofdiffuseparticles; key = spawning << 32 | count for one 64-bit scan
 __global__ void __launch_bounds__(256) k_df_count(DiffuseParams dp, float4* __restrict__ pot, uint32_t n,

@@ -119,7 +119,13 @@ def check_gpu_frames(oracle, d, gpu, reference: bool):
         if reference:
             assert len(slist) == len(d[f"f{fr}_free_list"])
             # potentials against the reference (float32 vs float32, different summation order)
-            assert float(np.abs(r["pot"] - d[f"f{fr}_pot"]).max()) < 1e-3
+            # where they are used: a particle whose clamped kinetic energy is 0 spawns
+            # nothing, and its trapped-air and wave-crest walks are skipped (left 0)
+            ref_pot = d[f"f{fr}_pot"]
+            assert float(np.abs(r["pot"][:, 2] - ref_pot[:, 2]).max(initial=0)) < 1e-5
+            moving = (r["pot"][:, 2] > 0) & (ref_pot[:, 2] > 0)
+            assert float(np.abs(r["pot"][moving] - ref_pot[moving]).max(initial=0)) < 1e-3
+            assert not r["pot"][r["pot"][:, 2] == 0][:, :2].any()
         # counts: exact from the GPU's own clamped potentials
         spos, svel = pos[perm], vel[perm]
         res = oracle.diffuse_frame(p, g, spos, svel, start, end, slist, np.zeros_like(spos, np.float64),
