@@ -482,22 +482,35 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         if st:
             stage_err.append(st)
 
+    # a staging thread of the loop's own, woken once per frame
+    go, done, stop = threading.Semaphore(0), threading.Semaphore(0), []
+
+    def stager():
+        while True:
+            go.acquire()
+            if stop:
+                return
+            stage_next()
+            done.release()
+
+    worker = threading.Thread(target=stager, daemon=True)
+    worker.start()
+
     def step_e2e():
         # the user's calls of a pipelined frame loop: take the frame staged during the
         # step before (its pinned copy and host-to-device copy ran while that frame
-        # computed), stage the next frame from another thread while this one runs,
-        # reconstruct with the triangle soup streamed into pinned host memory while the
-        # diffuse stage runs and the live diffuse particles streamed after it, wait for
-        # both.  Every step moves one frame's inputs host to device inside the timed
+        # computed), stage the next frame on the loop's staging thread while this one
+        # runs, reconstruct with the triangle soup streamed into pinned host memory while
+        # the diffuse stage runs and the live diffuse particles streamed after it, wait
+        # for both.  Every step moves one frame's inputs host to device inside the timed
         # region (the frame it stages) and reads its own results back.
         ctx.upload_staged()
-        t = threading.Thread(target=stage_next)
-        t.start()
+        go.release()
         ctx.run_frame()
         host["n_mesh"] = ctx.wait_mesh()
         if diffuse:
             host["n_diffuse"] = ctx.wait_diffuse()
-        t.join()
+        done.acquire()
         if stage_err:
             raise RuntimeError(f"pms_stage_particles failed: status {stage_err[0]}")
 
@@ -544,6 +557,9 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         step_e2e()
     ms_e2e = timer(step_e2e, args.steps)
     clk = clocks.stop() if clocks else None
+    stop.append(True)
+    go.release()
+    worker.join()
     ctx.upload_staged()                       # the frame staged by the last step
     ctx.stream_mesh_to_host(0, None, 0)
     if diffuse:
