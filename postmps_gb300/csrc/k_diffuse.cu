@@ -290,26 +290,22 @@ __global__ void __launch_bounds__(256) k_df_spawnlist(const unsigned long long* 
         if (key[i]) list[(uint32_t)(off[i] >> 32)] = i;
 }
 
-// neighbours of x within hd (squared distance <= hd^2), calculateofDiffuseType
-__device__ __forceinline__ int count_within(const KGrid& g, const DiffuseParams& dp, const uint2* __restrict__ cell_info,
-                                            const float4* __restrict__ spos, float px, float py, float pz, bool squared) {
-    const uint32_t rx = g.spres[0], rxy = g.spres[0] * g.spres[1];
+// Particles with |s|^2 <= hd^2 (the generator's test; calculateofDiffuseType) over the
+// diffuse box, walking only the rows and cells of the box that come within hd: a cell
+// left out holds no particle the count would take, so the count is the reference's.
+__device__ __forceinline__ int count_within_gen(const KGrid& g, const DiffuseParams& dp,
+                                                const uint32_t* __restrict__ cell_start, const float4* __restrict__ spos,
+                                                float px, float py, float pz) {
     uint3 lo, hi;
     diffuse_box(g, px, py, pz, lo, hi);
+    hi = make_uint3(hi.x + 1, hi.y + 1, hi.z + 1);          // row_walk takes [lo, hi)
+    const float r = dp.hd * kSupportGrow;
     int count = 0;
-    for (uint32_t z = lo.z; z <= hi.z; ++z)
-        for (uint32_t y = lo.y; y <= hi.y; ++y)
-            for (uint32_t x = lo.x; x <= hi.x; ++x) {
-                const uint2 ci = cell_info[z * rxy + y * rx + x];
-                const uint32_t m = ci.y & 0x7fffffffu;
-                for (uint32_t j = ci.x; j < ci.x + m; ++j) {
-                    const float4 q = spos[j];
-                    const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
-                    const float d2 = dot_rn(sx, sy, sz, sx, sy, sz);
-                    // the generator compares |s|^2 <= hd^2, the advection |s| <= hd
-                    if (squared ? (d2 <= dp.hd_sq) : (__fsqrt_rn(d2) <= dp.hd)) ++count;
-                }
-            }
+    row_walk(g, make_float3(px, py, pz), lo, hi, r * r, 1e-4f * g.sp_cs, cell_start, [&](uint32_t j) {
+        const float4 q = __ldg(&spos[j]);
+        const float sx = __fsub_rn(px, q.x), sy = __fsub_rn(py, q.y), sz = __fsub_rn(pz, q.z);
+        if (dot_rn(sx, sy, sz, sx, sy, sz) <= dp.hd_sq) ++count;
+    });
     return count;
 }
 
@@ -319,7 +315,7 @@ __device__ __forceinline__ int type_of(int density) { return density > kBubble ?
 __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams dp, const Counters* __restrict__ cnt,
                                                        const uint32_t* __restrict__ spawnlist,
                                                        const unsigned long long* __restrict__ off,
-                                                       const int32_t* __restrict__ num, const uint2* __restrict__ cell_info,
+                                                       const int32_t* __restrict__ num, const uint32_t* __restrict__ cell_start,
                                                        const float4* __restrict__ spos, const float4* __restrict__ svel,
                                                        DiffuseParticle* __restrict__ gen, uint32_t gen_cap,
                                                        const uint32_t* __restrict__ frame_dev, uint32_t frame_off,
@@ -346,7 +342,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_df_spawn(KGrid g, DiffuseParams
         e2x *= il; e2y *= il; e2z *= il;
         const int k = num[i];
         const uint32_t start = (uint32_t)(off[i] & 0xffffffffull);
-        const int type = type_of(count_within(g, dp, cell_info, spos, p.x, p.y, p.z, true));
+        const int type = type_of(count_within_gen(g, dp, cell_start, spos, p.x, p.y, p.z));
         for (int c = 0; c < k; ++c) {
             const uint64_t idif = (uint64_t)start + (uint64_t)c;
             const float u1 = spawn_uniform(dp.seed, frame, 3 * idif + 1);
@@ -724,7 +720,7 @@ static pms_status diffuse_tail(pms_ctx* ctx, const KGrid& g, const DiffuseParams
     if (spawn_bound)
         k_df_spawn<<<grid_for(spawn_bound, kThreads), kThreads, 0, ctx->stream>>>(
             g, dp, cnt, ctx->d_difflist.as<uint32_t>(), ctx->d_isdiffscan.as<unsigned long long>(), ctx->d_num.as<int32_t>(),
-            ctx->cell_info.as<uint2>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>(),
+            ctx->cell_start.as<uint32_t>(), ctx->spos.as<float4>(), ctx->svel.as<float4>(), ctx->d_gen.as<DiffuseParticle>(),
             dn.gen, frame_dev, frame_off, &cnt->err);
     if (spawn_bound) PMS_LAUNCHED(ctx);
     if (dn.old) {
