@@ -64,6 +64,20 @@ __global__ void k_counters_init(Counters* cnt, uint32_t n) {
     *cnt = c;
 }
 
+// The counters into the context's mapped pinned mirror, stored by a kernel: a
+// copy-engine transfer would queue behind a streamed mesh or diffuse copy.
+__global__ void k_publish_counters(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint32_t words) {
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+
+pms_status launch_publish_counters(pms_ctx* ctx) {
+    static_assert(sizeof(Counters) % 4 == 0, "counters are copied in 32-bit words");
+    k_publish_counters<<<1, 128, 0, ctx->stream>>>(ctx->counters.as<uint32_t>(), ctx->h_counters_dev,
+                                                   (uint32_t)(sizeof(Counters) / 4));
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 pms_status launch_bbox(pms_ctx* ctx) {
     Counters* cnt = ctx->counters.as<Counters>();
     k_counters_init<<<1, 1, 0, ctx->stream>>>(cnt, ctx->n);

@@ -149,23 +149,12 @@ __global__ void __launch_bounds__(kThreads) k_mc_emit(KGrid g, float iso, Counte
                                                       const uint4* __restrict__ cube, const float* __restrict__ fdense,
                                                       float* __restrict__ vert, float* __restrict__ vnorm,
                                                       const unsigned long long* __restrict__ frame_base,
-                                                      unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
+                                                      unsigned long long cap, int piece) {
     constexpr int kS = kNormals ? 6 : 3;       // staged floats per mesh vertex
     __shared__ float stage[kEmitWarps][kEmitStage / 6 * kS];
-    // the cubes whose first mesh vertex lies in [v_lo, v_hi): cube records are in
-    // ascending first-vertex order, so both ends are lower bounds
-    const uint32_t nvalid_all = cnt->nvalid;
-    auto lower = [&](uint32_t v) {
-        uint32_t a = 0, b = nvalid_all;
-        while (a < b) {
-            const uint32_t mid = (a + b) >> 1;
-            if (__ldg(&cube[mid]).z < v) a = mid + 1;
-            else b = mid;
-        }
-        return a;
-    };
-    const uint32_t ka = v_lo ? lower(v_lo) : 0u;
-    const uint32_t nvalid = v_hi == 0xffffffffu ? nvalid_all : lower(v_hi);
+    // one streamed piece covers the cubes [mc_piece[piece], mc_piece[piece + 1]); piece < 0: all of them
+    const uint32_t ka = piece < 0 ? 0u : cnt->mc_piece[piece];
+    const uint32_t nvalid = piece < 0 ? cnt->nvalid : cnt->mc_piece[piece + 1];
     // batched frames write behind the earlier frames' vertices, within cap
     const unsigned long long fb = frame_base ? *frame_base : 0ull;
     const uint32_t rx = g.scres[0], rxy = g.scres[0] * g.scres[1];
@@ -359,18 +348,48 @@ pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long lo
     return PMS_OK;
 }
 
+// The first cube of each of `pieces` vertex ranges: cube records are in ascending
+// first-vertex order, so it is the lower bound of the range's first vertex.
+__global__ void k_mc_piece_bounds(const uint4* __restrict__ cube, Counters* __restrict__ cnt, uint32_t pieces) {
+    const uint32_t q = threadIdx.x;
+    if (q > pieces) return;
+    const uint32_t n = cnt->nvalid;
+    uint32_t lo = 0u, hi = n;
+    if (q == pieces) lo = n;
+    else if (q > 0u) {
+        const uint32_t v = (uint32_t)(cnt->nmesh * q / pieces);
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (cube[mid].z < v) lo = mid + 1u;
+            else hi = mid;
+        }
+    }
+    cnt->mc_piece[q] = lo;
+}
+
+pms_status launch_mc_piece_bounds(pms_ctx* ctx, uint32_t pieces) {
+    if (pieces < 1u || pieces > (uint32_t)kMaxMcPieces) return pms_fail(ctx, PMS_ERR_INVALID_ARGUMENT, "emission pieces");
+    k_mc_piece_bounds<<<1, 32, 0, ctx->stream>>>(ctx->cube.as<uint4>(), ctx->counters.as<Counters>(), pieces);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, uint32_t v_lo, uint32_t v_hi) {
+                             unsigned long long cap, int piece, uint32_t pieces) {
     const KGrid g = kgrid_of(ctx->grid);
     Counters* cnt = ctx->counters.as<Counters>();
+    // a piece's grid covers its share of the cubes with room for an uneven split; the
+    // grid-stride loop takes whatever is left over
+    const uint64_t work = piece < 0 ? ctx->nvalid : ((uint64_t)ctx->nvalid * 5u / (4u * pieces) + 1u);
+    const unsigned blocks = grid_for(work, kThreads);
     if (vnorm)
-        k_mc_emit<true><<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-            g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, vnorm, frame_base, cap, v_lo,
-            v_hi);
+        k_mc_emit<true><<<blocks, kThreads, 0, ctx->stream>>>(g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(),
+                                                              ctx->fdense.as<float>(), vert, vnorm, frame_base, cap,
+                                                              piece);
     else
-        k_mc_emit<false><<<grid_for(ctx->nvalid, kThreads), kThreads, 0, ctx->stream>>>(
-            g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(), ctx->fdense.as<float>(), vert, nullptr, frame_base, cap,
-            v_lo, v_hi);
+        k_mc_emit<false><<<blocks, kThreads, 0, ctx->stream>>>(g, ctx->prm.iso_value, cnt, ctx->cube.as<uint4>(),
+                                                               ctx->fdense.as<float>(), vert, nullptr, frame_base,
+                                                               cap, piece);
     PMS_LAUNCHED(ctx);
     return PMS_OK;
 }
@@ -503,9 +522,9 @@ pms_status launch_weld(pms_ctx* ctx, uint32_t* ebits, uint32_t* wc, uint32_t* wp
     return PMS_OK;
 }
 
-pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo, uint32_t v_hi) {
+pms_status launch_mc_emit(pms_ctx* ctx, int piece, uint32_t pieces) {
     return launch_mc_emit_to(ctx, ctx->vert.as<float>(), ctx->mesh_normals ? ctx->vnorm.as<float>() : nullptr, nullptr,
-                             ~0ull, v_lo, v_hi);
+                             ~0ull, piece, pieces);
 }
 
 }  // namespace pms

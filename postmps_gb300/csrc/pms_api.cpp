@@ -103,7 +103,17 @@ extern "C" pms_status pms_create(const pms_config* cfg, int device, pms_ctx** ou
     if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return PMS_ERR_CUDA; }
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return PMS_ERR_CUDA; }
     c->own_stream = true;
-    if (cudaMallocHost(&c->h_counters, sizeof(Counters)) != cudaSuccess) { cudaStreamDestroy(c->stream); delete c; return PMS_ERR_OUT_OF_MEMORY; }
+    if (cudaHostAlloc(&c->h_counters, sizeof(Counters), cudaHostAllocMapped) != cudaSuccess) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return PMS_ERR_OUT_OF_MEMORY;
+    }
+    if (cudaHostGetDevicePointer((void**)&c->h_counters_dev, c->h_counters, 0) != cudaSuccess) {
+        cudaFreeHost(c->h_counters);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return PMS_ERR_CUDA;
+    }
     memset(c->h_counters, 0, sizeof(Counters));
     for (int i = 0; i <= kNumStages; ++i) cudaEventCreate(&c->ev[i]);
     if (c->counters.ensure(sizeof(Counters)) != cudaSuccess || c->tmp.ensure(64) != cudaSuccess) {
@@ -262,7 +272,8 @@ extern "C" pms_status pms_reserve(pms_ctx* c, uint32_t max_particles, uint64_t m
 
 namespace pms {
 pms_status sync_counters(pms_ctx* c) {
-    PMS_CUDA(c, cudaMemcpyAsync(c->h_counters, c->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream));
+    pms_status st = launch_publish_counters(c);
+    if (st) return st;
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
     return PMS_OK;
 }
@@ -548,12 +559,13 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         // a streamed mesh goes in pieces: the emission runs in vertex ranges and each
         // piece travels on the copy stream while the next is made and the stages after run
         const bool copy = c->out_pos && c->nmesh <= c->out_cap;
-        const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? 4u : 1u) : 0u;
+        const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? (uint32_t)kMaxMcPieces : 1u) : 0u;
         if (!pieces && (st = launch_mc_emit(c))) return st;
+        if (pieces > 1u && (st = launch_mc_piece_bounds(c, pieces))) return st;
         for (uint32_t q = 0; q < pieces; ++q) {
             const uint32_t v_lo = (uint32_t)((uint64_t)c->nmesh * q / pieces);
             const uint32_t v_end = (uint32_t)((uint64_t)c->nmesh * (q + 1) / pieces);
-            if ((st = launch_mc_emit(c, v_lo, q + 1 == pieces ? 0xffffffffu : v_end))) return st;
+            if ((st = launch_mc_emit(c, pieces > 1u ? (int)q : -1, pieces))) return st;
             PMS_CUDA(c, cudaEventRecord(c->mesh_ready, c->stream));
             PMS_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->mesh_ready, 0));
             PMS_CUDA(c, cudaMemcpyAsync(c->out_pos + 3 * (size_t)v_lo, c->vert.as<float>() + 3 * (size_t)v_lo,

@@ -46,6 +46,8 @@ struct DBuf {
 };
 
 // Counters kept on the device between stages (read back only on demand).
+static constexpr int kMaxMcPieces = 4;  // vertex ranges a streamed mesh is emitted in
+
 struct Counters {
     uint32_t n;             // particles
     uint32_t ns;            // surface particles
@@ -77,6 +79,7 @@ struct Counters {
     uint32_t n_tiles;       // scalar-grid tiles the band marking visits
     uint32_t n_weld;        // vertices of the welded mesh (crossed grid edges)
     uint32_t n_df_total;    // generated + carried diffuse particles of a batched frame
+    uint32_t mc_piece[kMaxMcPieces + 1];  // first cube of each streamed emission range, then nvalid
 };
 static constexpr int kLearnCounters = 6;
 
@@ -211,7 +214,8 @@ struct pms_ctx {
     uint32_t frame_index = 0;
 
     pms::DBuf counters;          // pms::Counters
-    pms::Counters* h_counters = nullptr;  // pinned mirror
+    pms::Counters* h_counters = nullptr;  // pinned mirror, mapped
+    uint32_t* h_counters_dev = nullptr;   // ... its device address
     pms::ScanTemp scan;
     pms::DBuf tmp;
 
@@ -261,6 +265,8 @@ pms_status scan_u64(pms_ctx* ctx, const unsigned long long* in, unsigned long lo
 
 // stage launchers (one .cu each)
 pms_status launch_bbox(pms_ctx* ctx);
+// the counters into the mapped mirror h_counters (one small kernel on the context's stream)
+pms_status launch_publish_counters(pms_ctx* ctx);
 pms_status launch_hash_sort(pms_ctx* ctx);
 pms_status launch_surface_cells(pms_ctx* ctx);
 pms_status launch_density_aniso(pms_ctx* ctx);
@@ -278,9 +284,11 @@ pms_status launch_bits_list(pms_ctx* ctx, const uint32_t* bm, const uint32_t* wp
 pms_status launch_mc_cases(pms_ctx* ctx);
 pms_status launch_mc_compact(pms_ctx* ctx);
 pms_status launch_mc_classify(pms_ctx* ctx);
-// [v_lo, v_hi): emit only the cubes whose first mesh vertex lies there (all by default)
-pms_status launch_mc_emit(pms_ctx* ctx, uint32_t v_lo = 0,
-                          uint32_t v_hi = 0xffffffffu);
+// the mesh in `pieces` vertex ranges [nmesh * q / pieces, nmesh * (q + 1) / pieces): the first
+// cube of each range into Counters::mc_piece (pieces <= kMaxMcPieces)
+pms_status launch_mc_piece_bounds(pms_ctx* ctx, uint32_t pieces);
+// piece q emits the cubes whose first mesh vertex lies in range q (all cubes for piece < 0)
+pms_status launch_mc_emit(pms_ctx* ctx, int piece = -1, uint32_t pieces = 1);
 pms_status launch_scalar_values(pms_ctx* ctx);
 // welded mesh from the valid-cube records (k_mc.cu): ebits of nw words zeroed and set,
 // n_unique its vertex count; vert / vnorm / idx may be null
@@ -288,8 +296,7 @@ pms_status launch_weld(pms_ctx* ctx, uint32_t* ebits, uint32_t* wc, uint32_t* wp
                        uint64_t cap, float* vert, float* vnorm, uint32_t* idx);
 // triangle soup into vert (+ 3 * *frame_base floats when frame_base is set), at most cap vertices
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
-                             unsigned long long cap, uint32_t v_lo = 0,
-                             uint32_t v_hi = 0xffffffffu);
+                             unsigned long long cap, int piece = -1, uint32_t pieces = 1);
 pms_status launch_diffuse(pms_ctx* ctx);
 // A batched frame's diffuse stage: every size is a capacity and every count lives on the
 // device, so it can be captured into a graph.  The carried particles come from ctx->d_old
