@@ -25,11 +25,14 @@ distance in units of h).
 
 `value` is measured with the inputs already on the device (device-to-device
 upload inside the step); `e2e` goes through the C ABI as a pipelined frame
-loop: each step takes the frame staged during the step before, stages the next
-frame from pinned host buffers (pms_stage_particles, on another thread, while
-its own frame runs) and reads its triangle soup (and live diffuse particles)
-back into pinned host memory, all inside the timed region.  L2 is flushed (a
-256 MiB write) between timed steps.
+loop, frames in flight on both ends: each step takes the frame staged during
+the step before, stages the next frame from pinned host buffers
+(pms_stage_particles, on another thread, while its own frame runs), streams its
+triangle soup (and live diffuse particles) into one of two alternating pinned
+host buffer sets and waits for the step before's, whose copies ran beside it.
+One CUDA-event interval covers the K steps and the drain of the last one's
+results.  L2 is flushed (a 256 MiB write) between steps; in the end-to-end loop
+the flushes lie inside the interval.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pms|reference]
 
@@ -462,6 +465,25 @@ class Timer:
         ms = sum(a.elapsed_time(b) for a, b in ev) / k
         return max_over_ranks(ms, self.world, "cuda")
 
+    def loop(self, fn, k, drain):
+        """One CUDA-event interval over k pipelined steps and the drain that waits for
+        the last step's results, the L2 flushes between steps included."""
+        torch = self.torch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if self.world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        self.flush.zero_()
+        e0.record(self.stream)
+        for i in range(k):
+            if i:
+                self.flush.zero_()
+            fn()
+        drain()
+        e1.record(self.stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / k, self.world, "cuda")
+
 
 def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bool, clocks=None) -> dict:
     pos, vel, rho = frame
@@ -496,23 +518,44 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
     worker = threading.Thread(target=stager, daemon=True)
     worker.start()
 
-    def step_e2e():
-        # the user's calls of a pipelined frame loop: take the frame staged during the
-        # step before (its pinned copy and host-to-device copy ran while that frame
-        # computed), stage the next frame on the loop's staging thread while this one
-        # runs, reconstruct with the triangle soup streamed into pinned host memory while
-        # the diffuse stage runs and the live diffuse particles streamed after it, wait
-        # for both.  Every step moves one frame's inputs host to device inside the timed
-        # region (the frame it stages) and reads its own results back.
-        ctx.upload_staged()
-        go.release()
-        ctx.run_frame()
+    def register(k):
+        sm, sd = host["sets"][k % 2]
+        ctx.stream_mesh_to_host(sm.data_ptr(), None, sm.numel() // 3)
+        if diffuse:
+            ctx.stream_diffuse_to_host(sd.data_ptr(), sd.numel() // 32)
+
+    def take():
         host["n_mesh"] = ctx.wait_mesh()
         if diffuse:
             host["n_diffuse"] = ctx.wait_diffuse()
+
+    def step_e2e():
+        # the user's calls of a pipelined frame loop, frames in flight on both ends:
+        # take the frame staged during the step before (its pinned copy and
+        # host-to-device copy ran while that frame computed) and stage the next on the
+        # loop's staging thread; reconstruct into this step's host buffer set (the two
+        # sets alternate), the triangle soup streamed while the diffuse stage runs and
+        # the live diffuse particles after it; then wait for the step before's results,
+        # whose copies ran beside this frame.  The drain after the last step waits for
+        # its own.  Every step moves one frame's inputs host to device inside the timed
+        # region and reads one frame's results back.
+        k = host["k"]
+        register(k)
+        ctx.upload_staged()
+        go.release()
+        ctx.run_frame()
+        if host["pending"]:
+            take()
+        host["pending"] = True
+        host["k"] = k + 1
         done.acquire()
         if stage_err:
             raise RuntimeError(f"pms_stage_particles failed: status {stage_err[0]}")
+
+    def drain():
+        if host["pending"]:
+            take()
+        host["pending"] = False
 
     stage_sum = {k: 0.0 for k in STAGES}
 
@@ -541,21 +584,20 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         end = ctx.counts().as_dict()
         counts["n_diffuse_first_last"] = [int(counts["n_diffuse"]), int(end["n_diffuse"])]
         counts["n_diffuse"] = (int(counts["n_diffuse"]) + int(end["n_diffuse"])) // 2
-    # the host mesh buffer (pinned), sized from the frame's mesh
-    host["mesh"] = torch.empty(max(3, int(3 * counts["n_mesh_vertices"] * 1.25)), dtype=torch.float32).pin_memory()
-    ctx.stream_mesh_to_host(host["mesh"].data_ptr(), None, host["mesh"].numel() // 3)
-    if diffuse:
-        # 32-byte records; the live set grows while the same frame repeats (a spawned
-        # particle lives LifefimeMultiplier frames per sibling), so the buffer has room for
-        # every particle the warm-up and timed frames spawn
-        cap = int(counts["n_generated_diffuse"]) * (args.warmup + args.steps + 2) + (1 << 20)
-        host["dbuf"] = torch.empty(32 * cap, dtype=torch.uint8).pin_memory()
-        ctx.stream_diffuse_to_host(host["dbuf"].data_ptr(), cap)
+    # two host buffer sets (pinned), the mesh's sized from the frame's mesh; the diffuse
+    # set's 32-byte records: the live set grows while the same frame repeats (a spawned
+    # particle lives LifefimeMultiplier frames per sibling), so the buffer has room for
+    # every particle the warm-up and timed frames spawn
+    cap = int(counts["n_generated_diffuse"]) * (args.warmup + args.steps + 2) + (1 << 20)
+    host["sets"] = [(torch.empty(max(3, int(3 * counts["n_mesh_vertices"] * 1.25)), dtype=torch.float32).pin_memory(),
+                     torch.empty(32 * cap if diffuse else 32, dtype=torch.uint8).pin_memory()) for _ in range(2)]
+    host["k"], host["pending"] = 0, False
     ctx.reset_diffuse()
     stage_next()                              # the first frame of the pipelined loop
     for _ in range(args.warmup):
         step_e2e()
-    ms_e2e = timer(step_e2e, args.steps)
+    drain()
+    ms_e2e = timer.loop(step_e2e, args.steps, drain)
     clk = clocks.stop() if clocks else None
     stop.append(True)
     go.release()
@@ -791,7 +833,7 @@ def run_pms(args) -> None:
         "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": dict(desc, path=("surface + diffuse" if diffuse else "surface (diffuse off)"), band=head_arm,
-                       l2="flushed (256 MiB write) between steps", parallelism=f"replicas x{world}",
+                       l2="flushed (256 MiB write) between steps (inside the end-to-end loop's interval)", parallelism=f"replicas x{world}",
                        step=("one pms_run_batch call (one CUDA graph launch)" if batched else "one frame")),
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": head["ms_e2e"], "h2d_bytes_per_step": head["h2d"],
                 "d2h_bytes_per_step": head["d2h"]},

@@ -227,11 +227,19 @@ pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint6
  * it (diffuse generation) run; nrm_xyz may be NULL, pos_xyz NULL unregisters.
  * pms_wait_mesh blocks until the copy has landed and returns the vertex count
  * (PMS_ERR_CAPACITY, with the count, when cap_vertices was too small; nothing
- * is copied then).  The buffers must stay valid until that wait, and the next
- * frame's marching cubes writes them again.  The emission runs in vertex ranges
- * and each range is copied while the next is made.  No
- * counterpart in the reference, which copies the soup back with a blocking
- * cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
+ * is copied then).  The emission runs in vertex ranges and each range is copied
+ * while the next is made.
+ * Frames in flight: each frame's copy keeps the buffers registered when it ran,
+ * and registering others does not wait for it.  pms_wait_mesh waits for the
+ * oldest frame not yet waited for.  So a caller that alternates two buffer sets
+ * can run frame k+1 before waiting for frame k, whose copy then overlaps frame
+ * k+1's stages.  A frame that streams into buffers that an earlier frame's
+ * pending copy also writes drops that earlier frame (and every older pending
+ * one) after its copy has landed, as does a fifth frame in flight for the
+ * oldest.  With one buffer set this is the plain case: each frame replaces the
+ * last, and the wait returns the newest.  Buffers stay valid until their frame's
+ * wait.  No counterpart in the reference, which copies the soup back with a
+ * blocking cudaMemcpy when it writes the PLY file (FileData.cpp:1300-1305). */
 pms_status pms_stream_mesh_to_host(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint64_t cap_vertices);
 pms_status pms_wait_mesh(pms_ctx* ctx, uint64_t* n_vertices);
 /* Welded (indexed) mesh of the current frame, after pms_marching_cubes: one vertex
@@ -270,7 +278,9 @@ typedef struct pms_diffuse_particle {
  * NULL unregisters.  pms_wait_diffuse blocks until it has landed and returns the
  * count (PMS_ERR_CAPACITY, with the count, when cap was too small; nothing is
  * copied then).  The next frame's diffuse stage waits on the device for the copy
- * before it moves those particles.  No counterpart in the reference, which copies
+ * before it moves those particles.  Frames in flight, their buffers and the
+ * order of the waits work as for pms_stream_mesh_to_host, with a queue of their
+ * own.  No counterpart in the reference, which copies
  * the particles back with blocking cudaMemcpy calls to write its diffuse files
  * (DiffuseGeneration.cu:760-867). */
 pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_particle* out, uint64_t cap);
@@ -279,7 +289,8 @@ pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n);
 /* Drops the diffuse particles carried between frames and restarts the frame
  * counter that seeds the spawn, so the next frame starts a sequence as a fresh
  * run does (the reference's DiffuseGeneration starts empty and has no reset;
- * DiffuseGeneration.cu:21-87).  Waits for a streamed copy still in flight. */
+ * DiffuseGeneration.cu:21-87).  Waits for the streamed copies still in flight;
+ * their frames can still be waited for with pms_wait_diffuse. */
 pms_status pms_reset_diffuse(pms_ctx* ctx);
 
 /* Intermediate arrays, for parity tests.  Bytes needed are written to *needed;

@@ -764,8 +764,8 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     Counters* cnt = ctx->counters.as<Counters>();
     pms_status st;
     if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
-    // last frame's live particles (moved in place below) may still be on their way to the host
-    if (ctx->dout_pending) PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->diffuse_copied, 0));
+    // earlier frames' live particles (moved in place below) may still be on their way to the host
+    PMS_CHECK(out_device_wait(ctx, ctx->diffuse_q));
     if ((st = diffuse_front(ctx, g, dp, cnt))) return st;
     if ((st = sync_counters(ctx))) return st;
     const uint32_t n_gen = ctx->h_counters->n_generated, n_spawn = ctx->h_counters->n_spawning;
@@ -786,15 +786,16 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     std::swap(ctx->d_all, ctx->d_old);               // the survivors are next frame's old particles
     if (ctx->dout) {
         // the live set to the registered host buffer, on the copy stream
-        ctx->dout_n = ctx->diffuse_old;
-        ctx->dout_overflow = ctx->dout_n > ctx->dout_cap;
+        int slot;
+        PMS_CHECK(out_begin(ctx, ctx->diffuse_q, ctx->dout, &slot));
+        const uint64_t m = ctx->diffuse_old;
         PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_ready, ctx->stream));
         PMS_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->diffuse_ready, 0));
-        if (!ctx->dout_overflow && ctx->dout_n)
-            PMS_CUDA(ctx, cudaMemcpyAsync(ctx->dout, ctx->d_old.p, sizeof(DiffuseParticle) * ctx->dout_n,
-                                          cudaMemcpyDeviceToHost, ctx->copy_stream));
-        PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_copied, ctx->copy_stream));
-        ctx->dout_pending = true;
+        if (m && m <= ctx->dout_cap)
+            PMS_CUDA(ctx, cudaMemcpyAsync(ctx->dout, ctx->d_old.p, sizeof(DiffuseParticle) * m, cudaMemcpyDeviceToHost,
+                                          ctx->copy_stream));
+        PMS_CUDA(ctx, cudaEventRecord(ctx->diffuse_q.ev[slot], ctx->copy_stream));
+        out_push(ctx->diffuse_q, slot, ctx->dout, m, ctx->dout_cap);
     }
     return PMS_OK;
 }
@@ -877,17 +878,8 @@ static_assert(sizeof(DiffuseParticle) == sizeof(pms_diffuse_particle), "diffuse 
 extern "C" pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_particle* out, uint64_t cap) {
     if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
-    if (ctx->dout_pending) PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
-    ctx->dout_pending = false;
-    if (out && !ctx->copy_stream) {
-        PMS_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->mesh_ready, cudaEventDisableTiming));
-        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->mesh_copied, cudaEventDisableTiming));
-    }
-    if (out && !ctx->diffuse_ready) {
-        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->diffuse_ready, cudaEventDisableTiming));
-        PMS_CUDA(ctx, cudaEventCreateWithFlags(&ctx->diffuse_copied, cudaEventDisableTiming));
-    }
+    // frames already on their way keep their own buffers
+    if (out) PMS_CHECK(pms::copy_stream_ready(ctx));
     ctx->dout = out;
     ctx->dout_cap = out ? cap : 0;
     return PMS_OK;
@@ -895,15 +887,15 @@ extern "C" pms_status pms_stream_diffuse_to_host(pms_ctx* ctx, pms_diffuse_parti
 
 extern "C" pms_status pms_wait_diffuse(pms_ctx* ctx, uint64_t* n) {
     if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
-    if (!ctx->dout) return pms_fail(ctx, PMS_ERR_STATE, "pms_wait_diffuse without pms_stream_diffuse_to_host");
-    if (!ctx->dout_pending) return pms_fail(ctx, PMS_ERR_STATE, "no diffuse particles streamed since the last wait");
+    if (!ctx->diffuse_q.count) return pms_fail(ctx, PMS_ERR_STATE, "no diffuse particles streamed since the last wait");
     cudaSetDevice(ctx->device);
-    PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
-    ctx->dout_pending = false;
-    if (n) *n = ctx->dout_n;
-    if (ctx->dout_overflow)
+    uint64_t m = 0, cap = 0;
+    bool overflow = false;
+    PMS_CHECK(pms::out_wait(ctx, ctx->diffuse_q, &m, &overflow, &cap));
+    if (n) *n = m;
+    if (overflow)
         return pms_fail(ctx, PMS_ERR_CAPACITY, "%llu diffuse particles, the host buffer holds %llu",
-                        (unsigned long long)ctx->dout_n, (unsigned long long)ctx->dout_cap);
+                        (unsigned long long)m, (unsigned long long)cap);
     return PMS_OK;
 }
 
@@ -916,12 +908,12 @@ extern "C" void pms_debug_wendland_tail(const float* d, const float* t, float* o
 extern "C" pms_status pms_reset_diffuse(pms_ctx* ctx) {
     if (!ctx) return PMS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);
-    // the carried set is the source of a streamed copy until diffuse_copied fires
-    if (ctx->dout) PMS_CUDA(ctx, cudaEventSynchronize(ctx->diffuse_copied));
+    // the carried set is the source of streamed copies until they have landed; frames
+    // streamed before the reset can still be waited for
+    PMS_CHECK(pms::out_sync(ctx, ctx->diffuse_q));
     PMS_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->diffuse_old = 0;
     ctx->frame_index = 0;
-    ctx->dout_pending = false;
     ctx->have_diffuse = false;
     return PMS_OK;
 }

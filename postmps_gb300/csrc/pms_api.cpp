@@ -142,9 +142,9 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (c->up_start) cudaEventDestroy(c->up_start);
     if (c->vel_ready) cudaEventDestroy(c->vel_ready);
     if (c->mesh_ready) cudaEventDestroy(c->mesh_ready);
-    if (c->mesh_copied) cudaEventDestroy(c->mesh_copied);
     if (c->diffuse_ready) cudaEventDestroy(c->diffuse_ready);
-    if (c->diffuse_copied) cudaEventDestroy(c->diffuse_copied);
+    for (OutQueue* q : {&c->mesh_q, &c->diffuse_q})
+        for (cudaEvent_t e : q->ev) if (e) cudaEventDestroy(e);
     if (c->stage_stream) { cudaStreamSynchronize(c->stage_stream); cudaStreamDestroy(c->stage_stream); }
     if (c->stage_ready) cudaEventDestroy(c->stage_ready);
     if (c->stage_free) cudaEventDestroy(c->stage_free);
@@ -271,6 +271,58 @@ extern "C" pms_status pms_reserve(pms_ctx* c, uint32_t max_particles, uint64_t m
 }
 
 namespace pms {
+pms_status copy_stream_ready(pms_ctx* c) {
+    if (c->copy_stream) return PMS_OK;
+    PMS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    PMS_CUDA(c, cudaEventCreateWithFlags(&c->mesh_ready, cudaEventDisableTiming));
+    PMS_CUDA(c, cudaEventCreateWithFlags(&c->diffuse_ready, cudaEventDisableTiming));
+    for (OutQueue* q : {&c->mesh_q, &c->diffuse_q})
+        for (cudaEvent_t& e : q->ev) PMS_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return PMS_OK;
+}
+
+pms_status out_begin(pms_ctx* c, OutQueue& q, const void* host, int* slot) {
+    int drop = 0;                          // records to drop from the head
+    for (int i = 0; i < q.count; ++i)
+        if (q.host[(q.head + i) % OutQueue::kSlots] == host) drop = i + 1;
+    if (q.count - drop == OutQueue::kSlots) drop = 1;
+    if (drop) PMS_CUDA(c, cudaEventSynchronize(q.ev[(q.head + drop - 1) % OutQueue::kSlots]));
+    q.head = (q.head + drop) % OutQueue::kSlots;
+    q.count -= drop;
+    *slot = (q.head + q.count) % OutQueue::kSlots;
+    return PMS_OK;
+}
+
+void out_push(OutQueue& q, int slot, const void* host, uint64_t n, uint64_t cap) {
+    q.host[slot] = host;
+    q.n[slot] = n;
+    q.cap[slot] = cap;
+    q.overflow[slot] = n > cap;
+    q.last = slot;
+    q.count++;
+}
+
+pms_status out_wait(pms_ctx* c, OutQueue& q, uint64_t* n, bool* overflow, uint64_t* cap) {
+    const int h = q.head;
+    PMS_CUDA(c, cudaEventSynchronize(q.ev[h]));
+    q.head = (h + 1) % OutQueue::kSlots;
+    q.count--;
+    *n = q.n[h];
+    *overflow = q.overflow[h];
+    *cap = q.cap[h];
+    return PMS_OK;
+}
+
+pms_status out_device_wait(pms_ctx* c, const OutQueue& q) {
+    if (q.last >= 0) PMS_CUDA(c, cudaStreamWaitEvent(c->stream, q.ev[q.last], 0));
+    return PMS_OK;
+}
+
+pms_status out_sync(pms_ctx* c, const OutQueue& q) {
+    if (q.last >= 0) PMS_CUDA(c, cudaEventSynchronize(q.ev[q.last]));
+    return PMS_OK;
+}
+
 pms_status sync_counters(pms_ctx* c) {
     pms_status st = launch_publish_counters(c);
     if (st) return st;
@@ -540,6 +592,7 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
     c->nvalid = 0;
     c->nmesh = 0;
     c->have_weld = false;
+    int slot = -1;                     // the frame's record in the streamed-mesh queue
     if (c->nv) {
         pms_status st;
         // the learned band's last border check already computed the final vertex set's cases
@@ -551,13 +604,17 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         c->nvalid = c->h_counters->nvalid;
         c->nmesh = c->h_counters->nmesh;
         const size_t M = c->nmesh ? c->nmesh : 1;
-        // the previous frame's mesh may still be on its way to the host
-        if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
-        PMS_CUDA(c, c->vert.ensure_grow(12 * M));
+        // earlier frames' meshes may still be on their way to the host: a buffer that
+        // grows waits for them on the host (its old allocation is freed), the emission
+        // on the device
         c->mesh_normals = c->out_pos && c->out_nrm;
+        if (c->vert.cap < 12 * M || (c->mesh_normals && c->vnorm.cap < 12 * M)) PMS_CHECK(out_sync(c, c->mesh_q));
+        PMS_CUDA(c, c->vert.ensure_grow(12 * M));
         if (c->mesh_normals) PMS_CUDA(c, c->vnorm.ensure_grow(12 * M));
+        PMS_CHECK(out_device_wait(c, c->mesh_q));
         // a streamed mesh goes in pieces: the emission runs in vertex ranges and each
         // piece travels on the copy stream while the next is made and the stages after run
+        if (c->out_pos) PMS_CHECK(out_begin(c, c->mesh_q, c->out_pos, &slot));
         const bool copy = c->out_pos && c->nmesh <= c->out_cap;
         const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? (uint32_t)kMaxMcPieces : 1u) : 0u;
         if (!pieces && (st = launch_mc_emit(c))) return st;
@@ -576,10 +633,9 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         }
     }
     if (c->out_pos) {
-        c->out_n = c->nmesh;
-        c->out_overflow = c->nmesh > c->out_cap;
-        PMS_CUDA(c, cudaEventRecord(c->mesh_copied, c->copy_stream));
-        c->out_pending = true;
+        if (slot < 0) PMS_CHECK(out_begin(c, c->mesh_q, c->out_pos, &slot));
+        PMS_CUDA(c, cudaEventRecord(c->mesh_q.ev[slot], c->copy_stream));
+        out_push(c->mesh_q, slot, c->out_pos, c->nmesh, c->out_cap);
     }
     c->have_mc = true;
     mark(c, kStageMc + 1);
@@ -695,7 +751,7 @@ extern "C" pms_status pms_download_mesh(pms_ctx* c, float* pos, float* nrm, uint
     if (cap < c->nmesh || !pos) return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices", (unsigned long long)c->nmesh);
     if (nrm && !c->mesh_normals) {
         // the normals on demand: the emission once more, with them (same positions)
-        if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
+        PMS_CHECK(out_sync(c, c->mesh_q));
         PMS_CUDA(c, c->vnorm.ensure(12 * c->nmesh));
         c->mesh_normals = true;
         pms_status st = launch_mc_emit(c);
@@ -757,13 +813,8 @@ extern "C" pms_status pms_download_welded_mesh(pms_ctx* c, float* pos, float* nr
 extern "C" pms_status pms_stream_mesh_to_host(pms_ctx* c, float* pos, float* nrm, uint64_t cap) {
     if (!c || (!pos && nrm)) return PMS_ERR_INVALID_ARGUMENT;
     cudaSetDevice(c->device);
-    if (c->out_pending) PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
-    c->out_pending = false;
-    if (pos && !c->copy_stream) {
-        PMS_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        PMS_CUDA(c, cudaEventCreateWithFlags(&c->mesh_ready, cudaEventDisableTiming));
-        PMS_CUDA(c, cudaEventCreateWithFlags(&c->mesh_copied, cudaEventDisableTiming));
-    }
+    // frames already on their way keep their own buffers
+    if (pos) PMS_CHECK(copy_stream_ready(c));
     c->out_pos = pos;
     c->out_nrm = pos ? nrm : nullptr;
     c->out_cap = pos ? cap : 0;
@@ -772,15 +823,15 @@ extern "C" pms_status pms_stream_mesh_to_host(pms_ctx* c, float* pos, float* nrm
 
 extern "C" pms_status pms_wait_mesh(pms_ctx* c, uint64_t* n_vertices) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
-    if (!c->out_pos) return pms_fail(c, PMS_ERR_STATE, "pms_wait_mesh without pms_stream_mesh_to_host");
-    if (!c->out_pending) return pms_fail(c, PMS_ERR_STATE, "no mesh streamed since the last wait");
+    if (!c->mesh_q.count) return pms_fail(c, PMS_ERR_STATE, "no mesh streamed since the last wait");
     cudaSetDevice(c->device);
-    PMS_CUDA(c, cudaEventSynchronize(c->mesh_copied));
-    c->out_pending = false;
-    if (n_vertices) *n_vertices = c->out_n;
-    if (c->out_overflow)
-        return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices, the host buffers %llu",
-                        (unsigned long long)c->out_n, (unsigned long long)c->out_cap);
+    uint64_t n = 0, cap = 0;
+    bool overflow = false;
+    PMS_CHECK(out_wait(c, c->mesh_q, &n, &overflow, &cap));
+    if (n_vertices) *n_vertices = n;
+    if (overflow)
+        return pms_fail(c, PMS_ERR_CAPACITY, "mesh has %llu vertices, the host buffers %llu", (unsigned long long)n,
+                        (unsigned long long)cap);
     return PMS_OK;
 }
 

@@ -104,6 +104,20 @@ struct McTables {
 const McTables& mc_tables_host();
 const char* mc_tables_origin();
 
+// Frames whose streamed output (mesh or diffuse particles) is on its way to a
+// registered host buffer, oldest first.  Each record's event fires when its copies
+// have landed; copies run in order on the copy stream, so the newest event covers
+// every older one.
+struct OutQueue {
+    static constexpr int kSlots = 4;   // frames in flight at most
+    cudaEvent_t ev[kSlots] = {};
+    const void* host[kSlots] = {};     // the buffer the frame's copy writes
+    uint64_t n[kSlots] = {}, cap[kSlots] = {};
+    bool overflow[kSlots] = {};
+    int head = 0, count = 0;           // oldest record, records pending
+    int last = -1;                     // newest record ever made (its event may have fired)
+};
+
 // Scan workspace.
 struct ScanTemp {
     DBuf partial;           // per-block partial sums (u64 capable)
@@ -144,18 +158,20 @@ struct pms_ctx {
     bool staged = false, stage_free_recorded = false;
     uint32_t staged_n = 0;
     bool vel_pending = false;
-    // mesh streamed to registered host buffers on a copy stream while later stages run
+    // mesh streamed to registered host buffers on a copy stream while later stages (and,
+    // with alternating buffers, later frames) run; out_* is the registration for the
+    // frames to come, mesh_q the frames on their way
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t mesh_ready = nullptr, mesh_copied = nullptr;
+    cudaEvent_t mesh_ready = nullptr;
     float* out_pos = nullptr;
     float* out_nrm = nullptr;
-    uint64_t out_cap = 0, out_n = 0;
-    bool out_pending = false, out_overflow = false;
+    uint64_t out_cap = 0;
+    pms::OutQueue mesh_q;
     // live diffuse particles streamed to a registered host buffer on the copy stream
     pms_diffuse_particle* dout = nullptr;
-    uint64_t dout_cap = 0, dout_n = 0;
-    bool dout_pending = false, dout_overflow = false;
-    cudaEvent_t diffuse_ready = nullptr, diffuse_copied = nullptr;
+    uint64_t dout_cap = 0;
+    cudaEvent_t diffuse_ready = nullptr;
+    pms::OutQueue diffuse_q;
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;
@@ -237,6 +253,11 @@ pms_status pms_fail(pms_ctx* ctx, pms_status s, const char* fmt, ...);
                                                                     : PMS_ERR_CUDA,            \
                             "%s: %s (%s:%d)", #call, cudaGetErrorString(e__), __FILE__, __LINE__); \
     } while (0)
+#define PMS_CHECK(expr)                                                                        \
+    do {                                                                                       \
+        const pms_status s__ = (expr);                                                         \
+        if (s__ != PMS_OK) return s__;                                                         \
+    } while (0)
 #define PMS_LAUNCHED(ctx)                                                                      \
     do {                                                                                       \
         (ctx)->launches++;                                                                     \
@@ -265,6 +286,19 @@ pms_status scan_u64(pms_ctx* ctx, const unsigned long long* in, unsigned long lo
 
 // stage launchers (one .cu each)
 pms_status launch_bbox(pms_ctx* ctx);
+// Streamed-output queues (pms_api.cpp).  copy_stream_ready creates the copy stream and
+// both queues' events.  out_begin picks the record slot of a frame about to stream into
+// `host`: records still pending on that buffer (and every older one) are waited for and
+// dropped, as is the oldest when all slots are taken.  out_push files the frame after
+// its copies and the slot's event were issued.  out_wait pops the oldest record.
+// out_device_wait orders the context's stream after every copy issued so far (before a
+// copy's device source is written again); out_sync waits on the host for them.
+pms_status copy_stream_ready(pms_ctx* ctx);
+pms_status out_begin(pms_ctx* ctx, OutQueue& q, const void* host, int* slot);
+void out_push(OutQueue& q, int slot, const void* host, uint64_t n, uint64_t cap);
+pms_status out_wait(pms_ctx* ctx, OutQueue& q, uint64_t* n, bool* overflow, uint64_t* cap);
+pms_status out_device_wait(pms_ctx* ctx, const OutQueue& q);
+pms_status out_sync(pms_ctx* ctx, const OutQueue& q);
 // the counters into the mapped mirror h_counters (one small kernel on the context's stream)
 pms_status launch_publish_counters(pms_ctx* ctx);
 pms_status launch_hash_sort(pms_ctx* ctx);

@@ -535,14 +535,15 @@ class Context:
         return pos, nrm
 
     def stream_mesh_to_host(self, pos_ptr: int, nrm_ptr: int | None, cap_vertices: int) -> None:
-        """Register page-locked host buffers (raw addresses) that each frame's
-        marching cubes fill on a copy stream while the later stages run;
-        pos_ptr 0 unregisters."""
+        """Register page-locked host buffers (raw addresses) that each following
+        frame's marching cubes fill on a copy stream while the later stages run;
+        pos_ptr 0 unregisters.  Frames already streaming keep their buffers, so
+        alternating two sets lets frame k+1 run before frame k is waited for."""
         self._call("pms_stream_mesh_to_host", C.c_void_p(pos_ptr or None), C.c_void_p(nrm_ptr or None),
                    C.c_uint64(cap_vertices))
 
     def wait_mesh(self) -> int:
-        """Wait for the streamed mesh of the last frame; returns its vertex count."""
+        """Wait for the oldest streamed mesh not yet waited for; returns its vertex count."""
         n = C.c_uint64()
         self._call("pms_wait_mesh", C.byref(n))
         return n.value
@@ -567,7 +568,7 @@ class Context:
         self._call("pms_stream_diffuse_to_host", C.c_void_p(ptr or None), C.c_uint64(cap))
 
     def wait_diffuse(self) -> int:
-        """Wait for the streamed live diffuse particles of the last frame; returns their count."""
+        """Wait for the oldest streamed live diffuse set not yet waited for; returns its count."""
         n = C.c_uint64()
         self._call("pms_wait_diffuse", C.byref(n))
         return n.value

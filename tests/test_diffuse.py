@@ -219,3 +219,67 @@ def test_streamed_diffuse_particles_equal_downloaded(pms_lib, tmp_config):
             ctx.wait_diffuse()
         assert ei.value.status == 4
         ctx.stream_diffuse_to_host(0, 0)
+
+
+@pytest.mark.gpu
+def test_frames_in_flight_equal_waited_frames(pms_lib, tmp_config):
+    """Streamed outputs with frames in flight: alternating two host buffer sets,
+    frame k+1 runs before frame k's mesh and diffuse particles are waited for,
+    and each wait returns the oldest frame's results, equal to those of a
+    context that waits after every frame.  One buffer set with two frames
+    unwaited keeps only the newest."""
+    import ctypes as C
+    import torch
+    from postmps_gb300 import synth
+    pms = pms_lib
+    pos, vel, rho = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"})))
+    frames = [((pos + np.float32(0.004 * f) * vel).astype(np.float32), vel, rho) for f in range(4)]
+    cap_v, cap_d = 8_000_000, 1 << 19
+    mk = lambda: (torch.empty(3 * cap_v, dtype=torch.float32).pin_memory(),
+                  torch.empty(32 * cap_d, dtype=torch.uint8).pin_memory())
+    sets = [mk(), mk()]
+
+    def register(ctx, s):
+        ctx.stream_mesh_to_host(s[0].data_ptr(), None, cap_v)
+        ctx.stream_diffuse_to_host(s[1].data_ptr(), cap_d)
+
+    def take(ctx, s):
+        n, m = ctx.wait_mesh(), ctx.wait_diffuse()
+        return s[0].numpy()[: 3 * n].copy(), s[1].numpy()[: 32 * m].copy()
+
+    with pms.Context(cfg, 0) as ctx:
+        register(ctx, sets[0])
+        waited = []
+        for fr in frames:
+            ctx.upload(*fr)
+            ctx.run_frame()
+            waited.append(take(ctx, sets[0]))
+    with pms.Context(cfg, 0) as ctx:
+        got = []
+        for k, fr in enumerate(frames):
+            register(ctx, sets[k % 2])
+            ctx.upload(*fr)
+            ctx.run_frame()
+            if k:
+                got.append(take(ctx, sets[(k - 1) % 2]))
+        got.append(take(ctx, sets[(len(frames) - 1) % 2]))
+        with pytest.raises(pms.PmsError):
+            ctx.wait_mesh()
+        # one buffer set, two frames unwaited: the second replaces the first
+        register(ctx, sets[0])
+        for fr in frames[:2]:
+            ctx.upload(*fr)
+            ctx.run_frame()
+        last = take(ctx, sets[0])
+        with pytest.raises(pms.PmsError):
+            ctx.wait_diffuse()
+        ctx.stream_mesh_to_host(0, None, 0)
+        ctx.stream_diffuse_to_host(0, 0)
+    assert len(got) == len(waited)
+    for (m0, d0), (m1, d1) in zip(waited, got):
+        assert len(m0) > 0 and len(d0) > 0
+        assert np.array_equal(m0, m1)
+        assert np.array_equal(d0, d1)
+    # the carried diffuse set grew over six frames in that context; the mesh is frame 1's
+    assert np.array_equal(last[0], waited[1][0])
