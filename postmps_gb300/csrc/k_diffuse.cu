@@ -756,9 +756,14 @@ static pms_status diffuse_tail(pms_ctx* ctx, const KGrid& g, const DiffuseParams
     return PMS_OK;
 }
 
-pms_status launch_diffuse(pms_ctx* ctx) {
-    const uint32_t n = ctx->n;
-    if (n == 0) { ctx->diffuse_old = 0; return PMS_OK; }
+// The single-frame diffuse stage in three parts, each with at most one host
+// synchronisation, at its start: the front (free surface, potentials, spawn counts),
+// the tail (spawn, update, delete/append) once the counts are on the host, and the
+// finish (the live count, the streamed copy).  A frame with surface reconstruction
+// runs the parts on a stream of their own between the surface stages.
+pms_status diffuse_part_front(pms_ctx* ctx) {
+    ctx->df_run = ctx->n != 0;
+    if (!ctx->df_run) { ctx->diffuse_old = 0; return PMS_OK; }
     const KGrid g = kgrid_of(ctx->grid);
     const DiffuseParams dp = diffuse_params(ctx);
     Counters* cnt = ctx->counters.as<Counters>();
@@ -766,11 +771,20 @@ pms_status launch_diffuse(pms_ctx* ctx) {
     if (!ctx->have_aniso && (st = launch_surface_cells(ctx))) return st;
     // earlier frames' live particles (moved in place below) may still be on their way to the host
     PMS_CHECK(out_device_wait(ctx, ctx->diffuse_q));
-    if ((st = diffuse_front(ctx, g, dp, cnt))) return st;
+    return diffuse_front(ctx, g, dp, cnt);
+}
+
+pms_status diffuse_part_tail(pms_ctx* ctx) {
+    if (!ctx->df_run) return PMS_OK;
+    const KGrid g = kgrid_of(ctx->grid);
+    const DiffuseParams dp = diffuse_params(ctx);
+    Counters* cnt = ctx->counters.as<Counters>();
+    pms_status st;
     if ((st = sync_counters(ctx))) return st;
     const uint32_t n_gen = ctx->h_counters->n_generated, n_spawn = ctx->h_counters->n_spawning;
     const uint32_t n_old = ctx->diffuse_old;
     const size_t total = (size_t)n_gen + n_old;
+    ctx->df_total = total;
     PMS_CUDA(ctx, ctx->d_gen.ensure_grow(sizeof(DiffuseParticle) * (n_gen ? n_gen : 1)));
     PMS_CUDA(ctx, ctx->d_all.ensure_grow(sizeof(DiffuseParticle) * (total ? total : 1)));
     PMS_CUDA(ctx, ctx->d_typescan.ensure_grow(8 * (total ? total : 1)));
@@ -780,9 +794,14 @@ pms_status launch_diffuse(pms_ctx* ctx) {
         PMS_CUDA(ctx, ctx->d_perm.ensure_grow(4 * (size_t)n_old));
     }
     const DfN dn = {n_gen, n_old, nullptr, nullptr, (uint32_t)(total ? total : 1), &cnt->err};
-    if ((st = diffuse_tail(ctx, g, dp, cnt, dn, n_spawn, nullptr, 0, &cnt->n_live))) return st;
+    return diffuse_tail(ctx, g, dp, cnt, dn, n_spawn, nullptr, 0, &cnt->n_live);
+}
+
+pms_status diffuse_part_finish(pms_ctx* ctx) {
+    if (!ctx->df_run) return PMS_OK;
+    pms_status st;
     if ((st = sync_counters(ctx))) return st;
-    ctx->diffuse_old = total ? ctx->h_counters->n_live : 0;
+    ctx->diffuse_old = ctx->df_total ? ctx->h_counters->n_live : 0;
     std::swap(ctx->d_all, ctx->d_old);               // the survivors are next frame's old particles
     if (ctx->dout) {
         // the live set to the registered host buffer, on the copy stream
@@ -798,6 +817,12 @@ pms_status launch_diffuse(pms_ctx* ctx) {
         out_push(ctx->diffuse_q, slot, ctx->dout, m, ctx->dout_cap);
     }
     return PMS_OK;
+}
+
+pms_status launch_diffuse(pms_ctx* ctx) {
+    PMS_CHECK(diffuse_part_front(ctx));
+    PMS_CHECK(diffuse_part_tail(ctx));
+    return diffuse_part_finish(ctx);
 }
 
 // every buffer of a batched frame's diffuse stage, for frames of up to nmax particles

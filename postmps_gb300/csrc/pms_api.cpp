@@ -61,6 +61,7 @@ static void for_each_dbuf(pms_ctx* c, F f) {
                     &c->d_freelist, &c->d_pot, &c->d_num, &c->d_numscan, &c->d_isdiff, &c->d_isdiffscan,
                     &c->d_difflist, &c->d_gen, &c->d_old, &c->d_all, &c->d_rand, &c->d_typescan,
                     &c->d_nrm_free, &c->d_tkey, &c->d_tscan, &c->d_perm, &c->counters, &c->scan.partial, &c->tmp,
+                    &c->df_scan.partial, &c->df_tmp,
                     &c->l_dens, &c->l_clist, &c->l_counts, &c->l_model, &c->l_q, &c->l_cert, &c->l_e_bm, &c->l_e_wc,
                     &c->l_e_wp, &c->l_e_list, &c->l_n_bm, &c->l_n_wc, &c->l_n_wp, &c->l_n_list, &c->l_field_new,
                     &c->l_cand, &c->l_logit, &c->l_label, &c->tile_bits, &c->tile_wc, &c->tile_wp, &c->tile_list,
@@ -141,6 +142,9 @@ extern "C" void pms_destroy(pms_ctx* c) {
     if (c->up_stream) { cudaStreamSynchronize(c->up_stream); cudaStreamDestroy(c->up_stream); }
     if (c->up_start) cudaEventDestroy(c->up_start);
     if (c->vel_ready) cudaEventDestroy(c->vel_ready);
+    if (c->df_stream) { cudaStreamSynchronize(c->df_stream); cudaStreamDestroy(c->df_stream); }
+    if (c->df_fork) cudaEventDestroy(c->df_fork);
+    if (c->df_join) cudaEventDestroy(c->df_join);
     if (c->mesh_ready) cudaEventDestroy(c->mesh_ready);
     if (c->diffuse_ready) cudaEventDestroy(c->diffuse_ready);
     for (OutQueue* q : {&c->mesh_q, &c->diffuse_q})
@@ -691,12 +695,81 @@ extern "C" pms_status pms_diffuse(pms_ctx* c) {
     return PMS_OK;
 }
 
+// The diffuse parts are issued on the context's diffuse stream with their own scan
+// scratch: the context's stream and scratch are swapped for them while in scope.
+namespace {
+struct OnDiffuseStream {
+    pms_ctx* c;
+    explicit OnDiffuseStream(pms_ctx* ctx) : c(ctx) { swap(); }
+    ~OnDiffuseStream() { swap(); }
+    void swap() {
+        std::swap(c->stream, c->df_stream);
+        std::swap(c->scan.partial, c->df_scan.partial);
+        std::swap(c->tmp, c->df_tmp);
+    }
+};
+}  // namespace
+
+// A frame with surface reconstruction and diffuse generation: the diffuse stage
+// depends only on the grid and the anisotropy pass, and the surface stages only on
+// those too, so after the anisotropy the diffuse parts run on a stream of their own
+// beside the band, field and marching cubes.  Each part is issued where the surface
+// chain has a long stretch of work queued: the front before the band's
+// synchronisation, the tail after the field is queued, the finish after the emission.
+// Results are those of the stages one after the other (no stage reads what the other
+// chain writes; counters are separate fields, errors are OR-ed).
+static pms_status run_frame_overlapped(pms_ctx* c) {
+    pms_status st;
+    if (!c->df_stream) {
+        int lo = 0, hi = 0;
+        PMS_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        PMS_CUDA(c, cudaStreamCreateWithPriority(&c->df_stream, cudaStreamNonBlocking, lo));
+        PMS_CUDA(c, cudaEventCreateWithFlags(&c->df_fork, cudaEventDisableTiming));
+        PMS_CUDA(c, cudaEventCreateWithFlags(&c->df_join, cudaEventDisableTiming));
+        PMS_CUDA(c, c->df_tmp.ensure(64));
+    }
+    if ((st = pms_anisotropy(c))) return st;
+    PMS_CUDA(c, cudaEventRecord(c->df_fork, c->stream));
+    PMS_CUDA(c, cudaStreamWaitEvent(c->df_stream, c->df_fork, 0));
+    {
+        OnDiffuseStream d(c);
+        if ((st = diffuse_part_front(c))) return st;
+    }
+    if (c->band_mode != PMS_BAND_PLAIN) {
+        if ((st = pms_band_learned(c))) return st;
+    } else {
+        if ((st = pms_band(c))) return st;
+        if ((st = pms_field(c))) return st;
+    }
+    {
+        OnDiffuseStream d(c);
+        if ((st = diffuse_part_tail(c))) return st;
+    }
+    if ((st = pms_marching_cubes(c))) return st;
+    {
+        OnDiffuseStream d(c);
+        if ((st = diffuse_part_finish(c))) return st;
+        // the diffuse stage's time runs from the anisotropy's end, where it forked
+        PMS_CUDA(c, cudaEventRecord(c->ev[kStageDiffuse + 1], c->stream));
+        PMS_CUDA(c, cudaEventRecord(c->df_join, c->stream));
+    }
+    c->ev_from[kStageDiffuse] = kStageAniso + 1;
+    c->ev_recorded[kStageDiffuse] = true;
+    PMS_CUDA(c, cudaStreamWaitEvent(c->stream, c->df_join, 0));
+    c->have_diffuse = true;
+    return PMS_OK;
+}
+
 extern "C" pms_status pms_run_frame(pms_ctx* c) {
     if (!c) return PMS_ERR_INVALID_ARGUMENT;
     pms_status st;
     if ((st = pms_build_grid(c))) return st;
-    if (c->cfg.is_surface && (st = c->band_mode != PMS_BAND_PLAIN ? pms_surface_learned(c) : pms_surface(c))) return st;
-    if (c->cfg.is_diffuse && (st = pms_diffuse(c))) return st;
+    if (c->cfg.is_surface && c->cfg.is_diffuse) {
+        if ((st = run_frame_overlapped(c))) return st;
+    } else {
+        if (c->cfg.is_surface && (st = c->band_mode != PMS_BAND_PLAIN ? pms_surface_learned(c) : pms_surface(c))) return st;
+        if (c->cfg.is_diffuse && (st = pms_diffuse(c))) return st;
+    }
     c->frame_index++;
     return PMS_OK;
 }

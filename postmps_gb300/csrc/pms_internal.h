@@ -172,6 +172,14 @@ struct pms_ctx {
     uint64_t dout_cap = 0;
     cudaEvent_t diffuse_ready = nullptr;
     pms::OutQueue diffuse_q;
+    // the diffuse stage beside the surface stages of a frame: its own stream and scan
+    // scratch (swapped in while its parts are issued), fork and join events
+    cudaStream_t df_stream = nullptr;
+    cudaEvent_t df_fork = nullptr, df_join = nullptr;
+    pms::ScanTemp df_scan;
+    pms::DBuf df_tmp;
+    bool df_run = false;               // the frame's diffuse parts have work (particles)
+    size_t df_total = 0;               // generated + carried particles of the frame
     bool own_stream = false;
     std::string last_error;
     uint64_t launches = 0;
@@ -332,6 +340,10 @@ pms_status launch_weld(pms_ctx* ctx, uint32_t* ebits, uint32_t* wc, uint32_t* wp
 pms_status launch_mc_emit_to(pms_ctx* ctx, float* vert, float* vnorm, const unsigned long long* frame_base,
                              unsigned long long cap, int piece = -1, uint32_t pieces = 1);
 pms_status launch_diffuse(pms_ctx* ctx);
+// launch_diffuse's three parts (k_diffuse.cu): front, tail, finish
+pms_status diffuse_part_front(pms_ctx* ctx);
+pms_status diffuse_part_tail(pms_ctx* ctx);
+pms_status diffuse_part_finish(pms_ctx* ctx);
 // A batched frame's diffuse stage: every size is a capacity and every count lives on the
 // device, so it can be captured into a graph.  The carried particles come from ctx->d_old
 // (their count at *old_dev, set by the frame before), the survivors go to ctx->d_all and
