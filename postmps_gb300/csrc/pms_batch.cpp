@@ -73,7 +73,7 @@ struct BatchState {
     // diffuse generation
     pms_ctx* dlane = nullptr;                    // the diffuse lane
     cudaEvent_t djoin = nullptr;
-    std::vector<cudaEvent_t> ev_surf, ev_diff;   // per frame: surface stages done, diffuse stage done
+    std::vector<cudaEvent_t> ev_surf, ev_diff;   // per frame: grid and anisotropy done (the diffuse fork), diffuse done
     DBuf dcnt, drun, dbase, darena;              // {carried count, first frame's number}, arena fill, offsets, arena
     uint64_t darena_cap = 0;
     uint32_t gen_cap = 0, old_cap = 0;
@@ -160,18 +160,24 @@ struct DiffuseLaneView {
 };
 
 // Stages of one frame without host synchronisation (the context points at the frame).
-// band: 0 plain, 1 learned (network + certification), 2 certification alone
-static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, int band) {
+// band: 0 plain, 1 learned (network + certification), 2 certification alone.
+// fork (when set) is recorded once the frame's grid and anisotropy are made: all the
+// diffuse stage reads, so the diffuse lane starts there, beside the band and field.
+static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, int band, cudaEvent_t fork) {
     pms_status st;
     Counters* cnt = c->counters.as<Counters>();
     const pms_grid& g = c->grid;
     c->nv = g.sc_size;                       // bounds for launch grids; kernels read the device counts
     c->nvalid = g.sc_size;
     if ((st = launch_bbox(c))) return st;    // resets the frame's counters
-    if (c->n == 0) return PMS_OK;
+    if (c->n == 0) {
+        if (fork) PMS_CUDA(c, cudaEventRecord(fork, c->stream));
+        return PMS_OK;
+    }
     if ((st = launch_hash_sort(c))) return st;
     if ((st = launch_surface_cells(c))) return st;
     if ((st = launch_density_aniso(c))) return st;
+    if (fork) PMS_CUDA(c, cudaEventRecord(fork, c->stream));
     if (band) {
         if ((st = launch_band(c))) return st;
         if ((st = launch_band_list(c))) return st;
@@ -237,12 +243,11 @@ static pms_status capture(pms_ctx* c, BatchState* b, int band, uint32_t nlanes, 
             views[l]->point(b, f);
             // external: recorded when the graph runs (a plain record inside a capture only orders work)
             if (cudaEventRecordWithFlags(b->ev[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
-            if ((st = capture_frame(lc, b, f, band))) break;
+            if ((st = capture_frame(lc, b, f, band, dl ? b->ev_surf[f] : nullptr))) break;
             if (cudaEventRecordWithFlags(b->ev_end[f], lc->stream, cudaEventRecordExternal) != cudaSuccess) { st = PMS_ERR_CUDA; break; }
             last[l] = (int)f;
             if (!dl) continue;
-            if (cudaEventRecord(b->ev_surf[f], lc->stream) != cudaSuccess ||
-                cudaStreamWaitEvent(dl->stream, b->ev_surf[f], 0) != cudaSuccess) {
+            if (cudaStreamWaitEvent(dl->stream, b->ev_surf[f], 0) != cudaSuccess) {
                 st = PMS_ERR_CUDA;
                 break;
             }
