@@ -620,7 +620,10 @@ extern "C" pms_status pms_marching_cubes(pms_ctx* c) {
         // piece travels on the copy stream while the next is made and the stages after run
         if (c->out_pos) PMS_CHECK(out_begin(c, c->mesh_q, c->out_pos, &slot));
         const bool copy = c->out_pos && c->nmesh <= c->out_cap;
-        const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) ? (uint32_t)kMaxMcPieces : 1u) : 0u;
+        // with an earlier frame's mesh still pending, the caller keeps frames in flight and this
+        // copy overlaps the next frame: one range, without the ranges' bounds and extra launches
+        const bool in_flight = c->mesh_q.count > 0;
+        const uint32_t pieces = copy ? (c->nmesh >= (1u << 16) && !in_flight ? (uint32_t)kMaxMcPieces : 1u) : 0u;
         if (!pieces && (st = launch_mc_emit(c))) return st;
         if (pieces > 1u && (st = launch_mc_piece_bounds(c, pieces))) return st;
         for (uint32_t q = 0; q < pieces; ++q) {
