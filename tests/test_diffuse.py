@@ -283,3 +283,36 @@ def test_frames_in_flight_equal_waited_frames(pms_lib, tmp_config):
         assert np.array_equal(d0, d1)
     # the carried diffuse set grew over six frames in that context; the mesh is frame 1's
     assert np.array_equal(last[0], waited[1][0])
+
+
+@pytest.mark.gpu
+def test_overlapped_frame_equals_stage_by_stage(pms_lib, tmp_config):
+    """pms_run_frame with surface and diffuse on runs the diffuse stage on a stream
+    of its own beside the band, field and marching cubes; calling the stages one
+    after the other on the context's stream (pms_build_grid, pms_surface,
+    pms_diffuse) gives the same mesh and the same live diffuse particles, bit for
+    bit, on a frame that carries particles from the frame before."""
+    from postmps_gb300 import synth
+    pms = pms_lib
+    pos, vel, rho = synth.crown_splash(n_slab=(60, 60, 12), n_ring=40000, radius=0.09)
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"})))
+    frames = [((pos + np.float32(0.004 * f) * vel).astype(np.float32), vel, rho) for f in range(2)]
+    out = []
+    for stepwise in (False, True):
+        with pms.Context(cfg, 0) as ctx:
+            ctx.upload(*frames[0])
+            ctx.run_frame()
+            ctx.upload(*frames[1])
+            if stepwise:
+                ctx.build_grid()
+                ctx.surface()
+                ctx.diffuse()
+            else:
+                ctx.run_frame()
+            live = ctx.diffuse_particles(-1)
+            out.append((ctx.mesh(normals=False)[0], live))
+    (m0, d0), (m1, d1) = out
+    assert len(m0) > 0 and len(d0["pos"]) > 0
+    assert np.array_equal(m0, m1)
+    for k in ("pos", "vel", "ttl", "type"):
+        np.testing.assert_array_equal(d0[k], d1[k])
