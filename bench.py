@@ -833,7 +833,9 @@ def run_pms(args) -> None:
         "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": dict(desc, path=("surface + diffuse" if diffuse else "surface (diffuse off)"), band=head_arm,
-                       l2="flushed (256 MiB write) between steps (inside the end-to-end loop's interval)", parallelism=f"replicas x{world}",
+                       l2=("flushed (256 MiB write) between steps" + ("" if batched else
+                                                                          " (inside the end-to-end loop's interval)")),
+                       parallelism=f"replicas x{world}",
                        step=("one pms_run_batch call (one CUDA graph launch)" if batched else "one frame")),
         "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": head["ms_e2e"], "h2d_bytes_per_step": head["h2d"],
                 "d2h_bytes_per_step": head["d2h"]},

@@ -711,6 +711,16 @@ struct OnDiffuseStream {
         std::swap(c->tmp, c->df_tmp);
     }
 };
+
+// Joins the diffuse stream back into the context's stream when the frame ends, on
+// every path: work of a frame that failed half way must not run into the next one.
+struct DiffuseJoin {
+    pms_ctx* c;
+    ~DiffuseJoin() {
+        cudaEventRecord(c->df_join, c->df_stream);
+        cudaStreamWaitEvent(c->stream, c->df_join, 0);
+    }
+};
 }  // namespace
 
 // A frame with surface reconstruction and diffuse generation: the diffuse stage
@@ -734,6 +744,7 @@ static pms_status run_frame_overlapped(pms_ctx* c) {
     if ((st = pms_anisotropy(c))) return st;
     PMS_CUDA(c, cudaEventRecord(c->df_fork, c->stream));
     PMS_CUDA(c, cudaStreamWaitEvent(c->df_stream, c->df_fork, 0));
+    DiffuseJoin join{c};
     {
         OnDiffuseStream d(c);
         if ((st = diffuse_part_front(c))) return st;
@@ -754,13 +765,11 @@ static pms_status run_frame_overlapped(pms_ctx* c) {
         if ((st = diffuse_part_finish(c))) return st;
         // the diffuse stage's time runs from the anisotropy's end, where it forked
         PMS_CUDA(c, cudaEventRecord(c->ev[kStageDiffuse + 1], c->stream));
-        PMS_CUDA(c, cudaEventRecord(c->df_join, c->stream));
     }
     c->ev_from[kStageDiffuse] = kStageAniso + 1;
     c->ev_recorded[kStageDiffuse] = true;
-    PMS_CUDA(c, cudaStreamWaitEvent(c->stream, c->df_join, 0));
     c->have_diffuse = true;
-    return PMS_OK;
+    return PMS_OK;                     // join: the frame's stream waits for the diffuse stream
 }
 
 extern "C" pms_status pms_run_frame(pms_ctx* c) {
