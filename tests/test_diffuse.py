@@ -316,3 +316,41 @@ def test_overlapped_frame_equals_stage_by_stage(pms_lib, tmp_config):
     assert np.array_equal(m0, m1)
     for k in ("pos", "vel", "ttl", "type"):
         np.testing.assert_array_equal(d0[k], d1[k])
+
+
+@pytest.mark.gpu
+def test_overlapped_empty_and_single_particle_frames(pms_lib, tmp_config):
+    """Empty and one-particle frames through the overlapped frame (surface and
+    diffuse on) with both outputs streamed and frames in flight, then a real frame:
+    nothing hangs or errors, the empty frame's mesh record comes back with 0 vertices
+    and the real frame's outputs are those of a fresh context."""
+    import torch
+    from postmps_gb300 import synth
+    pms = pms_lib
+    pos, vel, rho = synth.crown_splash(n_slab=(40, 40, 10), n_ring=20000, radius=0.07)
+    cfg = pms.load_config(tmp_config(synth.config_text(**synth.CROWN_KEYS, **{"config.isdiffusegeneration": "true"})))
+    mesh = [torch.empty(3 * 4_000_000, dtype=torch.float32).pin_memory() for _ in range(2)]
+    dif = [torch.empty(32 * (1 << 18), dtype=torch.uint8).pin_memory() for _ in range(2)]
+    with pms.Context(cfg, 0) as ctx:
+        seq = [(np.zeros((0, 3), np.float32), None, None), (np.array([[0.1, 0.2, 0.3]], np.float32), None, None)]
+        ns = []
+        for k, fr in enumerate(seq):
+            ctx.stream_mesh_to_host(mesh[k % 2].data_ptr(), None, 4_000_000)
+            ctx.stream_diffuse_to_host(dif[k % 2].data_ptr(), 1 << 18)
+            ctx.upload(*fr)
+            ctx.run_frame()
+        ns.append(ctx.wait_mesh())
+        ns.append(ctx.wait_mesh())
+        assert ns[0] == 0 and ns[1] % 3 == 0
+        ctx.reset_diffuse()
+        ctx.stream_mesh_to_host(0, None, 0)
+        ctx.stream_diffuse_to_host(0, 0)
+        ctx.upload(pos, vel, rho)
+        ctx.run_frame()
+        m_after = ctx.mesh(normals=False)[0]
+        d_after = ctx.diffuse_particles(-1)
+    with pms.Context(cfg, 0) as fresh:
+        fresh.upload(pos, vel, rho)
+        fresh.run_frame()
+        assert np.array_equal(m_after, fresh.mesh(normals=False)[0])
+        np.testing.assert_array_equal(d_after["pos"], fresh.diffuse_particles(-1)["pos"])
