@@ -658,15 +658,14 @@ def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None, diff
         ctx.run_batch(dframes, learned=mode)
 
     def step_e2e():
+        # the frames' soups land in the registered host arena inside the graph, each right
+        # after its frame's emission (pms_batch_stream_meshes); the live diffuse sets are
+        # read back after it
         ctx.run_batch(hframes, learned=mode)
         nd = 0
         for f in range(len(frames)):
             nv = C.c_uint64()
-            pms.lib().pms_batch_mesh(ctx.handle, f, None, 0, C.byref(nv))
-            buf = host.get(f)
-            if buf is None or buf.numel() < 3 * nv.value:
-                buf = host[f] = torch.empty(max(3, int(3 * nv.value * 1.25)), dtype=torch.float32).pin_memory()
-            ctx._call("pms_batch_mesh", f, buf.data_ptr(), buf.numel() // 3, C.byref(nv))
+            ctx.batch_mesh_range(f)
             if diffuse:
                 pms.lib().pms_batch_diffuse(ctx.handle, f, None, 0, C.byref(nv))
                 dbuf = host.get(("d", f))
@@ -693,12 +692,15 @@ def batch_arm(pms, ctx, frames, mode: str, args, timer, torch, clocks=None, diff
         c, fms = ctx.batch_frame(f)
         per_frame.append(fms)
         counts.append(c.as_dict())
+    mesh = sum(int(c["n_mesh_vertices"]) for c in counts)
+    host["arena"] = torch.empty(3 * (int(mesh * 1.25) + 1024), dtype=torch.float32).pin_memory()
+    ctx.batch_stream_meshes(host["arena"].data_ptr(), host["arena"].numel() // 3)
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
         if reset:
             reset()
     ms_e2e = timer(step_e2e, args.steps, reset)
-    mesh = sum(int(c["n_mesh_vertices"]) for c in counts)
+    ctx.batch_stream_meshes(0, 0)
     return {"ms": ms, "ms_e2e": ms_e2e, "launches": launches, "clocks": clk, "frame_ms": per_frame,
             "counts": counts, "info": ctx.batch_info(), "h2d": sum(28 * len(fr[0]) for fr in frames),
             "d2h": 12 * mesh + 32 * read["diffuse"]}

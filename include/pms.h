@@ -452,6 +452,18 @@ pms_status pms_run_batch(pms_ctx* ctx, const pms_frame* frames, uint32_t k, int 
 pms_status pms_batch_frame(pms_ctx* ctx, uint32_t f, pms_counts* counts, float* ms);
 /* Triangle soup of frame f (positions, 3 vertices per triangle). */
 pms_status pms_batch_mesh(pms_ctx* ctx, uint32_t f, float* pos_xyz, uint64_t cap, uint64_t* n_vertices);
+/* Registers a page-locked host arena (cudaHostAlloc or cudaHostRegister memory,
+ * mapped) of cap_vertices vertices that every following pms_run_batch fills inside
+ * its graph: each frame's soup is stored there by the SMs right after the frame's
+ * emission, on the frame's lane, while the other lanes compute.  Frame f's soup
+ * starts at vertex pms_batch_mesh_range's *first (the layout of the device arena);
+ * it has landed when pms_run_batch returns.  A batch whose meshes do not fit
+ * returns PMS_ERR_CAPACITY.  pos_xyz NULL unregisters; the graph is captured again
+ * when the registration changes.  No reference counterpart (its frames copy their
+ * soup back one by one, FileData.cpp:1300-1305). */
+pms_status pms_batch_stream_meshes(pms_ctx* ctx, float* pos_xyz, uint64_t cap_vertices);
+/* First vertex and vertex count of frame f's soup in the last batch's arenas. */
+pms_status pms_batch_mesh_range(pms_ctx* ctx, uint32_t f, uint64_t* first, uint64_t* n_vertices);
 /* Live diffuse particles of frame f of the last batch (after its delete/append),
  * as the 32-byte records of pms_stream_diffuse_to_host; *n receives the count
  * (PMS_ERR_CAPACITY, with the count, when cap is too small; out NULL: count only). */

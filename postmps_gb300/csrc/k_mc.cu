@@ -342,6 +342,38 @@ __global__ void k_batch_base(const Counters* __restrict__ cnt, unsigned long lon
     *base = atomicAdd(running, (unsigned long long)cnt->nmesh);
 }
 
+// A batched frame's triangle soup into mapped page-locked host memory, at the same
+// vertex offset as in the device arena: stores over the host link from the SMs, on
+// the frame's lane right after its emission, while the other lanes compute.  What
+// lies past the host arena's capacity is left out and flagged in *trunc.
+__global__ void __launch_bounds__(256) k_batch_mesh_to_host(const float* __restrict__ mesh,
+                                                            const unsigned long long* __restrict__ base_f,
+                                                            const Counters* __restrict__ cnt, unsigned long long dev_cap,
+                                                            float* __restrict__ host, unsigned long long host_cap,
+                                                            uint32_t* __restrict__ trunc) {
+    const unsigned long long b = *base_f;
+    unsigned long long n = cnt->nmesh;
+    if (b >= dev_cap) return;                          // the device arena overflowed: the batch runs again
+    if (b + n > dev_cap) n = dev_cap - b;
+    if (b + n > host_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(trunc, 1u);
+        n = b < host_cap ? host_cap - b : 0ull;
+    }
+    const float* __restrict__ src = mesh + 3 * b;
+    float* __restrict__ dst = host + 3 * b;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < 3 * n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        dst[i] = __ldcs(src + i);
+}
+
+pms_status launch_batch_mesh_to_host(pms_ctx* ctx, const float* mesh, const unsigned long long* base_f,
+                                     unsigned long long dev_cap, float* host, unsigned long long host_cap, uint32_t* trunc) {
+    k_batch_mesh_to_host<<<152 * 2, 256, 0, ctx->stream>>>(mesh, base_f, ctx->counters.as<Counters>(), dev_cap, host,
+                                                          host_cap, trunc);
+    PMS_LAUNCHED(ctx);
+    return PMS_OK;
+}
+
 pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long long* running, unsigned long long* base) {
     k_batch_base<<<1, 1, 0, ctx->stream>>>(cnt, running, base);
     PMS_LAUNCHED(ctx);

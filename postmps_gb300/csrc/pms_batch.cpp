@@ -50,6 +50,8 @@ pms_status ensure_band_buffers(pms_ctx* c, uint32_t nv);
 pms_status ensure_particle_buffers(pms_ctx* c, uint32_t n);
 pms_status ensure_grid_buffers(pms_ctx* c, const pms_grid& g);
 pms_status launch_batch_base(pms_ctx* ctx, const Counters* cnt, unsigned long long* running, unsigned long long* base);
+pms_status launch_batch_mesh_to_host(pms_ctx* ctx, const float* mesh, const unsigned long long* base_f,
+                                     unsigned long long dev_cap, float* host, unsigned long long host_cap, uint32_t* trunc);
 }  // namespace pms
 
 struct BatchState {
@@ -79,6 +81,11 @@ struct BatchState {
     uint32_t gen_cap = 0, old_cap = 0;
     void *d_in = nullptr, *d_out = nullptr;      // carried buffer the graph reads first / holds the survivors last
     std::vector<unsigned long long> hdbase;
+    // meshes streamed into a registered host arena inside the graph (pms_batch_stream_meshes)
+    float* h_mesh = nullptr;                     // host address, for the caller
+    float* h_mesh_dev = nullptr;                 // the same memory as the kernels see it
+    uint64_t h_mesh_cap = 0;                     // vertices
+    DBuf h_trunc;                                // set when a frame's soup did not fit the host arena
     ~BatchState() {
         if (exec) cudaGraphExecDestroy(exec);
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
@@ -90,7 +97,7 @@ struct BatchState {
         for (cudaEvent_t e : ev_diff) cudaEventDestroy(e);
         if (djoin) cudaEventDestroy(djoin);
         if (dlane) pms_destroy(dlane);
-        for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh, &dcnt, &drun, &dbase, &darena}) b->release();
+        for (DBuf* b : {&pos, &vel, &rho, &cnt, &base, &mesh, &dcnt, &drun, &dbase, &darena, &h_trunc}) b->release();
     }
 };
 
@@ -191,7 +198,11 @@ static pms_status capture_frame(pms_ctx* c, BatchState* b, uint32_t f, int band,
     }
     unsigned long long* base = b->base.as<unsigned long long>();
     if ((st = launch_batch_base(c, cnt, base + b->n.size(), base + f))) return st;
-    return launch_mc_emit_to(c, b->mesh.as<float>(), nullptr, base + f, b->mesh_cap);
+    if ((st = launch_mc_emit_to(c, b->mesh.as<float>(), nullptr, base + f, b->mesh_cap))) return st;
+    if (b->h_mesh_dev)
+        return launch_batch_mesh_to_host(c, b->mesh.as<float>(), base + f, b->mesh_cap, b->h_mesh_dev, b->h_mesh_cap,
+                                         b->h_trunc.as<uint32_t>());
+    return PMS_OK;
 }
 
 static constexpr uint32_t kBatchLanes = 4;
@@ -356,8 +367,10 @@ static uint64_t batch_signature(pms_ctx* c, BatchState* b, uint32_t nlanes, bool
     uint64_t h = 0;
     for (uint32_t l = 0; l < nlanes; ++l) h = h * 31u + dbuf_signature(lane_ctx(c, b, l), false);
     if (diffuse && b->dlane) h = h * 31u + dbuf_signature(b->dlane, true);
-    for (DBuf* x : {&b->pos, &b->vel, &b->rho, &b->cnt, &b->base, &b->mesh, &b->dcnt, &b->drun, &b->dbase, &b->darena})
+    for (DBuf* x : {&b->pos, &b->vel, &b->rho, &b->cnt, &b->base, &b->mesh, &b->dcnt, &b->drun, &b->dbase, &b->darena,
+                    &b->h_trunc})
         h = (h * 1099511628211ull) ^ (uint64_t)(uintptr_t)x->p ^ ((uint64_t)x->cap << 1);
+    h = (h * 1099511628211ull) ^ (uint64_t)(uintptr_t)b->h_mesh_dev ^ (b->h_mesh_cap << 1);
     return h;
 }
 
@@ -512,6 +525,7 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
                 PMS_CUDA(c, cudaMemcpyAsync(b->d_in, c->d_old.p, 32 * (size_t)c->diffuse_old, cudaMemcpyDeviceToDevice, c->stream));
             PMS_CUDA(c, cudaMemcpyAsync(b->dcnt.p, in, sizeof(in), cudaMemcpyHostToDevice, c->stream));
         }
+        if (b->h_mesh_dev) PMS_CUDA(c, cudaMemsetAsync(b->h_trunc.p, 0, sizeof(uint32_t), c->stream));
         PMS_CUDA(c, cudaGraphLaunch(b->exec, c->stream));
         c->launches += c->batch_launches;
         b->hbase.resize(k + 1);
@@ -526,7 +540,14 @@ extern "C" pms_status pms_run_batch(pms_ctx* c, const pms_frame* frames, uint32_
         }
         unsigned long long dfill = 0;
         if (diffuse) PMS_CUDA(c, cudaMemcpy(&dfill, b->drun.p, sizeof(dfill), cudaMemcpyDeviceToHost));
-        if (!overflow) break;
+        if (!overflow) {
+            uint32_t trunc = 0;
+            if (b->h_mesh_dev) PMS_CUDA(c, cudaMemcpy(&trunc, b->h_trunc.p, sizeof(trunc), cudaMemcpyDeviceToHost));
+            if (trunc)
+                return pms_fail(c, PMS_ERR_CAPACITY, "the batch's meshes have %llu vertices, the host arena holds %llu",
+                                (unsigned long long)b->hbase[k], (unsigned long long)b->h_mesh_cap);
+            break;
+        }
         if (attempt == attempts - 1) return pms_fail(c, PMS_ERR_CAPACITY, "batch capacity overflow");
         if (b->hbase[k] > b->mesh_cap) {
             b->mesh_cap = std::max<uint64_t>(2 * b->mesh_cap, b->hbase[k] + (b->hbase[k] >> 2));
@@ -617,6 +638,31 @@ extern "C" pms_status pms_batch_mesh(pms_ctx* c, uint32_t f, float* pos, uint64_
     cudaSetDevice(c->device);
     if (m) PMS_CUDA(c, cudaMemcpyAsync(pos, b->mesh.as<float>() + 3 * b->hbase[f], 12 * m, cudaMemcpyDeviceToHost, c->stream));
     PMS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_stream_meshes(pms_ctx* c, float* pos, uint64_t cap) {
+    if (!c) return PMS_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    BatchState* b = batch_of(c);
+    float* dev = nullptr;
+    if (pos && cudaHostGetDevicePointer((void**)&dev, pos, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return pms_fail(c, PMS_ERR_INVALID_ARGUMENT, "the host mesh arena is not mapped page-locked memory");
+    }
+    if (pos) PMS_CUDA(c, b->h_trunc.ensure(sizeof(uint32_t)));
+    b->h_mesh = pos;
+    b->h_mesh_dev = pos ? dev : nullptr;
+    b->h_mesh_cap = pos ? cap : 0;
+    return PMS_OK;
+}
+
+extern "C" pms_status pms_batch_mesh_range(pms_ctx* c, uint32_t f, uint64_t* first, uint64_t* n_out) {
+    if (!c || !c->batch || !first || !n_out) return PMS_ERR_INVALID_ARGUMENT;
+    BatchState* b = static_cast<BatchState*>(c->batch);
+    if (f >= b->n.size() || b->hbase.size() <= f) return PMS_ERR_INVALID_ARGUMENT;
+    *first = b->hbase[f];
+    *n_out = b->hcnt[f].nmesh;
     return PMS_OK;
 }
 

@@ -218,6 +218,8 @@ def lib() -> C.CDLL:
         L.pms_batch_frame.argtypes = [vp, C.c_uint32, C.POINTER(Counts), C.POINTER(C.c_float)]
         L.pms_batch_mesh.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
         L.pms_batch_diffuse.argtypes = [vp, C.c_uint32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+        L.pms_batch_stream_meshes.argtypes = [vp, vp, C.c_uint64]
+        L.pms_batch_mesh_range.argtypes = [vp, C.c_uint32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
         L.pms_batch_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.pms_save_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel), C.c_char_p]
         L.pms_load_band_model.argtypes = [C.c_char_p, C.POINTER(BandModel)]
@@ -489,6 +491,17 @@ class Context:
         if n.value:
             self._call("pms_batch_mesh", f, _ptr(out), n.value, C.byref(n))
         return out
+
+    def batch_stream_meshes(self, ptr: int, cap_vertices: int) -> None:
+        """Register a page-locked host arena (raw address) that each following batch
+        fills with its frames' soups inside the graph; ptr 0 unregisters."""
+        self._call("pms_batch_stream_meshes", C.c_void_p(ptr or None), C.c_uint64(cap_vertices))
+
+    def batch_mesh_range(self, f: int) -> tuple[int, int]:
+        """(first vertex, vertex count) of frame f's soup in the last batch's arenas."""
+        a, n = C.c_uint64(), C.c_uint64()
+        self._call("pms_batch_mesh_range", f, C.byref(a), C.byref(n))
+        return a.value, n.value
 
     def batch_diffuse(self, f: int) -> np.ndarray:
         """Live diffuse particles of frame f of the last batch: records of pos (3 float),

@@ -247,3 +247,39 @@ def test_batch_with_diffuse_equals_single_frames(pms_lib, tmp_config):
         caps = batch.batch_info()["captures"]
         check_batch([6, 7, 8, 9, 10])
         assert batch.batch_info()["captures"] == caps
+
+
+@pytest.mark.gpu
+def test_batch_meshes_streamed_inside_the_graph(pms_lib):
+    """pms_batch_stream_meshes: with a host arena registered, every frame's soup
+    lands there inside the graph at its pms_batch_mesh_range offset, equal to
+    pms_batch_mesh's; registering captures the graph again; an arena too small
+    for the batch reports PMS_ERR_CAPACITY; unregistering returns to downloads."""
+    import torch
+    pms = pms_lib
+    frames = _frames(5)
+    frames.insert(2, (np.zeros((0, 3), np.float32), None, None))
+    with _ctx(pms, 0.02) as ctx:
+        ctx.run_batch(frames)
+        ref = [ctx.batch_mesh(f) for f in range(len(frames))]
+        total = sum(len(m) for m in ref)
+        arena = torch.empty(3 * (total + 1000), dtype=torch.float32).pin_memory()
+        ctx.batch_stream_meshes(arena.data_ptr(), total + 1000)
+        caps = ctx.batch_info()["captures"]
+        for rep in range(2):
+            arena.zero_()
+            ctx.run_batch(frames)
+            assert ctx.batch_info()["captures"] == caps + 1      # captured once for the registration
+            host = arena.numpy().reshape(-1, 3)
+            for f in range(len(frames)):
+                first, n = ctx.batch_mesh_range(f)
+                assert n == len(ref[f])
+                assert np.array_equal(host[first:first + n], ref[f]), (rep, f)
+        small = torch.empty(3 * (total // 2), dtype=torch.float32).pin_memory()
+        ctx.batch_stream_meshes(small.data_ptr(), total // 2)
+        with pytest.raises(pms.PmsError) as ei:
+            ctx.run_batch(frames)
+        assert ei.value.status == 4
+        ctx.batch_stream_meshes(0, 0)
+        ctx.run_batch(frames)
+        assert np.array_equal(ctx.batch_mesh(3), ref[3])
