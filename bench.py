@@ -534,8 +534,8 @@ def single_frame_arm(pms, ctx, frame, mode: str, args, timer, torch, diffuse: bo
         # take the frame staged during the step before (its pinned copy and
         # host-to-device copy ran while that frame computed) and stage the next on the
         # loop's staging thread; reconstruct into this step's host buffer set (the two
-        # sets alternate), the triangle soup streamed while the diffuse stage runs and
-        # the live diffuse particles after it; then wait for the step before's results,
+        # sets alternate), the triangle soup streamed after the emission and the live
+        # diffuse particles after the diffuse stage; then wait for the step before's results,
         # whose copies ran beside this frame.  The drain after the last step waits for
         # its own.  Every step moves one frame's inputs host to device inside the timed
         # region and reads one frame's results back.
