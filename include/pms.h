@@ -202,7 +202,12 @@ pms_status pms_field(pms_ctx* ctx);             /* Anisotropic::estimationOfscal
 pms_status pms_marching_cubes(pms_ctx* ctx);    /* MarchingCube::triangulation, MarchingCube.cu:32-68 */
 pms_status pms_surface(pms_ctx* ctx);           /* SurfaceReconstruction::runsimulation, SurfaceReconstruction.cu:34-60 */
 pms_status pms_diffuse(pms_ctx* ctx);           /* DiffuseGeneration::runsimulation, DiffuseGeneration.cu:89-104 */
-pms_status pms_run_frame(pms_ctx* ctx);         /* one iteration of GPUPOST::runSimulation, GPUPOST.cpp:56-81 */
+/* One iteration of GPUPOST::runSimulation (GPUPOST.cpp:56-81): grid, then surface and
+ * diffuse as configured.  With both on, the diffuse stage runs on a stream of the
+ * context's own beside the band, field and marching cubes, forked after the
+ * anisotropy pass and joined back into the context's stream before the call returns;
+ * results are those of the stages one after the other. */
+pms_status pms_run_frame(pms_ctx* ctx);
 
 /* Density and velocity at every mesh vertex: MarchingCube::scalarvalue /
  * estimationOfScalarValue (MarchingCube.cu:153-163, MarchingCube_kernel.cuh:161-233),
