@@ -282,7 +282,7 @@ k_field(KGrid g, FieldParams fp, const Counters* __restrict__ cnt, const uint32_
                             for (int k = 0; k < K; ++k) nu += use[k] ? 1u : 0u;
                             my_pairs += (unsigned long long)(j1 - j0) * nu;
                         }
-#pragma unroll 2
+#pragma unroll 1
                         for (uint32_t j = j0; j < j1; ++j) {
                             const float4 q = __ldg(&spos[j]);
                             const float4 a0 = __ldg(&aniso[2 * (size_t)j]);      // {m00, 2 m01, 2 m02, h_s^2}
