@@ -233,7 +233,8 @@ pms_status pms_download_mesh(pms_ctx* ctx, float* pos_xyz, float* nrm_xyz, uint6
  * pms_wait_mesh blocks until the copy has landed and returns the vertex count
  * (PMS_ERR_CAPACITY, with the count, when cap_vertices was too small; nothing
  * is copied then).  The emission runs in vertex ranges and each range is copied
- * while the next is made.
+ * while the next is made (one range when an earlier frame's copy is still in
+ * flight: the copy then overlaps the next frame anyway).
  * Frames in flight: each frame's copy keeps the buffers registered when it ran,
  * and registering others does not wait for it.  pms_wait_mesh waits for the
  * oldest frame not yet waited for.  So a caller that alternates two buffer sets
