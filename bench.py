@@ -116,6 +116,15 @@ def write_config(keys: dict) -> str:
 # ---------------------------------------------------------------------------
 # algorithmic bytes per stage, from the frame's own counts
 # ---------------------------------------------------------------------------
+def dominant_stage(stage_ms: dict, alg: dict, diffuse: bool) -> str:
+    """The stage whose kernel the roofline reports: the longest on the frame's stream.  With
+    surface and diffuse on, the diffuse stage runs on its own stream beside the band, field
+    and marching cubes, so its time is a span from the anisotropy's end, not a cost of its
+    own, and it is left out."""
+    serial = [k for k in alg if not (diffuse and k == "diffuse")]
+    return max(serial, key=lambda k: stage_ms.get(k, 0.0))
+
+
 def algorithmic_bytes(c: dict, sp_size: int, sc_size: int, diffuse: bool, learned: bool) -> dict:
     N, Ns, Vs, Cv, M = c["n_particles"], c["n_surface_particles"], c["n_band_vertices"], c["n_valid_cubes"], \
         c["n_mesh_vertices"]
@@ -868,11 +877,7 @@ def run_pms(args) -> None:
     else:
         stage_ms = head["stage_ms"]
         alg = algorithmic_bytes(head["counts"], head["sp_size"], head["sc_size"], diffuse, head_arm != "plain")
-        # with surface and diffuse on, the diffuse stage runs on its own stream beside the band,
-        # field and marching cubes: its time is a span from the anisotropy's end, not a cost
-        # of its own, so the dominant kernel is chosen among the stages of the frame's stream
-        serial = [k for k in alg if not (diffuse and k == "diffuse")]
-        dom = max(serial, key=lambda k: stage_ms.get(k, 0.0))
+        dom = dominant_stage(stage_ms, alg, diffuse)
         achieved = alg[dom] / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else None
         traffic = None
         tfile = os.path.join(ROOT, "profiles", f"traffic_{desc['workload']}.json")

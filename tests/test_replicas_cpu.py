@@ -56,3 +56,16 @@ def test_single_rank_is_a_no_op():
     import bench
     assert bench.max_over_ranks(12.5, 1) == 12.5
     assert bench.job_throughput(500, 1, 10.0) == pytest.approx(50_000.0)
+
+
+def test_roofline_kernel_is_chosen_on_the_frame_stream():
+    """With diffuse generation on, the diffuse stage's time is a span beside the surface
+    stages, so the roofline's kernel is the longest stage of the frame's own stream."""
+    sys.path.insert(0, ROOT)
+    import bench
+    stage = {"grid": 0.2, "anisotropy": 0.95, "band": 0.92, "field": 2.78, "marching_cubes": 0.86, "diffuse": 4.56}
+    alg = {k: 1.0 for k in stage}
+    assert bench.dominant_stage(stage, alg, diffuse=True) == "field"
+    assert bench.dominant_stage(dict(stage, field=0.5), alg, diffuse=True) == "anisotropy"
+    # surface only: every stage is on the frame's stream
+    assert bench.dominant_stage(dict(stage, diffuse=9.0), alg, diffuse=False) == "diffuse"
