@@ -16,8 +16,10 @@
  *   - Host buffers are caller-owned plain arrays; positions and velocities are
  *     xyz-interleaved float32 (the reference's float3 layout).
  *   - Device buffers are owned by the context and reused (grow-only) across
- *     frames.  A context is bound to one device and one CUDA stream and is not
- *     thread-safe; use one context per host thread.
+ *     frames.  A context is bound to one device and one CUDA stream (its
+ *     copy, staging and diffuse streams are forked from and joined back into
+ *     it) and is not thread-safe; use one context per host thread (staging,
+ *     pms_stage_particles, is the one call another thread may make).
  *   - Counts stay on the device between stages; calls that return counts or
  *     data synchronise the context's stream.
  */
@@ -336,7 +338,9 @@ pms_status pms_debug_download(pms_ctx* ctx, int array_id, void* dst, uint64_t ca
 pms_status pms_debug_set_wait_limit(pms_ctx* ctx, int64_t polls);
 
 /* Device time of each stage of the last frame, in milliseconds (CUDA events on
- * the context stream): [grid, anisotropy, band, field, marching cubes, diffuse]. */
+ * the context stream): [grid, anisotropy, band, field, marching cubes, diffuse].
+ * When pms_run_frame ran the diffuse stage beside the surface stages, its figure
+ * is the span from the anisotropy's end to its own end. */
 pms_status pms_stage_times(pms_ctx* ctx, float* ms, int count);
 
 /* Number of kernels libpms launched since the context was created. */
