@@ -16,10 +16,11 @@
  *   - Host buffers are caller-owned plain arrays; positions and velocities are
  *     xyz-interleaved float32 (the reference's float3 layout).
  *   - Device buffers are owned by the context and reused (grow-only) across
- *     frames.  A context is bound to one device and one CUDA stream (its
- *     copy, staging and diffuse streams are forked from and joined back into
- *     it) and is not thread-safe; use one context per host thread (staging,
- *     pms_stage_particles, is the one call another thread may make).
+ *     frames.  A context is bound to one device and one CUDA stream (its copy
+ *     and staging streams run beside it and are waited for explicitly; the
+ *     diffuse stream of pms_run_frame is forked from it and joined back within
+ *     the call) and is not thread-safe; use one context per host thread
+ *     (pms_stage_particles is the one call another thread may make).
  *   - Counts stay on the device between stages; calls that return counts or
  *     data synchronise the context's stream.
  */
